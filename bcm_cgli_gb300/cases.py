@@ -1,0 +1,312 @@
+"""Synthetic BCM cases: cube grids, adjacency, flags, initial fields.
+
+A *case* is everything the hot path consumes, in the reference's own layout
+(``Array.h:13-44``): conservative state ``U[c][i][j][k][5]`` with ``S = n+4``
+cells per cube edge (two ghost layers each side), flags ``FWS[c][i][j][k]``,
+``cube_size[c]``, level ``csl[c]`` and adjacency ``adj_number[c][5][7]``
+(slot 1..4, direction 1..6 = -x,+x,-y,+y,-z,+z; ``BCM_Grid.cpp`` layout).
+Cube 0 is unused: the reference numbers cubes from 1 (``main.cpp:90``).
+
+All random inputs come from a counter-based generator (splitmix64 on the
+cell index) so fixtures are identical on every machine and numpy version.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+GAMMA = 1.4  # K, prm.h:1
+R_GAS = 287.0  # R, prm.h:2
+CV = 717.5  # Cv, prm.h:4
+PR_L = 0.72  # Pr_L, prm.h:6
+
+IFLUID, IGHOST, ISOLID = 1, 0, -1  # BCM.h:6-8
+
+
+def splitmix_uniform(seed: int, count: int) -> np.ndarray:
+    """Deterministic uniforms in [0,1) from splitmix64(seed*2^32 + index)."""
+    with np.errstate(over="ignore"):
+        x = (np.arange(count, dtype=np.uint64) + np.uint64(seed) * np.uint64(1 << 32))
+        x = x + np.uint64(0x9E3779B97F4A7C15)
+        z = x.copy()
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(11)).astype(np.float64) * (1.0 / (1 << 53))
+
+
+@dataclass
+class Phys:
+    """prm.h constants of one case (plus the MPI_Ncube norm normaliser)."""
+
+    mu_L: float = 0.0000185
+    rho0: float = 1.1842
+    U0: float = 38.889
+    Uin: float = 38.889
+    P0: float = 101300.0
+    mpi_ncube: int = 64
+
+    @property
+    def T0(self) -> float:
+        return self.P0 / self.rho0 / R_GAS
+
+
+@dataclass
+class Case:
+    n: int  # interior cells per cube edge (NcubeX)
+    ncube: int  # number of cube slots incl. the unused slot 0 (reference Ncube)
+    phys: Phys
+    cube_size: np.ndarray  # [ncube] f64
+    csl: np.ndarray  # [ncube] i32
+    origin: np.ndarray  # [ncube, 3] f64 (Xcube, Ycube, Zcube)
+    adj: np.ndarray  # [ncube, 5, 7] i32
+    fws: np.ndarray  # [ncube, S, S, S] i32
+    U: np.ndarray  # [ncube, S, S, S, 5] f64 initial state (all cells)
+    dT: float = 1e-4
+    dTau: float = 1e-4 / 200.0
+    e: float = 0.1
+    name: str = "case"
+    # IBM ghost tables, 1-based packed like BCM_Reading_IBM.cpp:53-73.
+    ibm_minus: tuple | None = None  # (weight[8n+1], GCindex[4n+1], IPsur[4n+1])
+    ibm_plus: tuple | None = None
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def S(self) -> int:
+        return self.n + 4
+
+    @property
+    def n_cells(self) -> int:
+        """Interior cells of all real cubes (the unit of the throughput metric)."""
+        return (self.ncube - 1) * self.n ** 3
+
+    def bc_lists(self):
+        """Boundary-cube lists by bounding box, as main.cpp:108-189 builds them.
+
+        Returns six int32 arrays (x lower, x upper, y lower, y upper, z lower,
+        z upper) of cube numbers in increasing order.
+        """
+        c = np.arange(1, self.ncube)
+        o = self.origin[1:]
+        s = self.cube_size[1:]
+        lo = [o[:, a].min() for a in range(3)]
+        hi = [(o[:, a] + s).max() for a in range(3)]
+        out = []
+        for a in range(3):
+            out.append(c[np.abs(o[:, a] - lo[a]) < 1e-7].astype(np.int32))
+            out.append(c[np.abs(o[:, a] + s - hi[a]) < 1e-7].astype(np.int32))
+        return out  # xl, xu, yl, yu, zl, zu
+
+    def cell_centres(self):
+        """Cell-centre coordinates [ncube, S] per axis: origin + (i-1.5)*dx
+        (BCM_Grid.cpp: Xcnt = Xcube + (i-1.5)*dx)."""
+        dx = self.cube_size / self.n
+        idx = np.arange(self.S, dtype=np.float64) - 1.5
+        return [self.origin[:, a][:, None] + idx[None, :] * dx[:, None] for a in range(3)]
+
+
+def periodic_box(ncx: int, ncy: int, ncz: int, n: int, length: float):
+    """Equal cubes tiling [0,L)^3 with wrap-around adjacency (slot 1 only).
+
+    Cube numbering is x-fastest from 1.  Returns (ncube, cube_size, csl,
+    origin, adj).  Periodicity comes only from the adjacency, like the
+    reference (which has no periodic boundary condition).
+    """
+    nc = ncx * ncy * ncz
+    ncube = nc + 1
+    size = length / ncx
+    cube_size = np.zeros(ncube)
+    cube_size[1:] = size
+    csl = np.zeros(ncube, np.int32)
+    csl[1:] = 1
+    origin = np.zeros((ncube, 3))
+    adj = np.zeros((ncube, 5, 7), np.int32)
+    def num(a, b, c):
+        return 1 + (a % ncx) + ncx * ((b % ncy) + ncy * (c % ncz))
+    for c in range(ncz):
+        for b in range(ncy):
+            for a in range(ncx):
+                k = num(a, b, c)
+                origin[k] = (a * size, b * size, c * size)
+                adj[k, 1, 1] = num(a - 1, b, c)
+                adj[k, 1, 2] = num(a + 1, b, c)
+                adj[k, 1, 3] = num(a, b - 1, c)
+                adj[k, 1, 4] = num(a, b + 1, c)
+                adj[k, 1, 5] = num(a, b, c - 1)
+                adj[k, 1, 6] = num(a, b, c + 1)
+    return ncube, cube_size, csl, origin, adj
+
+
+def open_box(ncx: int, ncy: int, ncz: int, n: int, length: float):
+    """Like periodic_box but without wrap-around: domain faces have no
+    neighbour, so the X/Y/Z boundary conditions stay visible."""
+    ncube, cube_size, csl, origin, adj = periodic_box(ncx, ncy, ncz, n, length)
+    for k in range(1, ncube):
+        a = int(round(origin[k, 0] / cube_size[k]))
+        b = int(round(origin[k, 1] / cube_size[k]))
+        c = int(round(origin[k, 2] / cube_size[k]))
+        if a == 0: adj[k, 1, 1] = 0
+        if a == ncx - 1: adj[k, 1, 2] = 0
+        if b == 0: adj[k, 1, 3] = 0
+        if b == ncy - 1: adj[k, 1, 4] = 0
+        if c == 0: adj[k, 1, 5] = 0
+        if c == ncz - 1: adj[k, 1, 6] = 0
+    return ncube, cube_size, csl, origin, adj
+
+
+def conservative(rho, u, v, w, p):
+    """(rho, rho u, rho v, rho w, E) with E = p/(K-1) + rho|u|^2/2."""
+    E = p / (GAMMA - 1) + 0.5 * rho * (u * u + v * v + w * w)
+    return np.stack([rho, rho * u, rho * v, rho * w, E], axis=-1)
+
+
+def _grid(case_geom, n):
+    ncube, cube_size, csl, origin, adj = case_geom
+    S = n + 4
+    dx = cube_size / n
+    idx = np.arange(S, dtype=np.float64) - 1.5
+    X = origin[:, 0][:, None, None, None] + idx[None, :, None, None] * dx[:, None, None, None]
+    Y = origin[:, 1][:, None, None, None] + idx[None, None, :, None] * dx[:, None, None, None]
+    Z = origin[:, 2][:, None, None, None] + idx[None, None, None, :] * dx[:, None, None, None]
+    X, Y, Z = np.broadcast_arrays(X, Y, Z)
+    return X, Y, Z
+
+
+def isentropic_vortex(ncx=4, n=16, length=1.0, mach=0.5, strength=5.0, radius=0.1,
+                      dT=1e-3, sub_ratio=200.0, name="vortex") -> Case:
+    """Inviscid isentropic vortex in a periodic box (ncx^3 cubes of n^3 cells).
+
+    Free stream rho0=1.1842 kg/m^3, P0=101300 Pa (the reference's defaults,
+    prm.h:27,37), U0 = mach * c0 along x.  Vortex of strength beta (in units
+    of U0) and core radius `radius` centred in the box:
+    u_theta = A r~ exp((1-r~^2)/2), A = beta U0 / (2 pi), r~ = r/radius;
+    isentropic radial equilibrium gives T = T0 - A^2 exp(1-r~^2) / (2 cp).
+    """
+    ph = Phys(mu_L=0.0, rho0=1.1842, P0=101300.0, mpi_ncube=ncx ** 3)
+    c0 = np.sqrt(GAMMA * ph.P0 / ph.rho0)
+    ph.U0 = ph.Uin = mach * c0
+    geom = periodic_box(ncx, ncx, ncx, n, length)
+    X, Y, Z = _grid(geom, n)
+    xc = yc = 0.5 * length
+    dxr = (X - xc) / radius
+    dyr = (Y - yc) / radius
+    r2 = dxr * dxr + dyr * dyr
+    A = strength * ph.U0 / (2 * np.pi)
+    g = np.exp(0.5 * (1 - r2))
+    u = ph.U0 - A * dyr * g
+    v = A * dxr * g
+    w = np.zeros_like(u)
+    cp = CV * GAMMA
+    T0 = ph.P0 / (ph.rho0 * R_GAS)
+    T = T0 - A * A * np.exp(1 - r2) / (2 * cp)
+    rho = ph.rho0 * (T / T0) ** (1.0 / (GAMMA - 1))
+    p = rho * R_GAS * T
+    U = conservative(rho, u, v, w, p)
+    ncube, cube_size, csl, origin, adj = geom
+    fws = np.full((ncube,) + (n + 4,) * 3, IFLUID, np.int32)
+    return Case(n=n, ncube=ncube, phys=ph, cube_size=cube_size, csl=csl, origin=origin,
+                adj=adj, fws=fws, U=np.ascontiguousarray(U), dT=dT, dTau=dT / sub_ratio,
+                name=name)
+
+
+def taylor_green(ncx=8, n=24, mach=0.1, reynolds=1600.0, dT=1e-4, sub_ratio=200.0,
+                 name="tgv") -> Case:
+    """Viscous Taylor-Green vortex in a periodic 2*pi box.
+
+    u = U0 sin x cos y cos z, v = -U0 cos x sin y cos z, w = 0,
+    p = P0 + rho0 U0^2/16 (cos 2x + cos 2y)(cos 2z + 2), rho = p/(R T0)
+    (isothermal start).  U0 = mach * c0 and the Sutherland reference
+    viscosity mu_L = rho0 U0 L / Re with L = 1 m.  dT and dTau default to the
+    reference's run parameters (main.cpp:57-58).
+    """
+    ph = Phys(rho0=1.1842, P0=101300.0, mpi_ncube=ncx ** 3)
+    c0 = np.sqrt(GAMMA * ph.P0 / ph.rho0)
+    ph.U0 = ph.Uin = mach * c0
+    ph.mu_L = ph.rho0 * ph.U0 * 1.0 / reynolds
+    geom = periodic_box(ncx, ncx, ncx, n, 2 * np.pi)
+    X, Y, Z = _grid(geom, n)
+    U0 = ph.U0
+    u = U0 * np.sin(X) * np.cos(Y) * np.cos(Z)
+    v = -U0 * np.cos(X) * np.sin(Y) * np.cos(Z)
+    w = np.zeros_like(u)
+    p = ph.P0 + ph.rho0 * U0 * U0 / 16.0 * (np.cos(2 * X) + np.cos(2 * Y)) * (np.cos(2 * Z) + 2)
+    T0 = ph.T0
+    rho = p / (R_GAS * T0)
+    U = conservative(rho, u, v, w, p)
+    ncube, cube_size, csl, origin, adj = geom
+    fws = np.full((ncube,) + (n + 4,) * 3, IFLUID, np.int32)
+    return Case(n=n, ncube=ncube, phys=ph, cube_size=cube_size, csl=csl, origin=origin,
+                adj=adj, fws=fws, U=np.ascontiguousarray(U), dT=dT, dTau=dT / sub_ratio,
+                name=name)
+
+
+def random_case(seed=1, ncx=2, ncy=2, ncz=2, n=4, periodic=False, viscous=True,
+                solid_frac=0.08, ghost_frac=0.05, noise=0.05, with_ibm=True,
+                name="random") -> Case:
+    """Small stress case for parity: perturbed uniform flow, random
+    fluid/ghost/solid flags (exercising every reconstruction fallback), open or
+    periodic box (BCs visible when open) and random IBM ghost tables.
+
+    Values stay physical (rho > 0, p > 0) so every branch is well defined.
+    """
+    ph = Phys(mu_L=0.0000185 if viscous else 0.0, rho0=1.1842, U0=38.889, Uin=38.889,
+              P0=101300.0, mpi_ncube=ncx * ncy * ncz)
+    geom = (periodic_box if periodic else open_box)(ncx, ncy, ncz, n, 1.0)
+    ncube, cube_size, csl, origin, adj = geom
+    S = n + 4
+    cnt = ncube * S ** 3
+    r = [splitmix_uniform(seed * 16 + t, cnt).reshape(ncube, S, S, S) for t in range(6)]
+    rho = ph.rho0 * (1 + noise * (r[0] - 0.5))
+    u = ph.U0 * (1 + 2 * noise * (r[1] - 0.5))
+    v = ph.U0 * 2 * noise * (r[2] - 0.5)
+    w = ph.U0 * 2 * noise * (r[3] - 0.5)
+    p = ph.P0 * (1 + noise * 0.1 * (r[4] - 0.5))
+    U = conservative(rho, u, v, w, p)
+    fws = np.full((ncube, S, S, S), IFLUID, np.int32)
+    fws[r[5] < solid_frac] = ISOLID
+    fws[(r[5] >= solid_frac) & (r[5] < solid_frac + ghost_frac)] = IGHOST
+    case = Case(n=n, ncube=ncube, phys=ph, cube_size=cube_size, csl=csl, origin=origin,
+                adj=adj, fws=fws, U=np.ascontiguousarray(U), dT=1e-4, dTau=1e-4 / 200.0,
+                name=name)
+    if with_ibm:
+        case.ibm_minus = random_ibm(seed * 16 + 7, case, count=6 * (ncube - 1))
+        case.ibm_plus = random_ibm(seed * 16 + 9, case, count=4 * (ncube - 1))
+    return case
+
+
+def random_ibm(seed: int, case: Case, count: int):
+    """Random IBM ghost tables (1-based packed).  Ghost cells are the case's
+    IGHOST-flagged interior cells; image-point stencils (i..i+1, j..j+1,
+    k..k+1) lie inside the padded cube.  About a quarter of entries put the
+    ghost inside its own stencil, and some weights exceed 0.9999, so every
+    special branch of BCM_Ghostcell_minus.cpp:192-449 runs.  Weights are
+    rounded to 6 decimals like the reference's IBM files (%f)."""
+    n, S = case.n, case.S
+    ghosts = np.argwhere(case.fws[1:, 2:n + 2, 2:n + 2, 2:n + 2] == IGHOST)
+    r = splitmix_uniform(seed, count * 16).reshape(count, 16)
+    GC = np.zeros(4 * count + 1, np.int32)
+    IP = np.zeros(4 * count + 1, np.int32)
+    W = np.zeros(8 * count + 1)
+    for e in range(count):
+        if len(ghosts):
+            g = ghosts[int(r[e, 0] * len(ghosts)) % len(ghosts)]
+            gc, gi, gj, gk = int(g[0]) + 1, int(g[1]) + 2, int(g[2]) + 2, int(g[3]) + 2
+        else:
+            gc = 1 + int(r[e, 0] * (case.ncube - 1))
+            gi, gj, gk = (2 + int(r[e, t] * n) for t in (1, 2, 3))
+        if r[e, 4] < 0.25:
+            # ghost inside its own stencil at offset (oi, oj, ok)
+            oi, oj, ok = (int(r[e, t] * 2) for t in (5, 6, 7))
+            ic, ii, jj, kk = gc, gi - oi, gj - oj, gk - ok
+        else:
+            ic = 1 + int(r[e, 5] * (case.ncube - 1))
+            ii, jj, kk = (1 + int(r[e, t] * (S - 3)) for t in (6, 7, 8))
+        w = r[e, 8:16] + 1e-3
+        if r[e, 9] < 0.1:
+            w[int(r[e, 10] * 8)] += 1e4  # one dominant weight (> 0.9999 after normalising)
+        w = np.round(w / w.sum(), 6)
+        GC[4 * e + 1:4 * e + 5] = (gc, gi, gj, gk)
+        IP[4 * e + 1:4 * e + 5] = (ic, ii, jj, kk)
+        W[8 * e + 1:8 * e + 9] = w
+    return W, GC, IP
