@@ -1,0 +1,246 @@
+"""Python mirror of the reference's hot-path interface, on the GPU library.
+
+Two layers, matching ``include/bcm_gb300.h``:
+
+* Reference-named functions (``BCM_Flux_XYZ_Viscous_Runge_kutta``,
+  ``BCM_X_boundary_condition``, ... ``BCM_Interface``) that take numpy arrays
+  in the reference layout and update them in place, with the reference's
+  argument order and meaning (``main.h:224-513``).  The reference's
+  compile-time ``Resolution.h``/``prm.h`` values are set with
+  :func:`set_reference_config`.
+* :class:`CaseContext`, the device-resident path: state stays in HBM and
+  whole dual-time steps run per call.
+
+Every call goes to the CUDA library; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import BcmgError, check, lib
+
+PRECISION_FP64 = 0
+PRECISION_SPLIT = 1
+
+
+def _dp(a):
+    if a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise BcmgError("expected a C-contiguous float64 array")
+    return a
+
+
+def _ip(a):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    return a if a.size else np.zeros(1, np.int32)
+
+
+def _raise_if_failed(name):
+    err = _lib.last_error()
+    if err:
+        raise BcmgError(f"{name}: {err}")
+
+
+# ---------------------------------------------------------------------------
+# Reference compile-time configuration
+# ---------------------------------------------------------------------------
+def set_reference_config(ncube_x=16, mpi_ncube=1150, mu_L=0.0000185, rho0=1.1842, U0=38.889,
+                         Uin=38.889, P0=101300.0):
+    """Resolution.h / prm.h values the reference-named functions use."""
+    cfg = _lib.RefConfig(ncube_x, mpi_ncube, mu_L, rho0, U0, Uin, P0)
+    check(lib().bcmg_set_reference_config(C.byref(cfg)))
+
+
+def reference_config_for(case):
+    ph = case.phys
+    set_reference_config(case.n, ph.mpi_ncube, ph.mu_L, ph.rho0, ph.U0, ph.Uin, ph.P0)
+
+
+# ---------------------------------------------------------------------------
+# Reference-named entry points (in place on host arrays)
+# ---------------------------------------------------------------------------
+def BCM_Flux_XYZ_Viscous_Runge_kutta(myid, ncube, RK, deltaT, deltaTau, e, FWS, csl, cube_size,
+                                     U1_, U1, U1q, U1p1, U1p2, Rku1, Residual1, er):
+    lib().BCM_Flux_XYZ_Viscous_Runge_kutta(
+        int(myid), int(ncube), int(RK), float(deltaT), float(deltaTau), float(e), _ip(FWS),
+        _ip(csl), _dp(cube_size), _dp(U1_), _dp(U1), _dp(U1q), _dp(U1p1), _dp(U1p2), _dp(Rku1),
+        _dp(Residual1), _dp(er))
+    _raise_if_failed("BCM_Flux_XYZ_Viscous_Runge_kutta")
+
+
+def _one_based(lst):
+    return np.concatenate([np.zeros(1, np.int32), np.asarray(lst, np.int32)])
+
+
+def BCM_X_boundary_condition(myid, nXbc_l, nXbc_u, Xbc_l, Xbc_u, U1_):
+    lib().BCM_X_boundary_condition(int(myid), int(nXbc_l), int(nXbc_u), _ip(Xbc_l),
+                                   _ip(Xbc_u), _dp(U1_))
+    _raise_if_failed("BCM_X_boundary_condition")
+
+
+def BCM_Y_boundary_condition(nYbc_l, nYbc_u, Ybc_l, Ybc_u, U1_):
+    lib().BCM_Y_boundary_condition(int(nYbc_l), int(nYbc_u), _ip(Ybc_l), _ip(Ybc_u), _dp(U1_))
+    _raise_if_failed("BCM_Y_boundary_condition")
+
+
+def BCM_Z_boundary_condition(nZbc_l, nZbc_u, Zbc_l, Zbc_u, U1_):
+    lib().BCM_Z_boundary_condition(int(nZbc_l), int(nZbc_u), _ip(Zbc_l), _ip(Zbc_u), _dp(U1_))
+    _raise_if_failed("BCM_Z_boundary_condition")
+
+
+def BCM_Ghostcell_minus(myid, NNBC, weight, GCindex, IPsur, FWS, U1_):
+    n = C.c_int(int(NNBC))
+    lib().BCM_Ghostcell_minus(int(myid), C.byref(n), _dp(weight), _ip(GCindex), _ip(IPsur),
+                              _ip(FWS), _dp(U1_))
+    _raise_if_failed("BCM_Ghostcell_minus")
+
+
+def BCM_Ghostcell_plus(myid, NNBC, weight, GCindex, IPsur, FWS, U1_):
+    n = C.c_int(int(NNBC))
+    lib().BCM_Ghostcell_plus(int(myid), C.byref(n), _dp(weight), _ip(GCindex), _ip(IPsur),
+                             _ip(FWS), _dp(U1_))
+    _raise_if_failed("BCM_Ghostcell_plus")
+
+
+def interface_lists(case):
+    """Same-level lists adjX_eq/adjY_eq/adjZ_eq (1-based) as
+    BCM_Interface_table.cpp:96-208 builds them."""
+    adj, csl = case.adj, case.csl
+    out = []
+    for ax in range(3):
+        d = 2 + 2 * ax
+        lst = []
+        for c in range(1, case.ncube):
+            slots = adj[c, 1:5, d]
+            if (slots > 0).any() and csl[c] == csl[slots.max()]:
+                lst.append(c)
+        out.append(_one_based(lst))
+    return out
+
+
+def BCM_Interface_for_case(case, U1_):
+    """BCM_Interface with single-process (empty exchange) arguments, like the
+    reference's call at main.cpp:1177-1204 on one rank."""
+    L = lib()
+    X, Y, Z = interface_lists(case)
+    z = np.zeros(4, np.int32)
+    d = np.zeros(4)
+    zp = z.ctypes.data_as(C.c_void_p)
+    dd = d.ctypes.data_as(C.c_void_p)
+    adj = np.ascontiguousarray(case.adj, np.int32)
+    csl = np.ascontiguousarray(case.csl, np.int32)
+    U = _dp(U1_)
+    args = [C.c_int(0), C.c_int(case.ncube), C.c_int(1), C.c_int(0), C.c_int(0), C.c_int(0),
+            C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(len(X) - 1), C.c_int(len(Y) - 1),
+            C.c_int(len(Z) - 1)] + [C.c_int(0)] * 12 + [zp] * 15 + [dd] * 4 + [zp] * 4 + \
+           [dd] * 4 + [zp] * 4 + [dd] * 4 + [zp] * 8 + \
+           [csl.ctypes.data_as(C.c_void_p), adj.ctypes.data_as(C.c_void_p),
+            X.ctypes.data_as(C.c_void_p), Y.ctypes.data_as(C.c_void_p),
+            Z.ctypes.data_as(C.c_void_p)] + [zp] * 12 + [U.ctypes.data_as(C.c_void_p)]
+    assert len(args) == 85
+    L.BCM_Interface(*args)
+    _raise_if_failed("BCM_Interface")
+
+
+# ---------------------------------------------------------------------------
+# Device-resident context
+# ---------------------------------------------------------------------------
+class CaseContext:
+    """A case resident in HBM (``bcmg_case_*``)."""
+
+    def __init__(self, case, precision=PRECISION_FP64):
+        self.case = case
+        ph = case.phys
+        self._keep = []
+
+        def arr(a, dt):
+            a = np.ascontiguousarray(a, dtype=dt)
+            if a.size == 0:
+                a = np.zeros(1, dt)
+            self._keep.append(a)
+            return a.ctypes.data
+
+        xl, xu, yl, yu, zl, zu = case.bc_lists()
+        d = _lib.CaseDesc()
+        d.n, d.ncube, d.mpi_ncube = case.n, case.ncube, ph.mpi_ncube
+        d.mu_L, d.rho0, d.U0, d.Uin, d.P0 = ph.mu_L, ph.rho0, ph.U0, ph.Uin, ph.P0
+        d.deltaT, d.deltaTau, d.e = case.dT, case.dTau, case.e
+        d.precision = precision
+        d.cube_size = arr(case.cube_size, np.float64)
+        d.csl = arr(case.csl, np.int32)
+        d.adj_number = arr(case.adj, np.int32)
+        d.FWS = arr(case.fws, np.int32)
+        d.nxl, d.nxu, d.nyl, d.nyu, d.nzl, d.nzu = map(len, (xl, xu, yl, yu, zl, zu))
+        d.xl, d.xu, d.yl, d.yu, d.zl, d.zu = (arr(a, np.int32) for a in (xl, xu, yl, yu, zl, zu))
+        if case.ibm_minus is not None:
+            W, G, I = case.ibm_minus
+            d.nminus = (len(G) - 1) // 4
+            d.w_minus, d.gc_minus, d.ip_minus = arr(W, np.float64), arr(G, np.int32), arr(I, np.int32)
+        if case.ibm_plus is not None:
+            W, G, I = case.ibm_plus
+            d.nplus = (len(G) - 1) // 4
+            d.w_plus, d.gc_plus, d.ip_plus = arr(W, np.float64), arr(G, np.int32), arr(I, np.int32)
+        h = C.c_void_p()
+        check(lib().bcmg_case_create(C.byref(d), C.byref(h)))
+        self._keep.clear()
+        self.h = h
+        self.shape = case.U.shape
+        self.emax = np.zeros(6)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().bcmg_case_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, U1_=None, U1=None, U1q=None):
+        ptr = lambda a: None if a is None else _dp(np.ascontiguousarray(a)).ctypes.data
+        keep = [a for a in (U1_, U1, U1q)]
+        check(lib().bcmg_case_set_state(self.h, ptr(U1_), ptr(U1), ptr(U1q)))
+        del keep
+
+    def get_state(self):
+        out = [np.empty(self.shape) for _ in range(3)]
+        check(lib().bcmg_case_get_state(self.h, *(a.ctypes.data for a in out)))
+        return out
+
+    def get_scratch(self):
+        out = [np.empty(self.shape) for _ in range(4)]
+        check(lib().bcmg_case_get_scratch(self.h, *(a.ctypes.data for a in out)))
+        return out  # U1p1, U1p2, Rku1, Residual1
+
+    def stage(self, RK):
+        check(lib().bcmg_case_stage(self.h, int(RK)))
+
+    def advance(self, steps, subiters, use_graph=True):
+        er = np.zeros(8)
+        check(lib().bcmg_case_advance(self.h, int(steps), int(subiters), int(bool(use_graph)),
+                                      er.ctypes.data, self.emax.ctypes.data))
+        return er
+
+    def sync(self):
+        check(lib().bcmg_case_sync(self.h))
+
+    def launch_count(self):
+        return int(lib().bcmg_case_launch_count(self.h))
+
+    def time_flux(self, reps=5):
+        ms = C.c_double()
+        check(lib().bcmg_case_time_flux(self.h, int(reps), C.byref(ms)))
+        return ms.value
+
+    def set_profiling(self, on=True):
+        check(lib().bcmg_case_set_profiling(self.h, int(bool(on))))
+
+    def profile(self):
+        ms = C.c_double()
+        n = C.c_longlong()
+        check(lib().bcmg_case_profile(self.h, C.byref(ms), C.byref(n)))
+        return ms.value, n.value

@@ -1,0 +1,987 @@
+// C ABI: drop-in twins of the reference routines and the device-resident
+// case context.  See include/bcm_gb300.h for the contract of every entry
+// point.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/bcm_gb300.h"
+#include "bcm_kernels.h"
+#include "bcm_tables.h"
+
+using namespace bcmg;
+
+namespace {
+
+thread_local std::string g_err;
+thread_local bool g_has_err = false;
+
+void set_err(const std::string &s) {
+  g_err = s;
+  g_has_err = true;
+}
+void clear_err() { g_has_err = false; }
+
+#define CK(expr)                                                                     \
+  do {                                                                               \
+    cudaError_t e__ = (expr);                                                        \
+    if (e__ != cudaSuccess) {                                                        \
+      set_err(std::string(#expr) + ": " + cudaGetErrorString(e__));                  \
+      return BCMG_ERR_CUDA;                                                          \
+    }                                                                                \
+  } while (0)
+
+template <typename T>
+cudaError_t dalloc(T **p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  return cudaMalloc((void **)p, sizeof(T) * count);
+}
+
+template <typename T>
+void dfree(T *&p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+__global__ void k_time_shift(int n, long long total, const double *U1_, double *U1,
+                             double *U1q) {
+  // main.cpp:1292-1315: U1q <- U1, U1 <- U1_ on interior cells.
+  const int S = n + 4;
+  const long long n3 = (long long)n * n * n;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int c = 1 + (int)(t / n3);
+    const int r = (int)(t % n3);
+    const size_t o = 5 * cell_index(S, c, 2 + r / (n * n), 2 + (r / n) % n, 2 + r % n);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      U1q[o + v] = U1[o + v];
+      U1[o + v] = U1_[o + v];
+    }
+  }
+}
+
+__global__ void k_emax(double *er, double *emax) {
+  // main.cpp:1249-1259: E_k = max(E_k, er_k); er_k /= E_k.
+  const int v = threadIdx.x + 1;
+  if (v <= 5) {
+    double E = emax[v] > er[v] ? emax[v] : er[v];
+    emax[v] = E;
+    er[v] = er[v] / E;
+  }
+}
+
+struct Ibm {
+  int nbc = 0;
+  double *w = nullptr;
+  int *gc = nullptr, *ip = nullptr, *order = nullptr;
+  std::vector<int> level_off;
+  void release() {
+    dfree(w);
+    dfree(gc);
+    dfree(ip);
+    dfree(order);
+    nbc = 0;
+    level_off.clear();
+  }
+};
+
+// Upload one IBM table (1-based packed) and its dependency levels.
+int ibm_upload(Ibm &t, int nbc, const double *w, const int *gc, const int *ip, int n, int ncube,
+               cudaStream_t s) {
+  t.release();
+  if (nbc <= 0) return BCMG_OK;
+  std::vector<int> order;
+  std::string err;
+  if (!build_ibm_levels(nbc, gc, ip, n, ncube, order, t.level_off, err)) {
+    set_err(err);
+    return BCMG_ERR_ARG;
+  }
+  t.nbc = nbc;
+  CK(dalloc(&t.w, (size_t)8 * nbc + 1));
+  CK(dalloc(&t.gc, (size_t)4 * nbc + 1));
+  CK(dalloc(&t.ip, (size_t)4 * nbc + 1));
+  CK(dalloc(&t.order, (size_t)nbc));
+  CK(cudaMemcpyAsync(t.w, w, sizeof(double) * (8 * (size_t)nbc + 1), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(t.gc, gc, sizeof(int) * (4 * (size_t)nbc + 1), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(t.ip, ip, sizeof(int) * (4 * (size_t)nbc + 1), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(t.order, order.data(), sizeof(int) * nbc, cudaMemcpyHostToDevice, s));
+  CK(cudaStreamSynchronize(s));
+  return BCMG_OK;
+}
+
+int ibm_run(const Ibm &t, int n, double rho0, double P0, double *U, cudaStream_t s,
+            long long *launches) {
+  for (size_t l = 1; l < t.level_off.size(); ++l) {
+    GhostArgs g;
+    g.n = n;
+    g.rho0 = rho0;
+    g.P0 = P0;
+    g.entries = t.order + t.level_off[l - 1];
+    g.weight = t.w;
+    g.GCindex = t.gc;
+    g.IPsur = t.ip;
+    g.U1_ = U;
+    CK(launch_ghost(g, t.level_off[l] - t.level_off[l - 1], s));
+    if (launches) ++*launches;
+  }
+  return BCMG_OK;
+}
+
+bool valid_n(int n) { return n >= 4 && n % 4 == 0 && n <= 256; }
+
+}  // namespace
+
+// ===========================================================================
+// Device-resident case context
+// ===========================================================================
+struct bcmg_case {
+  Phys ph{};
+  int ncube = 0, S = 0;
+  double dT = 0, dTau = 0, e = 0;
+  int precision = 0;
+  size_t ncell = 0;
+  cudaStream_t stream = nullptr;
+  double *U1_ = nullptr, *U1 = nullptr, *U1q = nullptr, *U1p1 = nullptr, *U1p2 = nullptr,
+         *Rku1 = nullptr, *Residual1 = nullptr;
+  int *FWS = nullptr;
+  double *cube_size = nullptr;
+  int *task_off = nullptr;
+  FaceTask *tasks = nullptr;
+  int *bc_cubes = nullptr, *bc_masks = nullptr;
+  int nbc = 0;
+  Ibm ibm;  // minus entries then plus entries, one combined schedule
+  double *partials = nullptr;
+  int nparts = 0;
+  double *er = nullptr, *emax = nullptr;  // device [8], [6]
+  cudaGraphExec_t graph = nullptr;
+  int graph_subiters = -1;
+  long long launches = 0;
+  bool profile = false;
+  std::vector<cudaEvent_t> ev;
+  size_t ev_used = 0;
+  double flux_ms = 0;
+  long long flux_launches = 0;
+
+  void release() {
+    if (graph) cudaGraphExecDestroy(graph);
+    graph = nullptr;
+    for (auto x : ev) cudaEventDestroy(x);
+    ev.clear();
+    dfree(U1_); dfree(U1); dfree(U1q); dfree(U1p1); dfree(U1p2); dfree(Rku1); dfree(Residual1);
+    dfree(FWS); dfree(cube_size); dfree(task_off); dfree(tasks); dfree(bc_cubes);
+    dfree(bc_masks); dfree(partials); dfree(er); dfree(emax);
+    ibm.release();
+    if (stream) cudaStreamDestroy(stream);
+    stream = nullptr;
+  }
+};
+
+namespace {
+
+int case_flux(bcmg_case *c) {
+  FluxArgs a;
+  a.ph = c->ph;
+  a.cube0 = 1;
+  a.dT = c->dT;
+  a.dTau = c->dTau;
+  a.e = c->e;
+  a.FWS = c->FWS;
+  a.cube_size = c->cube_size;
+  a.U1_ = c->U1_;
+  a.U1 = c->U1;
+  a.U1q = c->U1q;
+  a.Rku1 = c->Rku1;
+  a.Residual1 = c->Residual1;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (c->profile) {
+    while (c->ev.size() < c->ev_used + 2) {
+      cudaEvent_t x;
+      CK(cudaEventCreate(&x));
+      c->ev.push_back(x);
+    }
+    e0 = c->ev[c->ev_used];
+    e1 = c->ev[c->ev_used + 1];
+    c->ev_used += 2;
+    CK(cudaEventRecord(e0, c->stream));
+  }
+  CK(launch_flux_fp64(a, c->ncube - 1, c->stream));
+  if (c->profile) CK(cudaEventRecord(e1, c->stream));
+  ++c->launches;
+  return BCMG_OK;
+}
+
+int case_interface(bcmg_case *c) {
+  InterfaceArgs ia;
+  ia.n = c->ph.n;
+  ia.dst_cubes = nullptr;
+  ia.task_off = c->task_off;
+  ia.tasks = c->tasks;
+  ia.edge_cubes = c->ncube;
+  ia.U1_ = c->U1_;
+  CK(launch_interface(ia, c->ncube, c->stream));
+  ++c->launches;
+  return BCMG_OK;
+}
+
+int case_stage(bcmg_case *c, int RK) {
+  int r;
+  if (c->nbc > 0) {
+    BcArgs b;
+    b.n = c->ph.n;
+    b.Uin = c->ph.Uin;
+    b.cubes = c->bc_cubes;
+    b.masks = c->bc_masks;
+    b.axes = 7;
+    b.U1_ = c->U1_;
+    CK(launch_bc(b, c->nbc, c->stream));
+    ++c->launches;
+  }
+  if ((r = ibm_run(c->ibm, c->ph.n, c->ph.rho0, c->ph.P0, c->U1_, c->stream, &c->launches)))
+    return r;
+  if ((r = case_interface(c))) return r;
+  if ((r = case_flux(c))) return r;
+  RkArgs k;
+  k.ph = c->ph;
+  k.ncube = c->ncube;
+  k.RK = RK;
+  k.FWS = c->FWS;
+  k.U1_ = c->U1_;
+  k.U1p1 = c->U1p1;
+  k.U1p2 = c->U1p2;
+  k.Rku1 = c->Rku1;
+  k.Residual1 = c->Residual1;
+  k.partials = c->partials;
+  int nb = 0;
+  CK(launch_rk(k, &nb, c->stream));
+  ++c->launches;
+  if (RK == 3) {
+    CK(launch_norms(c->ph, c->partials, nb, c->er, c->stream));
+    ++c->launches;
+  }
+  return case_interface(c);
+}
+
+int case_step(bcmg_case *c, int subiters) {
+  int r;
+  for (int it = 0; it < subiters; ++it) {
+    for (int RK = 1; RK <= 3; ++RK)
+      if ((r = case_stage(c, RK))) return r;
+    k_emax<<<1, 32, 0, c->stream>>>(c->er, c->emax);
+    CK(cudaGetLastError());
+    ++c->launches;
+  }
+  const long long total = (long long)(c->ncube - 1) * c->ph.n * c->ph.n * c->ph.n;
+  if (total > 0) {
+    int blocks = (int)std::min<long long>((total + 255) / 256, 152 * 8);
+    k_time_shift<<<blocks, 256, 0, c->stream>>>(c->ph.n, total, c->U1_, c->U1, c->U1q);
+    CK(cudaGetLastError());
+    ++c->launches;
+  }
+  return BCMG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *bcmg_last_error(void) { return g_has_err ? g_err.c_str() : nullptr; }
+const char *bcmg_version(void) { return "bcm_gb300 0.1 (sm_103a)"; }
+
+int bcmg_case_create(const bcmg_case_desc *d, bcmg_case **out) {
+  clear_err();
+  if (!d || !out) {
+    set_err("null argument");
+    return BCMG_ERR_ARG;
+  }
+  *out = nullptr;
+  if (!valid_n(d->n)) {
+    set_err("n must be a multiple of 4 in [4, 256]");
+    return BCMG_ERR_ARG;
+  }
+  if (d->ncube < 2 || !d->cube_size || !d->csl || !d->adj_number || !d->FWS) {
+    set_err("ncube < 2 or missing geometry arrays");
+    return BCMG_ERR_ARG;
+  }
+  if (d->precision != BCMG_PRECISION_FP64) {
+    set_err("unknown or unavailable precision");
+    return BCMG_ERR_ARG;
+  }
+  for (int i = 1; i < d->ncube; ++i)
+    if (!(d->cube_size[i] > 0)) {
+      set_err("cube_size must be positive for cubes 1..ncube-1");
+      return BCMG_ERR_ARG;
+    }
+  bcmg_case *c = new bcmg_case();
+  auto fail = [&](int code) {
+    c->release();
+    delete c;
+    return code;
+  };
+  c->ph.n = d->n;
+  c->ph.mpi_ncube = d->mpi_ncube;
+  c->ph.mu_L = d->mu_L;
+  c->ph.rho0 = d->rho0;
+  c->ph.U0 = d->U0;
+  c->ph.Uin = d->Uin;
+  c->ph.P0 = d->P0;
+  c->ncube = d->ncube;
+  c->S = d->n + 4;
+  c->dT = d->deltaT;
+  c->dTau = d->deltaTau;
+  c->e = d->e;
+  c->precision = d->precision;
+  c->ncell = (size_t)d->ncube * c->S * c->S * c->S;
+  std::vector<int> off;
+  std::vector<FaceTask> tasks;
+  std::string err;
+  if (!build_interface_tasks(d->ncube, d->adj_number, d->csl, off, tasks, err)) {
+    set_err(err);
+    return fail(BCMG_ERR_ARG);
+  }
+  const int *lists[6] = {d->xl, d->xu, d->yl, d->yu, d->zl, d->zu};
+  const int counts[6] = {d->nxl, d->nxu, d->nyl, d->nyu, d->nzl, d->nzu};
+  for (int l = 0; l < 6; ++l)
+    if (counts[l] > 0 && !lists[l]) {
+      set_err("boundary list pointer missing");
+      return fail(BCMG_ERR_ARG);
+    }
+  std::vector<int> bcc, bcm;
+  if (!build_bc_entries(d->ncube, lists, counts, bcc, bcm, err)) {
+    set_err(err);
+    return fail(BCMG_ERR_ARG);
+  }
+  auto ck = [&](cudaError_t e, const char *what) {
+    if (e != cudaSuccess) set_err(std::string(what) + ": " + cudaGetErrorString(e));
+    return e == cudaSuccess;
+  };
+  if (!ck(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream"))
+    return fail(BCMG_ERR_CUDA);
+  const size_t nd = c->ncell * 5;
+  bool ok = ck(dalloc(&c->U1_, nd), "alloc") && ck(dalloc(&c->U1, nd), "alloc") &&
+            ck(dalloc(&c->U1q, nd), "alloc") && ck(dalloc(&c->U1p1, nd), "alloc") &&
+            ck(dalloc(&c->U1p2, nd), "alloc") && ck(dalloc(&c->Rku1, nd), "alloc") &&
+            ck(dalloc(&c->Residual1, nd), "alloc") && ck(dalloc(&c->FWS, c->ncell), "alloc") &&
+            ck(dalloc(&c->cube_size, (size_t)d->ncube), "alloc") &&
+            ck(dalloc(&c->task_off, off.size()), "alloc") &&
+            ck(dalloc(&c->tasks, tasks.size()), "alloc") &&
+            ck(dalloc(&c->bc_cubes, bcc.size()), "alloc") &&
+            ck(dalloc(&c->bc_masks, bcm.size()), "alloc") &&
+            ck(dalloc(&c->er, 8), "alloc") && ck(dalloc(&c->emax, 6), "alloc");
+  if (!ok) return fail(BCMG_ERR_CUDA);
+  RkArgs probe{};
+  probe.ph = c->ph;
+  probe.ncube = c->ncube;
+  c->nparts = rk_partial_blocks(probe);
+  if (!ck(dalloc(&c->partials, (size_t)c->nparts * 7), "alloc")) return fail(BCMG_ERR_CUDA);
+  cudaStream_t s = c->stream;
+  ok = ck(cudaMemsetAsync(c->U1_, 0, nd * 8, s), "memset") &&
+       ck(cudaMemsetAsync(c->U1, 0, nd * 8, s), "memset") &&
+       ck(cudaMemsetAsync(c->U1q, 0, nd * 8, s), "memset") &&
+       ck(cudaMemsetAsync(c->U1p1, 0, nd * 8, s), "memset") &&
+       ck(cudaMemsetAsync(c->U1p2, 0, nd * 8, s), "memset") &&
+       ck(cudaMemsetAsync(c->Rku1, 0, nd * 8, s), "memset") &&
+       ck(cudaMemsetAsync(c->Residual1, 0, nd * 8, s), "memset") &&
+       ck(cudaMemsetAsync(c->er, 0, 8 * 8, s), "memset") &&
+       ck(cudaMemsetAsync(c->emax, 0, 6 * 8, s), "memset") &&
+       ck(cudaMemcpyAsync(c->FWS, d->FWS, c->ncell * sizeof(int), cudaMemcpyHostToDevice, s),
+          "copy") &&
+       ck(cudaMemcpyAsync(c->cube_size, d->cube_size, sizeof(double) * d->ncube,
+                          cudaMemcpyHostToDevice, s), "copy") &&
+       ck(cudaMemcpyAsync(c->task_off, off.data(), sizeof(int) * off.size(),
+                          cudaMemcpyHostToDevice, s), "copy") &&
+       (tasks.empty() || ck(cudaMemcpyAsync(c->tasks, tasks.data(), sizeof(FaceTask) * tasks.size(),
+                                            cudaMemcpyHostToDevice, s), "copy")) &&
+       (bcc.empty() || (ck(cudaMemcpyAsync(c->bc_cubes, bcc.data(), sizeof(int) * bcc.size(),
+                                           cudaMemcpyHostToDevice, s), "copy") &&
+                        ck(cudaMemcpyAsync(c->bc_masks, bcm.data(), sizeof(int) * bcm.size(),
+                                           cudaMemcpyHostToDevice, s), "copy"))) &&
+       ck(cudaStreamSynchronize(s), "sync");
+  if (!ok) return fail(BCMG_ERR_CUDA);
+  c->nbc = (int)bcc.size();
+  // Combined IBM table: minus entries 1..nm then plus entries nm+1..nm+np
+  // (main.cpp:1168-1174 applies minus before plus).
+  const int nm = std::max(0, d->nminus), np = std::max(0, d->nplus);
+  if (nm + np > 0) {
+    if ((nm && (!d->w_minus || !d->gc_minus || !d->ip_minus)) ||
+        (np && (!d->w_plus || !d->gc_plus || !d->ip_plus))) {
+      set_err("IBM table pointer missing");
+      return fail(BCMG_ERR_ARG);
+    }
+    std::vector<double> w(8 * (size_t)(nm + np) + 1, 0.0);
+    std::vector<int> gc(4 * (size_t)(nm + np) + 1, 0), ip(4 * (size_t)(nm + np) + 1, 0);
+    if (nm) {
+      std::copy(d->w_minus + 1, d->w_minus + 1 + 8 * (size_t)nm, w.begin() + 1);
+      std::copy(d->gc_minus + 1, d->gc_minus + 1 + 4 * (size_t)nm, gc.begin() + 1);
+      std::copy(d->ip_minus + 1, d->ip_minus + 1 + 4 * (size_t)nm, ip.begin() + 1);
+    }
+    if (np) {
+      std::copy(d->w_plus + 1, d->w_plus + 1 + 8 * (size_t)np, w.begin() + 1 + 8 * (size_t)nm);
+      std::copy(d->gc_plus + 1, d->gc_plus + 1 + 4 * (size_t)np, gc.begin() + 1 + 4 * (size_t)nm);
+      std::copy(d->ip_plus + 1, d->ip_plus + 1 + 4 * (size_t)np, ip.begin() + 1 + 4 * (size_t)nm);
+    }
+    int r = ibm_upload(c->ibm, nm + np, w.data(), gc.data(), ip.data(), d->n, d->ncube, s);
+    if (r) return fail(r);
+  }
+  *out = c;
+  return BCMG_OK;
+}
+
+void bcmg_case_destroy(bcmg_case *c) {
+  if (!c) return;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  c->release();
+  delete c;
+}
+
+int bcmg_case_set_state(bcmg_case *c, const double *U1_, const double *U1, const double *U1q) {
+  clear_err();
+  if (!c) { set_err("null context"); return BCMG_ERR_ARG; }
+  const size_t b = c->ncell * 5 * sizeof(double);
+  if (U1_) CK(cudaMemcpyAsync(c->U1_, U1_, b, cudaMemcpyHostToDevice, c->stream));
+  if (U1) CK(cudaMemcpyAsync(c->U1, U1, b, cudaMemcpyHostToDevice, c->stream));
+  if (U1q) CK(cudaMemcpyAsync(c->U1q, U1q, b, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return BCMG_OK;
+}
+
+int bcmg_case_get_state(bcmg_case *c, double *U1_, double *U1, double *U1q) {
+  clear_err();
+  if (!c) { set_err("null context"); return BCMG_ERR_ARG; }
+  const size_t b = c->ncell * 5 * sizeof(double);
+  if (U1_) CK(cudaMemcpyAsync(U1_, c->U1_, b, cudaMemcpyDeviceToHost, c->stream));
+  if (U1) CK(cudaMemcpyAsync(U1, c->U1, b, cudaMemcpyDeviceToHost, c->stream));
+  if (U1q) CK(cudaMemcpyAsync(U1q, c->U1q, b, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return BCMG_OK;
+}
+
+int bcmg_case_get_scratch(bcmg_case *c, double *U1p1, double *U1p2, double *Rku1,
+                          double *Residual1) {
+  clear_err();
+  if (!c) { set_err("null context"); return BCMG_ERR_ARG; }
+  const size_t b = c->ncell * 5 * sizeof(double);
+  if (U1p1) CK(cudaMemcpyAsync(U1p1, c->U1p1, b, cudaMemcpyDeviceToHost, c->stream));
+  if (U1p2) CK(cudaMemcpyAsync(U1p2, c->U1p2, b, cudaMemcpyDeviceToHost, c->stream));
+  if (Rku1) CK(cudaMemcpyAsync(Rku1, c->Rku1, b, cudaMemcpyDeviceToHost, c->stream));
+  if (Residual1)
+    CK(cudaMemcpyAsync(Residual1, c->Residual1, b, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return BCMG_OK;
+}
+
+int bcmg_case_stage(bcmg_case *c, int RK) {
+  clear_err();
+  if (!c || RK < 1 || RK > 3) { set_err("bad context or RK"); return BCMG_ERR_ARG; }
+  c->launches = 0;
+  int r = case_stage(c, RK);
+  if (r) return r;
+  CK(cudaStreamSynchronize(c->stream));
+  return BCMG_OK;
+}
+
+int bcmg_case_advance(bcmg_case *c, int steps, int subiters, int use_graph, double *er,
+                      double *emax) {
+  clear_err();
+  if (!c || steps < 0 || subiters < 1) { set_err("bad arguments"); return BCMG_ERR_ARG; }
+  if (emax) CK(cudaMemcpyAsync(c->emax, emax, 6 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  c->launches = 0;
+  c->ev_used = 0;
+  if (use_graph && !c->profile) {
+    if (!c->graph || c->graph_subiters != subiters) {
+      if (c->graph) cudaGraphExecDestroy(c->graph);
+      c->graph = nullptr;
+      cudaGraph_t g;
+      CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      long long saved = c->launches;
+      int r = case_step(c, subiters);
+      cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+      if (r) return r;
+      if (ce != cudaSuccess) { set_err(cudaGetErrorString(ce)); return BCMG_ERR_CUDA; }
+      ce = cudaGraphInstantiate(&c->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (ce != cudaSuccess) { set_err(cudaGetErrorString(ce)); return BCMG_ERR_CUDA; }
+      c->graph_subiters = subiters;
+      c->launches = saved;
+    }
+    long long per = 0;
+    {
+      // kernel nodes per step, counted like case_step
+      int L = (int)(c->ibm.level_off.size() > 0 ? c->ibm.level_off.size() - 1 : 0);
+      long long stage = (c->nbc > 0) + L + 1 + 1 + 1 + 1;
+      per = subiters * (3 * stage + 1 + 1) + 1;
+    }
+    for (int s = 0; s < steps; ++s) CK(cudaGraphLaunch(c->graph, c->stream));
+    c->launches = per * steps;
+  } else {
+    for (int s = 0; s < steps; ++s) {
+      int r = case_step(c, subiters);
+      if (r) return r;
+    }
+  }
+  if (er) CK(cudaMemcpyAsync(er, c->er, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (emax) CK(cudaMemcpyAsync(emax, c->emax, 6 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (c->profile) {
+    for (size_t i = 0; i + 1 < c->ev_used; i += 2) {
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, c->ev[i], c->ev[i + 1]));
+      c->flux_ms += ms;
+      ++c->flux_launches;
+    }
+  }
+  return BCMG_OK;
+}
+
+int bcmg_case_sync(bcmg_case *c) {
+  clear_err();
+  if (!c) { set_err("null context"); return BCMG_ERR_ARG; }
+  CK(cudaStreamSynchronize(c->stream));
+  return BCMG_OK;
+}
+
+int bcmg_case_device_state(bcmg_case *c, double **U1_, double **U1, double **U1q) {
+  clear_err();
+  if (!c) { set_err("null context"); return BCMG_ERR_ARG; }
+  if (U1_) *U1_ = c->U1_;
+  if (U1) *U1 = c->U1;
+  if (U1q) *U1q = c->U1q;
+  return BCMG_OK;
+}
+
+long long bcmg_case_launch_count(const bcmg_case *c) { return c ? c->launches : 0; }
+
+int bcmg_case_time_flux(bcmg_case *c, int reps, double *ms) {
+  clear_err();
+  if (!c || reps < 1 || !ms) { set_err("bad arguments"); return BCMG_ERR_ARG; }
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  bool prof = c->profile;
+  c->profile = false;
+  int r = case_flux(c);  // warm-up
+  if (!r) {
+    cudaEventRecord(a, c->stream);
+    for (int i = 0; i < reps && !r; ++i) r = case_flux(c);
+    cudaEventRecord(b, c->stream);
+  }
+  c->profile = prof;
+  if (r) { cudaEventDestroy(a); cudaEventDestroy(b); return r; }
+  CK(cudaEventSynchronize(b));
+  float t = 0;
+  CK(cudaEventElapsedTime(&t, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *ms = t / reps;
+  return BCMG_OK;
+}
+
+// Per-launch timing of the flux kernel inside bcmg_case_advance (events on
+// the context's stream around every flux launch; graphs are not used while
+// profiling is on).  Totals accumulate until reset.
+int bcmg_case_set_profiling(bcmg_case *c, int on) {
+  clear_err();
+  if (!c) { set_err("null context"); return BCMG_ERR_ARG; }
+  c->profile = on != 0;
+  c->flux_ms = 0;
+  c->flux_launches = 0;
+  return BCMG_OK;
+}
+int bcmg_case_profile(const bcmg_case *c, double *flux_ms_total, long long *flux_launches) {
+  if (!c) return BCMG_ERR_ARG;
+  if (flux_ms_total) *flux_ms_total = c->flux_ms;
+  if (flux_launches) *flux_launches = c->flux_launches;
+  return BCMG_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Drop-in twins of the reference routines (reference compile-time config
+// held at run time).  Each call moves the caller's host arrays to the GPU,
+// runs the same kernels as the resident context, and moves results back.
+// ===========================================================================
+namespace {
+
+struct Compat {
+  bcmg_reference_config cfg = {16, 1150, 0.0000185, 1.1842, 38.889, 38.889, 101300.0};
+  cudaStream_t s = nullptr;
+  int ncube = 0, S = 0;  // sized for the last whole-array call
+  size_t ncell = 0;
+  double *U1_ = nullptr, *U1 = nullptr, *U1q = nullptr, *U1p1 = nullptr, *U1p2 = nullptr,
+         *Rku1 = nullptr, *Residual1 = nullptr, *cube_size = nullptr, *partials = nullptr,
+         *er = nullptr;
+  int *FWS = nullptr;
+  int nparts = 0;
+  // compact per-call cube buffer for routines that only touch listed cubes
+  double *cubes = nullptr;
+  size_t cubes_cap = 0;
+  int *ibuf = nullptr;
+  size_t ibuf_cap = 0;
+  FaceTask *tasks = nullptr;
+  size_t tasks_cap = 0;
+  Ibm ibm;
+
+  Phys phys() const {
+    Phys p;
+    p.n = cfg.ncube_x;
+    p.mpi_ncube = cfg.mpi_ncube;
+    p.mu_L = cfg.mu_L;
+    p.rho0 = cfg.rho0;
+    p.U0 = cfg.U0;
+    p.Uin = cfg.Uin;
+    p.P0 = cfg.P0;
+    return p;
+  }
+  int stream() {
+    if (!s) CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    return BCMG_OK;
+  }
+  int ensure_full(int nc) {
+    int r;
+    if ((r = stream())) return r;
+    const int Sx = cfg.ncube_x + 4;
+    if (nc == ncube && Sx == S && U1_) return BCMG_OK;
+    dfree(U1_); dfree(U1); dfree(U1q); dfree(U1p1); dfree(U1p2); dfree(Rku1);
+    dfree(Residual1); dfree(cube_size); dfree(partials); dfree(er); dfree(FWS);
+    ncube = nc;
+    S = Sx;
+    ncell = (size_t)nc * S * S * S;
+    const size_t nd = ncell * 5;
+    CK(dalloc(&U1_, nd)); CK(dalloc(&U1, nd)); CK(dalloc(&U1q, nd)); CK(dalloc(&U1p1, nd));
+    CK(dalloc(&U1p2, nd)); CK(dalloc(&Rku1, nd)); CK(dalloc(&Residual1, nd));
+    CK(dalloc(&cube_size, (size_t)nc)); CK(dalloc(&FWS, ncell)); CK(dalloc(&er, 8));
+    RkArgs probe{};
+    probe.ph = phys();
+    probe.ncube = nc;
+    nparts = rk_partial_blocks(probe);
+    CK(dalloc(&partials, (size_t)nparts * 7));
+    return BCMG_OK;
+  }
+  template <typename T>
+  int grow(T **p, size_t &cap, size_t need) {
+    if (need <= cap && *p) return BCMG_OK;
+    dfree(*p);
+    CK(dalloc(p, need));
+    cap = need;
+    return BCMG_OK;
+  }
+};
+
+Compat g_compat;
+
+// Gather the listed cubes of a host array into the compact device buffer
+// (slot 0 unused, slot m = cubes[m-1]); returns cube count.
+int gather_cubes(Compat &C, const std::vector<int> &cubes, const double *hostU) {
+  const size_t per = (size_t)C.S * C.S * C.S * 5;
+  int r;
+  if ((r = C.grow(&C.cubes, C.cubes_cap, per * (cubes.size() + 1)))) return r;
+  for (size_t m = 0; m < cubes.size(); ++m)
+    CK(cudaMemcpyAsync(C.cubes + per * (m + 1), hostU + per * cubes[m], per * sizeof(double),
+                       cudaMemcpyHostToDevice, C.s));
+  return BCMG_OK;
+}
+int scatter_cubes(Compat &C, const std::vector<int> &cubes, double *hostU) {
+  const size_t per = (size_t)C.S * C.S * C.S * 5;
+  for (size_t m = 0; m < cubes.size(); ++m)
+    CK(cudaMemcpyAsync(hostU + per * cubes[m], C.cubes + per * (m + 1), per * sizeof(double),
+                       cudaMemcpyDeviceToHost, C.s));
+  CK(cudaStreamSynchronize(C.s));
+  return BCMG_OK;
+}
+
+// One boundary-condition axis for the twins: lists are 1-based with counts.
+int compat_bc(int axis, int nl, int nu, const int *lo, const int *up, double *U) {
+  Compat &C = g_compat;
+  int r;
+  if ((r = C.stream())) return r;
+  C.S = C.cfg.ncube_x + 4;
+  if (nl < 0 || nu < 0 || (nl && !lo) || (nu && !up) || !U) {
+    set_err("bad boundary-condition arguments");
+    return BCMG_ERR_ARG;
+  }
+  std::vector<int> uniq;
+  for (int a = 1; a <= nl; ++a) uniq.push_back(lo[a]);
+  for (int a = 1; a <= nu; ++a) uniq.push_back(up[a]);
+  for (int c : uniq)
+    if (c <= 0) { set_err("boundary list holds a cube number < 1"); return BCMG_ERR_ARG; }
+  std::sort(uniq.begin(), uniq.end());
+  uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
+  if (uniq.empty()) return BCMG_OK;
+  std::vector<int> slot(uniq.back() + 1, 0);
+  for (size_t m = 0; m < uniq.size(); ++m) slot[uniq[m]] = (int)m + 1;
+  std::vector<int> cubes(uniq.size()), masks(uniq.size(), 0);
+  for (size_t m = 0; m < uniq.size(); ++m) cubes[m] = (int)m + 1;
+  for (int a = 1; a <= nl; ++a) masks[slot[lo[a]] - 1] |= 1 << (2 * axis);
+  for (int a = 1; a <= nu; ++a) masks[slot[up[a]] - 1] |= 2 << (2 * axis);
+  if ((r = gather_cubes(C, uniq, U))) return r;
+  if ((r = C.grow(&C.ibuf, C.ibuf_cap, 2 * cubes.size()))) return r;
+  CK(cudaMemcpyAsync(C.ibuf, cubes.data(), sizeof(int) * cubes.size(), cudaMemcpyHostToDevice, C.s));
+  CK(cudaMemcpyAsync(C.ibuf + cubes.size(), masks.data(), sizeof(int) * masks.size(),
+                     cudaMemcpyHostToDevice, C.s));
+  BcArgs b;
+  b.n = C.cfg.ncube_x;
+  b.Uin = C.cfg.Uin;
+  b.cubes = C.ibuf;
+  b.masks = C.ibuf + cubes.size();
+  b.axes = 1 << axis;
+  b.U1_ = C.cubes;
+  CK(launch_bc(b, (int)cubes.size(), C.s));
+  return scatter_cubes(C, uniq, U);
+}
+
+int compat_ghost(const int *NNBC, const double *weight, const int *GCindex, const int *IPsur,
+                 double *U) {
+  Compat &C = g_compat;
+  int r;
+  if ((r = C.stream())) return r;
+  C.S = C.cfg.ncube_x + 4;
+  if (!NNBC || *NNBC < 0 || !U || (*NNBC > 0 && (!weight || !GCindex || !IPsur))) {
+    set_err("bad ghost-cell arguments");
+    return BCMG_ERR_ARG;
+  }
+  const int nb = *NNBC;
+  if (nb == 0) return BCMG_OK;
+  // Remap the touched cubes to compact slots.
+  std::vector<int> uniq;
+  for (int e = 1; e <= nb; ++e) {
+    uniq.push_back(IPsur[4 * (e - 1) + 1]);
+    uniq.push_back(GCindex[4 * (e - 1) + 1]);
+  }
+  for (int c : uniq)
+    if (c <= 0) { set_err("IBM table holds a cube number < 1"); return BCMG_ERR_ARG; }
+  std::sort(uniq.begin(), uniq.end());
+  uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
+  std::vector<int> slot(uniq.back() + 1, 0);
+  for (size_t m = 0; m < uniq.size(); ++m) slot[uniq[m]] = (int)m + 1;
+  std::vector<int> gc(GCindex, GCindex + 4 * (size_t)nb + 1), ip(IPsur, IPsur + 4 * (size_t)nb + 1);
+  for (int e = 1; e <= nb; ++e) {
+    gc[4 * (e - 1) + 1] = slot[gc[4 * (e - 1) + 1]];
+    ip[4 * (e - 1) + 1] = slot[ip[4 * (e - 1) + 1]];
+  }
+  if ((r = ibm_upload(C.ibm, nb, weight, gc.data(), ip.data(), C.cfg.ncube_x,
+                      (int)uniq.size() + 1, C.s)))
+    return r;
+  if ((r = gather_cubes(C, uniq, U))) return r;
+  if ((r = ibm_run(C.ibm, C.cfg.ncube_x, C.cfg.rho0, C.cfg.P0, C.cubes, C.s, nullptr))) return r;
+  return scatter_cubes(C, uniq, U);
+}
+
+}  // namespace
+
+extern "C" {
+
+int bcmg_set_reference_config(const bcmg_reference_config *cfg) {
+  clear_err();
+  if (!cfg || !valid_n(cfg->ncube_x) || cfg->mpi_ncube < 1) {
+    set_err("invalid reference config (ncube_x multiple of 4, mpi_ncube >= 1)");
+    return BCMG_ERR_ARG;
+  }
+  g_compat.cfg = *cfg;
+  return BCMG_OK;
+}
+
+void bcmg_get_reference_config(bcmg_reference_config *cfg) {
+  if (cfg) *cfg = g_compat.cfg;
+}
+
+void BCM_Flux_XYZ_Viscous_Runge_kutta(int myid, int ncube, int RK, double deltaT,
+                                      double deltaTau, double e, int *FWS, int *csl,
+                                      double *cube_size, double *U1_, double *U1, double *U1q,
+                                      double *U1p1, double *U1p2, double *Rku1,
+                                      double *Residual1, double *er) {
+  (void)myid;
+  (void)csl;
+  clear_err();
+  Compat &C = g_compat;
+  if (ncube < 1 || RK < 1 || RK > 3 || !FWS || !cube_size || !U1_ || !U1 || !U1q || !U1p1 ||
+      !U1p2 || !Rku1 || !Residual1 || (RK == 3 && !er)) {
+    set_err("BCM_Flux_XYZ_Viscous_Runge_kutta: bad arguments");
+    return;
+  }
+  for (int i = 1; i < ncube; ++i)
+    if (!(cube_size[i] > 0)) {
+      set_err("BCM_Flux_XYZ_Viscous_Runge_kutta: cube_size must be positive");
+      return;
+    }
+  auto run = [&]() -> int {
+    int r;
+    if ((r = C.ensure_full(ncube))) return r;
+    const size_t b = C.ncell * 5 * sizeof(double);
+    cudaStream_t s = C.s;
+    CK(cudaMemcpyAsync(C.FWS, FWS, C.ncell * sizeof(int), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(C.cube_size, cube_size, sizeof(double) * ncube, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(C.U1_, U1_, b, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(C.U1, U1, b, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(C.U1q, U1q, b, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(C.U1p1, U1p1, b, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(C.U1p2, U1p2, b, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(C.Rku1, Rku1, b, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(C.Residual1, Residual1, b, cudaMemcpyHostToDevice, s));
+    FluxArgs a;
+    a.ph = C.phys();
+    a.cube0 = 1;
+    a.dT = deltaT;
+    a.dTau = deltaTau;
+    a.e = e;
+    a.FWS = C.FWS;
+    a.cube_size = C.cube_size;
+    a.U1_ = C.U1_;
+    a.U1 = C.U1;
+    a.U1q = C.U1q;
+    a.Rku1 = C.Rku1;
+    a.Residual1 = C.Residual1;
+    CK(launch_flux_fp64(a, ncube - 1, s));
+    RkArgs k;
+    k.ph = C.phys();
+    k.ncube = ncube;
+    k.RK = RK;
+    k.FWS = C.FWS;
+    k.U1_ = C.U1_;
+    k.U1p1 = C.U1p1;
+    k.U1p2 = C.U1p2;
+    k.Rku1 = C.Rku1;
+    k.Residual1 = C.Residual1;
+    k.partials = C.partials;
+    int nb = 0;
+    CK(launch_rk(k, &nb, s));
+    if (RK == 3) CK(launch_norms(C.phys(), C.partials, nb, C.er, s));
+    CK(cudaMemcpyAsync(U1_, C.U1_, b, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(Rku1, C.Rku1, b, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(Residual1, C.Residual1, b, cudaMemcpyDeviceToHost, s));
+    if (RK == 1) CK(cudaMemcpyAsync(U1p1, C.U1p1, b, cudaMemcpyDeviceToHost, s));
+    if (RK == 2) CK(cudaMemcpyAsync(U1p2, C.U1p2, b, cudaMemcpyDeviceToHost, s));
+    if (RK == 3) CK(cudaMemcpyAsync(er + 1, C.er + 1, 7 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return BCMG_OK;
+  };
+  run();
+}
+
+void BCM_X_boundary_condition(int myid, int nXbc_l, int nXbc_u, int *Xbc_l, int *Xbc_u,
+                              double *U1_) {
+  (void)myid;
+  clear_err();
+  compat_bc(0, nXbc_l, nXbc_u, Xbc_l, Xbc_u, U1_);
+}
+void BCM_Y_boundary_condition(int nYbc_l, int nYbc_u, int *Ybc_l, int *Ybc_u, double *U1_) {
+  clear_err();
+  compat_bc(1, nYbc_l, nYbc_u, Ybc_l, Ybc_u, U1_);
+}
+void BCM_Z_boundary_condition(int nZbc_l, int nZbc_u, int *Zbc_l, int *Zbc_u, double *U1_) {
+  clear_err();
+  compat_bc(2, nZbc_l, nZbc_u, Zbc_l, Zbc_u, U1_);
+}
+
+void BCM_Ghostcell_minus(int myid, int *NNBC, double *weight, int *GCindex, int *IPsur,
+                         int *FWS, double *U1_) {
+  (void)myid;
+  (void)FWS;
+  clear_err();
+  compat_ghost(NNBC, weight, GCindex, IPsur, U1_);
+}
+void BCM_Ghostcell_plus(int myid, int *NNBC, double *weight, int *GCindex, int *IPsur,
+                        int *FWS, double *U1_) {
+  (void)myid;
+  (void)FWS;
+  clear_err();
+  compat_ghost(NNBC, weight, GCindex, IPsur, U1_);
+}
+
+void BCM_Interface(int myid, int ncube, int mPI_Nadj, int ncpu_bs, int ncpu_eq, int ncpu_sb,
+                   int max_nei_bs, int max_nei_eq, int max_nei_sb, int nadjX_eq, int nadjY_eq,
+                   int nadjZ_eq, int nadjX_bs_plus, int nadjX_sb_plus, int nadjX_bs_minus,
+                   int nadjX_sb_minus, int nadjY_bs_plus, int nadjY_sb_plus,
+                   int nadjY_bs_minus, int nadjY_sb_minus, int nadjZ_bs_plus,
+                   int nadjZ_sb_plus, int nadjZ_bs_minus, int nadjZ_sb_minus, int *rank_map,
+                   int *MPI_cpu, int *MPI_cube, int *MPI_cpu_adj, int *MPI_cube_adj,
+                   int *MPI_direction, int *MPI_interface, int *neighbor_cpu_eq,
+                   int *Ncube_Ncpu_eq, int *neighbor_cpu_sb, int *Ncube_Ncpu_sb,
+                   int *neighbor_cpu_bs, int *Ncube_Ncpu_bs, int *Scube_Ncpu_eq,
+                   int *Rcube_Ncpu_eq, double *send_data_curr_eq, double *recv_data_curr_eq,
+                   double *send_data_neig_eq, double *recv_data_neig_eq, int *Sdir_eq,
+                   int *Rdir_eq, int *Scube_Ncpu_sb, int *Rcube_Ncpu_sb,
+                   double *send_data_curr_sb, double *recv_data_curr_sb,
+                   double *send_data_neig_sb, double *recv_data_neig_sb, int *Sdir_sb,
+                   int *Rdir_sb, int *Scube_Ncpu_bs, int *Rcube_Ncpu_bs,
+                   double *send_data_curr_bs, double *recv_data_curr_bs,
+                   double *send_data_neig_bs, double *recv_data_neig_bs, int *Sdir_bs,
+                   int *Rdir_bs, int *ist_eq, int *ist_sb, int *ist_bs, int *adjN_sb,
+                   int *RadjN_bs, int *SadjN_bs, int *csl, int *adj_number, int *adjX_eq,
+                   int *adjY_eq, int *adjZ_eq, int *adjX_bs_plus, int *adjX_sb_plus,
+                   int *adjX_bs_minus, int *adjX_sb_minus, int *adjY_bs_plus,
+                   int *adjY_sb_plus, int *adjY_bs_minus, int *adjY_sb_minus,
+                   int *adjZ_bs_plus, int *adjZ_sb_plus, int *adjZ_bs_minus,
+                   int *adjZ_sb_minus, double *U1_) {
+  (void)myid; (void)mPI_Nadj; (void)max_nei_bs; (void)max_nei_eq; (void)max_nei_sb;
+  (void)rank_map; (void)MPI_cpu; (void)MPI_cube; (void)MPI_cpu_adj; (void)MPI_cube_adj;
+  (void)MPI_direction; (void)MPI_interface; (void)neighbor_cpu_eq; (void)Ncube_Ncpu_eq;
+  (void)neighbor_cpu_sb; (void)Ncube_Ncpu_sb; (void)neighbor_cpu_bs; (void)Ncube_Ncpu_bs;
+  (void)Scube_Ncpu_eq; (void)Rcube_Ncpu_eq; (void)send_data_curr_eq; (void)recv_data_curr_eq;
+  (void)send_data_neig_eq; (void)recv_data_neig_eq; (void)Sdir_eq; (void)Rdir_eq;
+  (void)Scube_Ncpu_sb; (void)Rcube_Ncpu_sb; (void)send_data_curr_sb; (void)recv_data_curr_sb;
+  (void)send_data_neig_sb; (void)recv_data_neig_sb; (void)Sdir_sb; (void)Rdir_sb;
+  (void)Scube_Ncpu_bs; (void)Rcube_Ncpu_bs; (void)send_data_curr_bs; (void)recv_data_curr_bs;
+  (void)send_data_neig_bs; (void)recv_data_neig_bs; (void)Sdir_bs; (void)Rdir_bs;
+  (void)ist_eq; (void)ist_sb; (void)ist_bs; (void)adjN_sb; (void)RadjN_bs; (void)SadjN_bs;
+  (void)csl; (void)adjX_bs_plus; (void)adjX_sb_plus; (void)adjX_bs_minus; (void)adjX_sb_minus;
+  (void)adjY_bs_plus; (void)adjY_sb_plus; (void)adjY_bs_minus; (void)adjY_sb_minus;
+  (void)adjZ_bs_plus; (void)adjZ_sb_plus; (void)adjZ_bs_minus; (void)adjZ_sb_minus;
+  clear_err();
+  if (ncpu_bs || ncpu_eq || ncpu_sb) {
+    set_err("BCM_Interface: cross-rank exchange lists are not supported on one GPU");
+    return;
+  }
+  if (nadjX_bs_plus || nadjX_sb_plus || nadjX_bs_minus || nadjX_sb_minus || nadjY_bs_plus ||
+      nadjY_sb_plus || nadjY_bs_minus || nadjY_sb_minus || nadjZ_bs_plus || nadjZ_sb_plus ||
+      nadjZ_bs_minus || nadjZ_sb_minus) {
+    set_err("BCM_Interface: level-jump interfaces are not supported yet");
+    return;
+  }
+  if (ncube < 2 || !adj_number || !U1_ || nadjX_eq < 0 || nadjY_eq < 0 || nadjZ_eq < 0 ||
+      (nadjX_eq && !adjX_eq) || (nadjY_eq && !adjY_eq) || (nadjZ_eq && !adjZ_eq)) {
+    set_err("BCM_Interface: bad arguments");
+    return;
+  }
+  Compat &C = g_compat;
+  auto run = [&]() -> int {
+    int r;
+    std::vector<int> off;
+    std::vector<FaceTask> tasks;
+    std::string err;
+    const int *lists[3] = {adjX_eq, adjY_eq, adjZ_eq};
+    const int counts[3] = {nadjX_eq, nadjY_eq, nadjZ_eq};
+    if (!build_interface_tasks_from_lists(ncube, adj_number, lists, counts, off, tasks, err)) {
+      set_err("BCM_Interface: " + err);
+      return BCMG_ERR_ARG;
+    }
+    if ((r = C.ensure_full(ncube))) return r;
+    if ((r = C.grow(&C.ibuf, C.ibuf_cap, off.size()))) return r;
+    if ((r = C.grow(&C.tasks, C.tasks_cap, tasks.size()))) return r;
+    const size_t b = C.ncell * 5 * sizeof(double);
+    CK(cudaMemcpyAsync(C.ibuf, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice, C.s));
+    if (!tasks.empty())
+      CK(cudaMemcpyAsync(C.tasks, tasks.data(), sizeof(FaceTask) * tasks.size(),
+                         cudaMemcpyHostToDevice, C.s));
+    CK(cudaMemcpyAsync(C.U1_, U1_, b, cudaMemcpyHostToDevice, C.s));
+    InterfaceArgs ia;
+    ia.n = C.cfg.ncube_x;
+    ia.dst_cubes = nullptr;
+    ia.task_off = C.ibuf;
+    ia.tasks = C.tasks;
+    ia.edge_cubes = ncube;
+    ia.U1_ = C.U1_;
+    CK(launch_interface(ia, ncube, C.s));
+    CK(cudaMemcpyAsync(U1_, C.U1_, b, cudaMemcpyDeviceToHost, C.s));
+    CK(cudaStreamSynchronize(C.s));
+    return BCMG_OK;
+  };
+  run();
+}
+
+}  // extern "C"

@@ -1,0 +1,277 @@
+// Ghost-layer kernels around the flux: cube-to-cube interface, the X/Y/Z
+// boundary conditions and the immersed-boundary ghost cells.
+//
+// All three are pure data movement plus a little FP64 arithmetic; each is
+// organised so one CTA owns the cells it writes and only reads cells nobody
+// writes during the launch, which makes every launch race-free and gives the
+// reference's results exactly.
+#include <cuda_runtime.h>
+
+#include "bcm_common.cuh"
+#include "bcm_kernels.h"
+
+namespace bcmg {
+
+constexpr int kHaloThreads = 256;
+
+// ---------------------------------------------------------------------------
+// Interface (BCM_Interface.cpp).  Same-level faces (:1745-1783 x, :2608-2642
+// y, :3478-3512 z) copy the neighbour's two interior layers into this cube's
+// two ghost layers over the 16x16 (n x n) face; every read is an interior
+// cell, every write a ghost cell of the CTA's own cube.  After a CTA barrier
+// the edge ghosts are averaged in the reference's three ordered phases
+// (:5640-5732): i-edges, then j-edges, then k-edges.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kHaloThreads) k_interface(InterfaceArgs a) {
+  const int n = a.n, S = n + 4, nx = n + 1, nyy = n + 2;
+  const int c = blockIdx.x + 1;  // one CTA per cube 1..ncube-1
+  double *U = a.U1_;
+  const int t0 = a.task_off[c], t1 = a.task_off[c + 1];
+  for (int t = t0; t < t1; ++t) {
+    const FaceTask ft = a.tasks[t];
+    const int ax = ft.axis;
+    // Layer l (0,1): dst ghost index and src interior index along the axis.
+    // side 0: dst [l]     <- src [n+l]   (src is the -ax neighbour)
+    // side 1: dst [n+2+l] <- src [2+l]   (src is the +ax neighbour)
+    const int dbase = ft.side == 0 ? 0 : n + 2;
+    const int sbase = ft.side == 0 ? n : 2;
+    const int cells = 2 * n * n;
+    for (int w = threadIdx.x; w < cells * 5; w += kHaloThreads) {
+      const int v = w % 5, cell = w / 5;
+      const int l = cell / (n * n), p = 2 + (cell / n) % n, q = 2 + cell % n;
+      int di, dj, dk, si, sj, sk;
+      if (ax == 0) { di = dbase + l; si = sbase + l; dj = sj = p; dk = sk = q; }
+      else if (ax == 1) { dj = dbase + l; sj = sbase + l; di = si = p; dk = sk = q; }
+      else { dk = dbase + l; sk = sbase + l; di = si = p; dj = sj = q; }
+      U[5 * cell_index(S, c, di, dj, dk) + v] = U[5 * cell_index(S, ft.src, si, sj, sk) + v];
+    }
+  }
+  if (c >= a.edge_cubes) return;
+  __syncthreads();
+  auto Q = [&](int i, int j, int k) { return U + 5 * cell_index(S, c, i, j, k); };
+  // Phase 1: i-edges, i = 2..nx.
+  for (int w = threadIdx.x; w < 4 * n * 5; w += kHaloThreads) {
+    const int v = w % 5, e = (w / 5) % 4, i = 2 + (w / 20);
+    double *d;
+    const double *x, *y;
+    if (e == 0) { d = Q(i, 1, 1); x = Q(i, 1, 2); y = Q(i, 2, 1); }
+    else if (e == 1) { d = Q(i, nyy, 1); x = Q(i, nyy, 2); y = Q(i, nx, 1); }
+    else if (e == 2) { d = Q(i, 1, nyy); x = Q(i, 1, nx); y = Q(i, 2, nyy); }
+    else { d = Q(i, nyy, nyy); x = Q(i, nyy, nx); y = Q(i, nx, nyy); }
+    d[v] = 0.5 * (x[v] + y[v]);
+  }
+  __syncthreads();
+  // Phase 2: j-edges, j = 1..nyy.
+  for (int w = threadIdx.x; w < 4 * (n + 2) * 5; w += kHaloThreads) {
+    const int v = w % 5, e = (w / 5) % 4, j = 1 + (w / 20);
+    double *d;
+    const double *x, *y;
+    if (e == 0) { d = Q(1, j, 1); x = Q(1, j, 2); y = Q(2, j, 1); }
+    else if (e == 1) { d = Q(1, j, nyy); x = Q(2, j, nyy); y = Q(1, j, nx); }
+    else if (e == 2) { d = Q(nyy, j, 1); x = Q(nx, j, 1); y = Q(nyy, j, 2); }
+    else { d = Q(nyy, j, nyy); x = Q(nx, j, nyy); y = Q(nyy, j, nx); }
+    d[v] = 0.5 * (x[v] + y[v]);
+  }
+  __syncthreads();
+  // Phase 3: k-edges, k = 1..nyy.
+  for (int w = threadIdx.x; w < 4 * (n + 2) * 5; w += kHaloThreads) {
+    const int v = w % 5, e = (w / 5) % 4, k = 1 + (w / 20);
+    double *d;
+    const double *x, *y;
+    if (e == 0) { d = Q(1, 1, k); x = Q(1, 2, k); y = Q(2, 1, k); }
+    else if (e == 1) { d = Q(1, nyy, k); x = Q(2, nyy, k); y = Q(1, nx, k); }
+    else if (e == 2) { d = Q(nyy, 1, k); x = Q(nx, 1, k); y = Q(nyy, 2, k); }
+    else { d = Q(nyy, nyy, k); x = Q(nx, nyy, k); y = Q(nyy, nx, k); }
+    d[v] = 0.5 * (x[v] + y[v]);
+  }
+}
+
+cudaError_t launch_interface(const InterfaceArgs &a, int ncubes_total, cudaStream_t s) {
+  if (ncubes_total <= 1) return cudaSuccess;
+  k_interface<<<ncubes_total - 1, kHaloThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Boundary conditions (BCM_X/Y/Z_boundary_condition.cpp), one CTA per cube,
+// phases x -> y -> z with barriers: y reads x ghosts and z reads y ghosts of
+// the same cube (main.cpp:1161-1165 order).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kHaloThreads) k_bc(BcArgs a) {
+  const int n = a.n, S = n + 4, nx = n + 1, nxx = n + 2, nxxx = n + 3;
+  const int c = a.cubes[blockIdx.x];
+  const int m = a.masks[blockIdx.x];
+  double *U = a.U1_;
+  auto Q = [&](int i, int j, int k) { return U + 5 * cell_index(S, c, i, j, k); };
+  if (a.axes & 1) {
+    if (m & 1) {  // x lower: inflow, rho and p from cell 2, u = Uin (:43-80)
+      for (int w = threadIdx.x; w < n * n; w += kHaloThreads) {
+        const int j = 2 + w / n, k = 2 + w % n;
+        const double *q = Q(2, j, k);
+        double rho = q[0];
+        double U0 = q[1] / rho, V0 = q[2] / rho, W0 = q[3] / rho;
+        double VV = U0 * U0 + V0 * V0 + W0 * W0;
+        double P = (q[4] - 0.5 * rho * VV) * (BCMG_K - 1);
+        double Uu = a.Uin, Vv = 0., Ww = 0;
+        VV = Uu * Uu + Vv * Vv + Ww * Ww;
+        double o[5] = {rho, rho * Uu, rho * Vv, rho * Ww, P / (BCMG_K - 1) + 0.5 * rho * VV};
+        double *d1 = Q(1, j, k), *d0 = Q(0, j, k);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) { d1[v] = o[v]; d0[v] = o[v]; }
+      }
+    }
+    if (m & 2) {  // x upper: zero gradient (:85-118)
+      for (int w = threadIdx.x; w < n * n * 5; w += kHaloThreads) {
+        const int v = w % 5, j = 2 + (w / 5) / n, k = 2 + (w / 5) % n;
+        double x = Q(nx, j, k)[v];
+        Q(nxx, j, k)[v] = x;
+        Q(nxxx, j, k)[v] = x;
+      }
+    }
+    __syncthreads();
+  }
+  if (a.axes & 2) {
+    for (int w = threadIdx.x; w < (n + 4) * n * 5; w += kHaloThreads) {
+      const int v = w % 5, i = (w / 5) / n, k = 2 + (w / 5) % n;
+      if (m & 4) {  // y lower (:36-59)
+        double x = Q(i, 2, k)[v];
+        Q(i, 1, k)[v] = x;
+        Q(i, 0, k)[v] = x;
+      }
+      if (m & 8) {  // y upper (:62-85)
+        double x = Q(i, nx, k)[v];
+        Q(i, nxx, k)[v] = x;
+        Q(i, nxxx, k)[v] = x;
+      }
+    }
+    __syncthreads();
+  }
+  if (a.axes & 4) {
+    for (int w = threadIdx.x; w < (n + 4) * (n + 4) * 5; w += kHaloThreads) {
+      const int v = w % 5, i = (w / 5) / (n + 4), j = (w / 5) % (n + 4);
+      if (m & 16) {  // z lower: slip wall, rho*w negated (:42-65)
+        double x = Q(i, j, 2)[v];
+        if (v == 3) x = -x;
+        Q(i, j, 1)[v] = x;
+        Q(i, j, 0)[v] = x;
+      }
+      if (m & 32) {  // z upper (:70-92)
+        double x = Q(i, j, nx)[v];
+        Q(i, j, nxx)[v] = x;
+        Q(i, j, nxxx)[v] = x;
+      }
+    }
+  }
+}
+
+cudaError_t launch_bc(const BcArgs &a, int ncubes, cudaStream_t s) {
+  if (ncubes <= 0) return cudaSuccess;
+  k_bc<<<ncubes, kHaloThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// IBM ghost cells (BCM_Ghostcell_minus.cpp:72-489; _plus is identical).  One
+// thread per entry of one dependency level: within a level no entry reads a
+// cell another entry of the level writes, and the host orders the levels so
+// every read sees exactly the value the reference's serial loop sees.
+// ---------------------------------------------------------------------------
+__global__ void k_ghost(GhostArgs a, int count) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int e = a.entries[t];
+  const int S = a.n + 4;
+  const int b = (e - 1) * 4;
+  const int c = a.IPsur[b + 1], i = a.IPsur[b + 2], j = a.IPsur[b + 3], k = a.IPsur[b + 4];
+  const double rho0 = a.rho0, P0 = a.P0;
+  double rh[8], Uu[8], Vv[8], Ww[8], Pp[8];
+#pragma unroll
+  for (int m = 0; m < 8; ++m) {
+    // Order 000,100,010,001,110,101,011,111 (:81-145).
+    const int oi = (m == 1 || m == 4 || m == 5 || m == 7);
+    const int oj = (m == 2 || m == 4 || m == 6 || m == 7);
+    const int ok = (m == 3 || m == 5 || m == 6 || m == 7);
+    const double *q = a.U1_ + 5 * cell_index(S, c, i + oi, j + oj, k + ok);
+    rh[m] = q[0];
+    Uu[m] = q[1] / rh[m];
+    Vv[m] = q[2] / rh[m];
+    Ww[m] = q[3] / rh[m];
+    double VV = Uu[m] * Uu[m] + Vv[m] * Vv[m] + Ww[m] * Ww[m];
+    Pp[m] = (q[4] - 0.5 * rh[m] * VV) * (BCMG_K - 1);
+  }
+  const double *w = a.weight + (size_t)(e - 1) * 8 + 1;
+  double wl[8];
+#pragma unroll
+  for (int m = 0; m < 8; ++m) wl[m] = w[m];
+  const int gc = a.GCindex[b + 1], gi = a.GCindex[b + 2], gj = a.GCindex[b + 3],
+            gk = a.GCindex[b + 4];
+  double rho = wl[0] * (rh[0] - rho0);
+  double P = wl[0] * (Pp[0] - P0);
+  double U = wl[0] * Uu[0], V = wl[0] * Vv[0], W = wl[0] * Ww[0];
+#pragma unroll
+  for (int m = 1; m < 8; ++m) {
+    rho = rho + wl[m] * (rh[m] - rho0);
+    P = P + wl[m] * (Pp[m] - P0);
+    U = U + wl[m] * Uu[m];
+    V = V + wl[m] * Vv[m];
+    W = W + wl[m] * Ww[m];
+  }
+  rho = rho + rho0;
+  P = P + P0;
+  double VV = U * U + V * V + W * W;
+  double o[5] = {rho, 0.5 * rho * U, 0.5 * rho * V, 0.5 * rho * W,
+                 P / (BCMG_K - 1) + 0.5 * rho * 0.25 * VV};
+  // Ghost inside its own stencil (:192-449); like the reference, only the
+  // local indices are compared, not the cube.
+  const int s = (gi - i) + 2 * (gj - j) + 4 * (gk - k);
+  const bool self = (gi - i == 0 || gi - i == 1) && (gj - j == 0 || gj - j == 1) &&
+                    (gk - k == 0 || gk - k == 1);
+  if (self) {
+    // bit pattern (di,dj,dk) -> stencil slot in the 000,100,010,001,... order
+    const int slot_of[8] = {0, 1, 2, 4, 3, 5, 6, 7};
+    const int sl = slot_of[s];
+    double r2, p2;
+    if (wl[sl] > 0.9999) {
+      r2 = rh[sl];
+      p2 = Pp[sl];
+    } else {
+      double ar = 0, ap = 0;
+      bool first = true;
+#pragma unroll
+      for (int m = 0; m < 8; ++m) {
+        if (m == sl) continue;
+        double tr = wl[m] * (rh[m] - rho0), tp = wl[m] * (Pp[m] - P0);
+        if (first) { ar = tr; ap = tp; first = false; }
+        else { ar = ar + tr; ap = ap + tp; }
+      }
+      r2 = ar / (1 - wl[sl]) + rho0;
+      p2 = ap / (1 - wl[sl]) + P0;
+    }
+    double su = 0, sv = 0, sw = 0;
+    bool first = true;
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      if (m == sl) continue;
+      if (first) { su = wl[m] * Uu[m]; sv = wl[m] * Vv[m]; sw = wl[m] * Ww[m]; first = false; }
+      else { su = su + wl[m] * Uu[m]; sv = sv + wl[m] * Vv[m]; sw = sw + wl[m] * Ww[m]; }
+    }
+    double U2 = su / (2 - wl[sl]), V2 = sv / (2 - wl[sl]), W2 = sw / (2 - wl[sl]);
+    double VV2 = U2 * U2 + V2 * V2 + W2 * W2;
+    o[0] = r2;
+    o[1] = r2 * U2;
+    o[2] = r2 * V2;
+    o[3] = r2 * W2;
+    o[4] = p2 / (BCMG_K - 1) + 0.5 * r2 * VV2;
+  }
+  double *g = a.U1_ + 5 * cell_index(S, gc, gi, gj, gk);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) g[v] = o[v];
+}
+
+cudaError_t launch_ghost(const GhostArgs &a, int count, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  k_ghost<<<(count + 127) / 128, 128, 0, s>>>(a, count);
+  return cudaGetLastError();
+}
+
+}  // namespace bcmg

@@ -1,0 +1,93 @@
+// Kernel argument blocks and launchers shared by the C-ABI layer.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "bcm_common.cuh"
+
+namespace bcmg {
+
+struct FluxArgs {
+  Phys ph;
+  int cube0;  // first cube of this launch (cubes are 1-based)
+  double dT, dTau, e;
+  const int *FWS;
+  const double *cube_size;
+  const double *U1_, *U1, *U1q;
+  double *Rku1, *Residual1;
+};
+
+// FP64 residual + increment (bit-exact with the reference).
+cudaError_t launch_flux_fp64(const FluxArgs &a, int ncubes, cudaStream_t s);
+
+// Split-precision residual + increment: reconstruction, fluxes, viscous terms
+// and the preconditioner in FP32; state, BDF2 source, residual sum in FP64.
+cudaError_t launch_flux_split(const FluxArgs &a, int ncubes, cudaStream_t s);
+
+struct RkArgs {
+  Phys ph;
+  int ncube;  // cube slots incl. slot 0
+  int RK;
+  const int *FWS;
+  double *U1_, *U1p1, *U1p2;
+  const double *Rku1, *Residual1;
+  double *partials;  // [nblocks][7] norm/force partial sums (RK == 3)
+};
+
+// Stage combination (BCM_Flux...cpp:2417-2599) and, at RK 3, the per-block
+// partial sums of the change norms and force integrands.
+cudaError_t launch_rk(const RkArgs &a, int *nblocks_out, cudaStream_t s);
+// Number of partial-sum blocks launch_rk uses for this case (for sizing).
+int rk_partial_blocks(const RkArgs &a);
+// Deterministic final reduction of partials -> er[1..7] (device, 8 doubles).
+cudaError_t launch_norms(const Phys &ph, const double *partials, int nblocks, double *er,
+                         cudaStream_t s);
+
+// Interface: one CTA per destination cube pulls its ghost faces from the
+// neighbours' interiors (table built on the host) then runs the ordered
+// three-phase edge fill.  Task i of cube c: tasks[off[c] .. off[c+1]).
+struct FaceTask {
+  int32_t src;   // source cube
+  int8_t axis;   // 0 x, 1 y, 2 z
+  int8_t side;   // 0: dst low ghosts <- src high interior; 1: dst high ghosts <- src low interior
+  int8_t kind;   // 0 same-level copy
+  int8_t pad;
+};
+struct InterfaceArgs {
+  int n;
+  const int *dst_cubes;  // [ndst] cubes that get any face task, ascending
+  const int *task_off;   // [ndst+1]
+  const FaceTask *tasks;
+  int edge_cubes;        // cubes 1..edge_cubes-1 get the edge fill
+  double *U1_;
+};
+cudaError_t launch_interface(const InterfaceArgs &a, int ndst, cudaStream_t s);
+
+// X/Y/Z boundary conditions for a list of (cube, mask) pairs; mask bits
+// 0..5 = x lower, x upper, y lower, y upper, z lower, z upper.  axes selects
+// which of the three phases run (bit 0 x, 1 y, 2 z).
+struct BcArgs {
+  int n;
+  double Uin;
+  const int *cubes;
+  const int *masks;
+  int axes;
+  double *U1_;
+};
+cudaError_t launch_bc(const BcArgs &a, int ncubes, cudaStream_t s);
+
+// IBM ghost-cell fill for one dependency level of the combined entry list.
+struct GhostArgs {
+  int n;
+  double rho0, P0;
+  const int *entries;      // entry numbers (1-based) of this level
+  const double *weight;    // 1-based packed [8*nbc+1]
+  const int *GCindex;      // 1-based packed [4*nbc+1]
+  const int *IPsur;        // 1-based packed [4*nbc+1]
+  double *U1_;
+};
+cudaError_t launch_ghost(const GhostArgs &a, int count, cudaStream_t s);
+
+}  // namespace bcmg

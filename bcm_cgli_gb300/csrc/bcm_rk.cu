@@ -1,0 +1,148 @@
+// RK stage combination, change norms and force sums.
+//
+// BCM_Flux_XYZ_Viscous_Runge_kutta.cpp:2417-2652.  Fluid cells only are
+// updated; at stage 3 the L2 change norms of p, u, v, w, T over fluid cells
+// and the force sums over all interior cells are formed.  The reference sums
+// serially (its OpenMP accumulation at :2523 is unsynchronised); here each
+// block sums a fixed contiguous range of cells in a fixed tree order and a
+// single block adds the block sums in order, so the result is run-to-run
+// reproducible and equal to the serial sum within rounding.
+#include <cuda_runtime.h>
+
+#include "bcm_common.cuh"
+#include "bcm_kernels.h"
+
+namespace bcmg {
+
+constexpr int kRkThreads = 256;
+
+__global__ void __launch_bounds__(kRkThreads) k_rk(RkArgs a, long long total, long long chunk) {
+  const int n = a.ph.n, S = n + 4;
+  const long long beg = (long long)blockIdx.x * chunk;
+  const long long end = min(total, beg + chunk);
+  double s[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (long long t = beg + threadIdx.x; t < end; t += kRkThreads) {
+    const int c = 1 + (int)(t / ((long long)n * n * n));
+    const int r = (int)(t % ((long long)n * n * n));
+    const int i = 2 + r / (n * n), j = 2 + (r / n) % n, k = 2 + r % n;
+    const size_t o = cell_index(S, c, i, j, k);
+    double *q = a.U1_ + 5 * o;
+    const double *rk = a.Rku1 + 5 * o;
+    const bool fluid = a.FWS[o] == kFluid;
+    if (a.RK == 1) {
+      if (fluid) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          double x = q[v] + rk[v];
+          q[v] = x;
+          a.U1p1[5 * o + v] = x;
+        }
+      }
+    } else if (a.RK == 2) {
+      if (fluid) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          double x = 0.75 * q[v] + 0.25 * a.U1p1[5 * o + v] + 0.25 * rk[v];
+          q[v] = x;
+          a.U1p2[5 * o + v] = x;
+        }
+      }
+    } else {
+      if (fluid) {
+        const double K = BCMG_K;
+        (void)K;
+        double rhoold = q[0];
+        double Uold = q[1] / rhoold, Vold = q[2] / rhoold, Wold = q[3] / rhoold;
+        double VVold = Uold * Uold + Vold * Vold + Wold * Wold;
+        double Pold = (q[4] - 0.5 * rhoold * VVold) * (BCMG_K - 1);
+        double Told = Pold / rhoold;
+        double x[5];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          x[v] = 1.0 / 3.0 * q[v] + 2.0 / 3.0 * a.U1p2[5 * o + v] + 2.0 / 3.0 * rk[v];
+          q[v] = x[v];
+        }
+        double rho = x[0];
+        double U = x[1] / rho, V = x[2] / rho, W = x[3] / rho;
+        double VV = U * U + V * V + W * W;
+        double P = (x[4] - 0.5 * rho * VV) * (BCMG_K - 1);
+        double T = P / rho;
+        s[0] += (P - Pold) * (P - Pold);
+        s[1] += (U - Uold) * (U - Uold);
+        s[2] += (V - Vold) * (V - Vold);
+        s[3] += (W - Wold) * (W - Wold);
+        s[4] += (T - Told) * (T - Told);
+      }
+      s[5] += a.Residual1[5 * o + 0];
+      s[6] += a.Residual1[5 * o + 1];
+    }
+  }
+  if (a.RK != 3) return;
+  // Fixed-shape block reduction: warp shuffles then one lane per warp.
+  __shared__ double red[kRkThreads / 32][7];
+#pragma unroll
+  for (int m = 0; m < 7; ++m) {
+    double v = s[m];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][m] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 7) {
+    double v = 0;
+    for (int w = 0; w < kRkThreads / 32; ++w) v += red[w][threadIdx.x];
+    a.partials[(size_t)blockIdx.x * 7 + threadIdx.x] = v;
+  }
+}
+
+__global__ void k_norms(Phys ph, const double *partials, int nblocks, double *er) {
+  __shared__ double tot[7];
+  if (threadIdx.x < 7) {
+    double v = 0;
+    for (int b = 0; b < nblocks; ++b) v += partials[(size_t)b * 7 + threadIdx.x];
+    tot[threadIdx.x] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int n = ph.n;
+    double DN = 1. / (ph.mpi_ncube * n * n * n);
+    er[0] = 0;
+    for (int m = 0; m < 5; ++m) er[1 + m] = sqrt(tot[m]) * DN;
+    er[6] = tot[5] / (0.5 * ph.rho0 * ph.U0 * ph.U0 * 2.602);
+    er[7] = tot[6] / (0.5 * ph.rho0 * ph.U0 * ph.U0 * 2.602);
+  }
+}
+
+static void rk_geometry(const RkArgs &a, long long &total, long long &chunk, int &nb) {
+  const long long n3 = (long long)a.ph.n * a.ph.n * a.ph.n;
+  total = (long long)(a.ncube - 1) * n3;
+  nb = (int)((total + 4 * kRkThreads - 1) / (4 * kRkThreads));
+  if (nb > 152 * 16) nb = 152 * 16;
+  if (nb < 1) nb = 1;
+  chunk = (total + nb - 1) / nb;
+}
+
+int rk_partial_blocks(const RkArgs &a) {
+  long long total, chunk;
+  int nb;
+  rk_geometry(a, total, chunk, nb);
+  return nb;
+}
+
+cudaError_t launch_rk(const RkArgs &a, int *nblocks_out, cudaStream_t s) {
+  long long total, chunk;
+  int nb;
+  rk_geometry(a, total, chunk, nb);
+  if (nblocks_out) *nblocks_out = nb;
+  if (total <= 0) return cudaSuccess;
+  k_rk<<<nb, kRkThreads, 0, s>>>(a, total, chunk);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_norms(const Phys &ph, const double *partials, int nblocks, double *er,
+                         cudaStream_t s) {
+  k_norms<<<1, 32, 0, s>>>(ph, partials, nblocks, er);
+  return cudaGetLastError();
+}
+
+}  // namespace bcmg

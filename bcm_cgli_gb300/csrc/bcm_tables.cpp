@@ -1,0 +1,262 @@
+// Host-side table builders: they turn the reference's setup data (adjacency,
+// boundary-cube lists, IBM ghost tables) into conflict-free launch tables
+// for the GPU kernels, validating every index on the way so no kernel can
+// address memory outside the case's arrays.
+#include "bcm_tables.h"
+
+#include <algorithm>
+#include <cstdio>
+#include <unordered_map>
+
+namespace bcmg {
+
+static std::string fmt(const char *f, long long a = 0, long long b = 0, long long c = 0) {
+  char buf[256];
+  std::snprintf(buf, sizeof buf, f, a, b, c);
+  return buf;
+}
+
+// Neighbour classification as BCM_Interface_table.cpp:96-308: a cube has a
+// +dir neighbour when any of the four slots adj_number[c][1..4][dir] is
+// positive; the classifying cube is the largest slot value; the pair is
+// same-level when csl matches.  The copy partner is slot 1 (:1753).
+bool build_interface_tasks(int ncube, const int *adj, const int *csl, std::vector<int> &off,
+                           std::vector<FaceTask> &tasks, std::string &err) {
+  auto A = [&](int c, int s, int d) { return adj[(c * 5 + s) * 7 + d]; };
+  // Writers of each (dst cube, axis, side) face in the reference's order:
+  // x list, then y, then z; cubes ascending; per pair, first the partner's
+  // low ghosts then this cube's high ghosts (:1763, :1772).  Later writes
+  // win, so keep the last writer of each face.
+  std::vector<int> src_of((size_t)ncube * 6, 0);
+  for (int ax = 0; ax < 3; ++ax) {
+    const int dplus = 2 + 2 * ax, dminus = 1 + 2 * ax;
+    for (int c = 1; c < ncube; ++c) {
+      for (int s = 1; s <= 4; ++s)
+        for (int d = 1; d <= 6; ++d) {
+          int v = A(c, s, d);
+          if (v < 0 || v >= ncube) {
+            err = fmt("adj_number[%lld][%lld][*] out of range", c, s);
+            return false;
+          }
+        }
+      int any = 0, acube = 0;
+      for (int s = 1; s <= 4; ++s) {
+        any |= A(c, s, dplus) > 0;
+        acube = std::max(acube, A(c, s, dplus));
+      }
+      if (any) {
+        if (csl[c] != csl[acube]) {
+          err = fmt("cube %lld: level jump on axis %lld is not supported", c, ax);
+          return false;
+        }
+        const int c2 = A(c, 1, dplus);
+        if (c2 <= 0) {
+          err = fmt("cube %lld: +axis %lld neighbour missing from slot 1", c, ax);
+          return false;
+        }
+        src_of[(size_t)c2 * 6 + ax * 2 + 0] = c;  // c2 low ghosts <- c high interior
+        src_of[(size_t)c * 6 + ax * 2 + 1] = c2;  // c high ghosts <- c2 low interior
+      }
+      // Coarse/fine relations through the - direction (:215-308).
+      int anym = 0, am = 0;
+      for (int s = 1; s <= 4; ++s) {
+        anym |= A(c, s, dminus) > 0;
+        am = std::max(am, A(c, s, dminus));
+      }
+      if (anym && csl[c] != csl[am]) {
+        err = fmt("cube %lld: level jump on axis %lld is not supported", c, ax);
+        return false;
+      }
+    }
+  }
+  off.assign((size_t)ncube + 1, 0);
+  tasks.clear();
+  for (int c = 0; c < ncube; ++c) {
+    off[c] = (int)tasks.size();
+    if (c == 0) continue;
+    for (int ax = 0; ax < 3; ++ax)
+      for (int side = 0; side < 2; ++side) {
+        int src = src_of[(size_t)c * 6 + ax * 2 + side];
+        if (src > 0) {
+          FaceTask t;
+          t.src = src;
+          t.axis = (int8_t)ax;
+          t.side = (int8_t)side;
+          t.kind = 0;
+          t.pad = 0;
+          tasks.push_back(t);
+        }
+      }
+  }
+  off[ncube] = (int)tasks.size();
+  return true;
+}
+
+// The same face tasks from explicit reference lists (adjX_eq etc., 1-based
+// arrays with counts), as BCM_Interface receives them.
+bool build_interface_tasks_from_lists(int ncube, const int *adj, const int *const lists[3],
+                                      const int counts[3], std::vector<int> &off,
+                                      std::vector<FaceTask> &tasks, std::string &err) {
+  std::vector<int> src_of((size_t)ncube * 6, 0);
+  for (int ax = 0; ax < 3; ++ax) {
+    const int dplus = 2 + 2 * ax;
+    for (int a = 1; a <= counts[ax]; ++a) {
+      const int c = lists[ax][a];
+      if (c <= 0 || c >= ncube) {
+        err = fmt("interface list %lld entry %lld out of range", ax, a);
+        return false;
+      }
+      const int c2 = adj[(c * 5 + 1) * 7 + dplus];
+      if (c2 <= 0 || c2 >= ncube) {
+        err = fmt("cube %lld: neighbour on axis %lld out of range", c, ax);
+        return false;
+      }
+      src_of[(size_t)c2 * 6 + ax * 2 + 0] = c;
+      src_of[(size_t)c * 6 + ax * 2 + 1] = c2;
+    }
+  }
+  off.assign((size_t)ncube + 1, 0);
+  tasks.clear();
+  for (int c = 0; c < ncube; ++c) {
+    off[c] = (int)tasks.size();
+    if (c == 0) continue;
+    for (int ax = 0; ax < 3; ++ax)
+      for (int side = 0; side < 2; ++side) {
+        int src = src_of[(size_t)c * 6 + ax * 2 + side];
+        if (src > 0) {
+          FaceTask t;
+          t.src = src;
+          t.axis = (int8_t)ax;
+          t.side = (int8_t)side;
+          t.kind = 0;
+          t.pad = 0;
+          tasks.push_back(t);
+        }
+      }
+  }
+  off[ncube] = (int)tasks.size();
+  return true;
+}
+
+bool build_bc_entries(int ncube, const int *const lists[6], const int counts[6],
+                      std::vector<int> &cubes, std::vector<int> &masks, std::string &err) {
+  std::vector<int> m((size_t)ncube, 0);
+  for (int l = 0; l < 6; ++l)
+    for (int a = 0; a < counts[l]; ++a) {
+      int c = lists[l][a];
+      if (c <= 0 || c >= ncube) {
+        err = fmt("boundary list %lld entry %lld out of range", l, a);
+        return false;
+      }
+      m[c] |= 1 << l;
+    }
+  cubes.clear();
+  masks.clear();
+  for (int c = 1; c < ncube; ++c)
+    if (m[c]) {
+      cubes.push_back(c);
+      masks.push_back(m[c]);
+    }
+  return true;
+}
+
+// Dependency levels for the IBM ghost entries (BCM_Ghostcell_minus.cpp:72).
+// The reference applies entries serially; an entry may read a ghost another
+// entry writes.  Level(e) = 1 + the highest level among earlier entries
+// that write a cell e reads (read-after-write), read the cell e writes
+// (write-after-read) or write the same cell (write-after-write).  Entries of
+// one level touch disjoint written cells and read no cell written in that
+// level, so a level can run fully parallel and the sequence of levels
+// reproduces the serial result exactly.
+bool build_ibm_levels(int nbc, const int *GC, const int *IP, int n, int ncube,
+                      std::vector<int> &order, std::vector<int> &level_off, std::string &err) {
+  const int S = n + 4;
+  struct Tag {
+    int write = 0;  // level of the last writer
+    int read = 0;   // highest level of any reader so far
+  };
+  std::unordered_map<long long, Tag> cells;
+  cells.reserve((size_t)nbc * 9 + 16);
+  std::vector<int> lev((size_t)nbc + 1, 0);
+  int maxlev = 0;
+  auto key = [&](int c, int i, int j, int k) {
+    return (((long long)c * S + i) * S + j) * S + k;
+  };
+  for (int e = 1; e <= nbc; ++e) {
+    const int b = (e - 1) * 4;
+    const int c = IP[b + 1], i = IP[b + 2], j = IP[b + 3], k = IP[b + 4];
+    const int gc = GC[b + 1], gi = GC[b + 2], gj = GC[b + 3], gk = GC[b + 4];
+    if (c <= 0 || c >= ncube || i < 0 || j < 0 || k < 0 || i + 1 >= S || j + 1 >= S ||
+        k + 1 >= S) {
+      err = fmt("IBM entry %lld: image-point stencil out of range", e);
+      return false;
+    }
+    if (gc <= 0 || gc >= ncube || gi < 0 || gj < 0 || gk < 0 || gi >= S || gj >= S || gk >= S) {
+      err = fmt("IBM entry %lld: ghost cell out of range", e);
+      return false;
+    }
+    int L = 1;
+    for (int m = 0; m < 8; ++m) {
+      auto it = cells.find(key(c, i + (m & 1), j + ((m >> 1) & 1), k + ((m >> 2) & 1)));
+      if (it != cells.end()) L = std::max(L, it->second.write + 1);
+    }
+    const long long w = key(gc, gi, gj, gk);
+    auto it = cells.find(w);
+    if (it != cells.end()) L = std::max(L, std::max(it->second.read, it->second.write) + 1);
+    lev[e] = L;
+    maxlev = std::max(maxlev, L);
+    for (int m = 0; m < 8; ++m) {
+      Tag &t = cells[key(c, i + (m & 1), j + ((m >> 1) & 1), k + ((m >> 2) & 1))];
+      t.read = std::max(t.read, L);
+    }
+    cells[w].write = L;
+  }
+  level_off.assign((size_t)maxlev + 1, 0);
+  for (int e = 1; e <= nbc; ++e) level_off[lev[e]]++;
+  // prefix: level_off[l-1]..level_off[l] holds level l (levels 1..maxlev)
+  std::vector<int> start((size_t)maxlev + 2, 0);
+  for (int l = 1; l <= maxlev; ++l) start[l + 1] = start[l] + level_off[l];
+  order.assign((size_t)nbc, 0);
+  std::vector<int> fill(start.begin(), start.end());
+  for (int e = 1; e <= nbc; ++e) order[fill[lev[e]]++] = e;
+  level_off.assign((size_t)maxlev + 1, 0);
+  for (int l = 0; l <= maxlev; ++l) level_off[l] = start[l + 1];
+  return true;
+}
+
+}  // namespace bcmg
+
+// ---------------------------------------------------------------------------
+// C entry points exposing the table builders (diagnostics and host tests).
+// ---------------------------------------------------------------------------
+#include "../../include/bcm_gb300.h"
+
+extern "C" int bcmg_ibm_schedule(int nbc, const int *GCindex, const int *IPsur, int n, int ncube,
+                                 int *level_of_entry) {
+  std::vector<int> order, off;
+  std::string err;
+  if (nbc < 0 || (nbc > 0 && (!GCindex || !IPsur || !level_of_entry))) return -1;
+  if (!bcmg::build_ibm_levels(nbc, GCindex, IPsur, n, ncube, order, off, err)) return -1;
+  for (size_t l = 1; l < off.size(); ++l)
+    for (int t = off[l - 1]; t < off[l]; ++t) level_of_entry[order[t] - 1] = (int)l;
+  return (int)off.size() - 1;
+}
+
+extern "C" int bcmg_interface_tasks(int ncube, const int *adj_number, const int *csl,
+                                    int *task_off, int *task_words, int max_tasks) {
+  std::vector<int> off;
+  std::vector<bcmg::FaceTask> tasks;
+  std::string err;
+  if (ncube < 2 || !adj_number || !csl) return -1;
+  if (!bcmg::build_interface_tasks(ncube, adj_number, csl, off, tasks, err)) return -1;
+  if ((int)tasks.size() > max_tasks) return -2;
+  if (task_off)
+    for (size_t i = 0; i < off.size(); ++i) task_off[i] = off[i];
+  if (task_words)
+    for (size_t t = 0; t < tasks.size(); ++t) {
+      task_words[3 * t + 0] = tasks[t].src;
+      task_words[3 * t + 1] = tasks[t].axis;
+      task_words[3 * t + 2] = tasks[t].side;
+    }
+  return (int)tasks.size();
+}

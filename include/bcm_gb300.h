@@ -1,0 +1,233 @@
+/*
+ * bcm_gb300 — GB300 (sm_103a) implementation of BCM_CGLI's per-cube
+ * dual-time sub-iteration hot path, behind a C ABI.
+ *
+ * Two families of entry points:
+ *
+ *  1. Drop-in twins of the reference routines.  Same names, same parameter
+ *     order and meaning, same in-place semantics on caller-owned host arrays
+ *     in the reference layout U[Ncube][S][S][S][5] (S = NcubeX + 4),
+ *     FWS[Ncube][S][S][S], 1-based cube numbering.  The reference fixes the
+ *     resolution and prm.h constants at compile time; here they come from
+ *     bcmg_set_reference_config() (defaults: the reference's Resolution.h and
+ *     prm.h values).  Each call copies its arrays to the GPU, runs, and
+ *     copies the results back.  They return void like the reference; a
+ *     failure is reported by bcmg_last_error() (non-NULL after a failure).
+ *
+ *  2. A device-resident case context (bcmg_case_*): the state stays in HBM,
+ *     one call advances whole dual-time steps (optionally replayed from a
+ *     captured CUDA graph), and only the norms and snapshots cross to the
+ *     host.
+ *
+ * All functions are thread-compatible, not thread-safe: one caller thread
+ * per context (the reference is single-threaded at its call sites).
+ */
+#ifndef BCM_GB300_H
+#define BCM_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ----------------------------------------------------------------------- */
+/* Status                                                                  */
+/* ----------------------------------------------------------------------- */
+#define BCMG_OK 0
+#define BCMG_ERR_ARG 1        /* invalid argument / unsupported input */
+#define BCMG_ERR_CUDA 2       /* CUDA runtime error */
+#define BCMG_ERR_UNSUPPORTED 3 /* feature not available (e.g. multi-rank exchange) */
+
+/* Last error message of the calling thread, or NULL if the last call on
+ * this thread succeeded. */
+const char *bcmg_last_error(void);
+
+/* Library version string. */
+const char *bcmg_version(void);
+
+/* ----------------------------------------------------------------------- */
+/* Reference compile-time configuration (Resolution.h / prm.h).            */
+/* ----------------------------------------------------------------------- */
+typedef struct bcmg_reference_config {
+  int ncube_x;    /* NcubeX (Resolution.h:9); interior cells per cube edge */
+  int mpi_ncube;  /* MPI_Ncube (Resolution.h:3); norm normaliser */
+  double mu_L;    /* prm.h:5; 0 selects the inviscid kernel */
+  double rho0;    /* prm.h:27 */
+  double U0;      /* prm.h:29 */
+  double Uin;     /* prm.h:31 */
+  double P0;      /* prm.h:37 */
+} bcmg_reference_config;
+
+/* Sets the configuration the drop-in twins use; returns BCMG_OK. */
+int bcmg_set_reference_config(const bcmg_reference_config *cfg);
+void bcmg_get_reference_config(bcmg_reference_config *cfg);
+
+/* ----------------------------------------------------------------------- */
+/* 1. Drop-in twins of the reference routines                              */
+/* ----------------------------------------------------------------------- */
+
+/* Replaces BCM_Flux_XYZ_Viscous_Runge_kutta (main.h:473-513,
+ * BCM_Flux_XYZ_Viscous_Runge_kutta.cpp:18-2659): one RK stage of residual,
+ * pointwise-preconditioned increment and stage combination; at RK == 3 also
+ * the change norms er[1..5] and force sums er[6..7].  Bit-identical to the
+ * reference for U1_, U1p1, U1p2, Rku1 and Residual1.  csl is unused, as in
+ * the reference. */
+void BCM_Flux_XYZ_Viscous_Runge_kutta(int myid, int ncube, int RK, double deltaT,
+                                      double deltaTau, double e, int *FWS, int *csl,
+                                      double *cube_size, double *U1_, double *U1, double *U1q,
+                                      double *U1p1, double *U1p2, double *Rku1,
+                                      double *Residual1, double *er);
+
+/* Replaces BCM_X_boundary_condition (main.h:418-434,
+ * BCM_X_boundary_condition.cpp:19-122).  Xbc_l/Xbc_u are 1-based lists. */
+void BCM_X_boundary_condition(int myid, int nXbc_l, int nXbc_u, int *Xbc_l, int *Xbc_u,
+                              double *U1_);
+/* Replaces BCM_Y_boundary_condition (main.h:439-451, BCM_Y_boundary_condition.cpp:17-89). */
+void BCM_Y_boundary_condition(int nYbc_l, int nYbc_u, int *Ybc_l, int *Ybc_u, double *U1_);
+/* Replaces BCM_Z_boundary_condition (main.h:459-470, BCM_Z_boundary_condition.cpp:20-96). */
+void BCM_Z_boundary_condition(int nZbc_l, int nZbc_u, int *Zbc_l, int *Zbc_u, double *U1_);
+
+/* Replace BCM_Ghostcell_minus / BCM_Ghostcell_plus (main.h:378-413,
+ * BCM_Ghostcell_minus.cpp:17-495, BCM_Ghostcell_plus.cpp:16-489).  Tables
+ * are the 1-based packed arrays of BCM_Reading_IBM.cpp:53-73; entries are
+ * applied with the reference's serial-order semantics. */
+void BCM_Ghostcell_minus(int myid, int *NNBC, double *weight, int *GCindex, int *IPsur,
+                         int *FWS, double *U1_);
+void BCM_Ghostcell_plus(int myid, int *NNBC, double *weight, int *GCindex, int *IPsur,
+                        int *FWS, double *U1_);
+
+/* Replaces BCM_Interface (main.h:224-354, BCM_Interface.cpp:27-5735) with
+ * its full parameter list.  Single process: the cross-rank exchange lists
+ * must be empty (ncpu_bs == ncpu_eq == ncpu_sb == 0), otherwise the call
+ * fails with BCMG_ERR_UNSUPPORTED and leaves U1_ untouched.  Level-jump
+ * lists (bs/sb) are not supported yet and fail the same way. */
+void BCM_Interface(int myid, int ncube, int mPI_Nadj, int ncpu_bs, int ncpu_eq, int ncpu_sb,
+                   int max_nei_bs, int max_nei_eq, int max_nei_sb, int nadjX_eq, int nadjY_eq,
+                   int nadjZ_eq, int nadjX_bs_plus, int nadjX_sb_plus, int nadjX_bs_minus,
+                   int nadjX_sb_minus, int nadjY_bs_plus, int nadjY_sb_plus,
+                   int nadjY_bs_minus, int nadjY_sb_minus, int nadjZ_bs_plus,
+                   int nadjZ_sb_plus, int nadjZ_bs_minus, int nadjZ_sb_minus, int *rank_map,
+                   int *MPI_cpu, int *MPI_cube, int *MPI_cpu_adj, int *MPI_cube_adj,
+                   int *MPI_direction, int *MPI_interface, int *neighbor_cpu_eq,
+                   int *Ncube_Ncpu_eq, int *neighbor_cpu_sb, int *Ncube_Ncpu_sb,
+                   int *neighbor_cpu_bs, int *Ncube_Ncpu_bs, int *Scube_Ncpu_eq,
+                   int *Rcube_Ncpu_eq, double *send_data_curr_eq, double *recv_data_curr_eq,
+                   double *send_data_neig_eq, double *recv_data_neig_eq, int *Sdir_eq,
+                   int *Rdir_eq, int *Scube_Ncpu_sb, int *Rcube_Ncpu_sb,
+                   double *send_data_curr_sb, double *recv_data_curr_sb,
+                   double *send_data_neig_sb, double *recv_data_neig_sb, int *Sdir_sb,
+                   int *Rdir_sb, int *Scube_Ncpu_bs, int *Rcube_Ncpu_bs,
+                   double *send_data_curr_bs, double *recv_data_curr_bs,
+                   double *send_data_neig_bs, double *recv_data_neig_bs, int *Sdir_bs,
+                   int *Rdir_bs, int *ist_eq, int *ist_sb, int *ist_bs, int *adjN_sb,
+                   int *RadjN_bs, int *SadjN_bs, int *csl, int *adj_number, int *adjX_eq,
+                   int *adjY_eq, int *adjZ_eq, int *adjX_bs_plus, int *adjX_sb_plus,
+                   int *adjX_bs_minus, int *adjX_sb_minus, int *adjY_bs_plus,
+                   int *adjY_sb_plus, int *adjY_bs_minus, int *adjY_sb_minus,
+                   int *adjZ_bs_plus, int *adjZ_sb_plus, int *adjZ_bs_minus,
+                   int *adjZ_sb_minus, double *U1_);
+
+/* ----------------------------------------------------------------------- */
+/* 2. Device-resident case context                                         */
+/* ----------------------------------------------------------------------- */
+#define BCMG_PRECISION_FP64 0  /* bit-exact with the reference */
+#define BCMG_PRECISION_SPLIT 1 /* FP32 fluxes/preconditioner, FP64 state/source/norms */
+
+typedef struct bcmg_case_desc {
+  int n;          /* interior cells per cube edge */
+  int ncube;      /* cube slots including the unused slot 0 (reference Ncube) */
+  int mpi_ncube;  /* norm normaliser */
+  double mu_L, rho0, U0, Uin, P0;
+  double deltaT, deltaTau, e;
+  int precision;  /* BCMG_PRECISION_* */
+  const double *cube_size; /* [ncube] */
+  const int *csl;          /* [ncube] */
+  const int *adj_number;   /* [ncube][5][7] */
+  const int *FWS;          /* [ncube][S][S][S] */
+  /* Boundary-cube lists, 0-based arrays of cube numbers (main.cpp:147-189). */
+  int nxl, nxu, nyl, nyu, nzl, nzu;
+  const int *xl, *xu, *yl, *yu, *zl, *zu;
+  /* IBM ghost tables, 1-based packed (BCM_Reading_IBM.cpp). */
+  int nminus;
+  const double *w_minus;
+  const int *gc_minus, *ip_minus;
+  int nplus;
+  const double *w_plus;
+  const int *gc_plus, *ip_plus;
+} bcmg_case_desc;
+
+typedef struct bcmg_case bcmg_case;
+
+/* Creates a context on the current CUDA device and uploads geometry and
+ * tables.  The state arrays are allocated and zeroed. */
+int bcmg_case_create(const bcmg_case_desc *desc, bcmg_case **out);
+void bcmg_case_destroy(bcmg_case *c);
+
+/* Host <-> device state (full padded arrays, reference layout).  Any
+ * pointer may be NULL to skip that array. */
+int bcmg_case_set_state(bcmg_case *c, const double *U1_, const double *U1, const double *U1q);
+int bcmg_case_get_state(bcmg_case *c, double *U1_, double *U1, double *U1q);
+/* Scratch arrays as the reference keeps them (for parity checks). */
+int bcmg_case_get_scratch(bcmg_case *c, double *U1p1, double *U1p2, double *Rku1,
+                          double *Residual1);
+
+/* One stage of the reference loop (main.cpp:1161-1241): BCs, IBM ghosts,
+ * interface, flux/RK stage, interface. */
+int bcmg_case_stage(bcmg_case *c, int RK);
+
+/* `steps` dual-time steps of `subiters` sub-iterations each, followed by the
+ * time-level shift (main.cpp:1146-1357).  use_graph != 0 captures one step
+ * as a CUDA graph on first use and replays it.  er (8 doubles, 1-based like
+ * the reference) and emax (6 doubles, E1..E5 at 1..5) are updated on the
+ * host when non-NULL; emax carries the running maxima across calls. */
+int bcmg_case_advance(bcmg_case *c, int steps, int subiters, int use_graph, double *er,
+                      double *emax);
+
+/* Waits for all work of the context. */
+int bcmg_case_sync(bcmg_case *c);
+
+/* Device pointers of the state arrays (for zero-copy use by the caller). */
+int bcmg_case_device_state(bcmg_case *c, double **U1_, double **U1, double **U1q);
+
+/* Number of kernel launches issued by the last bcmg_case_advance call
+ * (counted on the host, graph replays count their nodes). */
+long long bcmg_case_launch_count(const bcmg_case *c);
+
+/* Times `reps` launches of the flux kernel alone on the current state with
+ * CUDA events on the context's stream; returns the average milliseconds per
+ * launch in *ms (the launch covers every cube once, RK stage 1 arithmetic,
+ * increments only: the state is not modified). */
+int bcmg_case_time_flux(bcmg_case *c, int reps, double *ms);
+
+/* Per-launch timing of the flux kernel inside bcmg_case_advance: with
+ * profiling on, CUDA events on the context's stream bracket every flux
+ * launch (graphs are not used while profiling).  bcmg_case_profile returns
+ * the accumulated milliseconds and launch count since profiling was
+ * (re)enabled. */
+int bcmg_case_set_profiling(bcmg_case *c, int on);
+int bcmg_case_profile(const bcmg_case *c, double *flux_ms_total, long long *flux_launches);
+
+/* ----------------------------------------------------------------------- */
+/* Host-side table builders (no GPU needed)                                */
+/* ----------------------------------------------------------------------- */
+
+/* Dependency levels of an IBM ghost table (1-based packed GCindex/IPsur of
+ * nbc entries, cube resolution n, ncube slots).  Entries of one level are
+ * independent; applying levels 1, 2, ... reproduces the reference's serial
+ * loop (BCM_Ghostcell_minus.cpp:72).  level_of_entry[e-1] receives entry e's
+ * level.  Returns the number of levels, or -1 for invalid input (an index
+ * outside the case's arrays). */
+int bcmg_ibm_schedule(int nbc, const int *GCindex, const int *IPsur, int n, int ncube,
+                      int *level_of_entry);
+
+/* Same-level interface copy tasks derived from adj_number/csl like
+ * BCM_Interface_table.cpp:96-208: task_off[ncube+1] (CSR by destination
+ * cube) and task_words[3*t..] = (source cube, axis 0..2, side 0 low / 1 high
+ * ghost layers).  Returns the task count, -1 for invalid input or a level
+ * jump, -2 if max_tasks is too small. */
+int bcmg_interface_tasks(int ncube, const int *adj_number, const int *csl, int *task_off,
+                         int *task_words, int max_tasks);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

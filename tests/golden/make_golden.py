@@ -1,0 +1,67 @@
+"""Generate tests/golden/golden.json from the REFERENCE's own compiled code.
+
+Runs each case of golden_cases.py through oracle/_ref (the reference's
+BCM_*.cpp compiled from /root/reference by oracle/ref_build.py, one OpenMP
+thread so its norm sums are serial) and records SHA-256 digests of every
+output array plus the norms.  Run here, where the reference sources exist:
+
+    python tests/golden/make_golden.py
+"""
+import hashlib
+import json
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path[:0] = [ROOT, os.path.join(ROOT, "oracle"), HERE]
+
+import numpy as np  # noqa: E402
+
+import oracle as O  # noqa: E402
+from golden_cases import RUN_STEPS, RUN_SUBITERS, canonical, golden_cases  # noqa: E402
+
+
+def digest(a):
+    return hashlib.sha256(canonical(a)).hexdigest()
+
+
+def main():
+    out = {}
+    for name, case in golden_cases().items():
+        ref = O.Ref(case)
+        ref.set_threads(1)
+        rec = {}
+        # single routines on the initial state
+        for r, fn in (("bc", lambda s: ref.bc(case, s.U1_)),
+                      ("ghost_minus", lambda s: ref.ghost(case, s.U1_, -1)),
+                      ("ghost_plus", lambda s: ref.ghost(case, s.U1_, 1)),
+                      ("interface", lambda s: ref.interface(case, s.U1_))):
+            st = O.State(case)
+            fn(st)
+            rec[r] = digest(st.U1_)
+        # three flux stages on the initial state
+        st = O.State(case)
+        for RK in (1, 2, 3):
+            ref.flux_stage(case, st, RK)
+            rec[f"flux{RK}"] = {k: digest(getattr(st, k))
+                                for k in ("U1_", "Rku1", "Residual1", "U1p1", "U1p2")}
+        rec["flux3_er"] = [repr(float(x)) for x in st.er]
+        # full loop
+        st = O.State(case)
+        ref.run(case, st, RUN_STEPS, RUN_SUBITERS)
+        rec["run"] = {k: digest(getattr(st, k)) for k in ("U1_", "U1", "U1q", "Rku1",
+                                                          "Residual1")}
+        rec["run_er"] = [repr(float(x)) for x in st.er]
+        rec["run_emax"] = [repr(float(x)) for x in st.Emax]
+        rec["run_sum"] = [repr(float(x)) for x in st.U1_.reshape(-1, 5).sum(axis=0)]
+        out[name] = rec
+        print(name, "done", file=sys.stderr)
+    with open(os.path.join(HERE, "golden.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py (reference compiled by "
+                                "oracle/ref_build.py, OMP_NUM_THREADS=1)",
+                   "steps": RUN_STEPS, "subiters": RUN_SUBITERS, "cases": out}, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,89 @@
+"""Pin the oracle (the C restatement in oracle/bcm_oracle.c) against the
+reference's own outputs: digests recorded by tests/golden/make_golden.py
+from the reference's compiled sources, and, where the reference sources are
+present, a direct bit-for-bit comparison on more random cases."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from golden import golden_cases as G
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = json.load(open(os.path.join(HERE, "golden", "golden.json")))
+
+
+def digest(a):
+    return hashlib.sha256(G.canonical(a)).hexdigest()
+
+
+@pytest.fixture(scope="module")
+def port():
+    p = O.Port()
+    p.set_threads(4)
+    return p
+
+
+@pytest.mark.parametrize("name", sorted(GOLD["cases"]))
+def test_routines_match_reference_digests(port, name):
+    case = G.golden_cases()[name]
+    rec = GOLD["cases"][name]
+    for r, fn in (("bc", lambda s: port.bc(case, s.U1_)),
+                  ("ghost_minus", lambda s: port.ghost(case, s.U1_, -1)),
+                  ("ghost_plus", lambda s: port.ghost(case, s.U1_, 1)),
+                  ("interface", lambda s: port.interface(case, s.U1_))):
+        st = O.State(case)
+        fn(st)
+        assert digest(st.U1_) == rec[r], f"{name}: {r} differs from the reference"
+    st = O.State(case)
+    for RK in (1, 2, 3):
+        port.flux_stage(case, st, RK)
+        for k, d in rec[f"flux{RK}"].items():
+            assert digest(getattr(st, k)) == d, f"{name}: flux stage {RK} {k}"
+    assert [repr(float(x)) for x in st.er] == rec["flux3_er"]
+
+
+@pytest.mark.parametrize("name", sorted(GOLD["cases"]))
+def test_full_loop_matches_reference_digests(port, name):
+    case = G.golden_cases()[name]
+    rec = GOLD["cases"][name]
+    st = O.State(case)
+    port.run(case, st, GOLD["steps"], GOLD["subiters"])
+    for k, d in rec["run"].items():
+        assert digest(getattr(st, k)) == d, f"{name}: run {k}"
+    assert [repr(float(x)) for x in st.er] == rec["run_er"]
+    assert [repr(float(x)) for x in st.Emax] == rec["run_emax"]
+
+
+@pytest.mark.skipif(not O.reference_available(), reason="reference sources not on this host")
+@pytest.mark.parametrize("seed", [21, 22, 23])
+def test_port_equals_reference_directly(port, seed):
+    from bcm_cgli_gb300 import cases
+    case = cases.random_case(seed=seed, n=4, periodic=bool(seed % 2), viscous=True)
+    ref = O.Ref(case)
+    ref.set_threads(1)
+    a, b = O.State(case), O.State(case)
+    port.run(case, a, 1, 2)
+    ref.run(case, b, 1, 2)
+    for k in ("U1_", "U1", "U1q", "Rku1", "Residual1", "U1p1", "U1p2"):
+        assert np.array_equal(getattr(a, k), getattr(b, k)), k
+    assert np.array_equal(a.er, b.er)
+
+
+def test_oracle_thread_count_invariant():
+    """The restatement's results do not depend on its thread count (its
+    order-sensitive sums are serial), unlike the reference's racy norms."""
+    from bcm_cgli_gb300 import cases
+    case = cases.random_case(seed=5, n=4)
+    p = O.Port()
+    out = []
+    for t in (1, 3):
+        p.set_threads(t)
+        st = O.State(case)
+        p.run(case, st, 1, 1)
+        out.append((st.U1_.copy(), st.er.copy()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
