@@ -206,8 +206,15 @@ class CaseContext:
         check(lib().bcmg_case_set_state(self.h, ptr(U1_), ptr(U1), ptr(U1q)))
         del keep
 
-    def get_state(self):
-        out = [np.empty(self.shape) for _ in range(3)]
+    def get_state(self, out=None):
+        """(U1_, U1, U1q) copied to host; `out` may supply the three arrays
+        (e.g. pinned buffers)."""
+        if out is None:
+            out = [np.empty(self.shape) for _ in range(3)]
+        for a in out:
+            _dp(a)
+            if a.shape != tuple(self.shape):
+                raise BcmgError("output array has the wrong shape")
         check(lib().bcmg_case_get_state(self.h, *(a.ctypes.data for a in out)))
         return out
 
@@ -244,3 +251,18 @@ class CaseContext:
         n = C.c_longlong()
         check(lib().bcmg_case_profile(self.h, C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+    def timer_mark(self, slot):
+        check(lib().bcmg_case_timer_mark(self.h, int(slot)))
+
+    def timer_elapsed(self, a, b):
+        ms = C.c_double()
+        check(lib().bcmg_case_timer_elapsed(self.h, int(a), int(b), C.byref(ms)))
+        return ms.value
+
+
+def probe_fp64_gflops():
+    """Measured FP64 FMA rate of the current GPU (GFLOP/s)."""
+    g = C.c_double()
+    check(lib().bcmg_probe_fp64_rate(C.byref(g)))
+    return g.value

@@ -23,6 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # (source, extra nvcc flags)
 UNITS = [
     ("bcm_flux_fp64.cu", ["--fmad=false"]),
+    ("bcm_flux_split.cu", []),
     ("bcm_rk.cu", ["--fmad=false"]),
     ("bcm_halo.cu", ["--fmad=false"]),
     ("bcm_capi.cu", ["--fmad=false"]),

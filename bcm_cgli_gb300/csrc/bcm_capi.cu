@@ -149,6 +149,7 @@ struct bcmg_case {
   cudaStream_t stream = nullptr;
   double *U1_ = nullptr, *U1 = nullptr, *U1q = nullptr, *U1p1 = nullptr, *U1p2 = nullptr,
          *Rku1 = nullptr, *Residual1 = nullptr;
+  float *M = nullptr, *Rku32 = nullptr;  // split precision: FP32 deltas, increments
   int *FWS = nullptr;
   double *cube_size = nullptr;
   int *task_off = nullptr;
@@ -167,13 +168,18 @@ struct bcmg_case {
   size_t ev_used = 0;
   double flux_ms = 0;
   long long flux_launches = 0;
+  std::vector<cudaEvent_t> marks;  // bcmg_case_timer_mark slots
 
   void release() {
+    for (auto x : marks)
+      if (x) cudaEventDestroy(x);
+    marks.clear();
     if (graph) cudaGraphExecDestroy(graph);
     graph = nullptr;
     for (auto x : ev) cudaEventDestroy(x);
     ev.clear();
     dfree(U1_); dfree(U1); dfree(U1q); dfree(U1p1); dfree(U1p2); dfree(Rku1); dfree(Residual1);
+    dfree(M); dfree(Rku32);
     dfree(FWS); dfree(cube_size); dfree(task_off); dfree(tasks); dfree(bc_cubes);
     dfree(bc_masks); dfree(partials); dfree(er); dfree(emax);
     ibm.release();
@@ -210,7 +216,27 @@ int case_flux(bcmg_case *c) {
     c->ev_used += 2;
     CK(cudaEventRecord(e0, c->stream));
   }
-  CK(launch_flux_fp64(a, c->ncube - 1, c->stream));
+  if (c->precision == BCMG_PRECISION_SPLIT) {
+    CK(launch_mirror(c->U1_, c->M, c->ph.n, c->ncube, c->ph.rho0, c->ph.P0, c->stream));
+    ++c->launches;
+    FluxSplitArgs sa;
+    sa.ph = c->ph;
+    sa.cube0 = 1;
+    sa.dT = c->dT;
+    sa.dTau = c->dTau;
+    sa.ef = (float)c->e;
+    sa.FWS = c->FWS;
+    sa.cube_size = c->cube_size;
+    sa.M = c->M;
+    sa.U1_ = c->U1_;
+    sa.U1 = c->U1;
+    sa.U1q = c->U1q;
+    sa.Rku32 = c->Rku32;
+    sa.Residual1 = c->Residual1;
+    CK(launch_flux_split(sa, c->ncube - 1, c->stream));
+  } else {
+    CK(launch_flux_fp64(a, c->ncube - 1, c->stream));
+  }
   if (c->profile) CK(cudaEventRecord(e1, c->stream));
   ++c->launches;
   return BCMG_OK;
@@ -258,7 +284,20 @@ int case_stage(bcmg_case *c, int RK) {
   k.Residual1 = c->Residual1;
   k.partials = c->partials;
   int nb = 0;
-  CK(launch_rk(k, &nb, c->stream));
+  if (c->precision == BCMG_PRECISION_SPLIT) {
+    RkSplitArgs ks;
+    ks.ph = c->ph;
+    ks.ncube = c->ncube;
+    ks.RK = RK;
+    ks.FWS = c->FWS;
+    ks.U1_ = c->U1_;
+    ks.Rku32 = c->Rku32;
+    ks.Residual1 = c->Residual1;
+    ks.partials = c->partials;
+    CK(launch_rk_split(ks, &nb, c->stream));
+  } else {
+    CK(launch_rk(k, &nb, c->stream));
+  }
   ++c->launches;
   if (RK == 3) {
     CK(launch_norms(c->ph, c->partials, nb, c->er, c->stream));
@@ -308,8 +347,8 @@ int bcmg_case_create(const bcmg_case_desc *d, bcmg_case **out) {
     set_err("ncube < 2 or missing geometry arrays");
     return BCMG_ERR_ARG;
   }
-  if (d->precision != BCMG_PRECISION_FP64) {
-    set_err("unknown or unavailable precision");
+  if (d->precision != BCMG_PRECISION_FP64 && d->precision != BCMG_PRECISION_SPLIT) {
+    set_err("unknown precision");
     return BCMG_ERR_ARG;
   }
   for (int i = 1; i < d->ncube; ++i)
@@ -374,6 +413,11 @@ int bcmg_case_create(const bcmg_case_desc *d, bcmg_case **out) {
             ck(dalloc(&c->bc_masks, bcm.size()), "alloc") &&
             ck(dalloc(&c->er, 8), "alloc") && ck(dalloc(&c->emax, 6), "alloc");
   if (!ok) return fail(BCMG_ERR_CUDA);
+  if (d->precision == BCMG_PRECISION_SPLIT &&
+      !(ck(dalloc(&c->M, nd), "alloc") && ck(dalloc(&c->Rku32, nd), "alloc") &&
+        ck(cudaMemset(c->M, 0, nd * sizeof(float)), "memset") &&
+        ck(cudaMemset(c->Rku32, 0, nd * sizeof(float)), "memset")))
+    return fail(BCMG_ERR_CUDA);
   RkArgs probe{};
   probe.ph = c->ph;
   probe.ncube = c->ncube;
@@ -513,7 +557,8 @@ int bcmg_case_advance(bcmg_case *c, int steps, int subiters, int use_graph, doub
     {
       // kernel nodes per step, counted like case_step
       int L = (int)(c->ibm.level_off.size() > 0 ? c->ibm.level_off.size() - 1 : 0);
-      long long stage = (c->nbc > 0) + L + 1 + 1 + 1 + 1;
+      long long stage = (c->nbc > 0) + L + 1 + 1 + 1 + 1 +
+                        (c->precision == BCMG_PRECISION_SPLIT ? 1 : 0);
       per = subiters * (3 * stage + 1 + 1) + 1;
     }
     for (int s = 0; s < steps; ++s) CK(cudaGraphLaunch(c->graph, c->stream));
@@ -982,6 +1027,85 @@ void BCM_Interface(int myid, int ncube, int mPI_Nadj, int ncpu_bs, int ncpu_eq, 
     return BCMG_OK;
   };
   run();
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Timing helpers: CUDA events on the context's stream, and a measured FP64
+// FMA rate (the ALU roof of the FP64 path; GB300's FP64 rate is a small
+// fraction of its FP32 rate).
+// ===========================================================================
+namespace {
+__global__ void k_dfma_chain(double *out, int iters, double a, double b) {
+  // 8 independent FMA chains per thread keep the FP64 pipe busy.
+  double x[8];
+#pragma unroll
+  for (int m = 0; m < 8; ++m) x[m] = threadIdx.x * 1e-9 + m;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int m = 0; m < 8; ++m) x[m] = fma(x[m], a, b);
+  }
+  double s = 0;
+#pragma unroll
+  for (int m = 0; m < 8; ++m) s += x[m];
+  if (s == 12345.678) out[0] = s;  // keeps the chains alive
+}
+}  // namespace
+
+extern "C" {
+
+int bcmg_case_timer_mark(bcmg_case *c, int slot) {
+  clear_err();
+  if (!c || slot < 0 || slot > 15) { set_err("bad timer slot"); return BCMG_ERR_ARG; }
+  static_assert(sizeof(cudaEvent_t) == sizeof(void *), "event handle size");
+  if (c->marks.empty()) {
+    c->marks.resize(16, nullptr);
+  }
+  if (!c->marks[slot]) CK(cudaEventCreate(&c->marks[slot]));
+  CK(cudaEventRecord(c->marks[slot], c->stream));
+  return BCMG_OK;
+}
+
+int bcmg_case_timer_elapsed(bcmg_case *c, int a, int b, double *ms) {
+  clear_err();
+  if (!c || !ms || a < 0 || b < 0 || a > 15 || b > 15 || c->marks.empty() || !c->marks[a] ||
+      !c->marks[b]) {
+    set_err("timer marks not recorded");
+    return BCMG_ERR_ARG;
+  }
+  CK(cudaEventSynchronize(c->marks[b]));
+  float t = 0;
+  CK(cudaEventElapsedTime(&t, c->marks[a], c->marks[b]));
+  *ms = t;
+  return BCMG_OK;
+}
+
+int bcmg_probe_fp64_rate(double *gflops) {
+  clear_err();
+  if (!gflops) { set_err("null argument"); return BCMG_ERR_ARG; }
+  int dev = 0, sms = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  double *out;
+  CK(cudaMalloc(&out, sizeof(double)));
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  const int blocks = sms * 4, threads = 256, iters = 4096;
+  k_dfma_chain<<<blocks, threads>>>(out, 64, 1.0000001, 1e-9);  // warm-up
+  CK(cudaEventRecord(a));
+  k_dfma_chain<<<blocks, threads>>>(out, iters, 1.0000001, 1e-9);
+  CK(cudaEventRecord(b));
+  CK(cudaEventSynchronize(b));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(out);
+  const double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
+  *gflops = flops / (ms * 1e-3) / 1e9;
+  return BCMG_OK;
 }
 
 }  // extern "C"

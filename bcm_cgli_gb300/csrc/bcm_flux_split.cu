@@ -1,0 +1,521 @@
+// Split-precision residual + preconditioned increment, and its stage update.
+//
+// Same operator as BCM_Flux_XYZ_Viscous_Runge_kutta (BCM_Flux_XYZ_Viscous_
+// Runge_kutta.cpp:326-2652) with the arithmetic split by where precision is
+// needed:
+//  * FP64: the conservative state Q (HBM), the time-level differences
+//    Q - Q^n and Q^n - Q^(n-1) of the BDF2 source (the cancellation in
+//    3Q - 4Q^n + Q^(n-1)), the state update Q += w * dQ, and the sums of the
+//    residual/force norms;
+//  * FP32: reconstruction, the preconditioned Roe flux, viscous gradients and
+//    stresses, the residual sum and the pointwise 5x5 preconditioner.
+// FP32 works on deltas from a per-case reference state (rho0, 0, 0, 0,
+// P0/(K-1)) formed in FP64 (k_mirror), so pressure jumps are p' = p - P0
+// differences and temperatures T' = T - T0 are O(1) numbers instead of
+// 1e5 Pa / 300 K values whose FP32 rounding would swamp the low-Mach jumps.
+// The constant P0 cancels exactly in every face-flux difference, so the
+// momentum and force terms use p'.  The preconditioner's
+// temp3 = H - H*K - VV + K*(T+VV) is formed as its exact identity
+// 0.5*(K-1)*VV (C = K*T), avoiding a 1e5-scale cancellation in FP32.
+#include <cuda_runtime.h>
+
+#include "bcm_common.cuh"
+#include "bcm_kernels.h"
+
+namespace bcmg {
+
+// ---------------------------------------------------------------------------
+// FP64 -> FP32 deltas of the state, all cells of all cubes (ghosts included).
+// ---------------------------------------------------------------------------
+__global__ void k_mirror(const double *__restrict__ U, float *__restrict__ M, size_t ncell_from,
+                         size_t ncell_to, double rho0, double E0) {
+  for (size_t c = ncell_from + blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < ncell_to;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const double *q = U + 5 * c;
+    float *m = M + 5 * c;
+    m[0] = (float)(q[0] - rho0);
+    m[1] = (float)q[1];
+    m[2] = (float)q[2];
+    m[3] = (float)q[3];
+    m[4] = (float)(q[4] - E0);
+  }
+}
+
+cudaError_t launch_mirror(const double *U, float *M, int n, int ncube, double rho0, double P0,
+                          cudaStream_t s) {
+  const size_t S = n + 4;
+  const size_t from = S * S * S, to = (size_t)ncube * S * S * S;  // skip cube slot 0
+  if (to <= from) return cudaSuccess;
+  const size_t cnt = to - from;
+  int blocks = (int)((cnt + 255) / 256);
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  k_mirror<<<blocks, 256, 0, s>>>(U, M, from, to, rho0, P0 / (BCMG_K - 1));
+  return cudaGetLastError();
+}
+
+struct PrimF {
+  float U, V, W, Tp;  // velocity, T - T0
+};
+
+template <int T>
+struct SplitSmem {
+  static constexpr int B = T + 2;
+  static constexpr int nPrim = B * B * B;
+  static constexpr int nCell = T * T * T;
+  static constexpr size_t bytes = sizeof(PrimF) * nPrim + 2 * sizeof(float) * 5 * nCell +
+                                  2 * sizeof(float) * nCell;
+};
+
+// Delta-form preconditioned Roe flux (same formulas as face_flux in
+// bcm_common.cuh, evaluated on deltas from the reference state).  Returns the
+// flux with P replaced by p' in the momentum terms (P0 cancels in every face
+// difference) and dPp = 0.5*(p'_L + p'_R).
+template <int AX>
+__device__ __forceinline__ void face_flux_delta(const float *ML, const float *MR, float e,
+                                                float rho0, float P0, float *F, float &dPp) {
+  const float K = 1.4f, Km1 = 0.4f;
+  float dU1 = MR[0] - ML[0], dU2 = MR[1] - ML[1], dU3 = MR[2] - ML[2], dU4 = MR[3] - ML[3],
+        dU5 = MR[4] - ML[4];
+  float _rho = rho0 + ML[0];
+  float _ir = 1.0f / _rho;
+  float _U = ML[1] * _ir, _V = ML[2] * _ir, _W = ML[3] * _ir;
+  float _VV = _U * _U + _V * _V + _W * _W;
+  float _pp = (ML[4] - 0.5f * _rho * _VV) * Km1;  // p' = p - P0
+  float _P = P0 + _pp;
+  float _C = K * _P * _ir;
+  float _H = 0.5f * _VV + _C * (1.0f / Km1);
+  float rho_ = rho0 + MR[0];
+  float ir_ = 1.0f / rho_;
+  float U_ = MR[1] * ir_, V_ = MR[2] * ir_, W_ = MR[3] * ir_;
+  float VV_ = U_ * U_ + V_ * V_ + W_ * W_;
+  float pp_ = (MR[4] - 0.5f * rho_ * VV_) * Km1;
+  float P_ = P0 + pp_;
+  float C_ = K * P_ * ir_;
+  float H_ = 0.5f * VV_ + C_ * (1.0f / Km1);
+  float temp5 = sqrtf(_rho), temp6 = sqrtf(rho_);
+  float it4 = 1.0f / (temp5 + temp6);
+  float rho = temp5 * temp6;
+  float U = (temp5 * _U + temp6 * U_) * it4;
+  float V = (temp5 * _V + temp6 * V_) * it4;
+  float W = (temp5 * _W + temp6 * W_) * it4;
+  float VV = U * U + V * V + W * W;
+  float H = (temp5 * _H + temp6 * H_) * it4;
+  float C = (H - 0.5f * VV) * Km1;
+  float q = VV / C;
+  float beta = q > e ? q : e;
+  const float un = AX == 0 ? U : (AX == 1 ? V : W);
+  const float _un = AX == 0 ? _U : (AX == 1 ? _V : _W);
+  const float un_ = AX == 0 ? U_ : (AX == 1 ? V_ : W_);
+  float temp = 0.5f * (1.0f + beta) * un;
+  float Sp = 0.5f * sqrtf(4.0f * beta * C + un * un * (1.0f - beta) * (1.0f - beta));
+  float iS = 1.0f / Sp;
+  float dp = pp_ - _pp;
+  float temp1 = dp / (rho * beta * C);
+  float tS = temp * iS;
+  float temp2 = tS * (un_ - _un);
+  float temp3 = 0.5f * (1.0f - beta) * un * temp * iS;
+  float an = fabsf(un);
+  float deltaU = (Sp - temp3 - beta * an) * temp1 + temp2;
+  float deltaP = tS * dp + (Sp - an + temp3) * rho * (un_ - _un);
+  float dr = deltaU * rho;
+  float Fav1 = an * dU1 + dr;
+  float Fav2 = an * dU2 + dr * U;
+  float Fav3 = an * dU3 + dr * V;
+  float Fav4 = an * dU4 + dr * W;
+  if (AX == 0) Fav2 += deltaP;
+  if (AX == 1) Fav3 += deltaP;
+  if (AX == 2) Fav4 += deltaP;
+  float Fav5 = an * dU5 + dr * H + deltaP * un;
+  F[0] = 0.5f * ((_rho * _un + rho_ * un_) - Fav1);
+  F[1] = AX == 0 ? 0.5f * ((_rho * _U * _U + _pp + rho_ * U_ * U_ + pp_) - Fav2)
+                 : 0.5f * ((_rho * _U * _un + rho_ * U_ * un_) - Fav2);
+  F[2] = AX == 1 ? 0.5f * ((_rho * _V * _V + _pp + rho_ * V_ * V_ + pp_) - Fav3)
+                 : 0.5f * ((_rho * _V * _un + rho_ * V_ * un_) - Fav3);
+  F[3] = AX == 2 ? 0.5f * ((_rho * _W * _W + _pp + rho_ * W_ * W_ + pp_) - Fav4)
+                 : 0.5f * ((_rho * _W * _un + rho_ * W_ * un_) - Fav4);
+  F[4] = 0.5f * ((_un * (3.5f * _P + 0.5f * _rho * _VV) + un_ * (3.5f * P_ + 0.5f * rho_ * VV_)) -
+                 Fav5);
+  dPp = 0.5f * (_pp + pp_);
+}
+
+template <int AX, bool FWD>
+__device__ __forceinline__ void visc_face_f(float mu_L, float T0, const PrimF &c, const PrimF &o,
+                                            float inv, const PrimF &a0, const PrimF &a1,
+                                            const PrimF &a2, const PrimF &a3, const PrimF &b0,
+                                            const PrimF &b1, const PrimF &b2, const PrimF &b3,
+                                            float *L) {
+  float Tm = T0 + 0.5f * (c.Tp + o.Tp);
+  float temp = Tm / T0;
+  float mu_E = mu_L * temp * sqrtf(temp) * (T0 + 110.f) / (Tm + 110.f);
+  float gn[4];
+  if (FWD) {
+    gn[0] = (o.U - c.U) * inv; gn[1] = (o.V - c.V) * inv;
+    gn[2] = (o.W - c.W) * inv; gn[3] = (o.Tp - c.Tp) * inv;
+  } else {
+    gn[0] = (c.U - o.U) * inv; gn[1] = (c.V - o.V) * inv;
+    gn[2] = (c.W - o.W) * inv; gn[3] = (c.Tp - o.Tp) * inv;
+  }
+  const float q = 0.25f * inv;
+  float ga[3], gb[3];
+  ga[0] = (a0.U + a1.U - a2.U - a3.U) * q;
+  ga[1] = (a0.V + a1.V - a2.V - a3.V) * q;
+  ga[2] = (a0.W + a1.W - a2.W - a3.W) * q;
+  gb[0] = (b0.U + b1.U - b2.U - b3.U) * q;
+  gb[1] = (b0.V + b1.V - b2.V - b3.V) * q;
+  gb[2] = (b0.W + b1.W - b2.W - b3.W) * q;
+  float d[3][3];
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    d[AX][m] = gn[m];
+    d[AX == 0 ? 1 : 0][m] = ga[m];
+    d[AX == 2 ? 1 : 2][m] = gb[m];
+  }
+  float div = d[0][0] + d[1][1] + d[2][2];
+  float Um = 0.5f * (c.U + o.U), Vm = 0.5f * (c.V + o.V), Wm = 0.5f * (c.W + o.W);
+  float s1, s2, s3;
+  if (AX == 0) {
+    s1 = mu_E * (2.f * d[0][0] - (2.f / 3.f) * div);
+    s2 = mu_E * (d[1][0] + d[0][1]);
+    s3 = mu_E * (d[2][0] + d[0][2]);
+  } else if (AX == 1) {
+    s1 = mu_E * (d[1][0] + d[0][1]);
+    s2 = mu_E * (2.f * d[1][1] - (2.f / 3.f) * div);
+    s3 = mu_E * (d[2][1] + d[1][2]);
+  } else {
+    s1 = mu_E * (d[2][0] + d[0][2]);
+    s2 = mu_E * (d[2][1] + d[1][2]);
+    s3 = mu_E * (2.f * d[2][2] - (2.f / 3.f) * div);
+  }
+  L[0] = s1;
+  L[1] = s2;
+  L[2] = s3;
+  L[3] = Um * s1 + Vm * s2 + Wm * s3 + mu_E * (float)(BCMG_CV * BCMG_K / BCMG_PR) * gn[3];
+}
+
+template <int T, bool VISCOUS>
+__global__ void __launch_bounds__(T *T *T, 1) k_flux_split(FluxSplitArgs a) {
+  using SM = SplitSmem<T>;
+  constexpr int B = SM::B;
+  constexpr int NT = T * T * T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  PrimF *prim = reinterpret_cast<PrimF *>(smem_raw);
+  float *Fb = reinterpret_cast<float *>(prim + SM::nPrim);
+  float *Ff = Fb + 5 * SM::nCell;
+  float *dPb = Ff + 5 * SM::nCell;
+  float *dPf = dPb + SM::nCell;
+
+  const int n = a.ph.n, S = n + 4, nx = n + 1;
+  const int nt = n / T;
+  const int tid = threadIdx.x;
+  const int tiles = nt * nt * nt;
+  const int cube = a.cube0 + blockIdx.x / tiles;
+  const int tl = blockIdx.x % tiles;
+  const int bi = 2 + (tl / (nt * nt)) * T, bj = 2 + ((tl / nt) % nt) * T, bk = 2 + (tl % nt) * T;
+  const float *__restrict__ M = a.M;
+  const int *__restrict__ F = a.FWS;
+  const size_t cb = cell_index(S, cube, 0, 0, 0);
+  const float rho0 = (float)a.ph.rho0, P0 = (float)a.ph.P0;
+  const float RT0 = (float)(a.ph.P0 / a.ph.rho0);  // R * T0
+  const float iR = (float)(1.0 / BCMG_R);
+
+  // Phase 1: primitives (u, v, w, T - T0) over the tile plus one halo cell.
+  for (int p = tid; p < SM::nPrim; p += NT) {
+    int li = p / (B * B), lj = (p / B) % B, lk = p % B;
+    const float *q =
+        M + 5 * (cb + ((size_t)(bi - 1 + li) * S + (bj - 1 + lj)) * S + (bk - 1 + lk));
+    float r = __ldg(q), m1 = __ldg(q + 1), m2 = __ldg(q + 2), m3 = __ldg(q + 3), e = __ldg(q + 4);
+    float rho = rho0 + r;
+    float ir = 1.0f / rho;
+    PrimF pr;
+    pr.U = m1 * ir;
+    pr.V = m2 * ir;
+    pr.W = m3 * ir;
+    float pp = (e - 0.5f * rho * (pr.U * pr.U + pr.V * pr.V + pr.W * pr.W)) * 0.4f;
+    pr.Tp = (pp - r * RT0) * ir * iR;  // T - T0 = (p' - rho' R T0) / (rho R)
+    prim[p] = pr;
+  }
+
+  const float dxf = (float)(a.cube_size[cube] / n);
+  const float inv = 1.0f / dxf;
+  float acc[5];
+  float dPdx = 0, dPdz = 0;
+
+#pragma unroll 1
+  for (int ax = 0; ax < 3; ++ax) {
+    for (int f = tid; f < (T + 1) * T * T; f += NT) {
+      const int fa = f / (T * T), p = (f / T) % T, q = f % T;
+      int li, lj, lk;
+      if (ax == 0) { li = fa; lj = p; lk = q; }
+      else if (ax == 1) { li = p; lj = fa; lk = q; }
+      else { li = p; lj = q; lk = fa; }
+      const int g = (ax == 0 ? bi + li : (ax == 1 ? bj + lj : bk + lk));
+      const ptrdiff_t stride = ax == 0 ? (ptrdiff_t)S * S : (ax == 1 ? (ptrdiff_t)S : 1);
+      const size_t c0 = cb + ((size_t)(bi + li) * S + (bj + lj)) * S + (bk + lk);
+      const int fm2 = __ldg(F + c0 - 2 * stride), fm1 = __ldg(F + c0 - stride),
+                f0 = __ldg(F + c0), fp1 = __ldg(F + c0 + stride);
+      const bool needB = fa < T, needF = fa > 0;
+      const int ob = order_backward(g, fm2, fm1, fp1);
+      const int of = order_forward(g, nx, fm2, f0, fp1);
+      const int slotB = (li * T + lj) * T + lk;
+      const int slotF = slotB - (ax == 0 ? T * T : (ax == 1 ? T : 1));
+      int nviews, ord0, ord1 = 0, dst0, dst1 = 0;
+      if (needB && needF && ob == of) { nviews = 1; ord0 = ob; dst0 = 3; }
+      else if (needB && needF) { nviews = 2; ord0 = ob; dst0 = 1; ord1 = of; dst1 = 2; }
+      else if (needB) { nviews = 1; ord0 = ob; dst0 = 1; }
+      else { nviews = 1; ord0 = of; dst0 = 2; }
+      const float *base = M + 5 * c0;
+      auto ld = [&](int d, int v) -> float { return __ldg(base + 5 * stride * d + v); };
+#pragma unroll 1
+      for (int w = 0; w < nviews; ++w) {
+        const int ord = w == 0 ? ord0 : ord1;
+        const int dst = w == 0 ? dst0 : dst1;
+        float ML[5], MR[5], Fx[5], dP;
+        recon<float>(ord, ld, ML, MR);
+        if (ax == 0) face_flux_delta<0>(ML, MR, a.ef, rho0, P0, Fx, dP);
+        else if (ax == 1) face_flux_delta<1>(ML, MR, a.ef, rho0, P0, Fx, dP);
+        else face_flux_delta<2>(ML, MR, a.ef, rho0, P0, Fx, dP);
+        if (dst & 1) {
+#pragma unroll
+          for (int v = 0; v < 5; ++v) Fb[5 * slotB + v] = Fx[v];
+          dPb[slotB] = dP;
+        }
+        if (dst & 2) {
+#pragma unroll
+          for (int v = 0; v < 5; ++v) Ff[5 * slotF + v] = Fx[v];
+          dPf[slotF] = dP;
+        }
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      float t = (Ff[5 * tid + v] - Fb[5 * tid + v]) * inv;
+      acc[v] = ax == 0 ? t : acc[v] + t;
+    }
+    if (ax == 0) dPdx = dPf[tid] - dPb[tid];
+    if (ax == 2) dPdz = dPf[tid] - dPb[tid];
+    __syncthreads();
+  }
+
+  const int mi = tid / (T * T), mj = (tid / T) % T, mk = tid % T;
+  auto P = [&](int di, int dj, int dk) -> const PrimF & {
+    return prim[((mi + 1 + di) * B + (mj + 1 + dj)) * B + (mk + 1 + dk)];
+  };
+  const PrimF &c = P(0, 0, 0);
+  float vF[5] = {0, 0, 0, 0, 0};
+  if (VISCOUS) {
+    const float T0 = (float)(a.ph.P0 / a.ph.rho0 / BCMG_R);
+    const float mu_L = (float)a.ph.mu_L;
+    float Lb[4], Lf[4], Mb[4], Mf[4], Nb[4], Nf[4];
+    visc_face_f<0, false>(mu_L, T0, c, P(-1, 0, 0), inv, P(0, 1, 0), P(-1, 1, 0), P(0, -1, 0),
+                          P(-1, -1, 0), P(0, 0, 1), P(-1, 0, 1), P(0, 0, -1), P(-1, 0, -1), Lb);
+    visc_face_f<0, true>(mu_L, T0, c, P(1, 0, 0), inv, P(0, 1, 0), P(1, 1, 0), P(0, -1, 0),
+                         P(1, -1, 0), P(0, 0, 1), P(1, 0, 1), P(0, 0, -1), P(1, 0, -1), Lf);
+    visc_face_f<1, false>(mu_L, T0, c, P(0, -1, 0), inv, P(1, 0, 0), P(1, -1, 0), P(-1, 0, 0),
+                          P(-1, -1, 0), P(0, 0, 1), P(0, -1, 1), P(0, 0, -1), P(0, -1, -1), Mb);
+    visc_face_f<1, true>(mu_L, T0, c, P(0, 1, 0), inv, P(1, 0, 0), P(1, 1, 0), P(-1, 0, 0),
+                         P(-1, 1, 0), P(0, 0, 1), P(0, 1, 1), P(0, 0, -1), P(0, 1, -1), Mf);
+    visc_face_f<2, false>(mu_L, T0, c, P(0, 0, -1), inv, P(1, 0, 0), P(1, 0, -1), P(-1, 0, 0),
+                          P(-1, 0, -1), P(0, 1, 0), P(0, 1, -1), P(0, -1, 0), P(0, -1, -1), Nb);
+    visc_face_f<2, true>(mu_L, T0, c, P(0, 0, 1), inv, P(1, 0, 0), P(1, 0, 1), P(-1, 0, 0),
+                         P(-1, 0, 1), P(0, 1, 0), P(0, 1, 1), P(0, -1, 0), P(0, -1, 1), Nf);
+#pragma unroll
+    for (int v = 1; v < 5; ++v)
+      vF[v] = ((Lf[v - 1] - Lb[v - 1]) + (Mf[v - 1] - Mb[v - 1]) + (Nf[v - 1] - Nb[v - 1])) * inv;
+  }
+
+  // BDF2 source from FP64 time-level differences, then FP32.
+  const size_t go = cb + ((size_t)(bi + mi) * S + (bj + mj)) * S + (bk + mk);
+  const double *u = a.U1_ + 5 * go;
+  const double *uu = a.U1 + 5 * go;
+  const double *uq = a.U1q + 5 * go;
+  const int IF = __ldg(F + go);
+  const float i2dt = (float)(1.0 / (2.0 * a.dT));
+  float Rk[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    const double x = __ldg(u + v), y = __ldg(uu + v), z = __ldg(uq + v);
+    const float d1 = (float)(x - y), d2 = (float)(y - z);
+    const float Rp = -(3.0f * d1 - d2) * i2dt;
+    Rk[v] = Rp - acc[v] + vF[v];
+  }
+  float *rk = a.Rku32 + 5 * go;
+  if (IF == kFluid) {
+    const float K = 1.4f, Km1 = 0.4f;
+    const float dT = (float)a.dT, dTau = (float)a.dTau;
+    const float *qm = M + 5 * go;
+    const float rho = rho0 + __ldg(qm);
+    const float Uc = c.U, Vc = c.V, Wc = c.W;
+    const float VV = Uc * Uc + Vc * Vc + Wc * Wc;
+    const float Pc = P0 + (__ldg(qm + 4) - 0.5f * rho * VV) * Km1;
+    const float Tt = Pc / rho;  // P/rho (:2302)
+    const float C = K * Tt;
+    const float H = 0.5f * VV + C / Km1;
+    const float qv = VV / C;
+    const float beta = qv > a.ef ? qv : a.ef;
+    const float itemp = 1.0f / (K * Tt * (2 * dT + 3 * dTau) * (2 * dT + 3 * beta * dTau));
+    const float temp2 = Km1 * (beta - 1) * dT * dT;
+    const float temp3 = 0.5f * Km1 * VV;  // == H - H*K - VV + K*(T+VV) since C = K*T
+    const float bm1 = beta - 1;
+    const float a4 = 4 * temp3 * bm1 * dT * dT;
+    const float D = 3 * K * Tt * beta * dTau;
+    float d[5][5];
+    d[0][0] = (2 * dT * (-2 * (-Km1 * (H - VV) - temp3 * beta) * dT + D)) * itemp;
+    d[0][1] = (-4 * Uc * temp2) * itemp;
+    d[0][2] = (-4 * Vc * temp2) * itemp;
+    d[0][3] = (-4 * Wc * temp2) * itemp;
+    d[0][4] = (4 * temp2) * itemp;
+    d[1][0] = Uc * a4 * itemp;
+    d[1][1] = (2 * dT * (2 * K * (Tt - Uc * Uc * bm1) * dT + 2 * Uc * Uc * bm1 * dT + D)) * itemp;
+    d[1][2] = (-4 * Uc * Vc * temp2) * itemp;
+    d[1][3] = (-4 * Uc * Wc * temp2) * itemp;
+    d[1][4] = (4 * Uc * temp2) * itemp;
+    d[2][0] = Vc * a4 * itemp;
+    d[2][1] = d[1][2];
+    d[2][2] = (2 * dT * (2 * K * (Tt - Vc * Vc * bm1) * dT + 2 * Vc * Vc * bm1 * dT + D)) * itemp;
+    d[2][3] = (-4 * Vc * Wc * temp2) * itemp;
+    d[2][4] = (4 * Vc * temp2) * itemp;
+    d[3][0] = Wc * a4 * itemp;
+    d[3][1] = d[1][3];
+    d[3][2] = d[2][3];
+    d[3][3] = (2 * dT * (2 * K * (Tt - Wc * Wc * bm1) * dT + 2 * Wc * Wc * bm1 * dT + D)) * itemp;
+    d[3][4] = (4 * Wc * temp2) * itemp;
+    d[4][0] = H * a4 * itemp;
+    d[4][1] = (-4 * H * Uc * temp2) * itemp;
+    d[4][2] = (-4 * H * Vc * temp2) * itemp;
+    d[4][3] = (-4 * H * Wc * temp2) * itemp;
+    d[4][4] = (2 * dT * (2 * H * Km1 * bm1 * dT + K * Tt * (2 * dT + 3 * beta * dTau))) * itemp;
+#pragma unroll
+    for (int r = 0; r < 5; ++r)
+      rk[r] = dTau * (d[r][0] * Rk[0] + d[r][1] * Rk[1] + d[r][2] * Rk[2] + d[r][3] * Rk[3] +
+                      d[r][4] * Rk[4]);
+  } else {
+#pragma unroll
+    for (int r = 0; r < 5; ++r) rk[r] = 0.f;
+    const double dx = a.cube_size[cube] / n;
+    const double dV = dx * dx * dx;
+    a.Residual1[5 * go + 0] = -((double)(-dPdx * inv) + (double)vF[1]) * dV;
+    a.Residual1[5 * go + 1] = -((double)(-dPdz * inv) + (double)vF[3]) * dV;
+  }
+}
+
+template <int T>
+static cudaError_t launch_split_t(const FluxSplitArgs &a, int ncubes, cudaStream_t s) {
+  const int nt = a.ph.n / T;
+  const size_t smem = SplitSmem<T>::bytes;
+  const unsigned grid = (unsigned)(ncubes * nt * nt * nt);
+  if (grid == 0) return cudaSuccess;
+  cudaError_t e;
+  if (a.ph.mu_L != 0.0) {
+    e = cudaFuncSetAttribute(k_flux_split<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    if (e != cudaSuccess) return e;
+    k_flux_split<T, true><<<grid, T * T * T, smem, s>>>(a);
+  } else {
+    e = cudaFuncSetAttribute(k_flux_split<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    if (e != cudaSuccess) return e;
+    k_flux_split<T, false><<<grid, T * T * T, smem, s>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_flux_split(const FluxSplitArgs &a, int ncubes, cudaStream_t s) {
+  if (a.ph.n % 8 == 0) return launch_split_t<8>(a, ncubes, s);
+  if (a.ph.n % 4 == 0) return launch_split_t<4>(a, ncubes, s);
+  return cudaErrorInvalidValue;
+}
+
+// ---------------------------------------------------------------------------
+// Stage update Q += w * dQ in FP64 (w = 1, 1/4, 2/3 for RK 1, 2, 3: the
+// reference's combinations 0.75 Q + 0.25 Q1 + 0.25 dQ and
+// 1/3 Q + 2/3 Q2 + 2/3 dQ, with Q1 = Q2 = Q on fluid cells at stage entry
+// because only ghost and non-fluid cells change between stages).  At RK 3
+// the change norms use FP32 differences formed from the increment and are
+// summed in FP64.
+// ---------------------------------------------------------------------------
+constexpr int kRkThreads = 256;
+
+__global__ void __launch_bounds__(kRkThreads) k_rk_split(RkSplitArgs a, long long total,
+                                                        long long chunk) {
+  const int n = a.ph.n, S = n + 4;
+  const long long beg = (long long)blockIdx.x * chunk;
+  const long long end = min(total, beg + chunk);
+  const float w = a.RK == 1 ? 1.0f : (a.RK == 2 ? 0.25f : (float)(2.0 / 3.0));
+  double s[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (long long t = beg + threadIdx.x; t < end; t += kRkThreads) {
+    const int c = 1 + (int)(t / ((long long)n * n * n));
+    const int r = (int)(t % ((long long)n * n * n));
+    const int i = 2 + r / (n * n), j = 2 + (r / n) % n, k = 2 + r % n;
+    const size_t o = cell_index(S, c, i, j, k);
+    if (a.FWS[o] == kFluid) {
+      double *q = a.U1_ + 5 * o;
+      const float *rk = a.Rku32 + 5 * o;
+      float dq[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) dq[v] = w * rk[v];
+      double q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3], q4 = q[4];
+      q[0] = q0 + (double)dq[0];
+      q[1] = q1 + (double)dq[1];
+      q[2] = q2 + (double)dq[2];
+      q[3] = q3 + (double)dq[3];
+      q[4] = q4 + (double)dq[4];
+      if (a.RK == 3) {
+        // old/new primitive differences from the increment, in FP32
+        const float rho = (float)q0, m1 = (float)q1, m2 = (float)q2, m3 = (float)q3;
+        const float dr = dq[0], d1 = dq[1], d2 = dq[2], d3 = dq[3], dE = dq[4];
+        const float ir = 1.0f / rho, irn = 1.0f / (rho + dr);
+        const float den = ir * irn;
+        const float dU = (d1 * rho - m1 * dr) * den;
+        const float dV = (d2 * rho - m2 * dr) * den;
+        const float dW = (d3 * rho - m3 * dr) * den;
+        const float mm = m1 * m1 + m2 * m2 + m3 * m3;
+        const float dKE = 0.5f * ((2.f * (m1 * d1 + m2 * d2 + m3 * d3) + d1 * d1 + d2 * d2 + d3 * d3) * rho -
+                                  mm * dr) * den;
+        const float dP = 0.4f * (dE - dKE);
+        const float Pold = (float)((q4 - 0.5 * (double)(mm * ir)) * (BCMG_K - 1));
+        const float dT = (dP * rho - Pold * dr) * den;
+        s[0] += (double)dP * (double)dP;
+        s[1] += (double)dU * (double)dU;
+        s[2] += (double)dV * (double)dV;
+        s[3] += (double)dW * (double)dW;
+        s[4] += (double)dT * (double)dT;
+      }
+    }
+    if (a.RK == 3) {
+      s[5] += a.Residual1[5 * o + 0];
+      s[6] += a.Residual1[5 * o + 1];
+    }
+  }
+  if (a.RK != 3) return;
+  __shared__ double red[kRkThreads / 32][7];
+#pragma unroll
+  for (int m = 0; m < 7; ++m) {
+    double v = s[m];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][m] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 7) {
+    double v = 0;
+    for (int wv = 0; wv < kRkThreads / 32; ++wv) v += red[wv][threadIdx.x];
+    a.partials[(size_t)blockIdx.x * 7 + threadIdx.x] = v;
+  }
+}
+
+cudaError_t launch_rk_split(const RkSplitArgs &a, int *nblocks_out, cudaStream_t s) {
+  RkArgs probe{};
+  probe.ph = a.ph;
+  probe.ncube = a.ncube;
+  const int nb = rk_partial_blocks(probe);
+  const long long n3 = (long long)a.ph.n * a.ph.n * a.ph.n;
+  const long long total = (long long)(a.ncube - 1) * n3;
+  const long long chunk = (total + nb - 1) / nb;
+  if (nblocks_out) *nblocks_out = nb;
+  if (total <= 0) return cudaSuccess;
+  k_rk_split<<<nb, kRkThreads, 0, s>>>(a, total, chunk);
+  return cudaGetLastError();
+}
+
+}  // namespace bcmg

@@ -22,9 +22,35 @@ struct FluxArgs {
 // FP64 residual + increment (bit-exact with the reference).
 cudaError_t launch_flux_fp64(const FluxArgs &a, int ncubes, cudaStream_t s);
 
-// Split-precision residual + increment: reconstruction, fluxes, viscous terms
-// and the preconditioner in FP32; state, BDF2 source, residual sum in FP64.
-cudaError_t launch_flux_split(const FluxArgs &a, int ncubes, cudaStream_t s);
+// Split-precision path (bcm_flux_split.cu): FP32 reconstruction, fluxes,
+// viscous terms and preconditioner on deltas from a reference state; FP64
+// state, time-level differences, update and norm sums.
+struct FluxSplitArgs {
+  Phys ph;
+  int cube0;
+  double dT, dTau;
+  float ef;  // e (beta floor)
+  const int *FWS;
+  const double *cube_size;
+  const float *M;  // FP32 deltas of U1_ (k_mirror)
+  const double *U1_, *U1, *U1q;
+  float *Rku32;  // FP32 increments
+  double *Residual1;
+};
+cudaError_t launch_mirror(const double *U, float *M, int n, int ncube, double rho0, double P0,
+                          cudaStream_t s);
+cudaError_t launch_flux_split(const FluxSplitArgs &a, int ncubes, cudaStream_t s);
+struct RkSplitArgs {
+  Phys ph;
+  int ncube;
+  int RK;
+  const int *FWS;
+  double *U1_;
+  const float *Rku32;
+  const double *Residual1;
+  double *partials;
+};
+cudaError_t launch_rk_split(const RkSplitArgs &a, int *nblocks_out, cudaStream_t s);
 
 struct RkArgs {
   Phys ph;

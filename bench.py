@@ -1,0 +1,318 @@
+"""Throughput benchmark of the BCM per-cube dual-time sub-iteration path.
+
+Workload: viscous Taylor-Green vortex, periodic 2*pi box of 8x8x8 cubes of
+24^3 cells (7,077,888 cells), Mach 0.1, Re 1600, Pr 0.72, seeded analytic
+initial field (synthetic; no dataset exists for this metric).  One bench
+step = one dual-time step of SUBITERS pseudo-time sub-iterations (3 RK
+stages each: BCs, IBM ghosts, interface, flux/RK, interface) plus the
+time-level shift, over every cube.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--precision fp64|split]
+
+Prints one JSON line (rank 0).  For N > 1 run under torchrun: every rank
+advances its own replica of the case (weak scaling, no data-path
+collective; the barrier and the max-over-ranks timing use the process
+group).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("cell-subiters/s FP64 vs split-FP32 at ≤1e-5 L2 err; HBM GB/s vs peak")
+UNIT = "cell-subiters/s"
+SUBITERS = 10
+# Algorithmic bytes per cell-stage of the flux/RK kernel: read U1_, U1, U1q
+# (40 B each) and the flag (4 B), write U1_ (40 B).
+BYTES_PER_CELL_STAGE = 164
+
+
+def workload_case():
+    from bcm_cgli_gb300 import cases
+    return cases.taylor_green(ncx=8, n=24)
+
+
+def workload_config(case, precision):
+    return {
+        "workload": "taylor-green vortex, periodic 2pi box, 8x8x8 cubes of 24^3 cells "
+                    "(7,077,888 cells), M=0.1, Re=1600, Pr=0.72, dT=1e-4, dTau=dT/200, "
+                    f"{SUBITERS} sub-iterations x 3 RK stages per dual-time step",
+        "cells": int(case.n_cells),
+        "subiters_per_step": SUBITERS,
+        "precision": precision,
+        "l2": "inputs larger than L2: each state array is "
+              f"{case.U.nbytes / 1e6:.0f} MB (7 arrays resident)",
+        "parallelism": "replica per GPU",
+    }
+
+
+# ---------------------------------------------------------------------------
+# distributed helpers (timing only)
+# ---------------------------------------------------------------------------
+class Dist:
+    def __init__(self, gpus: int):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            torch.cuda.set_device(self.local)
+            dist.init_process_group("nccl")
+            self.pg = dist
+            self.torch = torch
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        t = self.torch.tensor([x], dtype=self.torch.float64, device="cuda")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# clocks sampler (nvidia-smi during the timed region)
+# ---------------------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.p = None
+        self.out = []
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.out.append(line.strip())
+
+    def stop(self):
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU arm: the reference's algorithm on the host cores (oracle port here,
+# since the reference sources are not present on the GPU host)
+# ---------------------------------------------------------------------------
+def cpu_sample(case, subiters=1, threads=None):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    kind = "port"
+    runner = O.Port()
+    threads = threads or os.cpu_count() or 1
+    runner.set_threads(threads)
+    st = O.State(case)
+    t0 = time.perf_counter()
+    runner.run(case, st, 1, subiters)
+    dt = time.perf_counter() - t0
+    return {"value": case.n_cells * subiters / dt, "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": f"1 dual-time step x {subiters} sub-iteration(s) of the full workload "
+                      f"({case.n_cells} cells) through the C restatement of the reference "
+                      f"loop, OpenMP over cubes, {dt:.2f} s"}
+
+
+def run_reference_arm(args, dist):
+    if dist.rank != 0:
+        return
+    case = workload_case()
+    for _ in range(max(0, args.warmup)):
+        pass  # the CPU sample needs no warm-up; kept for the launch contract
+    vals, t_total = [], 0.0
+    for _ in range(max(1, args.steps)):
+        r = cpu_sample(case, subiters=1)
+        vals.append(r["value"])
+    v = float(np.median(vals))
+    r["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": case.n_cells * SUBITERS / v * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(case, "fp64"), "cpu_baseline": r,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def pinned_like(a):
+    try:
+        import torch
+        t = torch.empty(a.size, dtype=torch.float64, pin_memory=True)
+        out = t.numpy().reshape(a.shape)
+        out[...] = a
+        return out, t
+    except Exception:
+        return np.ascontiguousarray(a.copy()), None
+
+
+def run_gpu_arm(args, dist):
+    from bcm_cgli_gb300 import api
+    precision = api.PRECISION_SPLIT if args.precision == "split" else api.PRECISION_FP64
+    case = workload_case()
+    ctx = api.CaseContext(case, precision=precision)
+    ctx.set_state(case.U, case.U, case.U)
+    for _ in range(args.warmup):
+        ctx.advance(1, SUBITERS, use_graph=False)
+    ctx.set_profiling(True)
+    clocks = Clocks(dist.local)
+    clocks.start()
+    launches = 0
+    dist.barrier()
+    ctx.sync()
+    ctx.timer_mark(0)
+    for _ in range(args.steps):
+        ctx.advance(1, SUBITERS, use_graph=False)
+        launches += ctx.launch_count()
+    ctx.timer_mark(1)
+    ctx.sync()
+    dist.barrier()
+    ms = dist.max(ctx.timer_elapsed(0, 1))
+    clk = clocks.stop()
+    flux_ms, flux_n = ctx.profile()
+    ctx.set_profiling(False)
+    cell_subiters = case.n_cells * SUBITERS * args.steps * dist.world
+    value = cell_subiters / (ms * 1e-3)
+
+    # e2e: per step, host (pinned) -> device state, one dual-time step,
+    # device -> host state and norms, through the public C ABI.
+    hU, hold = pinned_like(case.U)
+    hU1, hold1 = pinned_like(case.U)
+    hU1q, hold1q = pinned_like(case.U)
+    dist.barrier()
+    ctx.sync()
+    ctx.timer_mark(2)
+    oU, ohold = pinned_like(case.U)
+    oU1, ohold1 = pinned_like(case.U)
+    oU1q, ohold1q = pinned_like(case.U)
+    for _ in range(args.steps):
+        ctx.set_state(hU, hU1, hU1q)
+        ctx.advance(1, SUBITERS, use_graph=True)
+        ctx.get_state(out=[oU, oU1, oU1q])  # full state back (U1_, U1, U1q)
+    ctx.timer_mark(3)
+    ctx.sync()
+    dist.barrier()
+    ms_e2e = dist.max(ctx.timer_elapsed(2, 3))
+    e2e = cell_subiters / (ms_e2e * 1e-3)
+    h2d = 3 * case.U.nbytes
+    d2h = 3 * case.U.nbytes + 8 * 8 + 6 * 8
+
+    # roofline of the dominant kernel (flux + preconditioned increment)
+    avg_flux_ms = flux_ms / max(1, flux_n)
+    alg_bytes = BYTES_PER_CELL_STAGE * case.n_cells
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = alg_bytes / (avg_flux_ms * 1e-3) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", f"flux_{args.precision}_tgv24_traffic.json")
+    if os.path.isfile(prof):
+        try:
+            traffic = json.load(open(prof)).get("dram_bytes_per_launch")
+        except Exception:
+            traffic = None
+    fp64_gflops = api.probe_fp64_gflops()
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "data": "synthetic", "config": workload_config(case, args.precision),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "traffic": traffic,
+                         "kernel": f"k_flux_{args.precision}",
+                         "alg_bytes_per_launch": alg_bytes,
+                         "avg_launch_ms": avg_flux_ms, "launches": flux_n,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+            "fp64_alu": {"measured_fma_gflops": fp64_gflops,
+                         "note": "FP64 FMA rate measured by bcmg_probe_fp64_rate on this GPU"},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches, "clocks": clk}
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_sample(case, subiters=1)
+    ctx.close()
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        # Rank 0 alone times the CPU implementation; other ranks exit at once.
+        class R0:
+            rank = int(os.environ.get("RANK", "0"))
+        run_reference_arm(args, R0())
+        return
+    dist = Dist(args.gpus)
+    run_gpu_arm(args, dist)
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -206,6 +206,17 @@ int bcmg_case_time_flux(bcmg_case *c, int reps, double *ms);
 int bcmg_case_set_profiling(bcmg_case *c, int on);
 int bcmg_case_profile(const bcmg_case *c, double *flux_ms_total, long long *flux_launches);
 
+/* Device-time marks on the context's stream: bcmg_case_timer_mark records
+ * event `slot` (0..15); bcmg_case_timer_elapsed waits for mark b and returns
+ * the milliseconds between marks a and b. */
+int bcmg_case_timer_mark(bcmg_case *c, int slot);
+int bcmg_case_timer_elapsed(bcmg_case *c, int a, int b, double *ms);
+
+/* Measured FP64 fused-multiply-add rate of the current device in GFLOP/s
+ * (2 flops per FMA), from a short dependent-chain kernel: the ALU roof for
+ * the FP64 path. */
+int bcmg_probe_fp64_rate(double *gflops);
+
 /* ----------------------------------------------------------------------- */
 /* Host-side table builders (no GPU needed)                                */
 /* ----------------------------------------------------------------------- */
