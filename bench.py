@@ -201,17 +201,19 @@ def pinned_like(a):
         return np.ascontiguousarray(a.copy()), None
 
 
-def run_gpu_arm(args, dist):
-    from bcm_cgli_gb300 import api
-    precision = api.PRECISION_SPLIT if args.precision == "split" else api.PRECISION_FP64
-    case = workload_case()
+def measure(api, case, precision_name, args, dist, clocks_on=True):
+    """Timed region for one precision: args.steps dual-time steps resident in
+    HBM, device-timed with CUDA events on the context's stream; the flux
+    kernel's launches are bracketed by events for its average duration."""
+    precision = api.PRECISION_SPLIT if precision_name == "split" else api.PRECISION_FP64
     ctx = api.CaseContext(case, precision=precision)
     ctx.set_state(case.U, case.U, case.U)
     for _ in range(args.warmup):
         ctx.advance(1, SUBITERS, use_graph=False)
     ctx.set_profiling(True)
-    clocks = Clocks(dist.local)
-    clocks.start()
+    clocks = Clocks(dist.local) if clocks_on else None
+    if clocks:
+        clocks.start()
     launches = 0
     dist.barrier()
     ctx.sync()
@@ -223,73 +225,124 @@ def run_gpu_arm(args, dist):
     ctx.sync()
     dist.barrier()
     ms = dist.max(ctx.timer_elapsed(0, 1))
-    clk = clocks.stop()
+    clk = clocks.stop() if clocks else None
     flux_ms, flux_n = ctx.profile()
     ctx.set_profiling(False)
     cell_subiters = case.n_cells * SUBITERS * args.steps * dist.world
-    value = cell_subiters / (ms * 1e-3)
+    out = {"value": cell_subiters / (ms * 1e-3), "ms_per_step": ms / args.steps,
+           "launches": launches, "flux_ms_avg": flux_ms / max(1, flux_n), "flux_launches": flux_n,
+           "clocks": clk, "ctx": ctx}
+    return out
 
+
+def rel_l2(a, b, n):
+    """Relative L2 error per conservative variable over interior cells; the
+    momentum components are also given relative to the momentum magnitude
+    (rho w of a 2-D or symmetric flow is ~0, so its own norm is no scale)."""
+    ai = a[1:, 2:n + 2, 2:n + 2, 2:n + 2].reshape(-1, 5)
+    bi = b[1:, 2:n + 2, 2:n + 2, 2:n + 2].reshape(-1, 5)
+    d = ai - bi
+    own = [float(np.linalg.norm(d[:, v]) / max(np.linalg.norm(bi[:, v]), 1e-300)) for v in range(5)]
+    mom = float(np.linalg.norm(bi[:, 1:4]))
+    scaled = [own[0]] + [float(np.linalg.norm(d[:, v]) / mom) for v in (1, 2, 3)] + [own[4]]
+    return own, scaled
+
+
+def run_gpu_arm(args, dist):
+    from bcm_cgli_gb300 import api
+    case = workload_case()
+    head = args.precision
+    other = "fp64" if head == "split" else "split"
+    m_head = measure(api, case, head, args, dist, clocks_on=True)
+    m_other = measure(api, case, other, args, dist, clocks_on=False) if not args.quick else None
+
+    # Accuracy of the split form against the FP64 path after one dual-time
+    # step from the same initial state (north-star bound: 1e-5 relative L2).
+    acc = None
+    if m_other is not None:
+        states = {}
+        for name, m in ((head, m_head), (other, m_other)):
+            ctx = m["ctx"]
+            ctx.set_state(case.U, case.U, case.U)
+            ctx.emax[:] = 0
+            ctx.advance(1, SUBITERS, use_graph=True)
+            states[name] = ctx.get_state()[0]
+        own, scaled = rel_l2(states["split"], states["fp64"], case.n)
+        acc = {"rel_l2_per_variable": own, "rel_l2_momentum_scaled": scaled,
+               "max_rel_l2": max(scaled), "bound": 1e-5,
+               "after": f"1 dual-time step ({SUBITERS} sub-iterations) from the same state"}
+
+    ctx = m_head["ctx"]
     # e2e: per step, host (pinned) -> device state, one dual-time step,
-    # device -> host state and norms, through the public C ABI.
+    # device -> host state, through the public C ABI.
     hU, hold = pinned_like(case.U)
     hU1, hold1 = pinned_like(case.U)
     hU1q, hold1q = pinned_like(case.U)
-    dist.barrier()
-    ctx.sync()
-    ctx.timer_mark(2)
     oU, ohold = pinned_like(case.U)
     oU1, ohold1 = pinned_like(case.U)
     oU1q, ohold1q = pinned_like(case.U)
+    dist.barrier()
+    ctx.sync()
+    ctx.timer_mark(2)
     for _ in range(args.steps):
         ctx.set_state(hU, hU1, hU1q)
         ctx.advance(1, SUBITERS, use_graph=True)
-        ctx.get_state(out=[oU, oU1, oU1q])  # full state back (U1_, U1, U1q)
+        ctx.get_state(out=[oU, oU1, oU1q])
     ctx.timer_mark(3)
     ctx.sync()
     dist.barrier()
     ms_e2e = dist.max(ctx.timer_elapsed(2, 3))
+    cell_subiters = case.n_cells * SUBITERS * args.steps * dist.world
     e2e = cell_subiters / (ms_e2e * 1e-3)
-    h2d = 3 * case.U.nbytes
-    d2h = 3 * case.U.nbytes + 8 * 8 + 6 * 8
 
-    # roofline of the dominant kernel (flux + preconditioned increment)
-    avg_flux_ms = flux_ms / max(1, flux_n)
-    alg_bytes = BYTES_PER_CELL_STAGE * case.n_cells
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    achieved = alg_bytes / (avg_flux_ms * 1e-3) / 1e9
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", f"flux_{args.precision}_tgv24_traffic.json")
-    if os.path.isfile(prof):
-        try:
-            traffic = json.load(open(prof)).get("dram_bytes_per_launch")
-        except Exception:
-            traffic = None
     fp64_gflops = api.probe_fp64_gflops()
 
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+    def roofline(m, prec):
+        alg_bytes = BYTES_PER_CELL_STAGE * case.n_cells
+        achieved = alg_bytes / (m["flux_ms_avg"] * 1e-3) / 1e9
+        traffic = None
+        prof = os.path.join(ROOT, "profiles", f"flux_{prec}_traffic.json")
+        if os.path.isfile(prof):
+            try:
+                t = json.load(open(prof))
+                traffic = t["dram_bytes_per_cell_stage"] * case.n_cells
+            except Exception:
+                traffic = None
+        return {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": traffic, "kernel": f"k_flux_{prec}",
+                "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": m["flux_ms_avg"],
+                "launches": m["flux_launches"],
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+
+    line = {"metric": METRIC, "value": m_head["value"], "unit": UNIT, "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": m_head["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if args.precision == "fp64" else "f32+f64",
-            "data": "synthetic", "config": workload_config(case, args.precision),
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved / hbm_peak, "traffic": traffic,
-                         "kernel": f"k_flux_{args.precision}",
-                         "alg_bytes_per_launch": alg_bytes,
-                         "avg_launch_ms": avg_flux_ms, "launches": flux_n,
-                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+            "dtype": "f64" if head == "fp64" else "f32+f64",
+            "data": "synthetic", "config": workload_config(case, head),
+            "roofline": roofline(m_head, head),
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 3 * case.U.nbytes,
+                    "d2h_bytes_per_step": 3 * case.U.nbytes},
+            "gpu_launches": m_head["launches"], "clocks": m_head["clocks"],
             "fp64_alu": {"measured_fma_gflops": fp64_gflops,
-                         "note": "FP64 FMA rate measured by bcmg_probe_fp64_rate on this GPU"},
-            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
-            "gpu_launches": launches, "clocks": clk}
+                         "note": "FP64 FMA rate of this GPU, measured by bcmg_probe_fp64_rate"}}
+    if m_other is not None:
+        line[other] = {"value": m_other["value"], "ms_per_step": m_other["ms_per_step"],
+                       "roofline": roofline(m_other, other), "gpu_launches": m_other["launches"]}
+        line["split_vs_fp64_speedup"] = (line["value"] / m_other["value"] if head == "split"
+                                         else m_other["value"] / line["value"])
+    if acc is not None:
+        line["accuracy"] = acc
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample(case, subiters=1)
-    ctx.close()
+    for m in (m_head, m_other):
+        if m is not None:
+            m["ctx"].close()
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -300,8 +353,12 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
+    ap.add_argument("--precision", default="split", choices=["fp64", "split"],
+                    help="path whose throughput is the headline value (the other is "
+                         "reported beside it)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true",
+                    help="headline path only (no second precision, no accuracy check)")
     args = ap.parse_args()
     if args.impl == "reference":
         # Rank 0 alone times the CPU implementation; other ranks exit at once.

@@ -1,0 +1,131 @@
+"""CPU tests of the host-side logic and of the C ABI surface (no GPU calls)."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle as O
+from bcm_cgli_gb300 import cases
+from bcm_cgli_gb300._lib import LIB_PATH, lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _header_functions():
+    names = set()
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if not fn.endswith(".h"):
+            continue
+        src = open(os.path.join(ROOT, "include", fn)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b([A-Za-z_]\w*)\s*\(", src,
+                             flags=re.M):
+            if m.group(1) not in ("if", "defined"):
+                names.add(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    assert os.path.isfile(LIB_PATH), "build the library first (__graft_entry__.build())"
+    L = C.CDLL(LIB_PATH)
+    names = _header_functions()
+    assert {"BCM_Flux_XYZ_Viscous_Runge_kutta", "BCM_Interface", "bcmg_case_create"} <= names
+    missing = [n for n in sorted(names) if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_reference_config_roundtrip():
+    from bcm_cgli_gb300 import api
+    api.set_reference_config(ncube_x=24, mpi_ncube=512, mu_L=0.0256, rho0=1.2, U0=34.6,
+                             Uin=34.6, P0=101300.0)
+    from bcm_cgli_gb300._lib import RefConfig
+    c = RefConfig()
+    lib().bcmg_get_reference_config(C.byref(c))
+    assert (c.ncube_x, c.mpi_ncube, c.mu_L) == (24, 512, 0.0256)
+    with pytest.raises(Exception):
+        api.set_reference_config(ncube_x=6)  # not a multiple of 4
+
+
+def _ibm_levels(case, table):
+    W, G, I = table
+    nbc = (len(G) - 1) // 4
+    lev = np.zeros(nbc, np.int32)
+    nl = lib().bcmg_ibm_schedule(nbc, np.ascontiguousarray(G, np.int32),
+                                 np.ascontiguousarray(I, np.int32), case.n, case.ncube, lev)
+    return nl, lev
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3, 4])
+def test_ibm_levels_reproduce_the_serial_loop(seed):
+    """Applying the ghost entries level by level (any order inside a level)
+    gives the reference's serial result bit for bit: run the oracle's serial
+    loop on the level-sorted table (reversed inside each level) and compare."""
+    case = cases.random_case(seed=seed, n=4)
+    W, G, I = case.ibm_minus
+    nl, lev = _ibm_levels(case, case.ibm_minus)
+    assert nl >= 1 and lev.min() >= 1
+    nbc = len(lev)
+    order = sorted(range(nbc), key=lambda e: (lev[e], -e))
+    W2 = np.concatenate([[0.0]] + [W[8 * e + 1:8 * e + 9] for e in order])
+    G2 = np.concatenate([[0]] + [G[4 * e + 1:4 * e + 5] for e in order]).astype(np.int32)
+    I2 = np.concatenate([[0]] + [I[4 * e + 1:4 * e + 5] for e in order]).astype(np.int32)
+    port = O.Port()
+    a, b = O.State(case), O.State(case)
+    port.ghost(case, a.U1_, -1)
+    case2 = cases.random_case(seed=seed, n=4)
+    case2.ibm_minus = (W2, G2, I2)
+    port.ghost(case2, b.U1_, -1)
+    assert np.array_equal(a.U1_, b.U1_)
+
+
+def test_ibm_levels_reject_out_of_range_indices():
+    case = cases.random_case(seed=1, n=4)
+    W, G, I = case.ibm_minus
+    I = I.copy()
+    I[4] = case.S - 1  # k + 1 would leave the padded cube
+    nl, _ = _ibm_levels(case, (W, G, I))
+    assert nl == -1
+
+
+def test_interface_tasks_match_reference_lists():
+    """Face tasks from adjacency equal the same-level pairs the reference's
+    BCM_Interface_table.cpp would list (periodic box: 6 faces per cube)."""
+    case = cases.taylor_green(ncx=3, n=4)
+    off = np.zeros(case.ncube + 1, np.int32)
+    words = np.zeros(3 * 6 * case.ncube, np.int32)
+    nt = lib().bcmg_interface_tasks(case.ncube, np.ascontiguousarray(case.adj, np.int32),
+                                    case.csl, off, words, 6 * case.ncube)
+    assert nt == 6 * (case.ncube - 1)
+    w = words[:3 * nt].reshape(-1, 3)
+    for c in range(1, case.ncube):
+        t = w[off[c]:off[c + 1]]
+        assert len(t) == 6
+        for src, ax, side in t:
+            # side 0: low ghosts from the -axis neighbour; 1: high from +axis
+            assert src == case.adj[c, 1, 1 + 2 * ax + side]
+
+
+def test_open_box_interface_tasks_skip_domain_faces():
+    ncube, cs, csl, org, adj = cases.open_box(2, 2, 2, 4, 1.0)
+    off = np.zeros(ncube + 1, np.int32)
+    words = np.zeros(3 * 6 * ncube, np.int32)
+    nt = lib().bcmg_interface_tasks(ncube, np.ascontiguousarray(adj, np.int32),
+                                    np.ascontiguousarray(csl, np.int32), off, words, 6 * ncube)
+    assert nt == 3 * (ncube - 1)  # each cube of a 2x2x2 open box has 3 neighbours
+
+
+@pytest.mark.skipif(not O.reference_available(), reason="reference sources not on this host")
+def test_reference_shim_compiles_against_main_h(tmp_path):
+    """The C++ shim provides exactly the signatures the reference's main.h
+    declares (compile-only check against the reference's own header)."""
+    src = tmp_path / "shim.cpp"
+    src.write_text('#include "Resolution.h"\n#include "main.h"\n'
+                   '#include "bcm_gb300_reference_shim.hpp"\n')
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-w",
+                        "-I", O.ref_build.REF_DIR, "-I", os.path.join(ROOT, "include"),
+                        "-I", os.path.join(ROOT, "oracle", "mpi_stub"), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
