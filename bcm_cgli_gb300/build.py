@@ -27,6 +27,7 @@ UNITS = [
     ("bcm_rk.cu", ["--fmad=false"]),
     ("bcm_halo.cu", ["--fmad=false"]),
     ("bcm_capi.cu", ["--fmad=false"]),
+    ("bcm_noalloc.cu", ["--fmad=false"]),
     ("bcm_tables.cpp", []),
 ]
 

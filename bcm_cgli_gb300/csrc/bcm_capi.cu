@@ -329,6 +329,15 @@ int case_step(bcmg_case *c, int subiters) {
 
 extern "C" {
 
+// Sets (msg != NULL) or clears (msg == NULL) the calling thread's last error;
+// used by entry points defined in other translation units.
+void bcmg_internal_set_error(const char *msg) {
+  if (msg)
+    set_err(msg);
+  else
+    clear_err();
+}
+
 const char *bcmg_last_error(void) { return g_has_err ? g_err.c_str() : nullptr; }
 const char *bcmg_version(void) { return "bcm_gb300 0.1 (sm_103a)"; }
 

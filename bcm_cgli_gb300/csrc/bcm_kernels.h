@@ -7,6 +7,8 @@
 
 #include "bcm_common.cuh"
 
+extern "C" void bcmg_internal_set_error(const char *msg);
+
 namespace bcmg {
 
 struct FluxArgs {
@@ -67,6 +69,8 @@ struct RkArgs {
 cudaError_t launch_rk(const RkArgs &a, int *nblocks_out, cudaStream_t s);
 // Number of partial-sum blocks launch_rk uses for this case (for sizing).
 int rk_partial_blocks(const RkArgs &a);
+// Same combination with an explicit chunk (cells per block) and block count.
+cudaError_t launch_rk_chunked(const RkArgs &a, long long chunk, int nblocks, cudaStream_t s);
 // Deterministic final reduction of partials -> er[1..7] (device, 8 doubles).
 cudaError_t launch_norms(const Phys &ph, const double *partials, int nblocks, double *er,
                          cudaStream_t s);

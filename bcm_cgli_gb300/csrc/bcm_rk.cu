@@ -146,3 +146,17 @@ cudaError_t launch_norms(const Phys &ph, const double *partials, int nblocks, do
 }
 
 }  // namespace bcmg
+
+namespace bcmg {
+
+// Stage combination with a caller-chosen chunk (cells per block) and block
+// count; partials must hold nblocks * 7 doubles.
+cudaError_t launch_rk_chunked(const RkArgs &a, long long chunk, int nblocks, cudaStream_t s) {
+  const long long n3 = (long long)a.ph.n * a.ph.n * a.ph.n;
+  const long long total = (long long)(a.ncube - 1) * n3;
+  if (total <= 0 || nblocks <= 0) return cudaSuccess;
+  k_rk<<<nblocks, kRkThreads, 0, s>>>(a, total, chunk);
+  return cudaGetLastError();
+}
+
+}  // namespace bcmg

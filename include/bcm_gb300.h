@@ -206,6 +206,31 @@ int bcmg_case_time_flux(bcmg_case *c, int reps, double *ms);
 int bcmg_case_set_profiling(bcmg_case *c, int on);
 int bcmg_case_profile(const bcmg_case *c, double *flux_ms_total, long long *flux_launches);
 
+/* One FP64 RK stage that allocates nothing.  No counterpart in the
+ * reference.  It serves callers that cannot let a library call cudaMalloc:
+ * solvers that hand out every device buffer from their own pre-sized arena,
+ * and latency-sensitive hosts that cannot accept the implicit device
+ * synchronisation an allocation may cause.  Same arithmetic and results as
+ * BCM_Flux_XYZ_Viscous_Runge_kutta (with the bcmg_set_reference_config
+ * values), but every array argument is a DEVICE pointer owned by the caller
+ * (cube_size and er included; er[0] is set to 0), the work is queued on
+ * `stream` (a cudaStream_t, NULL for the legacy default stream) and the call
+ * returns without waiting.  Its only scratch, the per-block norm partial
+ * sums, is a fixed static device array (8192 blocks x 7 doubles, 458 KB)
+ * that every GPU loading the library holds until the process exits; cases
+ * above 33,554,432 interior cells are rejected with BCMG_ERR_ARG.  The first
+ * call on a device looks up that array's device address (once per device,
+ * with that device current); make that first call before any stream
+ * capture.  Every call shares the scratch, and each call fully rewrites the
+ * part it reads, so nothing needs clearing; calls that overlap on the GPU
+ * (other streams, other host threads) race on it and must be serialised by
+ * the caller. */
+int bcmg_flux_rk_stage_noalloc(int ncube, int RK, double deltaT, double deltaTau, double e,
+                               const int *FWS, const double *cube_size, double *U1_,
+                               const double *U1, const double *U1q, double *U1p1,
+                               double *U1p2, double *Rku1, double *Residual1, double *er,
+                               void *stream);
+
 /* Device-time marks on the context's stream: bcmg_case_timer_mark records
  * event `slot` (0..15); bcmg_case_timer_elapsed waits for mark b and returns
  * the milliseconds between marks a and b. */
