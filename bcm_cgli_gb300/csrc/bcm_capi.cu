@@ -150,6 +150,7 @@ struct bcmg_case {
   double *U1_ = nullptr, *U1 = nullptr, *U1q = nullptr, *U1p1 = nullptr, *U1p2 = nullptr,
          *Rku1 = nullptr, *Residual1 = nullptr;
   float *M = nullptr, *Rku32 = nullptr;  // split precision: FP32 deltas, increments
+  float *D2 = nullptr;                   // split precision: FP32 of U1 - U1q
   int *FWS = nullptr;
   double *cube_size = nullptr;
   int *task_off = nullptr;
@@ -179,7 +180,7 @@ struct bcmg_case {
     for (auto x : ev) cudaEventDestroy(x);
     ev.clear();
     dfree(U1_); dfree(U1); dfree(U1q); dfree(U1p1); dfree(U1p2); dfree(Rku1); dfree(Residual1);
-    dfree(M); dfree(Rku32);
+    dfree(M); dfree(Rku32); dfree(D2);
     dfree(FWS); dfree(cube_size); dfree(task_off); dfree(tasks); dfree(bc_cubes);
     dfree(bc_masks); dfree(partials); dfree(er); dfree(emax);
     ibm.release();
@@ -231,6 +232,7 @@ int case_flux(bcmg_case *c) {
     sa.U1_ = c->U1_;
     sa.U1 = c->U1;
     sa.U1q = c->U1q;
+    sa.D2 = c->D2;
     sa.Rku32 = c->Rku32;
     sa.Residual1 = c->Residual1;
     CK(launch_flux_split(sa, c->ncube - 1, c->stream));
@@ -321,6 +323,10 @@ int case_step(bcmg_case *c, int subiters) {
     k_time_shift<<<blocks, 256, 0, c->stream>>>(c->ph.n, total, c->U1_, c->U1, c->U1q);
     CK(cudaGetLastError());
     ++c->launches;
+    if (c->precision == BCMG_PRECISION_SPLIT) {
+      CK(launch_level_diff(c->U1, c->U1q, c->D2, c->ph.n, c->ncube, c->stream));
+      ++c->launches;
+    }
   }
   return BCMG_OK;
 }
@@ -424,6 +430,7 @@ int bcmg_case_create(const bcmg_case_desc *d, bcmg_case **out) {
   if (!ok) return fail(BCMG_ERR_CUDA);
   if (d->precision == BCMG_PRECISION_SPLIT &&
       !(ck(dalloc(&c->M, nd), "alloc") && ck(dalloc(&c->Rku32, nd), "alloc") &&
+        ck(dalloc(&c->D2, nd), "alloc") && ck(cudaMemset(c->D2, 0, nd * sizeof(float)), "memset") &&
         ck(cudaMemset(c->M, 0, nd * sizeof(float)), "memset") &&
         ck(cudaMemset(c->Rku32, 0, nd * sizeof(float)), "memset")))
     return fail(BCMG_ERR_CUDA);
@@ -499,6 +506,8 @@ int bcmg_case_set_state(bcmg_case *c, const double *U1_, const double *U1, const
   if (U1_) CK(cudaMemcpyAsync(c->U1_, U1_, b, cudaMemcpyHostToDevice, c->stream));
   if (U1) CK(cudaMemcpyAsync(c->U1, U1, b, cudaMemcpyHostToDevice, c->stream));
   if (U1q) CK(cudaMemcpyAsync(c->U1q, U1q, b, cudaMemcpyHostToDevice, c->stream));
+  if (c->precision == BCMG_PRECISION_SPLIT && (U1 || U1q))
+    CK(launch_level_diff(c->U1, c->U1q, c->D2, c->ph.n, c->ncube, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return BCMG_OK;
 }
@@ -568,7 +577,7 @@ int bcmg_case_advance(bcmg_case *c, int steps, int subiters, int use_graph, doub
       int L = (int)(c->ibm.level_off.size() > 0 ? c->ibm.level_off.size() - 1 : 0);
       long long stage = (c->nbc > 0) + L + 1 + 1 + 1 + 1 +
                         (c->precision == BCMG_PRECISION_SPLIT ? 1 : 0);
-      per = subiters * (3 * stage + 1 + 1) + 1;
+      per = subiters * (3 * stage + 1 + 1) + 1 + (c->precision == BCMG_PRECISION_SPLIT ? 1 : 0);
     }
     for (int s = 0; s < steps; ++s) CK(cudaGraphLaunch(c->graph, c->stream));
     c->launches = per * steps;

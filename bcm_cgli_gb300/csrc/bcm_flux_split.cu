@@ -53,17 +53,46 @@ cudaError_t launch_mirror(const double *U, float *M, int n, int ncube, double rh
   return cudaGetLastError();
 }
 
+// Q^n - Q^(n-1) of the interior cells, formed in FP64 and stored in FP32,
+// once per physical time step (it is constant over the step's stages).
+__global__ void k_level_diff(const double *__restrict__ U1, const double *__restrict__ U1q,
+                             float *__restrict__ D2, int n, long long total) {
+  const int S = n + 4;
+  const long long n3 = (long long)n * n * n;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int c = 1 + (int)(t / n3);
+    const int r = (int)(t % n3);
+    const size_t o = 5 * cell_index(S, c, 2 + r / (n * n), 2 + (r / n) % n, 2 + r % n);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) D2[o + v] = (float)(U1[o + v] - U1q[o + v]);
+  }
+}
+
+cudaError_t launch_level_diff(const double *U1, const double *U1q, float *D2, int n, int ncube,
+                              cudaStream_t s) {
+  const long long total = (long long)(ncube - 1) * n * n * n;
+  if (total <= 0) return cudaSuccess;
+  int blocks = (int)((total + 255) / 256);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  k_level_diff<<<blocks, 256, 0, s>>>(U1, U1q, D2, n, total);
+  return cudaGetLastError();
+}
+
 struct PrimF {
   float U, V, W, Tp;  // velocity, T - T0
 };
 
 template <int T>
 struct SplitSmem {
-  static constexpr int B = T + 2;
+  static constexpr int B = T + 2;      // primitive box edge (tile + 1 halo)
+  static constexpr int X = T + 6;      // stencil box edge (tile + 3 halo)
   static constexpr int nPrim = B * B * B;
   static constexpr int nCell = T * T * T;
-  static constexpr size_t bytes = sizeof(PrimF) * nPrim + 2 * sizeof(float) * 5 * nCell +
-                                  2 * sizeof(float) * nCell;
+  static constexpr int nBox = X * X * X;
+  static constexpr size_t bytes = sizeof(float) * 5 * nBox /*state deltas*/ +
+                                  sizeof(PrimF) * nPrim + 2 * sizeof(float) * 5 * nCell +
+                                  2 * sizeof(float) * nCell + ((nBox + 15) / 16) * 16 /*flags*/;
 };
 
 // Delta-form preconditioned Roe flux (same formulas as face_flux in
@@ -196,13 +225,16 @@ template <int T, bool VISCOUS>
 __global__ void __launch_bounds__(T *T *T, 1) k_flux_split(FluxSplitArgs a) {
   using SM = SplitSmem<T>;
   constexpr int B = SM::B;
+  constexpr int X = SM::X;
   constexpr int NT = T * T * T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  PrimF *prim = reinterpret_cast<PrimF *>(smem_raw);
+  float *box = reinterpret_cast<float *>(smem_raw);  // [X][X][X][5] deltas
+  PrimF *prim = reinterpret_cast<PrimF *>(box + 5 * SM::nBox);
   float *Fb = reinterpret_cast<float *>(prim + SM::nPrim);
   float *Ff = Fb + 5 * SM::nCell;
   float *dPb = Ff + 5 * SM::nCell;
   float *dPf = dPb + SM::nCell;
+  signed char *fbox = reinterpret_cast<signed char *>(dPf + SM::nCell);  // [X][X][X] flags
 
   const int n = a.ph.n, S = n + 4, nx = n + 1;
   const int nt = n / T;
@@ -218,12 +250,46 @@ __global__ void __launch_bounds__(T *T *T, 1) k_flux_split(FluxSplitArgs a) {
   const float RT0 = (float)(a.ph.P0 / a.ph.rho0);  // R * T0
   const float iR = (float)(1.0 / BCMG_R);
 
+  // Phase 0: stage the stencil box (tile +- 3 cells, clipped to the padded
+  // cube) of FP32 deltas and flags into shared memory.  Each box row along k
+  // is a contiguous run of 5*X floats in the cube's AoS layout, so the loads
+  // are coalesced and many are in flight per thread.  Box cells outside the
+  // padded cube are never read by the stencil (the reconstruction order falls
+  // back before reaching them) and are left unset.
+  {
+    const int k0 = bk - 3;
+    const int klo = k0 < 0 ? -k0 : 0;                 // first valid column
+    const int khi = (k0 + X > S) ? S - k0 : X;        // one past the last
+    const int rowlen = 5 * (khi - klo);
+    for (int w = tid; w < X * X * rowlen; w += NT) {
+      const int row = w / rowlen, e = w % rowlen;
+      const int bi_ = row / X, bj_ = row % X;
+      const int gi = bi - 3 + bi_, gj = bj - 3 + bj_;
+      if (gi < 0 || gi >= S || gj < 0 || gj >= S) continue;
+      const size_t g = cb + ((size_t)gi * S + gj) * S + (k0 + klo);
+      box[(row * X + klo) * 5 + e] = __ldg(M + 5 * g + e);
+    }
+    for (int w = tid; w < X * X * (khi - klo); w += NT) {
+      const int row = w / (khi - klo), e = w % (khi - klo);
+      const int bi_ = row / X, bj_ = row % X;
+      const int gi = bi - 3 + bi_, gj = bj - 3 + bj_;
+      if (gi < 0 || gi >= S || gj < 0 || gj >= S) continue;
+      fbox[row * X + klo + e] = (signed char)__ldg(F + cb + ((size_t)gi * S + gj) * S + (k0 + klo + e));
+    }
+  }
+  __syncthreads();
+  auto BX = [&](int li, int lj, int lk) -> const float * {  // li.. relative to tile origin
+    return box + (((li + 3) * X + (lj + 3)) * X + (lk + 3)) * 5;
+  };
+  auto FL = [&](int li, int lj, int lk) -> int {
+    return fbox[((li + 3) * X + (lj + 3)) * X + (lk + 3)];
+  };
+
   // Phase 1: primitives (u, v, w, T - T0) over the tile plus one halo cell.
   for (int p = tid; p < SM::nPrim; p += NT) {
     int li = p / (B * B), lj = (p / B) % B, lk = p % B;
-    const float *q =
-        M + 5 * (cb + ((size_t)(bi - 1 + li) * S + (bj - 1 + lj)) * S + (bk - 1 + lk));
-    float r = __ldg(q), m1 = __ldg(q + 1), m2 = __ldg(q + 2), m3 = __ldg(q + 3), e = __ldg(q + 4);
+    const float *q = BX(li - 1, lj - 1, lk - 1);
+    float r = q[0], m1 = q[1], m2 = q[2], m3 = q[3], e = q[4];
     float rho = rho0 + r;
     float ir = 1.0f / rho;
     PrimF pr;
@@ -249,10 +315,10 @@ __global__ void __launch_bounds__(T *T *T, 1) k_flux_split(FluxSplitArgs a) {
       else if (ax == 1) { li = p; lj = fa; lk = q; }
       else { li = p; lj = q; lk = fa; }
       const int g = (ax == 0 ? bi + li : (ax == 1 ? bj + lj : bk + lk));
-      const ptrdiff_t stride = ax == 0 ? (ptrdiff_t)S * S : (ax == 1 ? (ptrdiff_t)S : 1);
-      const size_t c0 = cb + ((size_t)(bi + li) * S + (bj + lj)) * S + (bk + lk);
-      const int fm2 = __ldg(F + c0 - 2 * stride), fm1 = __ldg(F + c0 - stride),
-                f0 = __ldg(F + c0), fp1 = __ldg(F + c0 + stride);
+      const int di = ax == 0, dj = ax == 1, dk = ax == 2;
+      const int fm2 = FL(li - 2 * di, lj - 2 * dj, lk - 2 * dk),
+                fm1 = FL(li - di, lj - dj, lk - dk), f0 = FL(li, lj, lk),
+                fp1 = FL(li + di, lj + dj, lk + dk);
       const bool needB = fa < T, needF = fa > 0;
       const int ob = order_backward(g, fm2, fm1, fp1);
       const int of = order_forward(g, nx, fm2, f0, fp1);
@@ -263,8 +329,9 @@ __global__ void __launch_bounds__(T *T *T, 1) k_flux_split(FluxSplitArgs a) {
       else if (needB && needF) { nviews = 2; ord0 = ob; dst0 = 1; ord1 = of; dst1 = 2; }
       else if (needB) { nviews = 1; ord0 = ob; dst0 = 1; }
       else { nviews = 1; ord0 = of; dst0 = 2; }
-      const float *base = M + 5 * c0;
-      auto ld = [&](int d, int v) -> float { return __ldg(base + 5 * stride * d + v); };
+      const float *base = BX(li, lj, lk);
+      const int sstride = 5 * (ax == 0 ? X * X : (ax == 1 ? X : 1));
+      auto ld = [&](int d, int v) -> float { return base[sstride * d + v]; };
 #pragma unroll 1
       for (int w = 0; w < nviews; ++w) {
         const int ord = w == 0 ? ord0 : ord1;
@@ -328,14 +395,14 @@ __global__ void __launch_bounds__(T *T *T, 1) k_flux_split(FluxSplitArgs a) {
   const size_t go = cb + ((size_t)(bi + mi) * S + (bj + mj)) * S + (bk + mk);
   const double *u = a.U1_ + 5 * go;
   const double *uu = a.U1 + 5 * go;
-  const double *uq = a.U1q + 5 * go;
-  const int IF = __ldg(F + go);
+  const float *d2p = a.D2 + 5 * go;
+  const int IF = FL(mi, mj, mk);
   const float i2dt = (float)(1.0 / (2.0 * a.dT));
   float Rk[5];
 #pragma unroll
   for (int v = 0; v < 5; ++v) {
-    const double x = __ldg(u + v), y = __ldg(uu + v), z = __ldg(uq + v);
-    const float d1 = (float)(x - y), d2 = (float)(y - z);
+    const double x = __ldg(u + v), y = __ldg(uu + v);
+    const float d1 = (float)(x - y), d2 = __ldg(d2p + v);
     const float Rp = -(3.0f * d1 - d2) * i2dt;
     Rk[v] = Rp - acc[v] + vF[v];
   }
@@ -343,11 +410,11 @@ __global__ void __launch_bounds__(T *T *T, 1) k_flux_split(FluxSplitArgs a) {
   if (IF == kFluid) {
     const float K = 1.4f, Km1 = 0.4f;
     const float dT = (float)a.dT, dTau = (float)a.dTau;
-    const float *qm = M + 5 * go;
-    const float rho = rho0 + __ldg(qm);
+    const float *qm = BX(mi, mj, mk);
+    const float rho = rho0 + qm[0];
     const float Uc = c.U, Vc = c.V, Wc = c.W;
     const float VV = Uc * Uc + Vc * Vc + Wc * Wc;
-    const float Pc = P0 + (__ldg(qm + 4) - 0.5f * rho * VV) * Km1;
+    const float Pc = P0 + (qm[4] - 0.5f * rho * VV) * Km1;
     const float Tt = Pc / rho;  // P/rho (:2302)
     const float C = K * Tt;
     const float H = 0.5f * VV + C / Km1;

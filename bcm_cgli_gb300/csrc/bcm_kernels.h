@@ -36,12 +36,15 @@ struct FluxSplitArgs {
   const double *cube_size;
   const float *M;  // FP32 deltas of U1_ (k_mirror)
   const double *U1_, *U1, *U1q;
+  const float *D2;  // FP32 of the FP64 difference U1 - U1q (k_level_diff)
   float *Rku32;  // FP32 increments
   double *Residual1;
 };
 cudaError_t launch_mirror(const double *U, float *M, int n, int ncube, double rho0, double P0,
                           cudaStream_t s);
 cudaError_t launch_flux_split(const FluxSplitArgs &a, int ncubes, cudaStream_t s);
+cudaError_t launch_level_diff(const double *U1, const double *U1q, float *D2, int n, int ncube,
+                              cudaStream_t s);
 struct RkSplitArgs {
   Phys ph;
   int ncube;

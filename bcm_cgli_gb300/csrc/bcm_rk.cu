@@ -96,11 +96,16 @@ __global__ void __launch_bounds__(kRkThreads) k_rk(RkArgs a, long long total, lo
 }
 
 __global__ void k_norms(Phys ph, const double *partials, int nblocks, double *er) {
+  // One warp per quantity: lane l sums blocks l, l+32, ... in order, then a
+  // fixed shuffle tree; the result does not depend on timing.
   __shared__ double tot[7];
-  if (threadIdx.x < 7) {
+  const int m = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (m < 7) {
     double v = 0;
-    for (int b = 0; b < nblocks; ++b) v += partials[(size_t)b * 7 + threadIdx.x];
-    tot[threadIdx.x] = v;
+    for (int b = lane; b < nblocks; b += 32) v += partials[(size_t)b * 7 + m];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if (lane == 0) tot[m] = v;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -141,7 +146,7 @@ cudaError_t launch_rk(const RkArgs &a, int *nblocks_out, cudaStream_t s) {
 
 cudaError_t launch_norms(const Phys &ph, const double *partials, int nblocks, double *er,
                          cudaStream_t s) {
-  k_norms<<<1, 32, 0, s>>>(ph, partials, nblocks, er);
+  k_norms<<<1, 7 * 32, 0, s>>>(ph, partials, nblocks, er);
   return cudaGetLastError();
 }
 

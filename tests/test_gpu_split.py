@@ -1,0 +1,62 @@
+"""Split-precision path against the FP64 path (which is bit-exact with the
+reference).  Bound: relative L2 error <= 1e-5 per conservative variable
+(momentum components relative to the momentum-magnitude norm, since rho*w
+of these flows is ~0) after the same steps from the same state."""
+import numpy as np
+import pytest
+
+from bcm_cgli_gb300 import api, cases
+from golden import golden_cases as G
+
+pytestmark = pytest.mark.gpu
+
+SPLIT_BOUND = 1e-5
+
+
+def rel_l2(a, b, n):
+    ai = a[1:, 2:n + 2, 2:n + 2, 2:n + 2].reshape(-1, 5)
+    bi = b[1:, 2:n + 2, 2:n + 2, 2:n + 2].reshape(-1, 5)
+    d = ai - bi
+    mom = np.linalg.norm(bi[:, 1:4])
+    return [np.linalg.norm(d[:, 0]) / np.linalg.norm(bi[:, 0])] + \
+           [np.linalg.norm(d[:, v]) / mom for v in (1, 2, 3)] + \
+           [np.linalg.norm(d[:, 4]) / np.linalg.norm(bi[:, 4])]
+
+
+def run(case, precision, steps, subiters, graph=True):
+    ctx = api.CaseContext(case, precision=precision)
+    ctx.set_state(case.U, case.U, case.U)
+    er = ctx.advance(steps, subiters, use_graph=graph)
+    U = ctx.get_state()
+    ctx.close()
+    return U, er
+
+
+@pytest.mark.parametrize("name", sorted(G.golden_cases()))
+def test_split_within_bound_of_fp64(name):
+    case = G.golden_cases()[name]
+    (a, _, _), er_a = run(case, api.PRECISION_FP64, 2, 3)
+    (b, _, _), er_b = run(case, api.PRECISION_SPLIT, 2, 3)
+    err = rel_l2(b, a, case.n)
+    assert max(err) <= SPLIT_BOUND, err
+    # the change norms agree to FP32-level relative accuracy where they are
+    # not dominated by round-off (components of order 1 after normalisation)
+    for m in (1, 2, 3, 5):
+        assert abs(er_a[m] - er_b[m]) <= 1e-3 * max(abs(er_a[m]), 1e-12), (m, er_a, er_b)
+
+
+def test_split_graph_replay_is_identical():
+    case = G.golden_cases()["tgv_n8"]
+    (a, a1, a2), _ = run(case, api.PRECISION_SPLIT, 2, 2, graph=False)
+    (b, b1, b2), _ = run(case, api.PRECISION_SPLIT, 2, 2, graph=True)
+    assert np.array_equal(a, b) and np.array_equal(a1, b1) and np.array_equal(a2, b2)
+
+
+def test_split_vortex_config1_size():
+    """Config-1 size (4x4x4 cubes of 16^3, inviscid vortex, M 0.5): 3 dual-time
+    steps of 10 sub-iterations, split vs FP64."""
+    case = cases.isentropic_vortex(ncx=4, n=16)
+    (a, _, _), _ = run(case, api.PRECISION_FP64, 3, 10)
+    (b, _, _), _ = run(case, api.PRECISION_SPLIT, 3, 10)
+    err = rel_l2(b, a, case.n)
+    assert max(err) <= SPLIT_BOUND, err
