@@ -151,6 +151,7 @@ struct bcmg_case {
          *Rku1 = nullptr, *Residual1 = nullptr;
   float *M = nullptr, *Rku32 = nullptr;  // split precision: FP32 deltas, increments
   float *D2 = nullptr;                   // split precision: FP32 of U1 - U1q
+  float *inv_dx = nullptr;               // split precision: n / cube_size per cube
   int *FWS = nullptr;
   double *cube_size = nullptr;
   int *task_off = nullptr;
@@ -180,7 +181,7 @@ struct bcmg_case {
     for (auto x : ev) cudaEventDestroy(x);
     ev.clear();
     dfree(U1_); dfree(U1); dfree(U1q); dfree(U1p1); dfree(U1p2); dfree(Rku1); dfree(Residual1);
-    dfree(M); dfree(Rku32); dfree(D2);
+    dfree(M); dfree(Rku32); dfree(D2); dfree(inv_dx);
     dfree(FWS); dfree(cube_size); dfree(task_off); dfree(tasks); dfree(bc_cubes);
     dfree(bc_masks); dfree(partials); dfree(er); dfree(emax);
     ibm.release();
@@ -226,6 +227,15 @@ int case_flux(bcmg_case *c) {
     sa.dT = c->dT;
     sa.dTau = c->dTau;
     sa.ef = (float)c->e;
+    sa.rho0f = (float)c->ph.rho0;
+    sa.P0f = (float)c->ph.P0;
+    sa.RT0f = (float)(c->ph.P0 / c->ph.rho0);
+    sa.T0f = (float)(c->ph.P0 / c->ph.rho0 / BCMG_R);
+    sa.mu_Lf = (float)c->ph.mu_L;
+    sa.i2dtf = (float)(1.0 / (2.0 * c->dT));
+    sa.dTf = (float)c->dT;
+    sa.dTauf = (float)c->dTau;
+    sa.inv_dx = c->inv_dx;
     sa.FWS = c->FWS;
     sa.cube_size = c->cube_size;
     sa.M = c->M;
@@ -431,9 +441,17 @@ int bcmg_case_create(const bcmg_case_desc *d, bcmg_case **out) {
   if (d->precision == BCMG_PRECISION_SPLIT &&
       !(ck(dalloc(&c->M, nd), "alloc") && ck(dalloc(&c->Rku32, nd), "alloc") &&
         ck(dalloc(&c->D2, nd), "alloc") && ck(cudaMemset(c->D2, 0, nd * sizeof(float)), "memset") &&
+        ck(dalloc(&c->inv_dx, (size_t)d->ncube), "alloc") &&
         ck(cudaMemset(c->M, 0, nd * sizeof(float)), "memset") &&
         ck(cudaMemset(c->Rku32, 0, nd * sizeof(float)), "memset")))
     return fail(BCMG_ERR_CUDA);
+  if (c->inv_dx) {
+    std::vector<float> inv((size_t)d->ncube, 0.f);
+    for (int i = 1; i < d->ncube; ++i) inv[i] = (float)(d->n / d->cube_size[i]);
+    if (!ck(cudaMemcpy(c->inv_dx, inv.data(), sizeof(float) * inv.size(), cudaMemcpyHostToDevice),
+            "copy"))
+      return fail(BCMG_ERR_CUDA);
+  }
   RkArgs probe{};
   probe.ph = c->ph;
   probe.ncube = c->ncube;

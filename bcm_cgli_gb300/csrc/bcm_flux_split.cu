@@ -221,12 +221,18 @@ __device__ __forceinline__ void visc_face_f(float mu_L, float T0, const PrimF &c
   L[3] = Um * s1 + Vm * s2 + Wm * s3 + mu_E * (float)(BCMG_CV * BCMG_K / BCMG_PR) * gn[3];
 }
 
+// One thread per face of an axis ((T+1)*T*T, rounded up to whole warps: the
+// staging loop gives every warp whole rows), so the face phase runs in one
+// balanced round; the first T^3 threads also own one cell each.
+template <int T>
+__host__ __device__ constexpr int split_threads() { return (((T + 1) * T * T) + 31) / 32 * 32; }
+
 template <int T, bool VISCOUS>
-__global__ void __launch_bounds__(T *T *T, 1) k_flux_split(FluxSplitArgs a) {
+__global__ void __launch_bounds__(split_threads<T>(), 1) k_flux_split(FluxSplitArgs a) {
   using SM = SplitSmem<T>;
   constexpr int B = SM::B;
   constexpr int X = SM::X;
-  constexpr int NT = T * T * T;
+  constexpr int NT = split_threads<T>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float *box = reinterpret_cast<float *>(smem_raw);  // [X][X][X][5] deltas
   PrimF *prim = reinterpret_cast<PrimF *>(box + 5 * SM::nBox);
@@ -246,9 +252,9 @@ __global__ void __launch_bounds__(T *T *T, 1) k_flux_split(FluxSplitArgs a) {
   const float *__restrict__ M = a.M;
   const int *__restrict__ F = a.FWS;
   const size_t cb = cell_index(S, cube, 0, 0, 0);
-  const float rho0 = (float)a.ph.rho0, P0 = (float)a.ph.P0;
-  const float RT0 = (float)(a.ph.P0 / a.ph.rho0);  // R * T0
-  const float iR = (float)(1.0 / BCMG_R);
+  const float rho0 = a.rho0f, P0 = a.P0f;
+  const float RT0 = a.RT0f;  // R * T0
+  const float iR = 1.0f / 287.0f;
 
   // Phase 0: stage the stencil box (tile +- 3 cells, clipped to the padded
   // cube) of FP32 deltas and flags into shared memory.  Each box row along k
@@ -260,21 +266,20 @@ __global__ void __launch_bounds__(T *T *T, 1) k_flux_split(FluxSplitArgs a) {
     const int k0 = bk - 3;
     const int klo = k0 < 0 ? -k0 : 0;                 // first valid column
     const int khi = (k0 + X > S) ? S - k0 : X;        // one past the last
-    const int rowlen = 5 * (khi - klo);
-    for (int w = tid; w < X * X * rowlen; w += NT) {
-      const int row = w / rowlen, e = w % rowlen;
-      const int bi_ = row / X, bj_ = row % X;
+    const int ncol = khi - klo;
+    const int warp = tid >> 5, lane = tid & 31;
+    constexpr int NW = (NT + 31) / 32;
+    for (int row = warp; row < X * X; row += NW) {
+      const int bi_ = row / X, bj_ = row - (row / X) * X;
       const int gi = bi - 3 + bi_, gj = bj - 3 + bj_;
       if (gi < 0 || gi >= S || gj < 0 || gj >= S) continue;
       const size_t g = cb + ((size_t)gi * S + gj) * S + (k0 + klo);
-      box[(row * X + klo) * 5 + e] = __ldg(M + 5 * g + e);
-    }
-    for (int w = tid; w < X * X * (khi - klo); w += NT) {
-      const int row = w / (khi - klo), e = w % (khi - klo);
-      const int bi_ = row / X, bj_ = row % X;
-      const int gi = bi - 3 + bi_, gj = bj - 3 + bj_;
-      if (gi < 0 || gi >= S || gj < 0 || gj >= S) continue;
-      fbox[row * X + klo + e] = (signed char)__ldg(F + cb + ((size_t)gi * S + gj) * S + (k0 + klo + e));
+      const float *src = M + 5 * g;
+      float *dst = box + (row * X + klo) * 5;
+      for (int e = lane; e < 5 * ncol; e += 32) dst[e] = __ldg(src + e);
+      const int *fsrc = F + g;
+      signed char *fdst = fbox + row * X + klo;
+      for (int e = lane; e < ncol; e += 32) fdst[e] = (signed char)__ldg(fsrc + e);
     }
   }
   __syncthreads();
@@ -301,8 +306,7 @@ __global__ void __launch_bounds__(T *T *T, 1) k_flux_split(FluxSplitArgs a) {
     prim[p] = pr;
   }
 
-  const float dxf = (float)(a.cube_size[cube] / n);
-  const float inv = 1.0f / dxf;
+  const float inv = a.inv_dx[cube];
   float acc[5];
   float dPdx = 0, dPdz = 0;
 
@@ -354,15 +358,18 @@ __global__ void __launch_bounds__(T *T *T, 1) k_flux_split(FluxSplitArgs a) {
       }
     }
     __syncthreads();
+    if (tid < SM::nCell) {
 #pragma unroll
-    for (int v = 0; v < 5; ++v) {
-      float t = (Ff[5 * tid + v] - Fb[5 * tid + v]) * inv;
-      acc[v] = ax == 0 ? t : acc[v] + t;
+      for (int v = 0; v < 5; ++v) {
+        float t = (Ff[5 * tid + v] - Fb[5 * tid + v]) * inv;
+        acc[v] = ax == 0 ? t : acc[v] + t;
+      }
+      if (ax == 0) dPdx = dPf[tid] - dPb[tid];
+      if (ax == 2) dPdz = dPf[tid] - dPb[tid];
     }
-    if (ax == 0) dPdx = dPf[tid] - dPb[tid];
-    if (ax == 2) dPdz = dPf[tid] - dPb[tid];
     __syncthreads();
   }
+  if (tid >= SM::nCell) return;
 
   const int mi = tid / (T * T), mj = (tid / T) % T, mk = tid % T;
   auto P = [&](int di, int dj, int dk) -> const PrimF & {
@@ -371,8 +378,8 @@ __global__ void __launch_bounds__(T *T *T, 1) k_flux_split(FluxSplitArgs a) {
   const PrimF &c = P(0, 0, 0);
   float vF[5] = {0, 0, 0, 0, 0};
   if (VISCOUS) {
-    const float T0 = (float)(a.ph.P0 / a.ph.rho0 / BCMG_R);
-    const float mu_L = (float)a.ph.mu_L;
+    const float T0 = a.T0f;
+    const float mu_L = a.mu_Lf;
     float Lb[4], Lf[4], Mb[4], Mf[4], Nb[4], Nf[4];
     visc_face_f<0, false>(mu_L, T0, c, P(-1, 0, 0), inv, P(0, 1, 0), P(-1, 1, 0), P(0, -1, 0),
                           P(-1, -1, 0), P(0, 0, 1), P(-1, 0, 1), P(0, 0, -1), P(-1, 0, -1), Lb);
@@ -397,7 +404,7 @@ __global__ void __launch_bounds__(T *T *T, 1) k_flux_split(FluxSplitArgs a) {
   const double *uu = a.U1 + 5 * go;
   const float *d2p = a.D2 + 5 * go;
   const int IF = FL(mi, mj, mk);
-  const float i2dt = (float)(1.0 / (2.0 * a.dT));
+  const float i2dt = a.i2dtf;
   float Rk[5];
 #pragma unroll
   for (int v = 0; v < 5; ++v) {
@@ -409,7 +416,7 @@ __global__ void __launch_bounds__(T *T *T, 1) k_flux_split(FluxSplitArgs a) {
   float *rk = a.Rku32 + 5 * go;
   if (IF == kFluid) {
     const float K = 1.4f, Km1 = 0.4f;
-    const float dT = (float)a.dT, dTau = (float)a.dTau;
+    const float dT = a.dTf, dTau = a.dTauf;
     const float *qm = BX(mi, mj, mk);
     const float rho = rho0 + qm[0];
     const float Uc = c.U, Vc = c.V, Wc = c.W;
@@ -477,12 +484,12 @@ static cudaError_t launch_split_t(const FluxSplitArgs &a, int ncubes, cudaStream
     e = cudaFuncSetAttribute(k_flux_split<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
     if (e != cudaSuccess) return e;
-    k_flux_split<T, true><<<grid, T * T * T, smem, s>>>(a);
+    k_flux_split<T, true><<<grid, split_threads<T>(), smem, s>>>(a);
   } else {
     e = cudaFuncSetAttribute(k_flux_split<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
     if (e != cudaSuccess) return e;
-    k_flux_split<T, false><<<grid, T * T * T, smem, s>>>(a);
+    k_flux_split<T, false><<<grid, split_threads<T>(), smem, s>>>(a);
   }
   return cudaGetLastError();
 }

@@ -32,6 +32,10 @@ struct FluxSplitArgs {
   int cube0;
   double dT, dTau;
   float ef;  // e (beta floor)
+  // FP32 constants formed once on the host (FP64 arithmetic on the device
+  // costs 64 FP32 issue slots per instruction on this part)
+  float rho0f, P0f, RT0f, T0f, mu_Lf, i2dtf, dTf, dTauf;
+  const float *inv_dx;  // [ncube] n / cube_size
   const int *FWS;
   const double *cube_size;
   const float *M;  // FP32 deltas of U1_ (k_mirror)
