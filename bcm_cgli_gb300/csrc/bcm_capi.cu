@@ -149,7 +149,7 @@ struct bcmg_case {
   cudaStream_t stream = nullptr;
   double *U1_ = nullptr, *U1 = nullptr, *U1q = nullptr, *U1p1 = nullptr, *U1p2 = nullptr,
          *Rku1 = nullptr, *Residual1 = nullptr;
-  float *M = nullptr, *Rku32 = nullptr;  // split precision: FP32 deltas, increments
+  float *M = nullptr;                    // split precision: FP32 deltas of U1_
   float *D2 = nullptr;                   // split precision: FP32 of U1 - U1q
   float *inv_dx = nullptr;               // split precision: n / cube_size per cube
   int *FWS = nullptr;
@@ -181,7 +181,7 @@ struct bcmg_case {
     for (auto x : ev) cudaEventDestroy(x);
     ev.clear();
     dfree(U1_); dfree(U1); dfree(U1q); dfree(U1p1); dfree(U1p2); dfree(Rku1); dfree(Residual1);
-    dfree(M); dfree(Rku32); dfree(D2); dfree(inv_dx);
+    dfree(M); dfree(D2); dfree(inv_dx);
     dfree(FWS); dfree(cube_size); dfree(task_off); dfree(tasks); dfree(bc_cubes);
     dfree(bc_masks); dfree(partials); dfree(er); dfree(emax);
     ibm.release();
@@ -192,7 +192,7 @@ struct bcmg_case {
 
 namespace {
 
-int case_flux(bcmg_case *c) {
+int case_flux(bcmg_case *c, int RK) {
   FluxArgs a;
   a.ph = c->ph;
   a.cube0 = 1;
@@ -243,7 +243,8 @@ int case_flux(bcmg_case *c) {
     sa.U1 = c->U1;
     sa.U1q = c->U1q;
     sa.D2 = c->D2;
-    sa.Rku32 = c->Rku32;
+    sa.RK = RK;
+    sa.partials = c->partials;
     sa.Residual1 = c->Residual1;
     CK(launch_flux_split(sa, c->ncube - 1, c->stream));
   } else {
@@ -283,7 +284,17 @@ int case_stage(bcmg_case *c, int RK) {
   if ((r = ibm_run(c->ibm, c->ph.n, c->ph.rho0, c->ph.P0, c->U1_, c->stream, &c->launches)))
     return r;
   if ((r = case_interface(c))) return r;
-  if ((r = case_flux(c))) return r;
+  if ((r = case_flux(c, RK))) return r;
+  int nb = 0;
+  if (c->precision == BCMG_PRECISION_SPLIT) {
+    // the split flux kernel applied the stage update and wrote the partials
+    nb = flux_split_blocks(c->ph.n, c->ncube - 1);
+    if (RK == 3) {
+      CK(launch_norms(c->ph, c->partials, nb, c->er, c->stream));
+      ++c->launches;
+    }
+    return case_interface(c);
+  }
   RkArgs k;
   k.ph = c->ph;
   k.ncube = c->ncube;
@@ -295,21 +306,7 @@ int case_stage(bcmg_case *c, int RK) {
   k.Rku1 = c->Rku1;
   k.Residual1 = c->Residual1;
   k.partials = c->partials;
-  int nb = 0;
-  if (c->precision == BCMG_PRECISION_SPLIT) {
-    RkSplitArgs ks;
-    ks.ph = c->ph;
-    ks.ncube = c->ncube;
-    ks.RK = RK;
-    ks.FWS = c->FWS;
-    ks.U1_ = c->U1_;
-    ks.Rku32 = c->Rku32;
-    ks.Residual1 = c->Residual1;
-    ks.partials = c->partials;
-    CK(launch_rk_split(ks, &nb, c->stream));
-  } else {
-    CK(launch_rk(k, &nb, c->stream));
-  }
+  CK(launch_rk(k, &nb, c->stream));
   ++c->launches;
   if (RK == 3) {
     CK(launch_norms(c->ph, c->partials, nb, c->er, c->stream));
@@ -439,11 +436,11 @@ int bcmg_case_create(const bcmg_case_desc *d, bcmg_case **out) {
             ck(dalloc(&c->er, 8), "alloc") && ck(dalloc(&c->emax, 6), "alloc");
   if (!ok) return fail(BCMG_ERR_CUDA);
   if (d->precision == BCMG_PRECISION_SPLIT &&
-      !(ck(dalloc(&c->M, nd), "alloc") && ck(dalloc(&c->Rku32, nd), "alloc") &&
+      !(ck(dalloc(&c->M, nd), "alloc") &&
         ck(dalloc(&c->D2, nd), "alloc") && ck(cudaMemset(c->D2, 0, nd * sizeof(float)), "memset") &&
         ck(dalloc(&c->inv_dx, (size_t)d->ncube), "alloc") &&
         ck(cudaMemset(c->M, 0, nd * sizeof(float)), "memset") &&
-        ck(cudaMemset(c->Rku32, 0, nd * sizeof(float)), "memset")))
+        true))
     return fail(BCMG_ERR_CUDA);
   if (c->inv_dx) {
     std::vector<float> inv((size_t)d->ncube, 0.f);
@@ -456,6 +453,8 @@ int bcmg_case_create(const bcmg_case_desc *d, bcmg_case **out) {
   probe.ph = c->ph;
   probe.ncube = c->ncube;
   c->nparts = rk_partial_blocks(probe);
+  if (d->precision == BCMG_PRECISION_SPLIT)
+    c->nparts = std::max(c->nparts, flux_split_blocks(d->n, d->ncube - 1));
   if (!ck(dalloc(&c->partials, (size_t)c->nparts * 7), "alloc")) return fail(BCMG_ERR_CUDA);
   cudaStream_t s = c->stream;
   ok = ck(cudaMemsetAsync(c->U1_, 0, nd * 8, s), "memset") &&
@@ -593,8 +592,8 @@ int bcmg_case_advance(bcmg_case *c, int steps, int subiters, int use_graph, doub
     {
       // kernel nodes per step, counted like case_step
       int L = (int)(c->ibm.level_off.size() > 0 ? c->ibm.level_off.size() - 1 : 0);
-      long long stage = (c->nbc > 0) + L + 1 + 1 + 1 + 1 +
-                        (c->precision == BCMG_PRECISION_SPLIT ? 1 : 0);
+      // bc, IBM levels, interface, [mirror], flux, [rk], interface
+      long long stage = (c->nbc > 0) + L + 1 + 1 + 1 + 1;
       per = subiters * (3 * stage + 1 + 1) + 1 + (c->precision == BCMG_PRECISION_SPLIT ? 1 : 0);
     }
     for (int s = 0; s < steps; ++s) CK(cudaGraphLaunch(c->graph, c->stream));
@@ -645,12 +644,19 @@ int bcmg_case_time_flux(bcmg_case *c, int reps, double *ms) {
   CK(cudaEventCreate(&b));
   bool prof = c->profile;
   c->profile = false;
-  int r = case_flux(c);  // warm-up
+  const size_t bytes = c->ncell * 5 * sizeof(double);
+  // The split kernel applies its stage update in place: keep a copy of the
+  // state in the (split-unused) U1p1 buffer and restore it afterwards.
+  if (c->precision == BCMG_PRECISION_SPLIT)
+    CK(cudaMemcpyAsync(c->U1p1, c->U1_, bytes, cudaMemcpyDeviceToDevice, c->stream));
+  int r = case_flux(c, 1);  // warm-up
   if (!r) {
     cudaEventRecord(a, c->stream);
-    for (int i = 0; i < reps && !r; ++i) r = case_flux(c);
+    for (int i = 0; i < reps && !r; ++i) r = case_flux(c, 1);
     cudaEventRecord(b, c->stream);
   }
+  if (c->precision == BCMG_PRECISION_SPLIT)
+    CK(cudaMemcpyAsync(c->U1_, c->U1p1, bytes, cudaMemcpyDeviceToDevice, c->stream));
   c->profile = prof;
   if (r) { cudaEventDestroy(a); cudaEventDestroy(b); return r; }
   CK(cudaEventSynchronize(b));

@@ -1,4 +1,4 @@
-// Split-precision residual + preconditioned increment, and its stage update.
+// Split-precision residual, preconditioned increment and stage update, fused.
 //
 // Same operator as BCM_Flux_XYZ_Viscous_Runge_kutta (BCM_Flux_XYZ_Viscous_
 // Runge_kutta.cpp:326-2652) with the arithmetic split by where precision is
@@ -92,7 +92,10 @@ struct SplitSmem {
   static constexpr int nBox = X * X * X;
   static constexpr size_t bytes = sizeof(float) * 5 * nBox /*state deltas*/ +
                                   sizeof(PrimF) * nPrim + 2 * sizeof(float) * 5 * nCell +
-                                  2 * sizeof(float) * nCell + ((nBox + 15) / 16) * 16 /*flags*/;
+                                  2 * sizeof(float) * nCell /*dPb, dPf*/ +
+                                  sizeof(float) * 5 * nCell /*flux balance*/ +
+                                  2 * sizeof(float) * nCell /*x, z pressure differences*/ +
+                                  ((nBox + 15) / 16) * 16 /*flags*/;
 };
 
 // Delta-form preconditioned Roe flux (same formulas as face_flux in
@@ -221,14 +224,21 @@ __device__ __forceinline__ void visc_face_f(float mu_L, float T0, const PrimF &c
   L[3] = Um * s1 + Vm * s2 + Wm * s3 + mu_E * (float)(BCMG_CV * BCMG_K / BCMG_PR) * gn[3];
 }
 
-// One thread per face of an axis ((T+1)*T*T, rounded up to whole warps: the
-// staging loop gives every warp whole rows), so the face phase runs in one
-// balanced round; the first T^3 threads also own one cell each.
+// Threads per CTA: for 8^3 tiles, half the 576 faces of an axis (two faces
+// and up to two cells per thread) so that two CTAs (~110 KB shared memory
+// each) share an SM and one CTA's staging, barriers and FP64 tail overlap
+// the other's FP32 work; for 4^3 tiles one face per thread.  Whole warps
+// (the staging loop gives every warp whole rows).
 template <int T>
-__host__ __device__ constexpr int split_threads() { return (((T + 1) * T * T) + 31) / 32 * 32; }
+__host__ __device__ constexpr int split_threads() {
+  return T == 8 ? 288 : (((T + 1) * T * T) + 31) / 32 * 32;
+}
+template <int T>
+__host__ __device__ constexpr int split_ctas_per_sm() { return T == 8 ? 2 : 1; }
 
 template <int T, bool VISCOUS>
-__global__ void __launch_bounds__(split_threads<T>(), 1) k_flux_split(FluxSplitArgs a) {
+__global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
+    k_flux_split(FluxSplitArgs a) {
   using SM = SplitSmem<T>;
   constexpr int B = SM::B;
   constexpr int X = SM::X;
@@ -240,7 +250,10 @@ __global__ void __launch_bounds__(split_threads<T>(), 1) k_flux_split(FluxSplitA
   float *Ff = Fb + 5 * SM::nCell;
   float *dPb = Ff + 5 * SM::nCell;
   float *dPf = dPb + SM::nCell;
-  signed char *fbox = reinterpret_cast<signed char *>(dPf + SM::nCell);  // [X][X][X] flags
+  float *accS = dPf + SM::nCell;        // [nCell][5] Rfx/dx + Rfy/dy + Rfz/dz
+  float *dPxS = accS + 5 * SM::nCell;   // [nCell] x-face pressure difference
+  float *dPzS = dPxS + SM::nCell;       // [nCell] z-face pressure difference
+  signed char *fbox = reinterpret_cast<signed char *>(dPzS + SM::nCell);  // [X][X][X] flags
 
   const int n = a.ph.n, S = n + 4, nx = n + 1;
   const int nt = n / T;
@@ -307,8 +320,6 @@ __global__ void __launch_bounds__(split_threads<T>(), 1) k_flux_split(FluxSplitA
   }
 
   const float inv = a.inv_dx[cube];
-  float acc[5];
-  float dPdx = 0, dPdz = 0;
 
 #pragma unroll 1
   for (int ax = 0; ax < 3; ++ax) {
@@ -358,20 +369,27 @@ __global__ void __launch_bounds__(split_threads<T>(), 1) k_flux_split(FluxSplitA
       }
     }
     __syncthreads();
-    if (tid < SM::nCell) {
+    for (int cl = tid; cl < SM::nCell; cl += NT) {
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
-        float t = (Ff[5 * tid + v] - Fb[5 * tid + v]) * inv;
-        acc[v] = ax == 0 ? t : acc[v] + t;
+        float t = (Ff[5 * cl + v] - Fb[5 * cl + v]) * inv;
+        accS[5 * cl + v] = ax == 0 ? t : accS[5 * cl + v] + t;
       }
-      if (ax == 0) dPdx = dPf[tid] - dPb[tid];
-      if (ax == 2) dPdz = dPf[tid] - dPb[tid];
+      if (ax == 0) dPxS[cl] = dPf[cl] - dPb[cl];
+      if (ax == 2) dPzS[cl] = dPf[cl] - dPb[cl];
     }
     __syncthreads();
   }
-  if (tid >= SM::nCell) return;
-
-  const int mi = tid / (T * T), mj = (tid / T) % T, mk = tid % T;
+  // Norm / force partial sums of this CTA (stage 3), reduced below by all
+  // threads.
+  double s5[7] = {0, 0, 0, 0, 0, 0, 0};
+#pragma unroll 1
+  for (int cl = tid; cl < SM::nCell; cl += NT) {
+  const int mi = cl / (T * T), mj = (cl / T) % T, mk = cl % T;
+  float acc[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) acc[v] = accS[5 * cl + v];
+  const float dPdx = dPxS[cl], dPdz = dPzS[cl];
   auto P = [&](int di, int dj, int dk) -> const PrimF & {
     return prim[((mi + 1 + di) * B + (mj + 1 + dj)) * B + (mk + 1 + dk)];
   };
@@ -400,20 +418,21 @@ __global__ void __launch_bounds__(split_threads<T>(), 1) k_flux_split(FluxSplitA
 
   // BDF2 source from FP64 time-level differences, then FP32.
   const size_t go = cb + ((size_t)(bi + mi) * S + (bj + mj)) * S + (bk + mk);
-  const double *u = a.U1_ + 5 * go;
+  double *u = a.U1_ + 5 * go;  // only this thread reads or writes these cells
   const double *uu = a.U1 + 5 * go;
   const float *d2p = a.D2 + 5 * go;
   const int IF = FL(mi, mj, mk);
   const float i2dt = a.i2dtf;
   float Rk[5];
+  double xq[5];
 #pragma unroll
   for (int v = 0; v < 5; ++v) {
-    const double x = __ldg(u + v), y = __ldg(uu + v);
+    const double x = u[v], y = __ldg(uu + v);
+    xq[v] = x;
     const float d1 = (float)(x - y), d2 = __ldg(d2p + v);
     const float Rp = -(3.0f * d1 - d2) * i2dt;
     Rk[v] = Rp - acc[v] + vF[v];
   }
-  float *rk = a.Rku32 + 5 * go;
   if (IF == kFluid) {
     const float K = 1.4f, Km1 = 0.4f;
     const float dT = a.dTf, dTau = a.dTauf;
@@ -459,17 +478,65 @@ __global__ void __launch_bounds__(split_threads<T>(), 1) k_flux_split(FluxSplitA
     d[4][2] = (-4 * H * Vc * temp2) * itemp;
     d[4][3] = (-4 * H * Wc * temp2) * itemp;
     d[4][4] = (2 * dT * (2 * H * Km1 * bm1 * dT + K * Tt * (2 * dT + 3 * beta * dTau))) * itemp;
+    // Stage update Q += w dQ (w = 1, 1/4, 2/3): the reference's RK
+    // combinations with Q1 = Q2 = Q on fluid cells at stage entry.
+    const float w = a.RK == 1 ? 1.0f : (a.RK == 2 ? 0.25f : 2.0f / 3.0f);
+    float dq[5];
 #pragma unroll
-    for (int r = 0; r < 5; ++r)
-      rk[r] = dTau * (d[r][0] * Rk[0] + d[r][1] * Rk[1] + d[r][2] * Rk[2] + d[r][3] * Rk[3] +
-                      d[r][4] * Rk[4]);
+    for (int r = 0; r < 5; ++r) {
+      dq[r] = w * dTau * (d[r][0] * Rk[0] + d[r][1] * Rk[1] + d[r][2] * Rk[2] +
+                          d[r][3] * Rk[3] + d[r][4] * Rk[4]);
+      u[r] = xq[r] + (double)dq[r];
+    }
+    if (a.RK == 3) {
+      // Change norms of p, u, v, w, T from the increment, in FP32; summed
+      // in FP64 (BCM_Flux...cpp:2530-2566).
+      const float rf = rho, m1 = (float)xq[1], m2 = (float)xq[2], m3 = (float)xq[3];
+      const float dr = dq[0], e1 = dq[1], e2 = dq[2], e3 = dq[3], dE = dq[4];
+      const float den = 1.0f / (rf * (rf + dr));
+      const float dU = (e1 * rf - m1 * dr) * den;
+      const float dVv = (e2 * rf - m2 * dr) * den;
+      const float dW = (e3 * rf - m3 * dr) * den;
+      const float mm = m1 * m1 + m2 * m2 + m3 * m3;
+      const float dKE =
+          0.5f * ((2.f * (m1 * e1 + m2 * e2 + m3 * e3) + e1 * e1 + e2 * e2 + e3 * e3) * rf - mm * dr) * den;
+      const float dP = Km1 * (dE - dKE);
+      const float dTt = (dP * rf - Pc * dr) * den;
+      s5[0] += (double)(dP * dP);
+      s5[1] += (double)(dU * dU);
+      s5[2] += (double)(dVv * dVv);
+      s5[3] += (double)(dW * dW);
+      s5[4] += (double)(dTt * dTt);
+    }
   } else {
-#pragma unroll
-    for (int r = 0; r < 5; ++r) rk[r] = 0.f;
+    // Force integrands on non-fluid cells (:2395-2398); their sum over the
+    // case is er[6], er[7].
     const double dx = a.cube_size[cube] / n;
     const double dV = dx * dx * dx;
-    a.Residual1[5 * go + 0] = -((double)(-dPdx * inv) + (double)vF[1]) * dV;
-    a.Residual1[5 * go + 1] = -((double)(-dPdz * inv) + (double)vF[3]) * dV;
+    const double r0 = -((double)(-dPdx * inv) + (double)vF[1]) * dV;
+    const double r1 = -((double)(-dPdz * inv) + (double)vF[3]) * dV;
+    a.Residual1[5 * go + 0] = r0;
+    a.Residual1[5 * go + 1] = r1;
+    s5[5] += r0;
+    s5[6] += r1;
+  }
+  }  // cells of this thread
+  if (a.RK != 3) return;
+  __syncthreads();  // the face buffers are reused for the block reduction
+  double *red = reinterpret_cast<double *>(Fb);  // [NW][7]
+  constexpr int NWR = NT / 32;
+#pragma unroll
+  for (int m = 0; m < 7; ++m) {
+    double v = s5[m];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((tid & 31) == 0) red[(tid >> 5) * 7 + m] = v;
+  }
+  __syncthreads();
+  if (tid < 7) {
+    double v = 0;
+    for (int wv = 0; wv < NWR; ++wv) v += red[wv * 7 + tid];
+    a.partials[(size_t)blockIdx.x * 7 + tid] = v;
   }
 }
 
@@ -494,102 +561,16 @@ static cudaError_t launch_split_t(const FluxSplitArgs &a, int ncubes, cudaStream
   return cudaGetLastError();
 }
 
+int flux_split_blocks(int n, int ncubes) {
+  const int T = n % 8 == 0 ? 8 : 4;
+  const int nt = n / T;
+  return ncubes * nt * nt * nt;
+}
+
 cudaError_t launch_flux_split(const FluxSplitArgs &a, int ncubes, cudaStream_t s) {
   if (a.ph.n % 8 == 0) return launch_split_t<8>(a, ncubes, s);
   if (a.ph.n % 4 == 0) return launch_split_t<4>(a, ncubes, s);
   return cudaErrorInvalidValue;
-}
-
-// ---------------------------------------------------------------------------
-// Stage update Q += w * dQ in FP64 (w = 1, 1/4, 2/3 for RK 1, 2, 3: the
-// reference's combinations 0.75 Q + 0.25 Q1 + 0.25 dQ and
-// 1/3 Q + 2/3 Q2 + 2/3 dQ, with Q1 = Q2 = Q on fluid cells at stage entry
-// because only ghost and non-fluid cells change between stages).  At RK 3
-// the change norms use FP32 differences formed from the increment and are
-// summed in FP64.
-// ---------------------------------------------------------------------------
-constexpr int kRkThreads = 256;
-
-__global__ void __launch_bounds__(kRkThreads) k_rk_split(RkSplitArgs a, long long total,
-                                                        long long chunk) {
-  const int n = a.ph.n, S = n + 4;
-  const long long beg = (long long)blockIdx.x * chunk;
-  const long long end = min(total, beg + chunk);
-  const float w = a.RK == 1 ? 1.0f : (a.RK == 2 ? 0.25f : (float)(2.0 / 3.0));
-  double s[7] = {0, 0, 0, 0, 0, 0, 0};
-  for (long long t = beg + threadIdx.x; t < end; t += kRkThreads) {
-    const int c = 1 + (int)(t / ((long long)n * n * n));
-    const int r = (int)(t % ((long long)n * n * n));
-    const int i = 2 + r / (n * n), j = 2 + (r / n) % n, k = 2 + r % n;
-    const size_t o = cell_index(S, c, i, j, k);
-    if (a.FWS[o] == kFluid) {
-      double *q = a.U1_ + 5 * o;
-      const float *rk = a.Rku32 + 5 * o;
-      float dq[5];
-#pragma unroll
-      for (int v = 0; v < 5; ++v) dq[v] = w * rk[v];
-      double q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3], q4 = q[4];
-      q[0] = q0 + (double)dq[0];
-      q[1] = q1 + (double)dq[1];
-      q[2] = q2 + (double)dq[2];
-      q[3] = q3 + (double)dq[3];
-      q[4] = q4 + (double)dq[4];
-      if (a.RK == 3) {
-        // old/new primitive differences from the increment, in FP32
-        const float rho = (float)q0, m1 = (float)q1, m2 = (float)q2, m3 = (float)q3;
-        const float dr = dq[0], d1 = dq[1], d2 = dq[2], d3 = dq[3], dE = dq[4];
-        const float ir = 1.0f / rho, irn = 1.0f / (rho + dr);
-        const float den = ir * irn;
-        const float dU = (d1 * rho - m1 * dr) * den;
-        const float dV = (d2 * rho - m2 * dr) * den;
-        const float dW = (d3 * rho - m3 * dr) * den;
-        const float mm = m1 * m1 + m2 * m2 + m3 * m3;
-        const float dKE = 0.5f * ((2.f * (m1 * d1 + m2 * d2 + m3 * d3) + d1 * d1 + d2 * d2 + d3 * d3) * rho -
-                                  mm * dr) * den;
-        const float dP = 0.4f * (dE - dKE);
-        const float Pold = (float)((q4 - 0.5 * (double)(mm * ir)) * (BCMG_K - 1));
-        const float dT = (dP * rho - Pold * dr) * den;
-        s[0] += (double)dP * (double)dP;
-        s[1] += (double)dU * (double)dU;
-        s[2] += (double)dV * (double)dV;
-        s[3] += (double)dW * (double)dW;
-        s[4] += (double)dT * (double)dT;
-      }
-    }
-    if (a.RK == 3) {
-      s[5] += a.Residual1[5 * o + 0];
-      s[6] += a.Residual1[5 * o + 1];
-    }
-  }
-  if (a.RK != 3) return;
-  __shared__ double red[kRkThreads / 32][7];
-#pragma unroll
-  for (int m = 0; m < 7; ++m) {
-    double v = s[m];
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][m] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x < 7) {
-    double v = 0;
-    for (int wv = 0; wv < kRkThreads / 32; ++wv) v += red[wv][threadIdx.x];
-    a.partials[(size_t)blockIdx.x * 7 + threadIdx.x] = v;
-  }
-}
-
-cudaError_t launch_rk_split(const RkSplitArgs &a, int *nblocks_out, cudaStream_t s) {
-  RkArgs probe{};
-  probe.ph = a.ph;
-  probe.ncube = a.ncube;
-  const int nb = rk_partial_blocks(probe);
-  const long long n3 = (long long)a.ph.n * a.ph.n * a.ph.n;
-  const long long total = (long long)(a.ncube - 1) * n3;
-  const long long chunk = (total + nb - 1) / nb;
-  if (nblocks_out) *nblocks_out = nb;
-  if (total <= 0) return cudaSuccess;
-  k_rk_split<<<nb, kRkThreads, 0, s>>>(a, total, chunk);
-  return cudaGetLastError();
 }
 
 }  // namespace bcmg

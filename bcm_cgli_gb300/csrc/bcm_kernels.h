@@ -39,27 +39,20 @@ struct FluxSplitArgs {
   const int *FWS;
   const double *cube_size;
   const float *M;  // FP32 deltas of U1_ (k_mirror)
-  const double *U1_, *U1, *U1q;
+  double *U1_;     // updated in place for the CTA's own cells
+  const double *U1, *U1q;
   const float *D2;  // FP32 of the FP64 difference U1 - U1q (k_level_diff)
-  float *Rku32;  // FP32 increments
+  int RK;              // stage 1..3: the kernel applies the stage update
+  double *partials;    // [blocks][7] norm/force partial sums (stage 3)
   double *Residual1;
 };
+// Blocks of one split flux launch over ncubes cubes (one per tile).
+int flux_split_blocks(int n, int ncubes);
 cudaError_t launch_mirror(const double *U, float *M, int n, int ncube, double rho0, double P0,
                           cudaStream_t s);
 cudaError_t launch_flux_split(const FluxSplitArgs &a, int ncubes, cudaStream_t s);
 cudaError_t launch_level_diff(const double *U1, const double *U1q, float *D2, int n, int ncube,
                               cudaStream_t s);
-struct RkSplitArgs {
-  Phys ph;
-  int ncube;
-  int RK;
-  const int *FWS;
-  double *U1_;
-  const float *Rku32;
-  const double *Residual1;
-  double *partials;
-};
-cudaError_t launch_rk_split(const RkSplitArgs &a, int *nblocks_out, cudaStream_t s);
 
 struct RkArgs {
   Phys ph;
