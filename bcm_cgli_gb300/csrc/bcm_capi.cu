@@ -154,8 +154,9 @@ struct bcmg_case {
   float *inv_dx = nullptr;               // split precision: n / cube_size per cube
   int *FWS = nullptr;
   double *cube_size = nullptr;
-  int *task_off = nullptr;
+  int *task_cube = nullptr;  // destination cube of each face task
   FaceTask *tasks = nullptr;
+  int ntasks = 0;
   int *bc_cubes = nullptr, *bc_masks = nullptr;
   int nbc = 0;
   Ibm ibm;  // minus entries then plus entries, one combined schedule
@@ -182,7 +183,7 @@ struct bcmg_case {
     ev.clear();
     dfree(U1_); dfree(U1); dfree(U1q); dfree(U1p1); dfree(U1p2); dfree(Rku1); dfree(Residual1);
     dfree(M); dfree(D2); dfree(inv_dx);
-    dfree(FWS); dfree(cube_size); dfree(task_off); dfree(tasks); dfree(bc_cubes);
+    dfree(FWS); dfree(cube_size); dfree(task_cube); dfree(tasks); dfree(bc_cubes);
     dfree(bc_masks); dfree(partials); dfree(er); dfree(emax);
     ibm.release();
     if (stream) cudaStreamDestroy(stream);
@@ -258,13 +259,12 @@ int case_flux(bcmg_case *c, int RK) {
 int case_interface(bcmg_case *c) {
   InterfaceArgs ia;
   ia.n = c->ph.n;
-  ia.dst_cubes = nullptr;
-  ia.task_off = c->task_off;
+  ia.ntasks = c->ntasks;
+  ia.task_cube = c->task_cube;
   ia.tasks = c->tasks;
-  ia.edge_cubes = c->ncube;
   ia.U1_ = c->U1_;
   CK(launch_interface(ia, c->ncube, c->stream));
-  ++c->launches;
+  c->launches += c->ntasks > 0 ? 2 : 1;
   return BCMG_OK;
 }
 
@@ -405,6 +405,10 @@ int bcmg_case_create(const bcmg_case_desc *d, bcmg_case **out) {
     set_err(err);
     return fail(BCMG_ERR_ARG);
   }
+  std::vector<int> task_cube(tasks.size());
+  for (int cc = 1; cc < d->ncube; ++cc)
+    for (int t = off[cc]; t < off[cc + 1]; ++t) task_cube[t] = cc;
+  c->ntasks = (int)tasks.size();
   const int *lists[6] = {d->xl, d->xu, d->yl, d->yu, d->zl, d->zu};
   const int counts[6] = {d->nxl, d->nxu, d->nyl, d->nyu, d->nzl, d->nzu};
   for (int l = 0; l < 6; ++l)
@@ -429,7 +433,7 @@ int bcmg_case_create(const bcmg_case_desc *d, bcmg_case **out) {
             ck(dalloc(&c->U1p2, nd), "alloc") && ck(dalloc(&c->Rku1, nd), "alloc") &&
             ck(dalloc(&c->Residual1, nd), "alloc") && ck(dalloc(&c->FWS, c->ncell), "alloc") &&
             ck(dalloc(&c->cube_size, (size_t)d->ncube), "alloc") &&
-            ck(dalloc(&c->task_off, off.size()), "alloc") &&
+            ck(dalloc(&c->task_cube, tasks.size()), "alloc") &&
             ck(dalloc(&c->tasks, tasks.size()), "alloc") &&
             ck(dalloc(&c->bc_cubes, bcc.size()), "alloc") &&
             ck(dalloc(&c->bc_masks, bcm.size()), "alloc") &&
@@ -470,8 +474,9 @@ int bcmg_case_create(const bcmg_case_desc *d, bcmg_case **out) {
           "copy") &&
        ck(cudaMemcpyAsync(c->cube_size, d->cube_size, sizeof(double) * d->ncube,
                           cudaMemcpyHostToDevice, s), "copy") &&
-       ck(cudaMemcpyAsync(c->task_off, off.data(), sizeof(int) * off.size(),
-                          cudaMemcpyHostToDevice, s), "copy") &&
+       (tasks.empty() || ck(cudaMemcpyAsync(c->task_cube, task_cube.data(),
+                                            sizeof(int) * task_cube.size(),
+                                            cudaMemcpyHostToDevice, s), "copy")) &&
        (tasks.empty() || ck(cudaMemcpyAsync(c->tasks, tasks.data(), sizeof(FaceTask) * tasks.size(),
                                             cudaMemcpyHostToDevice, s), "copy")) &&
        (bcc.empty() || (ck(cudaMemcpyAsync(c->bc_cubes, bcc.data(), sizeof(int) * bcc.size(),
@@ -592,8 +597,10 @@ int bcmg_case_advance(bcmg_case *c, int steps, int subiters, int use_graph, doub
     {
       // kernel nodes per step, counted like case_step
       int L = (int)(c->ibm.level_off.size() > 0 ? c->ibm.level_off.size() - 1 : 0);
-      // bc, IBM levels, interface, [mirror], flux, [rk], interface
-      long long stage = (c->nbc > 0) + L + 1 + 1 + 1 + 1;
+      // bc, IBM levels, interface (faces + edges), [mirror], flux, [rk],
+      // interface (faces + edges)
+      const long long ifl = c->ntasks > 0 ? 2 : 1;
+      long long stage = (c->nbc > 0) + L + ifl + 1 + 1 + ifl;
       per = subiters * (3 * stage + 1 + 1) + 1 + (c->precision == BCMG_PRECISION_SPLIT ? 1 : 0);
     }
     for (int s = 0; s < steps; ++s) CK(cudaGraphLaunch(c->graph, c->stream));
@@ -1048,20 +1055,24 @@ void BCM_Interface(int myid, int ncube, int mPI_Nadj, int ncpu_bs, int ncpu_eq, 
       return BCMG_ERR_ARG;
     }
     if ((r = C.ensure_full(ncube))) return r;
-    if ((r = C.grow(&C.ibuf, C.ibuf_cap, off.size()))) return r;
+    std::vector<int> task_cube(tasks.size());
+    for (int cc = 1; cc < ncube; ++cc)
+      for (int t = off[cc]; t < off[cc + 1]; ++t) task_cube[t] = cc;
+    if ((r = C.grow(&C.ibuf, C.ibuf_cap, task_cube.size()))) return r;
     if ((r = C.grow(&C.tasks, C.tasks_cap, tasks.size()))) return r;
     const size_t b = C.ncell * 5 * sizeof(double);
-    CK(cudaMemcpyAsync(C.ibuf, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice, C.s));
+    if (!task_cube.empty())
+      CK(cudaMemcpyAsync(C.ibuf, task_cube.data(), sizeof(int) * task_cube.size(),
+                         cudaMemcpyHostToDevice, C.s));
     if (!tasks.empty())
       CK(cudaMemcpyAsync(C.tasks, tasks.data(), sizeof(FaceTask) * tasks.size(),
                          cudaMemcpyHostToDevice, C.s));
     CK(cudaMemcpyAsync(C.U1_, U1_, b, cudaMemcpyHostToDevice, C.s));
     InterfaceArgs ia;
     ia.n = C.cfg.ncube_x;
-    ia.dst_cubes = nullptr;
-    ia.task_off = C.ibuf;
+    ia.ntasks = (int)tasks.size();
+    ia.task_cube = C.ibuf;
     ia.tasks = C.tasks;
-    ia.edge_cubes = ncube;
     ia.U1_ = C.U1_;
     CK(launch_interface(ia, ncube, C.s));
     CK(cudaMemcpyAsync(U1_, C.U1_, b, cudaMemcpyDeviceToHost, C.s));

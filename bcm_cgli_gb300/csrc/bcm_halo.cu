@@ -17,37 +17,53 @@ constexpr int kHaloThreads = 256;
 // ---------------------------------------------------------------------------
 // Interface (BCM_Interface.cpp).  Same-level faces (:1745-1783 x, :2608-2642
 // y, :3478-3512 z) copy the neighbour's two interior layers into this cube's
-// two ghost layers over the 16x16 (n x n) face; every read is an interior
-// cell, every write a ghost cell of the CTA's own cube.  After a CTA barrier
-// the edge ghosts are averaged in the reference's three ordered phases
-// (:5640-5732): i-edges, then j-edges, then k-edges.
+// two ghost layers over the n x n face; every read is an interior cell, every
+// write a ghost cell of the task's destination cube, so all face tasks run in
+// parallel.  A second launch then averages the edge ghosts in the
+// reference's three ordered phases (:5640-5732): i-edges, then j-edges, then
+// k-edges.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kHaloThreads) k_interface(InterfaceArgs a) {
-  const int n = a.n, S = n + 4, nx = n + 1, nyy = n + 2;
-  const int c = blockIdx.x + 1;  // one CTA per cube 1..ncube-1
+// Face copies: one CTA per (destination cube, face task).  Work items are
+// (layer, row) pairs; a row is the n cells along the innermost index that
+// both source and destination store contiguously (k for x and y faces), so
+// lanes move consecutive doubles.  For z faces a row is one (i, j) column of
+// the two ghost layers.
+__global__ void __launch_bounds__(kHaloThreads) k_iface_faces(InterfaceArgs a) {
+  const int n = a.n, S = n + 4;
+  const int t = blockIdx.x;
+  const int c = a.task_cube[t];
+  const FaceTask ft = a.tasks[t];
+  const int ax = ft.axis;
+  const int dbase = ft.side == 0 ? 0 : n + 2;
+  const int sbase = ft.side == 0 ? n : 2;
   double *U = a.U1_;
-  const int t0 = a.task_off[c], t1 = a.task_off[c + 1];
-  for (int t = t0; t < t1; ++t) {
-    const FaceTask ft = a.tasks[t];
-    const int ax = ft.axis;
-    // Layer l (0,1): dst ghost index and src interior index along the axis.
-    // side 0: dst [l]     <- src [n+l]   (src is the -ax neighbour)
-    // side 1: dst [n+2+l] <- src [2+l]   (src is the +ax neighbour)
-    const int dbase = ft.side == 0 ? 0 : n + 2;
-    const int sbase = ft.side == 0 ? n : 2;
-    const int cells = 2 * n * n;
-    for (int w = threadIdx.x; w < cells * 5; w += kHaloThreads) {
-      const int v = w % 5, cell = w / 5;
-      const int l = cell / (n * n), p = 2 + (cell / n) % n, q = 2 + cell % n;
-      int di, dj, dk, si, sj, sk;
-      if (ax == 0) { di = dbase + l; si = sbase + l; dj = sj = p; dk = sk = q; }
-      else if (ax == 1) { dj = dbase + l; sj = sbase + l; di = si = p; dk = sk = q; }
-      else { dk = dbase + l; sk = sbase + l; di = si = p; dj = sj = q; }
-      U[5 * cell_index(S, c, di, dj, dk) + v] = U[5 * cell_index(S, ft.src, si, sj, sk) + v];
+  if (ax < 2) {
+    // rows: (layer l, transverse index p); each row = 5n doubles along k
+    const int rowlen = 5 * n;
+    for (int w = threadIdx.x; w < 2 * n * rowlen; w += kHaloThreads) {
+      const int row = w / rowlen, e = w - row * rowlen;
+      const int l = row / n, p = 2 + (row - l * n);
+      int di, dj, si, sj;
+      if (ax == 0) { di = dbase + l; si = sbase + l; dj = sj = p; }
+      else { dj = dbase + l; sj = sbase + l; di = si = p; }
+      U[5 * cell_index(S, c, di, dj, 2) + e] = U[5 * cell_index(S, ft.src, si, sj, 2) + e];
+    }
+  } else {
+    // z faces: per (i, j) the two layers are 10 contiguous doubles
+    for (int w = threadIdx.x; w < n * n * 10; w += kHaloThreads) {
+      const int col = w / 10, e = w - col * 10;
+      const int i = 2 + col / n, j = 2 + (col - (col / n) * n);
+      U[5 * cell_index(S, c, i, j, dbase) + e] = U[5 * cell_index(S, ft.src, i, j, sbase) + e];
     }
   }
-  if (c >= a.edge_cubes) return;
-  __syncthreads();
+}
+
+// Edge fill after all face copies (BCM_Interface.cpp:5640-5732): three
+// ordered phases per cube with CTA barriers in between.
+__global__ void __launch_bounds__(kHaloThreads) k_iface_edges(InterfaceArgs a) {
+  const int n = a.n, S = n + 4, nx = n + 1, nyy = n + 2;
+  const int c = blockIdx.x + 1;
+  double *U = a.U1_;
   auto Q = [&](int i, int j, int k) { return U + 5 * cell_index(S, c, i, j, k); };
   // Phase 1: i-edges, i = 2..nx.
   for (int w = threadIdx.x; w < 4 * n * 5; w += kHaloThreads) {
@@ -88,7 +104,12 @@ __global__ void __launch_bounds__(kHaloThreads) k_interface(InterfaceArgs a) {
 
 cudaError_t launch_interface(const InterfaceArgs &a, int ncubes_total, cudaStream_t s) {
   if (ncubes_total <= 1) return cudaSuccess;
-  k_interface<<<ncubes_total - 1, kHaloThreads, 0, s>>>(a);
+  if (a.ntasks > 0) {
+    k_iface_faces<<<a.ntasks, kHaloThreads, 0, s>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  k_iface_edges<<<ncubes_total - 1, kHaloThreads, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -75,9 +75,8 @@ cudaError_t launch_rk_chunked(const RkArgs &a, long long chunk, int nblocks, cud
 cudaError_t launch_norms(const Phys &ph, const double *partials, int nblocks, double *er,
                          cudaStream_t s);
 
-// Interface: one CTA per destination cube pulls its ghost faces from the
-// neighbours' interiors (table built on the host) then runs the ordered
-// three-phase edge fill.  Task i of cube c: tasks[off[c] .. off[c+1]).
+// Interface: face-copy tasks (destination cube, source cube, axis, side) built
+// on the host, then the ordered three-phase edge fill of every cube.
 struct FaceTask {
   int32_t src;   // source cube
   int8_t axis;   // 0 x, 1 y, 2 z
@@ -87,10 +86,9 @@ struct FaceTask {
 };
 struct InterfaceArgs {
   int n;
-  const int *dst_cubes;  // [ndst] cubes that get any face task, ascending
-  const int *task_off;   // [ndst+1]
-  const FaceTask *tasks;
-  int edge_cubes;        // cubes 1..edge_cubes-1 get the edge fill
+  int ntasks;             // face tasks (all destination cubes)
+  const int *task_cube;   // [ntasks] destination cube of each task
+  const FaceTask *tasks;  // [ntasks]
   double *U1_;
 };
 cudaError_t launch_interface(const InterfaceArgs &a, int ndst, cudaStream_t s);

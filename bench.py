@@ -107,7 +107,7 @@ class Clocks:
         try:
             self.p = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -347,10 +347,26 @@ def run_gpu_arm(args, dist):
         print(json.dumps(line), flush=True)
 
 
+def run_flux_only(args):
+    """Profiling target: the flux kernel alone on a Taylor-Green case of
+    ncx^3 cubes of 24^3 cells (ncx=6: 216 cubes, 3.0 M cells, 190 MB per
+    state array, above the 129 MB L2), one warm-up launch and `steps` timed
+    launches.  Used by the ncu commands recorded under profiles/."""
+    from bcm_cgli_gb300 import api, cases
+    case = cases.taylor_green(ncx=args.ncx, n=24)
+    prec = api.PRECISION_SPLIT if args.precision == "split" else api.PRECISION_FP64
+    ctx = api.CaseContext(case, precision=prec)
+    ctx.set_state(case.U, case.U, case.U)
+    ms = ctx.time_flux(reps=max(1, args.steps))
+    ctx.close()
+    print(json.dumps({"flux_only": args.precision, "cells": case.n_cells, "ms_per_launch": ms,
+                      "cell_stages_per_s": case.n_cells / (ms * 1e-3)}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="split", choices=["fp64", "split"],
@@ -359,7 +375,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true",
                     help="headline path only (no second precision, no accuracy check)")
+    ap.add_argument("--flux-only", action="store_true",
+                    help="time the flux kernel alone on a smaller case (profiling target)")
+    ap.add_argument("--ncx", type=int, default=6, help="cubes per edge for --flux-only")
     args = ap.parse_args()
+    if args.flux_only:
+        run_flux_only(args)
+        return
     if args.impl == "reference":
         # Rank 0 alone times the CPU implementation; other ranks exit at once.
         class R0:
