@@ -105,18 +105,26 @@ def BCM_Ghostcell_plus(myid, NNBC, weight, GCindex, IPsur, FWS, U1_):
 
 
 def interface_lists(case):
-    """Same-level lists adjX_eq/adjY_eq/adjZ_eq (1-based) as
-    BCM_Interface_table.cpp:96-208 builds them."""
+    """The 15 neighbour lists of BCM_Interface_table.cpp:96-308 (1-based
+    arrays): per axis x, y, z the same-level, big->small (+), small->big (+),
+    big->small (-) and small->big (-) lists."""
     adj, csl = case.adj, case.csl
     out = []
     for ax in range(3):
-        d = 2 + 2 * ax
-        lst = []
+        eq, bsp, sbp, bsm, sbm = [], [], [], [], []
         for c in range(1, case.ncube):
-            slots = adj[c, 1:5, d]
-            if (slots > 0).any() and csl[c] == csl[slots.max()]:
-                lst.append(c)
-        out.append(_one_based(lst))
+            plus = adj[c, 1:5, 2 + 2 * ax]
+            if (plus > 0).any():
+                a = plus.max()
+                (eq if csl[c] == csl[a] else (sbp if csl[c] < csl[a] else bsp)).append(c)
+            minus = adj[c, 1:5, 1 + 2 * ax]
+            if (minus > 0).any():
+                a = minus.max()
+                if csl[c] < csl[a]:
+                    sbm.append(c)
+                elif csl[c] > csl[a]:
+                    bsm.append(c)
+        out.append([_one_based(x) for x in (eq, bsp, sbp, bsm, sbm)])
     return out
 
 
@@ -124,7 +132,7 @@ def BCM_Interface_for_case(case, U1_):
     """BCM_Interface with single-process (empty exchange) arguments, like the
     reference's call at main.cpp:1177-1204 on one rank."""
     L = lib()
-    X, Y, Z = interface_lists(case)
+    lists = interface_lists(case)
     z = np.zeros(4, np.int32)
     d = np.zeros(4)
     zp = z.ctypes.data_as(C.c_void_p)
@@ -132,13 +140,15 @@ def BCM_Interface_for_case(case, U1_):
     adj = np.ascontiguousarray(case.adj, np.int32)
     csl = np.ascontiguousarray(case.csl, np.int32)
     U = _dp(U1_)
-    args = [C.c_int(0), C.c_int(case.ncube), C.c_int(1), C.c_int(0), C.c_int(0), C.c_int(0),
-            C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(len(X) - 1), C.c_int(len(Y) - 1),
-            C.c_int(len(Z) - 1)] + [C.c_int(0)] * 12 + [zp] * 15 + [dd] * 4 + [zp] * 4 + \
-           [dd] * 4 + [zp] * 4 + [dd] * 4 + [zp] * 8 + \
-           [csl.ctypes.data_as(C.c_void_p), adj.ctypes.data_as(C.c_void_p),
-            X.ctypes.data_as(C.c_void_p), Y.ctypes.data_as(C.c_void_p),
-            Z.ctypes.data_as(C.c_void_p)] + [zp] * 12 + [U.ctypes.data_as(C.c_void_p)]
+    cnt = lambda a: C.c_int(len(a) - 1)
+    ptr = lambda a: a.ctypes.data_as(C.c_void_p)
+    X, Y, Z = lists
+    args = ([C.c_int(0), C.c_int(case.ncube), C.c_int(1), C.c_int(0), C.c_int(0), C.c_int(0),
+             C.c_int(0), C.c_int(0), C.c_int(0), cnt(X[0]), cnt(Y[0]), cnt(Z[0])] +
+            [cnt(a) for a in X[1:] + Y[1:] + Z[1:]] +
+            [zp] * 15 + [dd] * 4 + [zp] * 4 + [dd] * 4 + [zp] * 4 + [dd] * 4 + [zp] * 8 +
+            [ptr(csl), ptr(adj), ptr(X[0]), ptr(Y[0]), ptr(Z[0])] +
+            [ptr(a) for a in X[1:] + Y[1:] + Z[1:]] + [ptr(U)])
     assert len(args) == 85
     L.BCM_Interface(*args)
     _raise_if_failed("BCM_Interface")

@@ -310,3 +310,113 @@ def random_ibm(seed: int, case: Case, count: int):
         IP[4 * e + 1:4 * e + 5] = (ic, ii, jj, kk)
         W[8 * e + 1:8 * e + 9] = w
     return W, GC, IP
+
+
+def two_level_box(ncx: int, ncy: int, ncz: int, n: int, length: float, refine, periodic=True):
+    """Coarse cubes tiling [0, ncx*size) x ... in which every coarse cube with
+    refine(a, b, c) true is replaced by 2x2x2 fine cubes (half size).
+
+    Adjacency follows the reference's grid-file convention (BCM_Grid.cpp):
+    adj[c][slot][dir], dir 1..6 = -x,+x,-y,+y,-z,+z.  A neighbour of equal or
+    larger size sits in slot 1; the four smaller neighbours across a face sit
+    in slots 1..4 ordered (lo,lo), (hi on the first tangential axis), (hi on
+    the second), (hi,hi), tangential axes in x<y<z order (BCM_Interface.cpp
+    :1825-1894).  csl = round(log2(size / smallest size)) (BCM_Grid.cpp:166).
+    Returns (ncube, cube_size, csl, origin, adj).
+    """
+    size = length / ncx
+    dims = (ncx, ncy, ncz)
+    coarse_ref = {(a, b, c): bool(refine(a, b, c))
+                  for a in range(ncx) for b in range(ncy) for c in range(ncz)}
+    cubes = []  # (level, (i, j, k) in units of own size)
+    for c in range(ncz):
+        for b in range(ncy):
+            for a in range(ncx):
+                if coarse_ref[(a, b, c)]:
+                    for dk in range(2):
+                        for dj in range(2):
+                            for di in range(2):
+                                cubes.append((0, (2 * a + di, 2 * b + dj, 2 * c + dk)))
+                else:
+                    cubes.append((1, (a, b, c)))
+    index = {cb: i + 1 for i, cb in enumerate(cubes)}
+    ncube = len(cubes) + 1
+    cube_size = np.zeros(ncube)
+    csl = np.zeros(ncube, np.int32)
+    origin = np.zeros((ncube, 3))
+    adj = np.zeros((ncube, 5, 7), np.int32)
+
+    def wrap(pos, lev):
+        out = []
+        for ax in range(3):
+            m = dims[ax] * (2 if lev == 0 else 1)
+            p = pos[ax]
+            if periodic:
+                p %= m
+            elif p < 0 or p >= m:
+                return None
+            out.append(p)
+        return tuple(out)
+
+    for (lev, pos), ci in index.items():
+        s = size if lev == 1 else size / 2
+        cube_size[ci] = s
+        csl[ci] = lev
+        origin[ci] = [pos[0] * s, pos[1] * s, pos[2] * s]
+        for ax in range(3):
+            t0, t1 = [t for t in range(3) if t != ax]
+            for sgn, d in ((-1, 1 + 2 * ax), (1, 2 + 2 * ax)):
+                q = list(pos)
+                q[ax] += sgn
+                if lev == 0:
+                    nb = wrap(q, 0)
+                    if nb is None:
+                        continue
+                    if (0, nb) in index:
+                        adj[ci, 1, d] = index[(0, nb)]
+                    else:
+                        cp = tuple(v // 2 for v in nb)
+                        adj[ci, 1, d] = index[(1, cp)]
+                else:
+                    nb = wrap(q, 1)
+                    if nb is None:
+                        continue
+                    if (1, nb) in index:
+                        adj[ci, 1, d] = index[(1, nb)]
+                    else:
+                        # four fine cubes on the shared face
+                        for slot, (h0, h1) in enumerate(((0, 0), (1, 0), (0, 1), (1, 1)), start=1):
+                            f = [2 * v for v in nb]
+                            f[ax] += 1 if sgn < 0 else 0  # fine layer touching this cube
+                            f[t0] += h0
+                            f[t1] += h1
+                            adj[ci, slot, d] = index[(0, tuple(f))]
+    return ncube, cube_size, csl, origin, adj
+
+
+def random_two_level_case(seed=1, ncx=2, ncy=2, ncz=2, n=4, periodic=True, viscous=True,
+                          noise=0.05, solid_frac=0.0, ghost_frac=0.0, name="two_level"):
+    """Random perturbed flow on a two-level grid: coarse cube (0,0,0) of the
+    ncx x ncy x ncz coarse tiling is refined into 8 fine cubes, so every face
+    kind of the level-jump interface occurs (BCM_Interface.cpp:1790-4358)."""
+    ph = Phys(mu_L=0.0000185 if viscous else 0.0, rho0=1.1842, U0=38.889, Uin=38.889,
+              P0=101300.0, mpi_ncube=0)
+    geom = two_level_box(ncx, ncy, ncz, n, 1.0, lambda a, b, c: (a, b, c) == (0, 0, 0),
+                         periodic=periodic)
+    ncube, cube_size, csl, origin, adj = geom
+    ph.mpi_ncube = ncube - 1
+    S = n + 4
+    cnt = ncube * S ** 3
+    r = [splitmix_uniform(seed * 16 + t, cnt).reshape(ncube, S, S, S) for t in range(6)]
+    rho = ph.rho0 * (1 + noise * (r[0] - 0.5))
+    u = ph.U0 * (1 + 2 * noise * (r[1] - 0.5))
+    v = ph.U0 * 2 * noise * (r[2] - 0.5)
+    w = ph.U0 * 2 * noise * (r[3] - 0.5)
+    p = ph.P0 * (1 + noise * 0.1 * (r[4] - 0.5))
+    U = conservative(rho, u, v, w, p)
+    fws = np.full((ncube, S, S, S), IFLUID, np.int32)
+    fws[r[5] < solid_frac] = ISOLID
+    fws[(r[5] >= solid_frac) & (r[5] < solid_frac + ghost_frac)] = IGHOST
+    return Case(n=n, ncube=ncube, phys=ph, cube_size=cube_size, csl=csl, origin=origin,
+                adj=adj, fws=fws, U=np.ascontiguousarray(U), dT=1e-4, dTau=1e-4 / 200.0,
+                name=name)

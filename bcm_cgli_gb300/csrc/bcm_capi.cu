@@ -1023,22 +1023,21 @@ void BCM_Interface(int myid, int ncube, int mPI_Nadj, int ncpu_bs, int ncpu_eq, 
   (void)Scube_Ncpu_bs; (void)Rcube_Ncpu_bs; (void)send_data_curr_bs; (void)recv_data_curr_bs;
   (void)send_data_neig_bs; (void)recv_data_neig_bs; (void)Sdir_bs; (void)Rdir_bs;
   (void)ist_eq; (void)ist_sb; (void)ist_bs; (void)adjN_sb; (void)RadjN_bs; (void)SadjN_bs;
-  (void)csl; (void)adjX_bs_plus; (void)adjX_sb_plus; (void)adjX_bs_minus; (void)adjX_sb_minus;
-  (void)adjY_bs_plus; (void)adjY_sb_plus; (void)adjY_bs_minus; (void)adjY_sb_minus;
-  (void)adjZ_bs_plus; (void)adjZ_sb_plus; (void)adjZ_bs_minus; (void)adjZ_sb_minus;
+  (void)adjX_sb_plus; (void)adjX_sb_minus; (void)adjY_sb_plus; (void)adjY_sb_minus;
+  (void)adjZ_sb_plus; (void)adjZ_sb_minus; (void)nadjX_sb_plus; (void)nadjX_sb_minus;
+  (void)nadjY_sb_plus; (void)nadjY_sb_minus; (void)nadjZ_sb_plus; (void)nadjZ_sb_minus;
   clear_err();
   if (ncpu_bs || ncpu_eq || ncpu_sb) {
     set_err("BCM_Interface: cross-rank exchange lists are not supported on one GPU");
     return;
   }
-  if (nadjX_bs_plus || nadjX_sb_plus || nadjX_bs_minus || nadjX_sb_minus || nadjY_bs_plus ||
-      nadjY_sb_plus || nadjY_bs_minus || nadjY_sb_minus || nadjZ_bs_plus || nadjZ_sb_plus ||
-      nadjZ_bs_minus || nadjZ_sb_minus) {
-    set_err("BCM_Interface: level-jump interfaces are not supported yet");
-    return;
-  }
-  if (ncube < 2 || !adj_number || !U1_ || nadjX_eq < 0 || nadjY_eq < 0 || nadjZ_eq < 0 ||
-      (nadjX_eq && !adjX_eq) || (nadjY_eq && !adjY_eq) || (nadjZ_eq && !adjZ_eq)) {
+  const int *lists[9] = {adjX_eq, adjX_bs_plus, adjX_bs_minus, adjY_eq, adjY_bs_plus,
+                         adjY_bs_minus, adjZ_eq, adjZ_bs_plus, adjZ_bs_minus};
+  const int counts[9] = {nadjX_eq, nadjX_bs_plus, nadjX_bs_minus, nadjY_eq, nadjY_bs_plus,
+                         nadjY_bs_minus, nadjZ_eq, nadjZ_bs_plus, nadjZ_bs_minus};
+  bool bad = ncube < 2 || !adj_number || !U1_ || !csl;
+  for (int l = 0; l < 9; ++l) bad |= counts[l] < 0 || (counts[l] > 0 && !lists[l]);
+  if (bad) {
     set_err("BCM_Interface: bad arguments");
     return;
   }
@@ -1048,9 +1047,8 @@ void BCM_Interface(int myid, int ncube, int mPI_Nadj, int ncpu_bs, int ncpu_eq, 
     std::vector<int> off;
     std::vector<FaceTask> tasks;
     std::string err;
-    const int *lists[3] = {adjX_eq, adjY_eq, adjZ_eq};
-    const int counts[3] = {nadjX_eq, nadjY_eq, nadjZ_eq};
-    if (!build_interface_tasks_from_lists(ncube, adj_number, lists, counts, off, tasks, err)) {
+    if (!build_interface_tasks_from_lists(ncube, adj_number, csl, lists, counts, off, tasks,
+                                          err)) {
       set_err("BCM_Interface: " + err);
       return BCMG_ERR_ARG;
     }

@@ -23,6 +23,63 @@ constexpr int kHaloThreads = 256;
 // reference's three ordered phases (:5640-5732): i-edges, then j-edges, then
 // k-edges.
 // ---------------------------------------------------------------------------
+// Level-jump faces (BCM_Interface.cpp:1790-2599 x, :2651-3470 y,
+// :3518-4358 z).  Sub-face slot s offsets the tangential axes (x<y<z order)
+// by ((s==2||s==4) n/2, (s==3||s==4) n/2).
+//  kind 1, coarse -> fine: the small cube's two ghost layers facing the big
+//    cube take the big cube's adjacent interior cell (n+1 or 2 along the
+//    axis, (p/2+1, q/2+1) + slot offset across it), both layers alike;
+//  kind 2, fine -> coarse: the big cube's two ghost layers over the slot's
+//    quadrant take 0.125 * the sum of the small cube's 2x2x2 interior cells,
+//    summed in the reference's order (000,100,010,001,110,101,011,111 in i,j,k).
+__device__ __forceinline__ void level_face(const InterfaceArgs &a, int c, const FaceTask &ft) {
+  const int n = a.n, S = n + 4, h = n / 2;
+  const int ax = ft.axis;
+  const int t0 = ax == 0 ? 1 : 0, t1 = ax == 2 ? 1 : 2;
+  const int o0 = (ft.slot == 2 || ft.slot == 4) ? h : 0;
+  const int o1 = (ft.slot == 3 || ft.slot == 4) ? h : 0;
+  double *U = a.U1_;
+  if (ft.kind == 1) {
+    const int gs = ft.side == 0 ? n + 1 : 2;
+    for (int w = threadIdx.x; w < 2 * n * n * 5; w += blockDim.x) {
+      const int v = w % 5, cell = w / 5;
+      const int l = cell / (n * n), p = 2 + (cell / n) % n, q = 2 + cell % n;
+      int d[3], sr[3];
+      d[ax] = ft.side == 0 ? l : n + 2 + l;
+      d[t0] = p;
+      d[t1] = q;
+      sr[ax] = gs;
+      sr[t0] = p / 2 + 1 + o0;
+      sr[t1] = q / 2 + 1 + o1;
+      U[5 * cell_index(S, c, d[0], d[1], d[2]) + v] =
+          U[5 * cell_index(S, ft.src, sr[0], sr[1], sr[2]) + v];
+    }
+  } else {
+    for (int w = threadIdx.x; w < 2 * h * h * 5; w += blockDim.x) {
+      const int v = w % 5, cell = w / 5;
+      const int l = cell / (h * h), p = 2 + (cell / h) % h, q = 2 + cell % h;
+      int d[3], b[3];
+      d[ax] = ft.side == 1 ? n + 2 + l : l;
+      d[t0] = p + o0;
+      d[t1] = q + o1;
+      b[ax] = ft.side == 1 ? 2 * (l + 1) : n - 2 + 2 * l;
+      b[t0] = (p - 1) * 2;
+      b[t1] = (q - 1) * 2;
+      const double *B = U + 5 * cell_index(S, ft.src, b[0], b[1], b[2]) + v;
+      const size_t si = (size_t)S * S * 5, sj = (size_t)S * 5, sk = 5;
+      double sum = B[0];
+      sum = sum + B[si];
+      sum = sum + B[sj];
+      sum = sum + B[sk];
+      sum = sum + B[si + sj];
+      sum = sum + B[si + sk];
+      sum = sum + B[sj + sk];
+      sum = sum + B[si + sj + sk];
+      U[5 * cell_index(S, c, d[0], d[1], d[2]) + v] = 0.125 * sum;
+    }
+  }
+}
+
 // Face copies: one CTA per (destination cube, face task).  Work items are
 // (layer, row) pairs; a row is the n cells along the innermost index that
 // both source and destination store contiguously (k for x and y faces), so
@@ -37,6 +94,10 @@ __global__ void __launch_bounds__(kHaloThreads) k_iface_faces(InterfaceArgs a) {
   const int dbase = ft.side == 0 ? 0 : n + 2;
   const int sbase = ft.side == 0 ? n : 2;
   double *U = a.U1_;
+  if (ft.kind != 0) {
+    level_face(a, c, ft);
+    return;
+  }
   if (ax < 2) {
     // rows: (layer l, transverse index p); each row = 5n doubles along k
     const int rowlen = 5 * n;

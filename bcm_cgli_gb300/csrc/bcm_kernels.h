@@ -80,9 +80,9 @@ cudaError_t launch_norms(const Phys &ph, const double *partials, int nblocks, do
 struct FaceTask {
   int32_t src;   // source cube
   int8_t axis;   // 0 x, 1 y, 2 z
-  int8_t side;   // 0: dst low ghosts <- src high interior; 1: dst high ghosts <- src low interior
-  int8_t kind;   // 0 same-level copy
-  int8_t pad;
+  int8_t side;   // 0: destination's low ghost layers, 1: its high ghost layers
+  int8_t kind;   // 0 same-level copy, 1 coarse->fine injection, 2 fine->coarse average
+  int8_t slot;   // kinds 1, 2: sub-face slot 1..4 of the small cube on the big face
 };
 struct InterfaceArgs {
   int n;

@@ -16,126 +16,174 @@ static std::string fmt(const char *f, long long a = 0, long long b = 0, long lon
   return buf;
 }
 
-// Neighbour classification as BCM_Interface_table.cpp:96-308: a cube has a
-// +dir neighbour when any of the four slots adj_number[c][1..4][dir] is
-// positive; the classifying cube is the largest slot value; the pair is
-// same-level when csl matches.  The copy partner is slot 1 (:1753).
-bool build_interface_tasks(int ncube, const int *adj, const int *csl, std::vector<int> &off,
-                           std::vector<FaceTask> &tasks, std::string &err) {
-  auto A = [&](int c, int s, int d) { return adj[(c * 5 + s) * 7 + d]; };
-  // Writers of each (dst cube, axis, side) face in the reference's order:
-  // x list, then y, then z; cubes ascending; per pair, first the partner's
-  // low ghosts then this cube's high ghosts (:1763, :1772).  Later writes
-  // win, so keep the last writer of each face.
-  std::vector<int> src_of((size_t)ncube * 6, 0);
-  for (int ax = 0; ax < 3; ++ax) {
-    const int dplus = 2 + 2 * ax, dminus = 1 + 2 * ax;
-    for (int c = 1; c < ncube; ++c) {
-      for (int s = 1; s <= 4; ++s)
-        for (int d = 1; d <= 6; ++d) {
-          int v = A(c, s, d);
-          if (v < 0 || v >= ncube) {
-            err = fmt("adj_number[%lld][%lld][*] out of range", c, s);
-            return false;
-          }
-        }
-      int any = 0, acube = 0;
-      for (int s = 1; s <= 4; ++s) {
-        any |= A(c, s, dplus) > 0;
-        acube = std::max(acube, A(c, s, dplus));
-      }
-      if (any) {
-        if (csl[c] != csl[acube]) {
-          err = fmt("cube %lld: level jump on axis %lld is not supported", c, ax);
-          return false;
-        }
-        const int c2 = A(c, 1, dplus);
-        if (c2 <= 0) {
-          err = fmt("cube %lld: +axis %lld neighbour missing from slot 1", c, ax);
-          return false;
-        }
-        src_of[(size_t)c2 * 6 + ax * 2 + 0] = c;  // c2 low ghosts <- c high interior
-        src_of[(size_t)c * 6 + ax * 2 + 1] = c2;  // c high ghosts <- c2 low interior
-      }
-      // Coarse/fine relations through the - direction (:215-308).
-      int anym = 0, am = 0;
-      for (int s = 1; s <= 4; ++s) {
-        anym |= A(c, s, dminus) > 0;
-        am = std::max(am, A(c, s, dminus));
-      }
-      if (anym && csl[c] != csl[am]) {
-        err = fmt("cube %lld: level jump on axis %lld is not supported", c, ax);
-        return false;
-      }
+namespace {
+
+// Collects face tasks in the reference's order (BCM_Interface.cpp: per axis
+// same-level copies, then blocks (a), (b), (c), (d) of the level jumps) and
+// keeps the last writer of each destination face (or face quadrant), which is
+// what the reference's serial loops leave behind.
+struct TaskSet {
+  int ncube;
+  // key: dst cube, axis, side -> whole-face writer (kind 0/1) or quadrant
+  // writers (kind 2, slots 1..4)
+  std::vector<FaceTask> whole;     // [ncube*6]
+  std::vector<FaceTask> quad;      // [ncube*6*4]
+  std::vector<char> has_whole, has_quad;
+  explicit TaskSet(int nc)
+      : ncube(nc), whole((size_t)nc * 6), quad((size_t)nc * 24), has_whole((size_t)nc * 6, 0),
+        has_quad((size_t)nc * 24, 0) {}
+  void put(int dst, int src, int ax, int side, int kind, int slot) {
+    FaceTask t;
+    t.src = src;
+    t.axis = (int8_t)ax;
+    t.side = (int8_t)side;
+    t.kind = (int8_t)kind;
+    t.slot = (int8_t)slot;
+    const size_t f = (size_t)dst * 6 + ax * 2 + side;
+    if (kind == 2) {
+      quad[f * 4 + (slot - 1)] = t;
+      has_quad[f * 4 + (slot - 1)] = 1;
+    } else {
+      whole[f] = t;
+      has_whole[f] = 1;
     }
   }
-  off.assign((size_t)ncube + 1, 0);
-  tasks.clear();
-  for (int c = 0; c < ncube; ++c) {
-    off[c] = (int)tasks.size();
-    if (c == 0) continue;
-    for (int ax = 0; ax < 3; ++ax)
-      for (int side = 0; side < 2; ++side) {
-        int src = src_of[(size_t)c * 6 + ax * 2 + side];
-        if (src > 0) {
-          FaceTask t;
-          t.src = src;
-          t.axis = (int8_t)ax;
-          t.side = (int8_t)side;
-          t.kind = 0;
-          t.pad = 0;
-          tasks.push_back(t);
+  bool finish(std::vector<int> &off, std::vector<FaceTask> &tasks, std::string &err) {
+    off.assign((size_t)ncube + 1, 0);
+    tasks.clear();
+    for (int c = 0; c < ncube; ++c) {
+      off[c] = (int)tasks.size();
+      if (c == 0) continue;
+      for (int fs = 0; fs < 6; ++fs) {
+        const size_t f = (size_t)c * 6 + fs;
+        bool anyq = false;
+        for (int q = 0; q < 4; ++q) anyq |= has_quad[f * 4 + q] != 0;
+        if (has_whole[f] && anyq) {
+          err = fmt("cube %lld: one face is both a whole-face and a sub-face destination "
+                    "(inconsistent adjacency)", c);
+          return false;
+        }
+        if (has_whole[f]) tasks.push_back(whole[f]);
+        for (int q = 0; q < 4; ++q)
+          if (has_quad[f * 4 + q]) tasks.push_back(quad[f * 4 + q]);
+      }
+    }
+    off[ncube] = (int)tasks.size();
+    return true;
+  }
+};
+
+bool check_adj(int ncube, const int *adj, std::string &err) {
+  for (int c = 1; c < ncube; ++c)
+    for (int s = 1; s <= 4; ++s)
+      for (int d = 1; d <= 6; ++d) {
+        int v = adj[(c * 5 + s) * 7 + d];
+        if (v < 0 || v >= ncube) {
+          err = fmt("adj_number[%lld][%lld][*] out of range", c, s);
+          return false;
         }
       }
-  }
-  off[ncube] = (int)tasks.size();
   return true;
 }
 
-// The same face tasks from explicit reference lists (adjX_eq etc., 1-based
-// arrays with counts), as BCM_Interface receives them.
-bool build_interface_tasks_from_lists(int ncube, const int *adj, const int *const lists[3],
-                                      const int counts[3], std::vector<int> &off,
-                                      std::vector<FaceTask> &tasks, std::string &err) {
-  std::vector<int> src_of((size_t)ncube * 6, 0);
-  for (int ax = 0; ax < 3; ++ax) {
-    const int dplus = 2 + 2 * ax;
-    for (int a = 1; a <= counts[ax]; ++a) {
-      const int c = lists[ax][a];
-      if (c <= 0 || c >= ncube) {
-        err = fmt("interface list %lld entry %lld out of range", ax, a);
-        return false;
-      }
-      const int c2 = adj[(c * 5 + 1) * 7 + dplus];
-      if (c2 <= 0 || c2 >= ncube) {
-        err = fmt("cube %lld: neighbour on axis %lld out of range", c, ax);
-        return false;
-      }
-      src_of[(size_t)c2 * 6 + ax * 2 + 0] = c;
-      src_of[(size_t)c * 6 + ax * 2 + 1] = c2;
-    }
+// Tasks of the four level-jump blocks of one big cube B on axis ax; pm 0:
+// its +ax neighbours are the small cubes, pm 1: its -ax neighbours.
+void level_tasks(TaskSet &T, const int *adj, int B, int ax, int pm, bool inject) {
+  const int dir = pm == 0 ? 2 + 2 * ax : 1 + 2 * ax;
+  for (int sl = 1; sl <= 4; ++sl) {
+    const int sc = adj[(B * 5 + sl) * 7 + dir];
+    if (sc <= 0) continue;
+    if (inject)
+      T.put(sc, B, ax, pm == 0 ? 0 : 1, 1, sl);  // (a) / (b): small's ghosts facing B
+    else
+      T.put(B, sc, ax, pm == 0 ? 1 : 0, 2, sl);  // (c) / (d): B's quadrant
   }
-  off.assign((size_t)ncube + 1, 0);
-  tasks.clear();
-  for (int c = 0; c < ncube; ++c) {
-    off[c] = (int)tasks.size();
-    if (c == 0) continue;
-    for (int ax = 0; ax < 3; ++ax)
-      for (int side = 0; side < 2; ++side) {
-        int src = src_of[(size_t)c * 6 + ax * 2 + side];
-        if (src > 0) {
-          FaceTask t;
-          t.src = src;
-          t.axis = (int8_t)ax;
-          t.side = (int8_t)side;
-          t.kind = 0;
-          t.pad = 0;
-          tasks.push_back(t);
+}
+
+}  // namespace
+
+// Face tasks from adjacency, classifying neighbours like
+// BCM_Interface_table.cpp:96-308: a cube has a +dir (-dir) relation when any
+// of the four slots adj_number[c][1..4][dir] is positive; the classifying
+// cube is the largest slot value; same level when csl matches, big->small
+// when this cube's csl is larger.  The same-level copy partner is slot 1
+// (:1753).  Level jumps must be 2:1.
+bool build_interface_tasks(int ncube, const int *adj, const int *csl, std::vector<int> &off,
+                           std::vector<FaceTask> &tasks, std::string &err) {
+  if (!check_adj(ncube, adj, err)) return false;
+  auto A = [&](int c, int s, int d) { return adj[(c * 5 + s) * 7 + d]; };
+  TaskSet T(ncube);
+  for (int ax = 0; ax < 3; ++ax) {
+    std::vector<int> bsp, bsm;
+    for (int c = 1; c < ncube; ++c) {
+      for (int pm = 0; pm < 2; ++pm) {
+        const int dir = pm == 0 ? 2 + 2 * ax : 1 + 2 * ax;
+        int any = 0, acube = 0;
+        for (int s = 1; s <= 4; ++s) {
+          any |= A(c, s, dir) > 0;
+          acube = std::max(acube, A(c, s, dir));
+        }
+        if (!any) continue;
+        const int dl = csl[c] - csl[acube];
+        if (dl > 1 || dl < -1) {
+          err = fmt("cube %lld: level jump larger than 2:1 on axis %lld", c, ax);
+          return false;
+        }
+        if (pm == 0 && dl == 0) {
+          const int c2 = A(c, 1, dir);
+          if (c2 <= 0) {
+            err = fmt("cube %lld: +axis %lld neighbour missing from slot 1", c, ax);
+            return false;
+          }
+          T.put(c2, c, ax, 0, 0, 0);  // c2 low ghosts <- c high interior
+          T.put(c, c2, ax, 1, 0, 0);  // c high ghosts <- c2 low interior
+        }
+        if (dl == 1) (pm == 0 ? bsp : bsm).push_back(c);
+      }
+    }
+    for (int B : bsp) level_tasks(T, adj, B, ax, 0, true);
+    for (int B : bsm) level_tasks(T, adj, B, ax, 1, true);
+    for (int B : bsp) level_tasks(T, adj, B, ax, 0, false);
+    for (int B : bsm) level_tasks(T, adj, B, ax, 1, false);
+  }
+  return T.finish(off, tasks, err);
+}
+
+// The same tasks from explicit reference lists (adjX_eq, adjX_bs_plus,
+// adjX_bs_minus, ... 1-based with counts), as BCM_Interface receives them.
+bool build_interface_tasks_from_lists(int ncube, const int *adj, const int *csl,
+                                      const int *const lists[9], const int counts[9],
+                                      std::vector<int> &off, std::vector<FaceTask> &tasks,
+                                      std::string &err) {
+  (void)csl;
+  if (!check_adj(ncube, adj, err)) return false;
+  TaskSet T(ncube);
+  for (int ax = 0; ax < 3; ++ax) {
+    for (int l = 0; l < 3; ++l)
+      for (int a = 1; a <= counts[3 * ax + l]; ++a) {
+        const int c = lists[3 * ax + l][a];
+        if (c <= 0 || c >= ncube) {
+          err = fmt("interface list %lld entry %lld out of range", 3 * ax + l, a);
+          return false;
         }
       }
+    const int dplus = 2 + 2 * ax;
+    for (int a = 1; a <= counts[3 * ax]; ++a) {
+      const int c = lists[3 * ax][a];
+      const int c2 = adj[(c * 5 + 1) * 7 + dplus];
+      if (c2 <= 0) {
+        err = fmt("cube %lld: neighbour on axis %lld missing", c, ax);
+        return false;
+      }
+      T.put(c2, c, ax, 0, 0, 0);
+      T.put(c, c2, ax, 1, 0, 0);
+    }
+    for (int a = 1; a <= counts[3 * ax + 1]; ++a) level_tasks(T, adj, lists[3 * ax + 1][a], ax, 0, true);
+    for (int a = 1; a <= counts[3 * ax + 2]; ++a) level_tasks(T, adj, lists[3 * ax + 2][a], ax, 1, true);
+    for (int a = 1; a <= counts[3 * ax + 1]; ++a) level_tasks(T, adj, lists[3 * ax + 1][a], ax, 0, false);
+    for (int a = 1; a <= counts[3 * ax + 2]; ++a) level_tasks(T, adj, lists[3 * ax + 2][a], ax, 1, false);
   }
-  off[ncube] = (int)tasks.size();
-  return true;
+  return T.finish(off, tasks, err);
 }
 
 bool build_bc_entries(int ncube, const int *const lists[6], const int counts[6],
@@ -254,9 +302,11 @@ extern "C" int bcmg_interface_tasks(int ncube, const int *adj_number, const int 
     for (size_t i = 0; i < off.size(); ++i) task_off[i] = off[i];
   if (task_words)
     for (size_t t = 0; t < tasks.size(); ++t) {
-      task_words[3 * t + 0] = tasks[t].src;
-      task_words[3 * t + 1] = tasks[t].axis;
-      task_words[3 * t + 2] = tasks[t].side;
+      task_words[5 * t + 0] = tasks[t].src;
+      task_words[5 * t + 1] = tasks[t].axis;
+      task_words[5 * t + 2] = tasks[t].side;
+      task_words[5 * t + 3] = tasks[t].kind;
+      task_words[5 * t + 4] = tasks[t].slot;
     }
   return (int)tasks.size();
 }

@@ -96,10 +96,10 @@ void BCM_Ghostcell_plus(int myid, int *NNBC, double *weight, int *GCindex, int *
                         int *FWS, double *U1_);
 
 /* Replaces BCM_Interface (main.h:224-354, BCM_Interface.cpp:27-5735) with
- * its full parameter list.  Single process: the cross-rank exchange lists
- * must be empty (ncpu_bs == ncpu_eq == ncpu_sb == 0), otherwise the call
- * fails with BCMG_ERR_UNSUPPORTED and leaves U1_ untouched.  Level-jump
- * lists (bs/sb) are not supported yet and fail the same way. */
+ * its full parameter list: same-level copies, 2:1 coarse/fine level jumps
+ * (from the bs lists) and the ordered edge fill.  Single process: the
+ * cross-rank exchange lists must be empty (ncpu_bs == ncpu_eq == ncpu_sb ==
+ * 0), otherwise the call fails and leaves U1_ untouched. */
 void BCM_Interface(int myid, int ncube, int mPI_Nadj, int ncpu_bs, int ncpu_eq, int ncpu_sb,
                    int max_nei_bs, int max_nei_eq, int max_nei_sb, int nadjX_eq, int nadjY_eq,
                    int nadjZ_eq, int nadjX_bs_plus, int nadjX_sb_plus, int nadjX_bs_minus,
@@ -255,11 +255,13 @@ int bcmg_probe_fp64_rate(double *gflops);
 int bcmg_ibm_schedule(int nbc, const int *GCindex, const int *IPsur, int n, int ncube,
                       int *level_of_entry);
 
-/* Same-level interface copy tasks derived from adj_number/csl like
- * BCM_Interface_table.cpp:96-208: task_off[ncube+1] (CSR by destination
- * cube) and task_words[3*t..] = (source cube, axis 0..2, side 0 low / 1 high
- * ghost layers).  Returns the task count, -1 for invalid input or a level
- * jump, -2 if max_tasks is too small. */
+/* Interface copy tasks derived from adj_number/csl like
+ * BCM_Interface_table.cpp:96-308: task_off[ncube+1] (CSR by destination
+ * cube) and task_words[5*t..] = (source cube, axis 0..2, side 0 low / 1 high
+ * ghost layers, kind 0 same-level / 1 coarse->fine / 2 fine->coarse, sub-face
+ * slot 1..4 for kinds 1 and 2).  Returns the task count, -1 for invalid input
+ * (out-of-range adjacency, a jump larger than 2:1, inconsistent faces), -2
+ * if max_tasks is too small. */
 int bcmg_interface_tasks(int ncube, const int *adj_number, const int *csl, int *task_off,
                          int *task_words, int max_tasks);
 

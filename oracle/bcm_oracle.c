@@ -693,12 +693,79 @@ void bcmo_interface(const bcmo_phys *ph, int ncube, const int *adj, const int *c
   }
 }
 
-/* Level jumps (coarse<->fine faces) are not part of this restatement yet;
- * a grid with level jumps is rejected by the callers.  Kept as a hook so the
- * call order above matches BCM_Interface.cpp (local copies, then edges). */
+/* Level jumps between a cube B and its four half-size neighbours across one
+ * face (BCM_Interface.cpp:1790-2599 x, :2651-3470 y, :3518-4358 z; lists as
+ * BCM_Interface_table.cpp:96-308 builds them).  For axis a with tangential
+ * axes t0 < t1, sub-face slot s (1..4) offsets (t0, t1) by
+ * ((s==2||s==4)*n/2, (s==3||s==4)*n/2).  Four blocks per axis:
+ *  (a) B bigger than its +a neighbours: each small cube's low ghost layers
+ *      l=0,1 <- B's cell (n+1, p/2+1+o0, q/2+1+o1) (injection, :1790-1899);
+ *  (b) B bigger than its -a neighbours: each small cube's high ghost layers
+ *      n+2+l <- B's cell (2, p/2+1+o0, q/2+1+o1) (:1903-2022);
+ *  (c) B's high ghost layers n+2+l over the slot's quadrant <- 0.125 * the sum
+ *      of the small cube's 2x2x2 cells at along-axis 2l+2 (:2026-2314);
+ *  (d) B's low ghost layers l <- 0.125 * sum at along-axis n-2+2l (:2318-2599).
+ * Every read is an interior cell, every write a ghost cell, so the blocks
+ * commute with each other and with the same-level copies. */
+static void lvl_index(int ax, int g, int p, int q, int *ijk) {
+  int t0 = ax == 0 ? 1 : 0, t1 = ax == 2 ? 1 : 2;
+  ijk[ax] = g;
+  ijk[t0] = p;
+  ijk[t1] = q;
+}
+
 void bcmo_interface_levels(const bcmo_phys *ph, int ncube, const int *adj, const int *csl,
                            double *U1_) {
-  (void)ph; (void)ncube; (void)adj; (void)csl; (void)U1_;
+  const int n = ph->n, S = n + 4, h = n / 2;
+  static const int off8[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1},
+                                 {1, 1, 0}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
+  for (int ax = 0; ax < 3; ++ax) {
+    for (int pm = 0; pm < 2; ++pm) { /* pm 0: +a neighbours (bs_plus), 1: -a (bs_minus) */
+      const int dir = pm == 0 ? 2 + 2 * ax : 1 + 2 * ax;
+      for (int B = 1; B < ncube; ++B) {
+        int any = 0, acube = 0;
+        for (int sl = 1; sl <= 4; ++sl) {
+          int v = adj[(B * 5 + sl) * 7 + dir];
+          any |= v > 0;
+          if (v > acube) acube = v;
+        }
+        if (!any || !(csl[B] > csl[acube])) continue;
+        for (int sl = 1; sl <= 4; ++sl) {
+          const int sc = adj[(B * 5 + sl) * 7 + dir];
+          if (sc <= 0) continue;
+          const int o0 = (sl == 2 || sl == 4) ? h : 0, o1 = (sl == 3 || sl == 4) ? h : 0;
+          /* (a) / (b): coarse -> fine injection into the small cube */
+          for (int l = 0; l < 2; ++l)
+            for (int p = 2; p <= n + 1; ++p)
+              for (int q = 2; q <= n + 1; ++q) {
+                int d[3], sidx[3];
+                lvl_index(ax, pm == 0 ? l : n + 2 + l, p, q, d);
+                lvl_index(ax, pm == 0 ? n + 1 : 2, p / 2 + 1 + o0, q / 2 + 1 + o1, sidx);
+                memmove(U1_ + 5 * at(S, sc, d[0], d[1], d[2]),
+                        U1_ + 5 * at(S, B, sidx[0], sidx[1], sidx[2]), 5 * sizeof(double));
+              }
+          /* (c) / (d): fine -> coarse 8-cell average into B */
+          for (int l = 0; l < 2; ++l)
+            for (int p = 2; p <= h + 1; ++p)
+              for (int q = 2; q <= h + 1; ++q) {
+                int d[3], b[3];
+                lvl_index(ax, pm == 0 ? n + 2 + l : l, p + o0, q + o1, d);
+                lvl_index(ax, pm == 0 ? 2 * (l + 1) : n - 2 + 2 * l, (p - 1) * 2, (q - 1) * 2, b);
+                double *dst = U1_ + 5 * at(S, B, d[0], d[1], d[2]);
+                for (int v = 0; v < 5; ++v) {
+                  double sum = 0;
+                  for (int m = 0; m < 8; ++m) {
+                    double x = U1_[5 * at(S, sc, b[0] + off8[m][0], b[1] + off8[m][1],
+                                          b[2] + off8[m][2]) + v];
+                    sum = m == 0 ? x : sum + x;
+                  }
+                  dst[v] = 0.125 * sum;
+                }
+              }
+        }
+      }
+    }
+  }
 }
 
 /* Time-level shift on interior cells (main.cpp:1292-1315). */

@@ -26,6 +26,11 @@ def golden_cases():
         "vortex_n8": cases.isentropic_vortex(ncx=2, n=8, dT=1e-3),
         # viscous Taylor-Green, 2x2x2 cubes of 8^3 (config-2 physics, small)
         "tgv_n8": cases.taylor_green(ncx=2, n=8),
+        # two cube levels (one coarse cube refined 2:1), periodic and open:
+        # every coarse<->fine interface block (config-3 structure, small)
+        "two_level_periodic_n4": cases.random_two_level_case(seed=5, n=4, periodic=True,
+                                                             solid_frac=0.03, ghost_frac=0.03),
+        "two_level_open_n8": cases.random_two_level_case(seed=6, n=8, periodic=False),
     }
 
 

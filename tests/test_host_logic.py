@@ -95,15 +95,16 @@ def test_interface_tasks_match_reference_lists():
     BCM_Interface_table.cpp would list (periodic box: 6 faces per cube)."""
     case = cases.taylor_green(ncx=3, n=4)
     off = np.zeros(case.ncube + 1, np.int32)
-    words = np.zeros(3 * 6 * case.ncube, np.int32)
+    words = np.zeros(5 * 6 * case.ncube, np.int32)
     nt = lib().bcmg_interface_tasks(case.ncube, np.ascontiguousarray(case.adj, np.int32),
                                     case.csl, off, words, 6 * case.ncube)
     assert nt == 6 * (case.ncube - 1)
-    w = words[:3 * nt].reshape(-1, 3)
+    w = words[:5 * nt].reshape(-1, 5)
     for c in range(1, case.ncube):
         t = w[off[c]:off[c + 1]]
         assert len(t) == 6
-        for src, ax, side in t:
+        for src, ax, side, kind, slot in t:
+            assert kind == 0
             # side 0: low ghosts from the -axis neighbour; 1: high from +axis
             assert src == case.adj[c, 1, 1 + 2 * ax + side]
 
@@ -111,10 +112,48 @@ def test_interface_tasks_match_reference_lists():
 def test_open_box_interface_tasks_skip_domain_faces():
     ncube, cs, csl, org, adj = cases.open_box(2, 2, 2, 4, 1.0)
     off = np.zeros(ncube + 1, np.int32)
-    words = np.zeros(3 * 6 * ncube, np.int32)
+    words = np.zeros(5 * 6 * ncube, np.int32)
     nt = lib().bcmg_interface_tasks(ncube, np.ascontiguousarray(adj, np.int32),
                                     np.ascontiguousarray(csl, np.int32), off, words, 6 * ncube)
     assert nt == 3 * (ncube - 1)  # each cube of a 2x2x2 open box has 3 neighbours
+
+
+def test_two_level_interface_tasks():
+    """A refined coarse cube in a periodic 2x2x2 coarse box: every face of the
+    8 fine cubes that touches a coarse cube gets one coarse->fine task; each
+    coarse face next to the refined block gets four fine->coarse quadrant
+    tasks (slots 1..4)."""
+    case = cases.random_two_level_case(seed=1, n=4)
+    off = np.zeros(case.ncube + 1, np.int32)
+    words = np.zeros(5 * 24 * case.ncube, np.int32)
+    nt = lib().bcmg_interface_tasks(case.ncube, np.ascontiguousarray(case.adj, np.int32),
+                                    case.csl, off, words, 24 * case.ncube)
+    assert nt > 0
+    w = words[:5 * nt].reshape(-1, 5)
+    kinds = np.bincount(w[:, 3], minlength=3)
+    fine = [c for c in range(1, case.ncube) if case.csl[c] == 0]
+    # each fine cube: 3 of its 6 faces touch coarse cubes (periodic 2x2x2 box)
+    assert kinds[1] == 3 * len(fine)
+    # each coarse face adjoining the refined block: 4 quadrant tasks
+    assert kinds[2] % 4 == 0 and kinds[2] > 0
+    for c in range(1, case.ncube):
+        t = w[off[c]:off[c + 1]]
+        faces = {}
+        for src, ax, side, kind, slot in t:
+            faces.setdefault((ax, side), []).append((kind, slot))
+        for f, ks in faces.items():
+            assert (len(ks) == 1 and ks[0][0] in (0, 1)) or sorted(ks) == [(2, s) for s in (1, 2, 3, 4)]
+
+
+def test_level_jump_beyond_2_to_1_is_rejected():
+    case = cases.random_two_level_case(seed=1, n=4)
+    csl = case.csl.copy()
+    csl[csl == 1] = 3  # make the coarse cubes 8x the fine size
+    off = np.zeros(case.ncube + 1, np.int32)
+    words = np.zeros(5 * 24 * case.ncube, np.int32)
+    nt = lib().bcmg_interface_tasks(case.ncube, np.ascontiguousarray(case.adj, np.int32), csl,
+                                    off, words, 24 * case.ncube)
+    assert nt == -1
 
 
 @pytest.mark.skipif(not O.reference_available(), reason="reference sources not on this host")
