@@ -420,3 +420,106 @@ def random_two_level_case(seed=1, ncx=2, ncy=2, ncz=2, n=4, periodic=True, visco
     return Case(n=n, ncube=ncube, phys=ph, cube_size=cube_size, csl=csl, origin=origin,
                 adj=adj, fws=fws, U=np.ascontiguousarray(U), dT=1e-4, dTau=1e-4 / 200.0,
                 name=name)
+
+
+def sphere_ibm(n=16, coarse=2.0, box=((-10.0, 20.0), (-10.0, 10.0), (-10.0, 10.0)),
+               refine_box=((-2.0, 4.0), (-2.0, 2.0), (-2.0, 2.0)), diameter=1.0, mach=0.3,
+               reynolds=300.0, noise=1e-4, seed=7, dT=1e-4, sub_ratio=200.0, name="sphere"):
+    """Flow past a sphere with immersed-boundary ghost cells on a two-level grid.
+
+    Coarse cubes of edge `coarse` tile `box`; those inside `refine_box` are
+    split into 2x2x2 fine cubes (2:1).  Flags from the analytic sphere
+    (BCM.h:6-8): cells whose centre lies inside are solid, solid cells with a
+    fluid face neighbour are IBM ghost cells.  Each ghost cell gets the image
+    point mirrored across the surface, the 8 cells around it in its own cube
+    (IPsur) and trilinear weights in the reference's 000,100,010,001,110,101,
+    011,111 order rounded to 6 decimals (BCM_Immersed_boundary.cpp writes them
+    with %f); ghosts with x < 0 go to the "minus" list, the rest to "plus".
+    Free stream at `mach`, Re on the diameter, seeded density noise; solid
+    cells at rest (BCM_Initial_condition.cpp).  Domain faces carry the
+    reference's X/Y/Z boundary conditions.
+    """
+    (x0, x1), (y0, y1), (z0, z1) = box
+    ncx, ncy, ncz = (int(round((x1 - x0) / coarse)), int(round((y1 - y0) / coarse)),
+                     int(round((z1 - z0) / coarse)))
+    (rx0, rx1), (ry0, ry1), (rz0, rz1) = refine_box
+
+    def refine(a, b, c):
+        cx0, cy0, cz0 = x0 + a * coarse, y0 + b * coarse, z0 + c * coarse
+        return (cx0 >= rx0 - 1e-9 and cx0 + coarse <= rx1 + 1e-9 and cy0 >= ry0 - 1e-9 and
+                cy0 + coarse <= ry1 + 1e-9 and cz0 >= rz0 - 1e-9 and cz0 + coarse <= rz1 + 1e-9)
+
+    ncube, cube_size, csl, origin, adj = two_level_box(ncx, ncy, ncz, n, ncx * coarse, refine,
+                                                       periodic=False)
+    origin = origin + np.array([x0, y0, z0])
+    S = n + 4
+    ph = Phys(rho0=1.1842, P0=101300.0, mpi_ncube=ncube - 1)
+    c0 = np.sqrt(GAMMA * ph.P0 / ph.rho0)
+    ph.U0 = ph.Uin = mach * c0
+    ph.mu_L = ph.rho0 * ph.U0 * diameter / reynolds
+    R = 0.5 * diameter
+    geom = (ncube, cube_size, csl, origin, adj)
+    X, Y, Z = _grid(geom, n)
+    r = np.sqrt(X * X + Y * Y + Z * Z)
+    solid = r < R
+    fws = np.where(solid, ISOLID, IFLUID).astype(np.int32)
+    # ghost = solid with a fluid face neighbour (inside the padded cube)
+    ghost = np.zeros_like(solid)
+    for ax in (1, 2, 3):
+        for sh in (1, -1):
+            nb = np.roll(~solid, sh, axis=ax)
+            edge = [slice(None)] * 4
+            edge[ax] = 0 if sh == 1 else S - 1
+            nb[tuple(edge)] = False
+            ghost |= solid & nb
+    fws[ghost] = IGHOST
+    fws[0] = IFLUID
+    # IBM tables for interior ghost cells
+    entries = {"minus": [], "plus": []}
+    idx = np.argwhere(ghost[1:, 2:n + 2, 2:n + 2, 2:n + 2])
+    for cc, ii, jj, kk in idx:
+        c, i, j, k = int(cc) + 1, int(ii) + 2, int(jj) + 2, int(kk) + 2
+        dx = cube_size[c] / n
+        xg = np.array([X[c, i, j, k], Y[c, i, j, k], Z[c, i, j, k]])
+        rg = np.linalg.norm(xg)
+        xs = xg * (R / max(rg, 1e-12))
+        xi = 2 * xs - xg
+        # base cell of the 8-cell box containing the image point, kept inside
+        # the padded cube: centre of cell m is origin + (m - 1.5) dx
+        f = (xi - origin[c]) / dx + 1.5
+        base = np.clip(np.floor(f).astype(int), 1, S - 2)
+        t = np.clip(f - base, 0.0, 1.0)
+        wx, wy, wz = t
+        w = np.array([(1 - wx) * (1 - wy) * (1 - wz), wx * (1 - wy) * (1 - wz),
+                      (1 - wx) * wy * (1 - wz), (1 - wx) * (1 - wy) * wz, wx * wy * (1 - wz),
+                      wx * (1 - wy) * wz, (1 - wx) * wy * wz, wx * wy * wz])
+        w = np.round(w, 6)
+        e = (c, i, j, k, c, int(base[0]), int(base[1]), int(base[2]), w)
+        entries["minus" if xg[0] < 0 else "plus"].append(e)
+
+    def pack(lst):
+        m = len(lst)
+        GC = np.zeros(4 * m + 1, np.int32)
+        IP = np.zeros(4 * m + 1, np.int32)
+        W = np.zeros(8 * m + 1)
+        for q, (c, i, j, k, ic, bi, bj, bk, w) in enumerate(lst):
+            GC[4 * q + 1:4 * q + 5] = (c, i, j, k)
+            IP[4 * q + 1:4 * q + 5] = (ic, bi, bj, bk)
+            W[8 * q + 1:8 * q + 9] = w
+        return W, GC, IP
+
+    cnt = ncube * S ** 3
+    rnd = splitmix_uniform(seed, cnt).reshape(ncube, S, S, S)
+    rho = ph.rho0 * (1 + noise * (rnd - 0.5))
+    u = np.full_like(rho, ph.U0)
+    zero = np.zeros_like(rho)
+    p = np.full_like(rho, ph.P0)
+    U = conservative(rho, u, zero, zero, p)
+    rest = conservative(np.full_like(rho, ph.rho0), zero, zero, zero, p)
+    U = np.where(solid[..., None], rest, U)
+    case = Case(n=n, ncube=ncube, phys=ph, cube_size=cube_size, csl=csl, origin=origin, adj=adj,
+                fws=fws, U=np.ascontiguousarray(U), dT=dT, dTau=dT / sub_ratio, name=name)
+    case.ibm_minus = pack(entries["minus"])
+    case.ibm_plus = pack(entries["plus"])
+    case.meta.update(area_ratio=2.602 / (np.pi / 4 * diameter ** 2), ghosts=int(ghost[1:].sum()))
+    return case

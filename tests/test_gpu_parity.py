@@ -193,3 +193,28 @@ def test_invalid_inputs_fail_loudly():
     with pytest.raises(api.BcmgError):
         api.BCM_X_boundary_condition(0, 1, 0, np.array([0, 99], np.int32)[:1].repeat(2) * 0 - 1,
                                      np.zeros(1, np.int32), U)
+
+
+def _small_sphere():
+    return cases.sphere_ibm(n=8, coarse=2.0, box=((-2, 4), (-2, 2), (-2, 2)),
+                            refine_box=((-2, 2), (-2, 2), (-2, 2)))
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_sphere_ibm_two_level_bitwise(port, graph):
+    """Sphere with IBM ghost cells on a two-level grid with open-domain
+    boundary conditions: every hot-path component in one loop."""
+    case = _small_sphere()
+    a = O.State(case)
+    port.run(case, a, 2, 2)
+    ctx = api.CaseContext(case)
+    ctx.set_state(case.U, case.U, case.U)
+    er = ctx.advance(2, 2, use_graph=graph)
+    U1_, U1, U1q = ctx.get_state()
+    assert np.array_equal(U1_, a.U1_) and np.array_equal(U1, a.U1) and np.array_equal(U1q, a.U1q)
+    assert np.allclose(er[1:6], a.er[1:6], rtol=1e-12, atol=0)
+    # force integrals (drag / lift like terms, er[6], er[7])
+    scale = np.abs(a.Residual1).max() / (0.5 * case.phys.rho0 * case.phys.U0 ** 2 * 2.602)
+    assert abs(er[6] - a.er[6]) <= 1e-12 * max(abs(a.er[6]), scale)
+    assert abs(er[7] - a.er[7]) <= 1e-12 * max(abs(a.er[7]), scale)
+    ctx.close()

@@ -60,3 +60,15 @@ def test_split_vortex_config1_size():
     (b, _, _), _ = run(case, api.PRECISION_SPLIT, 3, 10)
     err = rel_l2(b, a, case.n)
     assert max(err) <= SPLIT_BOUND, err
+
+
+def test_split_sphere_forces_within_bound():
+    """Sphere IBM case: split state within the bound and the drag/lift
+    integrals (er[6], er[7]) within 0.1% of the FP64 path."""
+    case = cases.sphere_ibm(n=8, coarse=2.0, box=((-2, 4), (-2, 2), (-2, 2)),
+                            refine_box=((-2, 2), (-2, 2), (-2, 2)))
+    (a, _, _), er_a = run(case, api.PRECISION_FP64, 2, 3)
+    (b, _, _), er_b = run(case, api.PRECISION_SPLIT, 2, 3)
+    err = rel_l2(b, a, case.n)
+    assert max(err) <= SPLIT_BOUND, err
+    assert abs(er_b[6] - er_a[6]) <= 1e-3 * abs(er_a[6]), (er_a[6], er_b[6])
