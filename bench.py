@@ -38,21 +38,44 @@ SUBITERS = 10
 BYTES_PER_CELL_STAGE = 164
 
 
+WORKLOADS = {
+    # the metric's configuration (largest single-GPU config it is quoted on)
+    "tgv": ("taylor-green vortex, periodic 2pi box, 8x8x8 cubes of 24^3 cells "
+            "(7,077,888 cells), M=0.1, Re=1600, Pr=0.72, dT=1e-4, dTau=dT/200"),
+    # the reference's CPU-runnable case
+    "vortex": ("inviscid isentropic vortex, periodic unit box, 4x4x4 cubes of 16^3 cells "
+               "(262,144 cells), M=0.5, strength 5, dT=1e-3, dTau=dT/200"),
+    # immersed-boundary sphere on two cube levels
+    "sphere": ("sphere D=1 with IBM ghost cells, domain [-10,20]x[-10,10]^2, coarse cubes of "
+               "2 refined 2:1 in [-2,4]x[-2,2]^2, 1584 cubes of 16^3 (6,488,064 cells), "
+               "M=0.3, Re=300, inflow/outflow/slip boundaries, dT=1e-4, dTau=dT/200"),
+    # large single case
+    "tgv32": ("taylor-green vortex, periodic 2pi box, 16x16x16 cubes of 32^3 cells "
+              "(134,217,728 cells), M=0.1, Re=1600, dT=1e-4, dTau=dT/200"),
+}
+WORKLOAD = "tgv"
+
+
 def workload_case():
     from bcm_cgli_gb300 import cases
+    if WORKLOAD == "vortex":
+        return cases.isentropic_vortex(ncx=4, n=16)
+    if WORKLOAD == "sphere":
+        return cases.sphere_ibm()
+    if WORKLOAD == "tgv32":
+        return cases.taylor_green(ncx=16, n=32)
     return cases.taylor_green(ncx=8, n=24)
 
 
 def workload_config(case, precision):
     return {
-        "workload": "taylor-green vortex, periodic 2pi box, 8x8x8 cubes of 24^3 cells "
-                    "(7,077,888 cells), M=0.1, Re=1600, Pr=0.72, dT=1e-4, dTau=dT/200, "
-                    f"{SUBITERS} sub-iterations x 3 RK stages per dual-time step",
+        "workload": WORKLOADS[WORKLOAD] + f"; {SUBITERS} sub-iterations x 3 RK stages per "
+                                          "dual-time step",
         "cells": int(case.n_cells),
         "subiters_per_step": SUBITERS,
         "precision": precision,
-        "l2": "inputs larger than L2: each state array is "
-              f"{case.U.nbytes / 1e6:.0f} MB (7 arrays resident)",
+        "l2": "each state array is "
+              f"{case.U.nbytes / 1e6:.0f} MB (L2 is 129 MB)",
         "parallelism": "replica per GPU",
     }
 
@@ -235,6 +258,29 @@ def measure(api, case, precision_name, args, dist, clocks_on=True):
     return out
 
 
+def measure_e2e(ctx, case, args, dist, cell_subiters):
+    """Per step: host (pinned) -> device state (U1_, U1, U1q), one dual-time
+    step, device -> host state, through the public C ABI; device-timed."""
+    hU, hold = pinned_like(case.U)
+    hU1, hold1 = pinned_like(case.U)
+    hU1q, hold1q = pinned_like(case.U)
+    oU, ohold = pinned_like(case.U)
+    oU1, ohold1 = pinned_like(case.U)
+    oU1q, ohold1q = pinned_like(case.U)
+    dist.barrier()
+    ctx.sync()
+    ctx.timer_mark(2)
+    for _ in range(args.steps):
+        ctx.set_state(hU, hU1, hU1q)
+        ctx.advance(1, SUBITERS, use_graph=True)
+        ctx.get_state(out=[oU, oU1, oU1q])
+    ctx.timer_mark(3)
+    ctx.sync()
+    dist.barrier()
+    ms_e2e = dist.max(ctx.timer_elapsed(2, 3))
+    return cell_subiters / (ms_e2e * 1e-3)
+
+
 def rel_l2(a, b, n):
     """Relative L2 error per conservative variable over interior cells; the
     momentum components are also given relative to the momentum magnitude
@@ -265,37 +311,29 @@ def run_gpu_arm(args, dist):
             ctx = m["ctx"]
             ctx.set_state(case.U, case.U, case.U)
             ctx.emax[:] = 0
-            ctx.advance(1, SUBITERS, use_graph=True)
+            m["er"] = ctx.advance(1, SUBITERS, use_graph=True)
             states[name] = ctx.get_state()[0]
         own, scaled = rel_l2(states["split"], states["fp64"], case.n)
         acc = {"rel_l2_per_variable": own, "rel_l2_momentum_scaled": scaled,
                "max_rel_l2": max(scaled), "bound": 1e-5,
                "after": f"1 dual-time step ({SUBITERS} sub-iterations) from the same state"}
+        if WORKLOAD == "sphere":
+            # drag / lift from the force integrals er[6], er[7] (normalised by
+            # 0.5 rho0 U0^2 * 2.602 in the reference) re-scaled to the sphere's
+            # frontal area
+            ratio = case.meta["area_ratio"]
+            f = {name: (-m["er"][6] * ratio, -m["er"][7] * ratio)
+                 for name, m in ((head, m_head), (other, m_other))}
+            acc["cd_cl"] = {k: list(v) for k, v in f.items()}
+            acc["cd_rel_err"] = abs(f["split"][0] - f["fp64"][0]) / abs(f["fp64"][0])
 
     ctx = m_head["ctx"]
-    # e2e: per step, host (pinned) -> device state, one dual-time step,
-    # device -> host state, through the public C ABI.
-    hU, hold = pinned_like(case.U)
-    hU1, hold1 = pinned_like(case.U)
-    hU1q, hold1q = pinned_like(case.U)
-    oU, ohold = pinned_like(case.U)
-    oU1, ohold1 = pinned_like(case.U)
-    oU1q, ohold1q = pinned_like(case.U)
-    dist.barrier()
-    ctx.sync()
-    ctx.timer_mark(2)
-    for _ in range(args.steps):
-        ctx.set_state(hU, hU1, hU1q)
-        ctx.advance(1, SUBITERS, use_graph=True)
-        ctx.get_state(out=[oU, oU1, oU1q])
-    ctx.timer_mark(3)
-    ctx.sync()
-    dist.barrier()
-    ms_e2e = dist.max(ctx.timer_elapsed(2, 3))
     cell_subiters = case.n_cells * SUBITERS * args.steps * dist.world
-    e2e = cell_subiters / (ms_e2e * 1e-3)
-
+    e2e = None
+    if not args.no_e2e:
+        e2e = measure_e2e(ctx, case, args, dist, cell_subiters)
     peaks = {}
+
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
@@ -326,8 +364,8 @@ def run_gpu_arm(args, dist):
             "dtype": "f64" if head == "fp64" else "f32+f64",
             "data": "synthetic", "config": workload_config(case, head),
             "roofline": roofline(m_head, head),
-            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 3 * case.U.nbytes,
-                    "d2h_bytes_per_step": 3 * case.U.nbytes},
+            "e2e": ({"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 3 * case.U.nbytes,
+                     "d2h_bytes_per_step": 3 * case.U.nbytes} if e2e is not None else None),
             "gpu_launches": m_head["launches"], "clocks": m_head["clocks"],
             "fp64_alu": {"measured_fma_gflops": fp64_gflops,
                          "note": "FP64 FMA rate of this GPU, measured by bcmg_probe_fp64_rate"}}
@@ -373,12 +411,17 @@ def main():
                     help="path whose throughput is the headline value (the other is "
                          "reported beside it)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end measurement")
     ap.add_argument("--quick", action="store_true",
                     help="headline path only (no second precision, no accuracy check)")
     ap.add_argument("--flux-only", action="store_true",
                     help="time the flux kernel alone on a smaller case (profiling target)")
     ap.add_argument("--ncx", type=int, default=6, help="cubes per edge for --flux-only")
+    ap.add_argument("--workload", default="tgv", choices=sorted(WORKLOADS),
+                    help="tgv (default, the metric's configuration), vortex, sphere, tgv32")
     args = ap.parse_args()
+    global WORKLOAD
+    WORKLOAD = args.workload
     if args.flux_only:
         run_flux_only(args)
         return
