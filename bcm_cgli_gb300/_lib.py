@@ -86,6 +86,11 @@ def _declare(L):
     L.bcmg_case_profile.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
     L.bcmg_case_timer_mark.argtypes = [P, C.c_int]
     L.bcmg_case_timer_elapsed.argtypes = [P, C.c_int, C.c_int, C.POINTER(C.c_double)]
+    L.bcmg_batch_create.argtypes = [C.c_int, C.POINTER(CaseDesc), C.POINTER(P)]
+    L.bcmg_case_ncase.argtypes = [P]
+    L.bcmg_case_case_cubes.argtypes = [P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.bcmg_case_set_case_state.argtypes = [P, C.c_int, P, P, P]
+    L.bcmg_case_get_case_state.argtypes = [P, C.c_int, P, P, P]
     L.bcmg_probe_fp64_rate.argtypes = [C.POINTER(C.c_double)]
     L.bcmg_ibm_schedule.argtypes = [C.c_int, ip, ip, C.c_int, C.c_int, ip]
     L.bcmg_interface_tasks.argtypes = [C.c_int, ip, ip, ip, ip, C.c_int]

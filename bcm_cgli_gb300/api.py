@@ -157,46 +157,54 @@ def BCM_Interface_for_case(case, U1_):
 # ---------------------------------------------------------------------------
 # Device-resident context
 # ---------------------------------------------------------------------------
+def _case_desc(case, precision, keep):
+    """bcmg_case_desc of one case; the arrays it points at are appended to
+    `keep` (they must outlive the create call)."""
+    ph = case.phys
+
+    def arr(a, dt):
+        a = np.ascontiguousarray(a, dtype=dt)
+        if a.size == 0:
+            a = np.zeros(1, dt)
+        keep.append(a)
+        return a.ctypes.data
+
+    xl, xu, yl, yu, zl, zu = case.bc_lists()
+    d = _lib.CaseDesc()
+    d.n, d.ncube, d.mpi_ncube = case.n, case.ncube, ph.mpi_ncube
+    d.mu_L, d.rho0, d.U0, d.Uin, d.P0 = ph.mu_L, ph.rho0, ph.U0, ph.Uin, ph.P0
+    d.deltaT, d.deltaTau, d.e = case.dT, case.dTau, case.e
+    d.precision = precision
+    d.cube_size = arr(case.cube_size, np.float64)
+    d.csl = arr(case.csl, np.int32)
+    d.adj_number = arr(case.adj, np.int32)
+    d.FWS = arr(case.fws, np.int32)
+    d.nxl, d.nxu, d.nyl, d.nyu, d.nzl, d.nzu = map(len, (xl, xu, yl, yu, zl, zu))
+    d.xl, d.xu, d.yl, d.yu, d.zl, d.zu = (arr(a, np.int32) for a in (xl, xu, yl, yu, zl, zu))
+    if case.ibm_minus is not None:
+        W, G, I = case.ibm_minus
+        d.nminus = (len(G) - 1) // 4
+        d.w_minus, d.gc_minus, d.ip_minus = arr(W, np.float64), arr(G, np.int32), arr(I, np.int32)
+    if case.ibm_plus is not None:
+        W, G, I = case.ibm_plus
+        d.nplus = (len(G) - 1) // 4
+        d.w_plus, d.gc_plus, d.ip_plus = arr(W, np.float64), arr(G, np.int32), arr(I, np.int32)
+    return d
+
+
 class CaseContext:
     """A case resident in HBM (``bcmg_case_*``)."""
 
     def __init__(self, case, precision=PRECISION_FP64):
         self.case = case
-        ph = case.phys
-        self._keep = []
-
-        def arr(a, dt):
-            a = np.ascontiguousarray(a, dtype=dt)
-            if a.size == 0:
-                a = np.zeros(1, dt)
-            self._keep.append(a)
-            return a.ctypes.data
-
-        xl, xu, yl, yu, zl, zu = case.bc_lists()
-        d = _lib.CaseDesc()
-        d.n, d.ncube, d.mpi_ncube = case.n, case.ncube, ph.mpi_ncube
-        d.mu_L, d.rho0, d.U0, d.Uin, d.P0 = ph.mu_L, ph.rho0, ph.U0, ph.Uin, ph.P0
-        d.deltaT, d.deltaTau, d.e = case.dT, case.dTau, case.e
-        d.precision = precision
-        d.cube_size = arr(case.cube_size, np.float64)
-        d.csl = arr(case.csl, np.int32)
-        d.adj_number = arr(case.adj, np.int32)
-        d.FWS = arr(case.fws, np.int32)
-        d.nxl, d.nxu, d.nyl, d.nyu, d.nzl, d.nzu = map(len, (xl, xu, yl, yu, zl, zu))
-        d.xl, d.xu, d.yl, d.yu, d.zl, d.zu = (arr(a, np.int32) for a in (xl, xu, yl, yu, zl, zu))
-        if case.ibm_minus is not None:
-            W, G, I = case.ibm_minus
-            d.nminus = (len(G) - 1) // 4
-            d.w_minus, d.gc_minus, d.ip_minus = arr(W, np.float64), arr(G, np.int32), arr(I, np.int32)
-        if case.ibm_plus is not None:
-            W, G, I = case.ibm_plus
-            d.nplus = (len(G) - 1) // 4
-            d.w_plus, d.gc_plus, d.ip_plus = arr(W, np.float64), arr(G, np.int32), arr(I, np.int32)
+        keep = []
+        d = _case_desc(case, precision, keep)
         h = C.c_void_p()
         check(lib().bcmg_case_create(C.byref(d), C.byref(h)))
-        self._keep.clear()
+        del keep
         self.h = h
         self.shape = case.U.shape
+        self.ncase = 1
         self.emax = np.zeros(6)
 
     def close(self):
@@ -237,10 +245,11 @@ class CaseContext:
         check(lib().bcmg_case_stage(self.h, int(RK)))
 
     def advance(self, steps, subiters, use_graph=True):
-        er = np.zeros(8)
+        """er (8 doubles, 1-based like the reference); for a batch [ncase, 8]."""
+        er = np.zeros(8 * self.ncase)
         check(lib().bcmg_case_advance(self.h, int(steps), int(subiters), int(bool(use_graph)),
                                       er.ctypes.data, self.emax.ctypes.data))
-        return er
+        return er.reshape(self.ncase, 8) if isinstance(self, BatchContext) else er
 
     def sync(self):
         check(lib().bcmg_case_sync(self.h))
@@ -269,6 +278,44 @@ class CaseContext:
         ms = C.c_double()
         check(lib().bcmg_case_timer_elapsed(self.h, int(a), int(b), C.byref(ms)))
         return ms.value
+
+
+class BatchContext(CaseContext):
+    """Several independent cases (same n) advanced together in one context
+    (``bcmg_batch_create``): one flat cube list, per-case constants, norms
+    and convergence maxima."""
+
+    def __init__(self, case_list, precision=PRECISION_FP64):
+        self.cases = list(case_list)
+        keep = []
+        descs = (_lib.CaseDesc * len(self.cases))(
+            *[_case_desc(c, precision, keep) for c in self.cases])
+        h = C.c_void_p()
+        check(lib().bcmg_batch_create(len(self.cases), descs, C.byref(h)))
+        del keep
+        self.h = h
+        self.case = None
+        self.ncase = len(self.cases)
+        n = self.cases[0].n
+        self.shape = (1 + sum(c.ncube - 1 for c in self.cases), n + 4, n + 4, n + 4, 5)
+        self.emax = np.zeros((self.ncase, 6))
+
+    def case_cubes(self, q):
+        """(first flat cube, the case's own cube-slot count)."""
+        a, b = C.c_int(), C.c_int()
+        check(lib().bcmg_case_case_cubes(self.h, int(q), C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def set_case_state(self, q, U1_=None, U1=None, U1q=None):
+        arrs = [None if a is None else _dp(np.ascontiguousarray(a)) for a in (U1_, U1, U1q)]
+        check(lib().bcmg_case_set_case_state(self.h, int(q),
+                                             *(None if a is None else a.ctypes.data for a in arrs)))
+
+    def get_case_state(self, q):
+        shape = self.cases[q].U.shape
+        out = [np.empty(shape) for _ in range(3)]
+        check(lib().bcmg_case_get_case_state(self.h, int(q), *(a.ctypes.data for a in out)))
+        return out
 
 
 def probe_fp64_gflops():

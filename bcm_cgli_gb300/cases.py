@@ -523,3 +523,71 @@ def sphere_ibm(n=16, coarse=2.0, box=((-10.0, 20.0), (-10.0, 10.0), (-10.0, 10.0
     case.ibm_plus = pack(entries["plus"])
     case.meta.update(area_ratio=2.602 / (np.pi / 4 * diameter ** 2), ghosts=int(ghost[1:].sum()))
     return case
+
+
+def sphere_cubes(target, n=16, mach=0.3, reynolds=300.0, seed=7, dT=None, sub_ratio=200.0,
+                 name=None):
+    """Sphere flow (D = 1, IBM ghost cells, two levels) with about `target`
+    cubes: coarse cubes of edge 1 tile an mx x my x mz box (x about 1.5
+    times y and z); the 2x2x2 coarse cubes around the sphere are split into
+    64 fine cubes of edge 0.5, so the count is mx*my*mz + 56 (64 at least).
+    dT defaults to a convective CFL of 0.5 on the fine cells."""
+    m = max(target - 56, 8)
+    my = max(2, int(round((m / 1.5) ** (1.0 / 3.0))))
+    mx = max(2, int(round(m / (my * my))))
+    ix0 = max(0, min(mx - 2, mx // 3 - 1))
+    iy0 = (my - 2) // 2
+    x0, y0 = -(ix0 + 1.0), -(iy0 + 1.0)
+    if dT is None:
+        c0 = np.sqrt(GAMMA * 101300.0 / 1.1842)
+        dT = 0.5 * (0.5 / n) / (mach * c0)
+    return sphere_ibm(n=n, coarse=1.0, box=((x0, x0 + mx), (y0, y0 + my), (y0, y0 + my)),
+                      refine_box=((-1.0, 1.0), (-1.0, 1.0), (-1.0, 1.0)), mach=mach,
+                      reynolds=reynolds, seed=seed, dT=dT, sub_ratio=sub_ratio,
+                      name=name or f"sphere{mx}x{my}x{my}")
+
+
+def sphere_batch(ncase=16, seed=2024, n=16, lo=64, hi=2048):
+    """Independent sphere flows for one batched context: cube counts drawn
+    from the seed in [lo, hi] (realised to the nearest mx*my*mz + 56), Mach
+    uniform in [0.1, 0.6], Re uniform in [100, 1000], per-case dT (CFL 0.5 on
+    the fine cells) and per-case density-noise seeds."""
+    r = splitmix_uniform(seed, 3 * ncase).reshape(ncase, 3)
+    out = []
+    for q in range(ncase):
+        target = lo + int(r[q, 0] * (hi - lo + 1))
+        mach = 0.1 + 0.5 * float(r[q, 1])
+        re = 100.0 + 900.0 * float(r[q, 2])
+        out.append(sphere_cubes(min(target, hi), n=n, mach=mach, reynolds=re, seed=seed + 1 + q,
+                                name=f"sphere{q}"))
+    return out
+
+
+class CaseBatch:
+    """Cases advanced together in one batched context: `U` is the flat state
+    of the batch (case q's cubes 1.. follow case q-1's; slot 0 unused), the
+    layout bcmg_batch_create gives the device arrays."""
+
+    def __init__(self, case_list, name="batch"):
+        self.cases = list(case_list)
+        self.n = self.cases[0].n
+        self.name = name
+        self.ncube = 1 + sum(c.ncube - 1 for c in self.cases)
+        self.meta = {}
+        self._U = None
+
+    @property
+    def n_cells(self) -> int:
+        return sum(c.n_cells for c in self.cases)
+
+    @property
+    def U(self) -> np.ndarray:
+        if self._U is None:
+            S = self.n + 4
+            U = np.zeros((self.ncube, S, S, S, 5))
+            g = 1
+            for c in self.cases:
+                U[g:g + c.ncube - 1] = c.U[1:]
+                g += c.ncube - 1
+            self._U = U
+        return self._U

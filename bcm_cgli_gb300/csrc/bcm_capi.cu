@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -67,7 +68,10 @@ __global__ void k_time_shift(int n, long long total, const double *U1_, double *
 }
 
 __global__ void k_emax(double *er, double *emax) {
-  // main.cpp:1249-1259: E_k = max(E_k, er_k); er_k /= E_k.
+  // main.cpp:1249-1259: E_k = max(E_k, er_k); er_k /= E_k.  One block per
+  // case: er[8q..], emax[6q..].
+  er += 8 * (size_t)blockIdx.x;
+  emax += 6 * (size_t)blockIdx.x;
   const int v = threadIdx.x + 1;
   if (v <= 5) {
     double E = emax[v] > er[v] ? emax[v] : er[v];
@@ -116,7 +120,7 @@ int ibm_upload(Ibm &t, int nbc, const double *w, const int *gc, const int *ip, i
 }
 
 int ibm_run(const Ibm &t, int n, double rho0, double P0, double *U, cudaStream_t s,
-            long long *launches) {
+            long long *launches, const Batch &bt = Batch()) {
   for (size_t l = 1; l < t.level_off.size(); ++l) {
     GhostArgs g;
     g.n = n;
@@ -127,6 +131,7 @@ int ibm_run(const Ibm &t, int n, double rho0, double P0, double *U, cudaStream_t
     g.GCindex = t.gc;
     g.IPsur = t.ip;
     g.U1_ = U;
+    g.bt = bt;
     CK(launch_ghost(g, t.level_off[l] - t.level_off[l - 1], s));
     if (launches) ++*launches;
   }
@@ -162,7 +167,26 @@ struct bcmg_case {
   Ibm ibm;  // minus entries then plus entries, one combined schedule
   double *partials = nullptr;
   int nparts = 0;
-  double *er = nullptr, *emax = nullptr;  // device [8], [6]
+  double *er = nullptr, *emax = nullptr;  // device [8 ncase], [6 ncase]
+  // Batches (bcmg_batch_create): several cases end to end in one flat cube
+  // list; case q owns cubes [case_cube0[q], case_cube0[q+1]).
+  bool batched = false;
+  int ncase = 1;
+  std::vector<int> case_cube0;
+  std::vector<CaseConst> hcases;
+  CaseConst *cases = nullptr;   // device [ncase]
+  int *cube_case = nullptr;     // device [ncube]
+  long long *rk_blk = nullptr;  // device [nrk+1]: FP64 stage-update blocks
+  int nrk = 0;
+  int *case_blk_rk = nullptr, *case_blk_flux = nullptr;  // device [ncase+1]
+  Batch bt() const {
+    Batch b;
+    if (batched) {
+      b.cube_case = cube_case;
+      b.cases = cases;
+    }
+    return b;
+  }
   cudaGraphExec_t graph = nullptr;
   int graph_subiters = -1;
   long long launches = 0;
@@ -185,6 +209,7 @@ struct bcmg_case {
     dfree(M); dfree(D2); dfree(inv_dx);
     dfree(FWS); dfree(cube_size); dfree(task_cube); dfree(tasks); dfree(bc_cubes);
     dfree(bc_masks); dfree(partials); dfree(er); dfree(emax);
+    dfree(cases); dfree(cube_case); dfree(rk_blk); dfree(case_blk_rk); dfree(case_blk_flux);
     ibm.release();
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
@@ -207,6 +232,7 @@ int case_flux(bcmg_case *c, int RK) {
   a.U1q = c->U1q;
   a.Rku1 = c->Rku1;
   a.Residual1 = c->Residual1;
+  a.bt = c->bt();
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (c->profile) {
     while (c->ev.size() < c->ev_used + 2) {
@@ -220,7 +246,8 @@ int case_flux(bcmg_case *c, int RK) {
     CK(cudaEventRecord(e0, c->stream));
   }
   if (c->precision == BCMG_PRECISION_SPLIT) {
-    CK(launch_mirror(c->U1_, c->M, c->ph.n, c->ncube, c->ph.rho0, c->ph.P0, c->stream));
+    CK(launch_mirror(c->U1_, c->M, c->ph.n, c->ncube, c->ph.rho0, c->ph.P0, c->bt(),
+                     c->stream));
     ++c->launches;
     FluxSplitArgs sa;
     sa.ph = c->ph;
@@ -247,6 +274,7 @@ int case_flux(bcmg_case *c, int RK) {
     sa.RK = RK;
     sa.partials = c->partials;
     sa.Residual1 = c->Residual1;
+    sa.bt = c->bt();
     CK(launch_flux_split(sa, c->ncube - 1, c->stream));
   } else {
     CK(launch_flux_fp64(a, c->ncube - 1, c->stream));
@@ -278,10 +306,12 @@ int case_stage(bcmg_case *c, int RK) {
     b.masks = c->bc_masks;
     b.axes = 7;
     b.U1_ = c->U1_;
+    b.bt = c->bt();
     CK(launch_bc(b, c->nbc, c->stream));
     ++c->launches;
   }
-  if ((r = ibm_run(c->ibm, c->ph.n, c->ph.rho0, c->ph.P0, c->U1_, c->stream, &c->launches)))
+  if ((r = ibm_run(c->ibm, c->ph.n, c->ph.rho0, c->ph.P0, c->U1_, c->stream, &c->launches,
+                   c->bt())))
     return r;
   if ((r = case_interface(c))) return r;
   if ((r = case_flux(c, RK))) return r;
@@ -290,7 +320,11 @@ int case_stage(bcmg_case *c, int RK) {
     // the split flux kernel applied the stage update and wrote the partials
     nb = flux_split_blocks(c->ph.n, c->ncube - 1);
     if (RK == 3) {
-      CK(launch_norms(c->ph, c->partials, nb, c->er, c->stream));
+      if (c->batched)
+        CK(launch_norms_batch(c->ph.n, c->cases, c->case_blk_flux, c->ncase, c->partials, c->er,
+                              c->stream));
+      else
+        CK(launch_norms(c->ph, c->partials, nb, c->er, c->stream));
       ++c->launches;
     }
     return case_interface(c);
@@ -306,10 +340,19 @@ int case_stage(bcmg_case *c, int RK) {
   k.Rku1 = c->Rku1;
   k.Residual1 = c->Residual1;
   k.partials = c->partials;
-  CK(launch_rk(k, &nb, c->stream));
+  if (c->batched) {
+    k.blk_beg = c->rk_blk;
+    CK(launch_rk_table(k, c->nrk, c->stream));
+  } else {
+    CK(launch_rk(k, &nb, c->stream));
+  }
   ++c->launches;
   if (RK == 3) {
-    CK(launch_norms(c->ph, c->partials, nb, c->er, c->stream));
+    if (c->batched)
+      CK(launch_norms_batch(c->ph.n, c->cases, c->case_blk_rk, c->ncase, c->partials, c->er,
+                            c->stream));
+    else
+      CK(launch_norms(c->ph, c->partials, nb, c->er, c->stream));
     ++c->launches;
   }
   return case_interface(c);
@@ -320,7 +363,7 @@ int case_step(bcmg_case *c, int subiters) {
   for (int it = 0; it < subiters; ++it) {
     for (int RK = 1; RK <= 3; ++RK)
       if ((r = case_stage(c, RK))) return r;
-    k_emax<<<1, 32, 0, c->stream>>>(c->er, c->emax);
+    k_emax<<<c->ncase, 32, 0, c->stream>>>(c->er, c->emax);
     CK(cudaGetLastError());
     ++c->launches;
   }
@@ -354,7 +397,50 @@ void bcmg_internal_set_error(const char *msg) {
 const char *bcmg_last_error(void) { return g_has_err ? g_err.c_str() : nullptr; }
 const char *bcmg_version(void) { return "bcm_gb300 0.1 (sm_103a)"; }
 
-int bcmg_case_create(const bcmg_case_desc *d, bcmg_case **out) {
+}  // extern "C"
+
+namespace {
+
+// Per-case tables of a batch, formed by bcmg_batch_create.
+struct BatchInit {
+  std::vector<CaseConst> cases;
+  std::vector<int> case_cube0;  // [ncase+1]
+};
+
+CaseConst case_const(const bcmg_case_desc &d) {
+  CaseConst q{};
+  q.mu_L = d.mu_L;
+  q.rho0 = d.rho0;
+  q.U0 = d.U0;
+  q.Uin = d.Uin;
+  q.P0 = d.P0;
+  q.dT = d.deltaT;
+  q.dTau = d.deltaTau;
+  q.e = d.e;
+  q.mpi_ncube = d.mpi_ncube;
+  q.ef = (float)d.e;
+  q.rho0f = (float)d.rho0;
+  q.P0f = (float)d.P0;
+  q.RT0f = (float)(d.P0 / d.rho0);
+  q.T0f = (float)(d.P0 / d.rho0 / BCMG_R);
+  q.mu_Lf = (float)d.mu_L;
+  q.i2dtf = (float)(1.0 / (2.0 * d.deltaT));
+  q.dTf = (float)d.deltaT;
+  q.dTauf = (float)d.deltaTau;
+  return q;
+}
+
+int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out);
+
+}  // namespace
+
+extern "C" int bcmg_case_create(const bcmg_case_desc *d, bcmg_case **out) {
+  return create_common(d, nullptr, out);
+}
+
+namespace {
+
+int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out) {
   clear_err();
   if (!d || !out) {
     set_err("null argument");
@@ -398,6 +484,12 @@ int bcmg_case_create(const bcmg_case_desc *d, bcmg_case **out) {
   c->e = d->e;
   c->precision = d->precision;
   c->ncell = (size_t)d->ncube * c->S * c->S * c->S;
+  if (bi) {
+    c->batched = true;
+    c->ncase = (int)bi->cases.size();
+    c->hcases = bi->cases;
+    c->case_cube0 = bi->case_cube0;
+  }
   std::vector<int> off;
   std::vector<FaceTask> tasks;
   std::string err;
@@ -437,7 +529,8 @@ int bcmg_case_create(const bcmg_case_desc *d, bcmg_case **out) {
             ck(dalloc(&c->tasks, tasks.size()), "alloc") &&
             ck(dalloc(&c->bc_cubes, bcc.size()), "alloc") &&
             ck(dalloc(&c->bc_masks, bcm.size()), "alloc") &&
-            ck(dalloc(&c->er, 8), "alloc") && ck(dalloc(&c->emax, 6), "alloc");
+            ck(dalloc(&c->er, 8 * (size_t)c->ncase), "alloc") &&
+            ck(dalloc(&c->emax, 6 * (size_t)c->ncase), "alloc");
   if (!ok) return fail(BCMG_ERR_CUDA);
   if (d->precision == BCMG_PRECISION_SPLIT &&
       !(ck(dalloc(&c->M, nd), "alloc") &&
@@ -459,6 +552,46 @@ int bcmg_case_create(const bcmg_case_desc *d, bcmg_case **out) {
   c->nparts = rk_partial_blocks(probe);
   if (d->precision == BCMG_PRECISION_SPLIT)
     c->nparts = std::max(c->nparts, flux_split_blocks(d->n, d->ncube - 1));
+  if (c->batched) {
+    // Stage-update blocks of about equal size that never straddle two cases
+    // (per-case norms), the flux kernel's per-case block ranges (one block
+    // per tile, cubes in order), and the cube -> case map.
+    const long long n3 = (long long)d->n * d->n * d->n;
+    const long long total = (long long)(d->ncube - 1) * n3;
+    long long nbt = std::min<long long>(std::max<long long>((total + 1023) / 1024, 1), 152 * 16);
+    const long long chunk = (total + nbt - 1) / nbt;
+    const int tiles = flux_split_blocks(d->n, 1);
+    std::vector<long long> blk;
+    std::vector<int> cbr(c->ncase + 1), cbf(c->ncase + 1), cube_case(d->ncube, 0);
+    for (int q = 0; q < c->ncase; ++q) {
+      cbr[q] = (int)blk.size();
+      cbf[q] = (c->case_cube0[q] - 1) * tiles;
+      const long long b0 = (c->case_cube0[q] - 1) * n3, b1 = (c->case_cube0[q + 1] - 1) * n3;
+      for (long long x = b0; x < b1; x += chunk) blk.push_back(x);
+      for (int g = c->case_cube0[q]; g < c->case_cube0[q + 1]; ++g) cube_case[g] = q;
+    }
+    cbr[c->ncase] = (int)blk.size();
+    cbf[c->ncase] = (d->ncube - 1) * tiles;
+    blk.push_back(total);
+    c->nrk = (int)blk.size() - 1;
+    if (d->precision == BCMG_PRECISION_FP64) c->nparts = std::max(c->nparts, c->nrk);
+    ok = ck(dalloc(&c->cases, (size_t)c->ncase), "alloc") &&
+         ck(dalloc(&c->cube_case, (size_t)d->ncube), "alloc") &&
+         ck(dalloc(&c->rk_blk, blk.size()), "alloc") &&
+         ck(dalloc(&c->case_blk_rk, cbr.size()), "alloc") &&
+         ck(dalloc(&c->case_blk_flux, cbf.size()), "alloc") &&
+         ck(cudaMemcpy(c->cases, c->hcases.data(), sizeof(CaseConst) * c->ncase,
+                       cudaMemcpyHostToDevice), "copy") &&
+         ck(cudaMemcpy(c->cube_case, cube_case.data(), sizeof(int) * cube_case.size(),
+                       cudaMemcpyHostToDevice), "copy") &&
+         ck(cudaMemcpy(c->rk_blk, blk.data(), sizeof(long long) * blk.size(),
+                       cudaMemcpyHostToDevice), "copy") &&
+         ck(cudaMemcpy(c->case_blk_rk, cbr.data(), sizeof(int) * cbr.size(),
+                       cudaMemcpyHostToDevice), "copy") &&
+         ck(cudaMemcpy(c->case_blk_flux, cbf.data(), sizeof(int) * cbf.size(),
+                       cudaMemcpyHostToDevice), "copy");
+    if (!ok) return fail(BCMG_ERR_CUDA);
+  }
   if (!ck(dalloc(&c->partials, (size_t)c->nparts * 7), "alloc")) return fail(BCMG_ERR_CUDA);
   cudaStream_t s = c->stream;
   ok = ck(cudaMemsetAsync(c->U1_, 0, nd * 8, s), "memset") &&
@@ -468,8 +601,8 @@ int bcmg_case_create(const bcmg_case_desc *d, bcmg_case **out) {
        ck(cudaMemsetAsync(c->U1p2, 0, nd * 8, s), "memset") &&
        ck(cudaMemsetAsync(c->Rku1, 0, nd * 8, s), "memset") &&
        ck(cudaMemsetAsync(c->Residual1, 0, nd * 8, s), "memset") &&
-       ck(cudaMemsetAsync(c->er, 0, 8 * 8, s), "memset") &&
-       ck(cudaMemsetAsync(c->emax, 0, 6 * 8, s), "memset") &&
+       ck(cudaMemsetAsync(c->er, 0, 8 * 8 * (size_t)c->ncase, s), "memset") &&
+       ck(cudaMemsetAsync(c->emax, 0, 6 * 8 * (size_t)c->ncase, s), "memset") &&
        ck(cudaMemcpyAsync(c->FWS, d->FWS, c->ncell * sizeof(int), cudaMemcpyHostToDevice, s),
           "copy") &&
        ck(cudaMemcpyAsync(c->cube_size, d->cube_size, sizeof(double) * d->ncube,
@@ -513,6 +646,10 @@ int bcmg_case_create(const bcmg_case_desc *d, bcmg_case **out) {
   *out = c;
   return BCMG_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 void bcmg_case_destroy(bcmg_case *c) {
   if (!c) return;
@@ -573,7 +710,9 @@ int bcmg_case_advance(bcmg_case *c, int steps, int subiters, int use_graph, doub
                       double *emax) {
   clear_err();
   if (!c || steps < 0 || subiters < 1) { set_err("bad arguments"); return BCMG_ERR_ARG; }
-  if (emax) CK(cudaMemcpyAsync(c->emax, emax, 6 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (emax)
+    CK(cudaMemcpyAsync(c->emax, emax, 6 * sizeof(double) * c->ncase, cudaMemcpyHostToDevice,
+                       c->stream));
   c->launches = 0;
   c->ev_used = 0;
   if (use_graph && !c->profile) {
@@ -611,8 +750,12 @@ int bcmg_case_advance(bcmg_case *c, int steps, int subiters, int use_graph, doub
       if (r) return r;
     }
   }
-  if (er) CK(cudaMemcpyAsync(er, c->er, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-  if (emax) CK(cudaMemcpyAsync(emax, c->emax, 6 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (er)
+    CK(cudaMemcpyAsync(er, c->er, 8 * sizeof(double) * c->ncase, cudaMemcpyDeviceToHost,
+                       c->stream));
+  if (emax)
+    CK(cudaMemcpyAsync(emax, c->emax, 6 * sizeof(double) * c->ncase, cudaMemcpyDeviceToHost,
+                       c->stream));
   CK(cudaStreamSynchronize(c->stream));
   if (c->profile) {
     for (size_t i = 0; i + 1 < c->ev_used; i += 2) {
@@ -691,6 +834,195 @@ int bcmg_case_profile(const bcmg_case *c, double *flux_ms_total, long long *flux
   if (flux_ms_total) *flux_ms_total = c->flux_ms;
   if (flux_launches) *flux_launches = c->flux_launches;
   return BCMG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batches: independent cases (same n and precision) laid end to end in one
+// flat cube list.  Case q's cube l (1-based) becomes cube case_cube0[q]+l-1;
+// its adjacency, boundary lists and IBM tables are renumbered the same way,
+// so every table-driven kernel (interface, boundaries, ghost cells) runs over
+// all cases at once and no task crosses from one case into another.  The
+// constants each case takes from its own prm.h / time steps go to a device
+// table indexed through a cube -> case map.
+// ---------------------------------------------------------------------------
+int bcmg_batch_create(int ncase, const bcmg_case_desc *descs, bcmg_case **out) {
+  clear_err();
+  if (!out || !descs || ncase < 1) {
+    set_err("null argument or ncase < 1");
+    return BCMG_ERR_ARG;
+  }
+  *out = nullptr;
+  const int n = descs[0].n, prec = descs[0].precision;
+  const int S = n + 4;
+  const size_t S3 = (size_t)S * S * S;
+  long long total = 1;
+  for (int q = 0; q < ncase; ++q) {
+    const bcmg_case_desc &d = descs[q];
+    char msg[160];
+    if (d.n != n || d.precision != prec) {
+      std::snprintf(msg, sizeof msg, "case %d: every case of a batch needs the same n and precision", q);
+      set_err(msg);
+      return BCMG_ERR_ARG;
+    }
+    if (d.ncube < 2 || !d.cube_size || !d.csl || !d.adj_number || !d.FWS) {
+      std::snprintf(msg, sizeof msg, "case %d: ncube < 2 or missing geometry arrays", q);
+      set_err(msg);
+      return BCMG_ERR_ARG;
+    }
+    if (!(d.deltaT > 0) || !(d.deltaTau > 0) || d.mpi_ncube < 1 || !(d.rho0 > 0)) {
+      std::snprintf(msg, sizeof msg, "case %d: deltaT, deltaTau, rho0 must be positive and mpi_ncube >= 1", q);
+      set_err(msg);
+      return BCMG_ERR_ARG;
+    }
+    total += d.ncube - 1;
+  }
+  if (total > (1LL << 30)) {
+    set_err("batch too large");
+    return BCMG_ERR_ARG;
+  }
+  const int ncube = (int)total;
+  std::vector<double> cube_size(ncube, 0.0);
+  std::vector<int> csl(ncube, 0), adj((size_t)ncube * 35, 0);
+  std::vector<int> fws;
+  try {
+    fws.assign((size_t)ncube * S3, 1);
+  } catch (const std::bad_alloc &) {
+    set_err("host memory for the batch's flag array");
+    return BCMG_ERR_ARG;
+  }
+  std::vector<int> bc[6];
+  std::vector<double> w(1, 0.0);
+  std::vector<int> gc(1, 0), ip(1, 0);
+  BatchInit bi;
+  bi.case_cube0.push_back(1);
+  double mu_any = 0.0;
+  for (int q = 0; q < ncase; ++q) {
+    const bcmg_case_desc &d = descs[q];
+    const int g0 = bi.case_cube0.back();
+    const int shift = g0 - 1;
+    char msg[200];
+    auto bad = [&](const char *what) {
+      std::snprintf(msg, sizeof msg, "case %d: %s", q, what);
+      set_err(msg);
+      return BCMG_ERR_ARG;
+    };
+    for (int l = 1; l < d.ncube; ++l) {
+      if (!(d.cube_size[l] > 0)) return bad("cube_size must be positive for cubes 1..ncube-1");
+      cube_size[shift + l] = d.cube_size[l];
+      csl[shift + l] = d.csl[l];
+      for (int t = 0; t < 35; ++t) {
+        const int v = d.adj_number[(size_t)l * 35 + t];
+        if (v < 0 || v >= d.ncube) return bad("adj_number out of range");
+        adj[(size_t)(shift + l) * 35 + t] = v > 0 ? v + shift : 0;
+      }
+    }
+    std::copy(d.FWS + S3, d.FWS + (size_t)d.ncube * S3, fws.begin() + (size_t)g0 * S3);
+    const int *lists[6] = {d.xl, d.xu, d.yl, d.yu, d.zl, d.zu};
+    const int counts[6] = {d.nxl, d.nxu, d.nyl, d.nyu, d.nzl, d.nzu};
+    for (int k = 0; k < 6; ++k) {
+      if (counts[k] < 0 || (counts[k] > 0 && !lists[k])) return bad("boundary list missing");
+      for (int m = 0; m < counts[k]; ++m) {
+        const int v = lists[k][m];
+        if (v < 1 || v >= d.ncube) return bad("boundary list entry out of range");
+        bc[k].push_back(v + shift);
+      }
+    }
+    // IBM entries: this case's minus list, then its plus list (main.cpp
+    // applies minus before plus); cube numbers renumbered.
+    for (int side = 0; side < 2; ++side) {
+      const int cnt = side == 0 ? d.nminus : d.nplus;
+      const double *W = side == 0 ? d.w_minus : d.w_plus;
+      const int *G = side == 0 ? d.gc_minus : d.gc_plus;
+      const int *I = side == 0 ? d.ip_minus : d.ip_plus;
+      if (cnt <= 0) continue;
+      if (!W || !G || !I) return bad("IBM table pointer missing");
+      for (int e = 0; e < cnt; ++e) {
+        for (int m = 0; m < 8; ++m) w.push_back(W[8 * (size_t)e + 1 + m]);
+        for (int m = 0; m < 4; ++m) {
+          int gv = G[4 * (size_t)e + 1 + m], iv = I[4 * (size_t)e + 1 + m];
+          if (m == 0) {
+            if (gv < 1 || gv >= d.ncube || iv < 1 || iv >= d.ncube)
+              return bad("IBM cube number out of range");
+            gv += shift;
+            iv += shift;
+          }
+          gc.push_back(gv);
+          ip.push_back(iv);
+        }
+      }
+    }
+    bi.cases.push_back(case_const(d));
+    bi.case_cube0.push_back(g0 + d.ncube - 1);
+    if (mu_any == 0.0 && d.mu_L != 0.0) mu_any = d.mu_L;
+  }
+  bcmg_case_desc m = descs[0];
+  m.ncube = ncube;
+  m.mu_L = mu_any;  // viscous kernels when any case is viscous
+  m.cube_size = cube_size.data();
+  m.csl = csl.data();
+  m.adj_number = adj.data();
+  m.FWS = fws.data();
+  m.nxl = (int)bc[0].size(); m.nxu = (int)bc[1].size(); m.nyl = (int)bc[2].size();
+  m.nyu = (int)bc[3].size(); m.nzl = (int)bc[4].size(); m.nzu = (int)bc[5].size();
+  m.xl = bc[0].data(); m.xu = bc[1].data(); m.yl = bc[2].data();
+  m.yu = bc[3].data(); m.zl = bc[4].data(); m.zu = bc[5].data();
+  m.nminus = (int)((gc.size() - 1) / 4);
+  m.w_minus = w.data();
+  m.gc_minus = gc.data();
+  m.ip_minus = ip.data();
+  m.nplus = 0;
+  m.w_plus = nullptr;
+  m.gc_plus = m.ip_plus = nullptr;
+  return create_common(&m, &bi, out);
+}
+
+int bcmg_case_ncase(const bcmg_case *c) { return c ? c->ncase : 0; }
+
+int bcmg_case_case_cubes(const bcmg_case *c, int q, int *cube0, int *ncube) {
+  clear_err();
+  if (!c || q < 0 || q >= c->ncase) { set_err("bad context or case"); return BCMG_ERR_ARG; }
+  const int a = c->batched ? c->case_cube0[q] : 1;
+  const int b = c->batched ? c->case_cube0[q + 1] : c->ncube;
+  if (cube0) *cube0 = a;
+  if (ncube) *ncube = b - a + 1;  // the case's own cube slots incl. its unused slot 0
+  return BCMG_OK;
+}
+
+// Copies between one case's own arrays [ncube_q][S][S][S][5] (slot 0
+// skipped) and its cubes in the flat list.
+static int case_copy(bcmg_case *c, int q, double *const host[3], bool to_device) {
+  int g0 = 0, nq = 0;
+  int r = bcmg_case_case_cubes(c, q, &g0, &nq);
+  if (r) return r;
+  const size_t cube_d = (size_t)c->S * c->S * c->S * 5;
+  const size_t bytes = (size_t)(nq - 1) * cube_d * sizeof(double);
+  double *dev[3] = {c->U1_, c->U1, c->U1q};
+  for (int a = 0; a < 3; ++a) {
+    if (!host[a]) continue;
+    if (to_device)
+      CK(cudaMemcpyAsync(dev[a] + (size_t)g0 * cube_d, host[a] + cube_d, bytes,
+                         cudaMemcpyHostToDevice, c->stream));
+    else
+      CK(cudaMemcpyAsync(host[a] + cube_d, dev[a] + (size_t)g0 * cube_d, bytes,
+                         cudaMemcpyDeviceToHost, c->stream));
+  }
+  if (to_device && c->precision == BCMG_PRECISION_SPLIT && (host[1] || host[2]))
+    CK(launch_level_diff(c->U1, c->U1q, c->D2, c->ph.n, c->ncube, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return BCMG_OK;
+}
+
+int bcmg_case_set_case_state(bcmg_case *c, int q, const double *U1_, const double *U1,
+                             const double *U1q) {
+  clear_err();
+  double *h[3] = {const_cast<double *>(U1_), const_cast<double *>(U1), const_cast<double *>(U1q)};
+  return case_copy(c, q, h, true);
+}
+
+int bcmg_case_get_case_state(bcmg_case *c, int q, double *U1_, double *U1, double *U1q) {
+  clear_err();
+  double *h[3] = {U1_, U1, U1q};
+  return case_copy(c, q, h, false);
 }
 
 }  // extern "C"

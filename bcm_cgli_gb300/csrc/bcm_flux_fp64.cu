@@ -139,6 +139,12 @@ __global__ void __launch_bounds__(T *T *T, 1) k_flux_fp64(FluxArgs a) {
   const double *__restrict__ U = a.U1_;
   const int *__restrict__ F = a.FWS;
   const size_t cb = cell_index(S, cube, 0, 0, 0);
+  // Constants of the cube's case (kernel arguments for a single case).
+  double e = a.e, dT = a.dT, dTau = a.dTau, mu_L = a.ph.mu_L, rho0 = a.ph.rho0, P0 = a.ph.P0;
+  if (a.bt.cube_case) {
+    const CaseConst *q = a.bt.cases + __ldg(a.bt.cube_case + cube);
+    e = q->e; dT = q->dT; dTau = q->dTau; mu_L = q->mu_L; rho0 = q->rho0; P0 = q->P0;
+  }
 
   // Phase 1: primitives over the tile plus a one-cell halo (edges included).
   for (int p = tid; p < SM::nPrim; p += NT) {
@@ -195,9 +201,9 @@ __global__ void __launch_bounds__(T *T *T, 1) k_flux_fp64(FluxArgs a) {
         const int dst = w == 0 ? dst0 : dst1;
         double ML[5], MR[5], Fx[5], dP;
         recon<double>(ord, ld, ML, MR);
-        if (ax == 0) face_flux<0, double>(ML, MR, a.e, Fx, dP);
-        else if (ax == 1) face_flux<1, double>(ML, MR, a.e, Fx, dP);
-        else face_flux<2, double>(ML, MR, a.e, Fx, dP);
+        if (ax == 0) face_flux<0, double>(ML, MR, e, Fx, dP);
+        else if (ax == 1) face_flux<1, double>(ML, MR, e, Fx, dP);
+        else face_flux<2, double>(ML, MR, e, Fx, dP);
         if (dst & 1) {
 #pragma unroll
           for (int v = 0; v < 5; ++v) Fb[5 * slotB + v] = Fx[v];
@@ -229,8 +235,7 @@ __global__ void __launch_bounds__(T *T *T, 1) k_flux_fp64(FluxArgs a) {
   const Prim &c = P(0, 0, 0);
   double vF[5] = {0, 0, 0, 0, 0};
   if (VISCOUS) {
-    const double T0 = a.ph.P0 / a.ph.rho0 / BCMG_R;
-    const double mu_L = a.ph.mu_L;
+    const double T0 = P0 / rho0 / BCMG_R;
     const double Tc = Tcs[tid];
     double Lb[4], Lf[4], Mb[4], Mf[4], Nb[4], Nf[4];
     visc_face<0, false>(mu_L, T0, Tc, c, P(-1, 0, 0), inv, P(0, 1, 0), P(-1, 1, 0), P(0, -1, 0),
@@ -257,7 +262,6 @@ __global__ void __launch_bounds__(T *T *T, 1) k_flux_fp64(FluxArgs a) {
   const double *uu = a.U1 + 5 * go;
   const double *uq = a.U1q + 5 * go;
   const int IF = __ldg(F + go);
-  const double dT = a.dT, dTau = a.dTau;
   double Rk[5];
 #pragma unroll
   for (int v = 0; v < 5; ++v) {
@@ -276,7 +280,7 @@ __global__ void __launch_bounds__(T *T *T, 1) k_flux_fp64(FluxArgs a) {
     const double Tt = Pc / rho;
     const double H = 0.5 * VV + C / (BCMG_K - 1);
     const double qv = VV / C;
-    const double beta = qv > a.e ? qv : a.e;
+    const double beta = qv > e ? qv : e;
     const double temp = K * Tt * (2 * dT + 3 * dTau) * (2 * dT + 3 * beta * dTau);
     const double temp2 = (BCMG_K - 1) * (beta - 1) * dT * dT;
     const double temp3 = H - H * K - VV + K * (Tt + VV);

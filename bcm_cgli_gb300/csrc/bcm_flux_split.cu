@@ -28,9 +28,15 @@ namespace bcmg {
 // FP64 -> FP32 deltas of the state, all cells of all cubes (ghosts included).
 // ---------------------------------------------------------------------------
 __global__ void k_mirror(const double *__restrict__ U, float *__restrict__ M, size_t ncell_from,
-                         size_t ncell_to, double rho0, double E0) {
+                         size_t ncell_to, double rho0_, double E0_, Batch bt, size_t cube_cells) {
   for (size_t c = ncell_from + blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < ncell_to;
        c += (size_t)gridDim.x * blockDim.x) {
+    double rho0 = rho0_, E0 = E0_;
+    if (bt.cube_case) {  // the reference state of the cell's case
+      const CaseConst *cq = bt.cases + __ldg(bt.cube_case + c / cube_cells);
+      rho0 = cq->rho0;
+      E0 = cq->P0 / (BCMG_K - 1);
+    }
     const double *q = U + 5 * c;
     float *m = M + 5 * c;
     m[0] = (float)(q[0] - rho0);
@@ -42,14 +48,14 @@ __global__ void k_mirror(const double *__restrict__ U, float *__restrict__ M, si
 }
 
 cudaError_t launch_mirror(const double *U, float *M, int n, int ncube, double rho0, double P0,
-                          cudaStream_t s) {
+                          const Batch &bt, cudaStream_t s) {
   const size_t S = n + 4;
   const size_t from = S * S * S, to = (size_t)ncube * S * S * S;  // skip cube slot 0
   if (to <= from) return cudaSuccess;
   const size_t cnt = to - from;
   int blocks = (int)((cnt + 255) / 256);
   if (blocks > 152 * 16) blocks = 152 * 16;
-  k_mirror<<<blocks, 256, 0, s>>>(U, M, from, to, rho0, P0 / (BCMG_K - 1));
+  k_mirror<<<blocks, 256, 0, s>>>(U, M, from, to, rho0, P0 / (BCMG_K - 1), bt, S * S * S);
   return cudaGetLastError();
 }
 
@@ -265,8 +271,14 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
   const float *__restrict__ M = a.M;
   const int *__restrict__ F = a.FWS;
   const size_t cb = cell_index(S, cube, 0, 0, 0);
-  const float rho0 = a.rho0f, P0 = a.P0f;
-  const float RT0 = a.RT0f;  // R * T0
+  // Constants of the cube's case (kernel arguments for a single case).
+  float rho0 = a.rho0f, P0 = a.P0f, RT0 = a.RT0f /* R * T0 */, ef = a.ef, T0c = a.T0f,
+        mu_Lc = a.mu_Lf, i2dtc = a.i2dtf, dTc = a.dTf, dTauc = a.dTauf;
+  if (a.bt.cube_case) {
+    const CaseConst *cq = a.bt.cases + __ldg(a.bt.cube_case + cube);
+    rho0 = cq->rho0f; P0 = cq->P0f; RT0 = cq->RT0f; ef = cq->ef; T0c = cq->T0f;
+    mu_Lc = cq->mu_Lf; i2dtc = cq->i2dtf; dTc = cq->dTf; dTauc = cq->dTauf;
+  }
   const float iR = 1.0f / 287.0f;
 
   // Phase 0: stage the stencil box (tile +- 3 cells, clipped to the padded
@@ -353,9 +365,9 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
         const int dst = w == 0 ? dst0 : dst1;
         float ML[5], MR[5], Fx[5], dP;
         recon<float>(ord, ld, ML, MR);
-        if (ax == 0) face_flux_delta<0>(ML, MR, a.ef, rho0, P0, Fx, dP);
-        else if (ax == 1) face_flux_delta<1>(ML, MR, a.ef, rho0, P0, Fx, dP);
-        else face_flux_delta<2>(ML, MR, a.ef, rho0, P0, Fx, dP);
+        if (ax == 0) face_flux_delta<0>(ML, MR, ef, rho0, P0, Fx, dP);
+        else if (ax == 1) face_flux_delta<1>(ML, MR, ef, rho0, P0, Fx, dP);
+        else face_flux_delta<2>(ML, MR, ef, rho0, P0, Fx, dP);
         if (dst & 1) {
 #pragma unroll
           for (int v = 0; v < 5; ++v) Fb[5 * slotB + v] = Fx[v];
@@ -396,8 +408,8 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
   const PrimF &c = P(0, 0, 0);
   float vF[5] = {0, 0, 0, 0, 0};
   if (VISCOUS) {
-    const float T0 = a.T0f;
-    const float mu_L = a.mu_Lf;
+    const float T0 = T0c;
+    const float mu_L = mu_Lc;
     float Lb[4], Lf[4], Mb[4], Mf[4], Nb[4], Nf[4];
     visc_face_f<0, false>(mu_L, T0, c, P(-1, 0, 0), inv, P(0, 1, 0), P(-1, 1, 0), P(0, -1, 0),
                           P(-1, -1, 0), P(0, 0, 1), P(-1, 0, 1), P(0, 0, -1), P(-1, 0, -1), Lb);
@@ -422,7 +434,7 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
   const double *uu = a.U1 + 5 * go;
   const float *d2p = a.D2 + 5 * go;
   const int IF = FL(mi, mj, mk);
-  const float i2dt = a.i2dtf;
+  const float i2dt = i2dtc;
   float Rk[5];
   double xq[5];
 #pragma unroll
@@ -435,7 +447,7 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
   }
   if (IF == kFluid) {
     const float K = 1.4f, Km1 = 0.4f;
-    const float dT = a.dTf, dTau = a.dTauf;
+    const float dT = dTc, dTau = dTauc;
     const float *qm = BX(mi, mj, mk);
     const float rho = rho0 + qm[0];
     const float Uc = c.U, Vc = c.V, Wc = c.W;
@@ -445,7 +457,7 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
     const float C = K * Tt;
     const float H = 0.5f * VV + C / Km1;
     const float qv = VV / C;
-    const float beta = qv > a.ef ? qv : a.ef;
+    const float beta = qv > ef ? qv : ef;
     const float itemp = 1.0f / (K * Tt * (2 * dT + 3 * dTau) * (2 * dT + 3 * beta * dTau));
     const float temp2 = Km1 * (beta - 1) * dT * dT;
     const float temp3 = 0.5f * Km1 * VV;  // == H - H*K - VV + K*(T+VV) since C = K*T

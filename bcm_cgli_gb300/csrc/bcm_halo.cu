@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(kHaloThreads) k_bc(BcArgs a) {
         double U0 = q[1] / rho, V0 = q[2] / rho, W0 = q[3] / rho;
         double VV = U0 * U0 + V0 * V0 + W0 * W0;
         double P = (q[4] - 0.5 * rho * VV) * (BCMG_K - 1);
-        double Uu = a.Uin, Vv = 0., Ww = 0;
+        double Uu = a.bt.cube_case ? a.bt.cases[a.bt.cube_case[c]].Uin : a.Uin, Vv = 0., Ww = 0;
         VV = Uu * Uu + Vv * Vv + Ww * Ww;
         double o[5] = {rho, rho * Uu, rho * Vv, rho * Ww, P / (BCMG_K - 1) + 0.5 * rho * VV};
         double *d1 = Q(1, j, k), *d0 = Q(0, j, k);
@@ -265,7 +265,12 @@ __global__ void k_ghost(GhostArgs a, int count) {
   const int S = a.n + 4;
   const int b = (e - 1) * 4;
   const int c = a.IPsur[b + 1], i = a.IPsur[b + 2], j = a.IPsur[b + 3], k = a.IPsur[b + 4];
-  const double rho0 = a.rho0, P0 = a.P0;
+  double rho0 = a.rho0, P0 = a.P0;
+  if (a.bt.cube_case) {  // the case of the stencil's cube
+    const CaseConst &cq = a.bt.cases[a.bt.cube_case[c]];
+    rho0 = cq.rho0;
+    P0 = cq.P0;
+  }
   double rh[8], Uu[8], Vv[8], Ww[8], Pp[8];
 #pragma unroll
   for (int m = 0; m < 8; ++m) {

@@ -11,6 +11,23 @@ extern "C" void bcmg_internal_set_error(const char *msg);
 
 namespace bcmg {
 
+// Constants of one case in a batch: several independent cases laid end to
+// end in one flat cube list (same n), each with the values the reference
+// takes from its own prm.h / Resolution.h and its own time steps.  FP32
+// copies for the split path are formed once on the host.
+struct CaseConst {
+  double mu_L, rho0, U0, Uin, P0;
+  double dT, dTau, e;
+  int mpi_ncube;
+  float ef, rho0f, P0f, RT0f, T0f, mu_Lf, i2dtf, dTf, dTauf;
+};
+// Cube -> case map of a batch.  cube_case == nullptr: a single case whose
+// constants are the scalar fields of the argument block.
+struct Batch {
+  const int *cube_case = nullptr;    // [ncube] case of each cube (slot 0 unused)
+  const CaseConst *cases = nullptr;  // [ncase]
+};
+
 struct FluxArgs {
   Phys ph;
   int cube0;  // first cube of this launch (cubes are 1-based)
@@ -19,6 +36,7 @@ struct FluxArgs {
   const double *cube_size;
   const double *U1_, *U1, *U1q;
   double *Rku1, *Residual1;
+  Batch bt;
 };
 
 // FP64 residual + increment (bit-exact with the reference).
@@ -45,11 +63,12 @@ struct FluxSplitArgs {
   int RK;              // stage 1..3: the kernel applies the stage update
   double *partials;    // [blocks][7] norm/force partial sums (stage 3)
   double *Residual1;
+  Batch bt;
 };
 // Blocks of one split flux launch over ncubes cubes (one per tile).
 int flux_split_blocks(int n, int ncubes);
 cudaError_t launch_mirror(const double *U, float *M, int n, int ncube, double rho0, double P0,
-                          cudaStream_t s);
+                          const Batch &bt, cudaStream_t s);
 cudaError_t launch_flux_split(const FluxSplitArgs &a, int ncubes, cudaStream_t s);
 cudaError_t launch_level_diff(const double *U1, const double *U1q, float *D2, int n, int ncube,
                               cudaStream_t s);
@@ -62,6 +81,10 @@ struct RkArgs {
   double *U1_, *U1p1, *U1p2;
   const double *Rku1, *Residual1;
   double *partials;  // [nblocks][7] norm/force partial sums (RK == 3)
+  // Batches: block b sums interior cells [blk_beg[b], blk_beg[b+1]) of the
+  // flat numbering (c-1)*n^3 + r, so no block straddles two cases.  nullptr:
+  // equal chunks over all cubes.
+  const long long *blk_beg = nullptr;
 };
 
 // Stage combination (BCM_Flux...cpp:2417-2599) and, at RK 3, the per-block
@@ -74,6 +97,12 @@ cudaError_t launch_rk_chunked(const RkArgs &a, long long chunk, int nblocks, cud
 // Deterministic final reduction of partials -> er[1..7] (device, 8 doubles).
 cudaError_t launch_norms(const Phys &ph, const double *partials, int nblocks, double *er,
                          cudaStream_t s);
+// Batches: case q reduces partial blocks [case_blk[q], case_blk[q+1]) into
+// er[8q .. 8q+7] with its own normalisers.
+cudaError_t launch_norms_batch(int n, const CaseConst *cases, const int *case_blk, int ncase,
+                               const double *partials, double *er, cudaStream_t s);
+// Batch form of launch_rk over an explicit block table (nblocks blocks).
+cudaError_t launch_rk_table(const RkArgs &a, int nblocks, cudaStream_t s);
 
 // Interface: face-copy tasks (destination cube, source cube, axis, side) built
 // on the host, then the ordered three-phase edge fill of every cube.
@@ -103,6 +132,7 @@ struct BcArgs {
   const int *masks;
   int axes;
   double *U1_;
+  Batch bt;  // batches: Uin of the cube's case
 };
 cudaError_t launch_bc(const BcArgs &a, int ncubes, cudaStream_t s);
 
@@ -115,6 +145,7 @@ struct GhostArgs {
   const int *GCindex;      // 1-based packed [4*nbc+1]
   const int *IPsur;        // 1-based packed [4*nbc+1]
   double *U1_;
+  Batch bt;  // batches: rho0, P0 of the ghost cell's case
 };
 cudaError_t launch_ghost(const GhostArgs &a, int count, cudaStream_t s);
 

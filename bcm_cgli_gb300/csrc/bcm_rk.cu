@@ -18,8 +18,12 @@ constexpr int kRkThreads = 256;
 
 __global__ void __launch_bounds__(kRkThreads) k_rk(RkArgs a, long long total, long long chunk) {
   const int n = a.ph.n, S = n + 4;
-  const long long beg = (long long)blockIdx.x * chunk;
-  const long long end = min(total, beg + chunk);
+  long long beg = (long long)blockIdx.x * chunk;
+  long long end = min(total, beg + chunk);
+  if (a.blk_beg) {  // batches: the block's range lies inside one case
+    beg = a.blk_beg[blockIdx.x];
+    end = a.blk_beg[blockIdx.x + 1];
+  }
   double s[7] = {0, 0, 0, 0, 0, 0, 0};
   for (long long t = beg + threadIdx.x; t < end; t += kRkThreads) {
     const int c = 1 + (int)(t / ((long long)n * n * n));
@@ -95,26 +99,47 @@ __global__ void __launch_bounds__(kRkThreads) k_rk(RkArgs a, long long total, lo
   }
 }
 
-__global__ void k_norms(Phys ph, const double *partials, int nblocks, double *er) {
-  // One warp per quantity: lane l sums blocks l, l+32, ... in order, then a
-  // fixed shuffle tree; the result does not depend on timing.
-  __shared__ double tot[7];
+// Sum of partial blocks [b0, b1) per quantity into tot[0..6] (block of 7
+// warps).  One warp per quantity: lane l sums blocks b0+l, b0+l+32, ... in
+// order, then a fixed shuffle tree; the result does not depend on timing.
+__device__ void sum_partials(const double *partials, int b0, int b1, double *tot) {
   const int m = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (m < 7) {
     double v = 0;
-    for (int b = lane; b < nblocks; b += 32) v += partials[(size_t)b * 7 + m];
+    for (int b = b0 + lane; b < b1; b += 32) v += partials[(size_t)b * 7 + m];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
     if (lane == 0) tot[m] = v;
   }
   __syncthreads();
+}
+
+// er[1..5] = L2 change norms / (MPI_Ncube n^3), er[6], er[7] = force sums /
+// (0.5 rho0 U0^2 2.602) (BCM_Flux...cpp:2628-2650).
+__device__ void write_norms(int n, int mpi_ncube, double rho0, double U0, const double *tot,
+                            double *er) {
+  double DN = 1. / (mpi_ncube * n * n * n);
+  er[0] = 0;
+  for (int m = 0; m < 5; ++m) er[1 + m] = sqrt(tot[m]) * DN;
+  er[6] = tot[5] / (0.5 * rho0 * U0 * U0 * 2.602);
+  er[7] = tot[6] / (0.5 * rho0 * U0 * U0 * 2.602);
+}
+
+__global__ void k_norms(Phys ph, const double *partials, int nblocks, double *er) {
+  __shared__ double tot[7];
+  sum_partials(partials, 0, nblocks, tot);
+  if (threadIdx.x == 0) write_norms(ph.n, ph.mpi_ncube, ph.rho0, ph.U0, tot, er);
+}
+
+// One CTA per case of a batch.
+__global__ void k_norms_batch(int n, const CaseConst *cases, const int *case_blk,
+                              const double *partials, double *er) {
+  __shared__ double tot[7];
+  const int q = blockIdx.x;
+  sum_partials(partials, case_blk[q], case_blk[q + 1], tot);
   if (threadIdx.x == 0) {
-    const int n = ph.n;
-    double DN = 1. / (ph.mpi_ncube * n * n * n);
-    er[0] = 0;
-    for (int m = 0; m < 5; ++m) er[1 + m] = sqrt(tot[m]) * DN;
-    er[6] = tot[5] / (0.5 * ph.rho0 * ph.U0 * ph.U0 * 2.602);
-    er[7] = tot[6] / (0.5 * ph.rho0 * ph.U0 * ph.U0 * 2.602);
+    const CaseConst &c = cases[q];
+    write_norms(n, c.mpi_ncube, c.rho0, c.U0, tot, er + 8 * (size_t)q);
   }
 }
 
@@ -147,6 +172,19 @@ cudaError_t launch_rk(const RkArgs &a, int *nblocks_out, cudaStream_t s) {
 cudaError_t launch_norms(const Phys &ph, const double *partials, int nblocks, double *er,
                          cudaStream_t s) {
   k_norms<<<1, 7 * 32, 0, s>>>(ph, partials, nblocks, er);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_norms_batch(int n, const CaseConst *cases, const int *case_blk, int ncase,
+                               const double *partials, double *er, cudaStream_t s) {
+  if (ncase <= 0) return cudaSuccess;
+  k_norms_batch<<<ncase, 7 * 32, 0, s>>>(n, cases, case_blk, partials, er);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rk_table(const RkArgs &a, int nblocks, cudaStream_t s) {
+  if (nblocks <= 0 || !a.blk_beg) return cudaErrorInvalidValue;
+  k_rk<<<nblocks, kRkThreads, 0, s>>>(a, 0, 0);
   return cudaGetLastError();
 }
 

@@ -206,6 +206,27 @@ int bcmg_case_time_flux(bcmg_case *c, int reps, double *ms);
 int bcmg_case_set_profiling(bcmg_case *c, int on);
 int bcmg_case_profile(const bcmg_case *c, double *flux_ms_total, long long *flux_launches);
 
+/* Batch of independent cases in one context.  No counterpart in the
+ * reference, which runs one case per process: here the cases (same n and
+ * precision; any cube counts, constants, time steps, boundaries and IBM
+ * tables) are laid end to end in one flat cube list, so each stage is the
+ * same launches as for one case, over all cubes of all cases.  Case q's
+ * cube l becomes cube cube0_q + l - 1 (bcmg_case_case_cubes); every other
+ * bcmg_case_* call works on the whole batch, and bcmg_case_advance's er and
+ * emax become [ncase][8] and [ncase][6] (per case, each with its own
+ * normalisers).  Each case's state evolves exactly as it would in a context
+ * of its own. */
+int bcmg_batch_create(int ncase, const bcmg_case_desc *descs, bcmg_case **out);
+int bcmg_case_ncase(const bcmg_case *c);
+/* First flat cube of case q and the case's own cube-slot count (ncube of
+ * its descriptor, unused slot 0 included). */
+int bcmg_case_case_cubes(const bcmg_case *c, int q, int *cube0, int *ncube);
+/* State of case q in its own layout [ncube_q][S][S][S][5] (slot 0 ignored);
+ * any pointer may be NULL. */
+int bcmg_case_set_case_state(bcmg_case *c, int q, const double *U1_, const double *U1,
+                             const double *U1q);
+int bcmg_case_get_case_state(bcmg_case *c, int q, double *U1_, double *U1, double *U1q);
+
 /* One FP64 RK stage that allocates nothing.  No counterpart in the
  * reference.  It serves callers that cannot let a library call cudaMalloc:
  * solvers that hand out every device buffer from their own pre-sized arena,

@@ -168,3 +168,27 @@ def test_reference_shim_compiles_against_main_h(tmp_path):
                         "-I", os.path.join(ROOT, "oracle", "mpi_stub"), str(src)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
+
+
+def test_batch_create_rejects_mismatched_cases_before_touching_the_gpu():
+    """bcmg_batch_create validates every case on the host first: different n,
+    out-of-range adjacency and boundary entries are refused with an error
+    naming the case, before any device work."""
+    import ctypes as C
+    from bcm_cgli_gb300 import _lib, api
+    a = cases.random_case(seed=1, n=4, periodic=True)
+    b = cases.random_case(seed=2, n=8, periodic=True)
+    keep = []
+    descs = (_lib.CaseDesc * 2)(api._case_desc(a, 0, keep), api._case_desc(b, 0, keep))
+    h = C.c_void_p()
+    L = _lib.lib()
+    assert L.bcmg_batch_create(2, descs, C.byref(h)) != 0
+    assert "case 1" in _lib.last_error() and "same n" in _lib.last_error()
+    c = cases.random_case(seed=3, n=4, periodic=False)
+    bad_adj = c.adj.copy()
+    bad_adj[1, 1, 2] = c.ncube + 5
+    c.adj = bad_adj
+    descs = (_lib.CaseDesc * 2)(api._case_desc(a, 0, keep), api._case_desc(c, 0, keep))
+    assert L.bcmg_batch_create(2, descs, C.byref(h)) != 0
+    assert "case 1" in _lib.last_error() and "adj_number" in _lib.last_error()
+    assert L.bcmg_batch_create(0, descs, C.byref(h)) != 0
