@@ -24,6 +24,8 @@ from ._lib import BcmgError, check, lib
 
 PRECISION_FP64 = 0
 PRECISION_SPLIT = 1
+METHOD_RK3 = 0  # the reference's preconditioned three-stage RK (bit-exact)
+METHOD_LUSGS = 1  # LU-SGS sub-iterations (no reference counterpart)
 
 
 def _dp(a):
@@ -240,6 +242,11 @@ class CaseContext:
         out = [np.empty(self.shape) for _ in range(4)]
         check(lib().bcmg_case_get_scratch(self.h, *(a.ctypes.data for a in out)))
         return out  # U1p1, U1p2, Rku1, Residual1
+
+    def set_method(self, method, cfl=0.0, omega=1.5):
+        """Sub-iteration method of advance(): METHOD_RK3 or METHOD_LUSGS
+        (pseudo-time CFL, 0 for none; relaxation omega in [1, 4])."""
+        check(lib().bcmg_case_set_method(self.h, int(method), float(cfl), float(omega)))
 
     def stage(self, RK):
         check(lib().bcmg_case_stage(self.h, int(RK)))

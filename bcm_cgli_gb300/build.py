@@ -30,6 +30,7 @@ UNITS = [
     ("bcm_halo.cu", ["--fmad=false"]),
     ("bcm_capi.cu", ["--fmad=false"]),
     ("bcm_noalloc.cu", ["--fmad=false"]),
+    ("bcm_lusgs.cu", ["--fmad=false"]),
     ("bcm_tables.cpp", []),
 ]
 

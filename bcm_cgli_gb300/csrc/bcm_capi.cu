@@ -179,6 +179,11 @@ struct bcmg_case {
   long long *rk_blk = nullptr;  // device [nrk+1]: FP64 stage-update blocks
   int nrk = 0;
   int *case_blk_rk = nullptr, *case_blk_flux = nullptr;  // device [ncase+1]
+  int *case_blk_cube = nullptr;                           // device [ncase+1]
+  // Sub-iteration method (bcmg_case_set_method): RK3 (the reference's) or
+  // LU-SGS with its pseudo-time CFL (0: none) and relaxation factor.
+  int method = BCMG_METHOD_RK3;
+  double lu_cfl = 0.0, lu_omega = 1.5;
   Batch bt() const {
     Batch b;
     if (batched) {
@@ -210,6 +215,7 @@ struct bcmg_case {
     dfree(FWS); dfree(cube_size); dfree(task_cube); dfree(tasks); dfree(bc_cubes);
     dfree(bc_masks); dfree(partials); dfree(er); dfree(emax);
     dfree(cases); dfree(cube_case); dfree(rk_blk); dfree(case_blk_rk); dfree(case_blk_flux);
+    dfree(case_blk_cube);
     ibm.release();
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
@@ -233,6 +239,11 @@ int case_flux(bcmg_case *c, int RK) {
   a.Rku1 = c->Rku1;
   a.Residual1 = c->Residual1;
   a.bt = c->bt();
+  a.raw = RK == 0;  // residual only (LU-SGS)
+  if (RK == 0 && c->precision == BCMG_PRECISION_SPLIT) {
+    set_err("LU-SGS residual mode is not available for the split-precision path");
+    return BCMG_ERR_ARG;
+  }
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (c->profile) {
     while (c->ev.size() < c->ev_used + 2) {
@@ -296,7 +307,9 @@ int case_interface(bcmg_case *c) {
   return BCMG_OK;
 }
 
-int case_stage(bcmg_case *c, int RK) {
+// Boundary conditions, IBM ghost cells and interface ahead of each update
+// (main.cpp:1161-1204).
+int case_prologue(bcmg_case *c) {
   int r;
   if (c->nbc > 0) {
     BcArgs b;
@@ -313,7 +326,43 @@ int case_stage(bcmg_case *c, int RK) {
   if ((r = ibm_run(c->ibm, c->ph.n, c->ph.rho0, c->ph.P0, c->U1_, c->stream, &c->launches,
                    c->bt())))
     return r;
-  if ((r = case_interface(c))) return r;
+  return case_interface(c);
+}
+
+// One LU-SGS sub-iteration: prologue, residual, sweeps with the update and
+// per-cube norm partials, norms, interface.
+int case_lusgs(bcmg_case *c) {
+  int r;
+  if ((r = case_prologue(c))) return r;
+  if ((r = case_flux(c, 0))) return r;
+  LusgsArgs l;
+  l.ph = c->ph;
+  l.dT = c->dT;
+  l.cfl = c->lu_cfl;
+  l.omega = c->lu_omega;
+  l.FWS = c->FWS;
+  l.cube_size = c->cube_size;
+  l.U1_ = c->U1_;
+  l.Rku1 = c->Rku1;
+  l.coefA = c->U1p1;
+  l.coefB = c->U1p2;
+  l.Residual1 = c->Residual1;
+  l.partials = c->partials;
+  l.bt = c->bt();
+  CK(launch_lusgs(l, c->ncube - 1, c->stream));
+  ++c->launches;
+  if (c->batched)
+    CK(launch_norms_batch(c->ph.n, c->cases, c->case_blk_cube, c->ncase, c->partials, c->er,
+                          c->stream));
+  else
+    CK(launch_norms(c->ph, c->partials, c->ncube - 1, c->er, c->stream));
+  ++c->launches;
+  return case_interface(c);
+}
+
+int case_stage(bcmg_case *c, int RK) {
+  int r;
+  if ((r = case_prologue(c))) return r;
   if ((r = case_flux(c, RK))) return r;
   int nb = 0;
   if (c->precision == BCMG_PRECISION_SPLIT) {
@@ -361,8 +410,12 @@ int case_stage(bcmg_case *c, int RK) {
 int case_step(bcmg_case *c, int subiters) {
   int r;
   for (int it = 0; it < subiters; ++it) {
-    for (int RK = 1; RK <= 3; ++RK)
-      if ((r = case_stage(c, RK))) return r;
+    if (c->method == BCMG_METHOD_LUSGS) {
+      if ((r = case_lusgs(c))) return r;
+    } else {
+      for (int RK = 1; RK <= 3; ++RK)
+        if ((r = case_stage(c, RK))) return r;
+    }
     k_emax<<<c->ncase, 32, 0, c->stream>>>(c->er, c->emax);
     CK(cudaGetLastError());
     ++c->launches;
@@ -552,6 +605,7 @@ int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out)
   c->nparts = rk_partial_blocks(probe);
   if (d->precision == BCMG_PRECISION_SPLIT)
     c->nparts = std::max(c->nparts, flux_split_blocks(d->n, d->ncube - 1));
+  c->nparts = std::max(c->nparts, d->ncube - 1);  // LU-SGS: one block per cube
   if (c->batched) {
     // Stage-update blocks of about equal size that never straddle two cases
     // (per-case norms), the flux kernel's per-case block ranges (one block
@@ -562,7 +616,9 @@ int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out)
     const long long chunk = (total + nbt - 1) / nbt;
     const int tiles = flux_split_blocks(d->n, 1);
     std::vector<long long> blk;
-    std::vector<int> cbr(c->ncase + 1), cbf(c->ncase + 1), cube_case(d->ncube, 0);
+    std::vector<int> cbr(c->ncase + 1), cbf(c->ncase + 1), cbc(c->ncase + 1),
+        cube_case(d->ncube, 0);
+    for (int q = 0; q <= c->ncase; ++q) cbc[q] = c->case_cube0[q] - 1;
     for (int q = 0; q < c->ncase; ++q) {
       cbr[q] = (int)blk.size();
       cbf[q] = (c->case_cube0[q] - 1) * tiles;
@@ -580,6 +636,9 @@ int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out)
          ck(dalloc(&c->rk_blk, blk.size()), "alloc") &&
          ck(dalloc(&c->case_blk_rk, cbr.size()), "alloc") &&
          ck(dalloc(&c->case_blk_flux, cbf.size()), "alloc") &&
+         ck(dalloc(&c->case_blk_cube, cbc.size()), "alloc") &&
+         ck(cudaMemcpy(c->case_blk_cube, cbc.data(), sizeof(int) * cbc.size(),
+                       cudaMemcpyHostToDevice), "copy") &&
          ck(cudaMemcpy(c->cases, c->hcases.data(), sizeof(CaseConst) * c->ncase,
                        cudaMemcpyHostToDevice), "copy") &&
          ck(cudaMemcpy(c->cube_case, cube_case.data(), sizeof(int) * cube_case.size(),
@@ -740,7 +799,10 @@ int bcmg_case_advance(bcmg_case *c, int steps, int subiters, int use_graph, doub
       // interface (faces + edges)
       const long long ifl = c->ntasks > 0 ? 2 : 1;
       long long stage = (c->nbc > 0) + L + ifl + 1 + 1 + ifl;
-      per = subiters * (3 * stage + 1 + 1) + 1 + (c->precision == BCMG_PRECISION_SPLIT ? 1 : 0);
+      // LU-SGS: prologue, residual, sweeps, norms, interface
+      long long lu = (c->nbc > 0) + L + ifl + 1 + 1 + 1 + ifl;
+      long long sub = c->method == BCMG_METHOD_LUSGS ? lu : 3 * stage + 1;
+      per = subiters * (sub + 1) + 1 + (c->precision == BCMG_PRECISION_SPLIT ? 1 : 0);
     }
     for (int s = 0; s < steps; ++s) CK(cudaGraphLaunch(c->graph, c->stream));
     c->launches = per * steps;
@@ -974,6 +1036,30 @@ int bcmg_batch_create(int ncase, const bcmg_case_desc *descs, bcmg_case **out) {
   m.w_plus = nullptr;
   m.gc_plus = m.ip_plus = nullptr;
   return create_common(&m, &bi, out);
+}
+
+int bcmg_case_set_method(bcmg_case *c, int method, double cfl, double omega) {
+  clear_err();
+  if (!c) { set_err("null context"); return BCMG_ERR_ARG; }
+  if (method != BCMG_METHOD_RK3 && method != BCMG_METHOD_LUSGS) {
+    set_err("unknown method");
+    return BCMG_ERR_ARG;
+  }
+  if (method == BCMG_METHOD_LUSGS && !(cfl >= 0 && omega >= 1 && omega <= 4)) {
+    set_err("LU-SGS needs cfl >= 0 (0: no pseudo-time term) and 1 <= omega <= 4");
+    return BCMG_ERR_ARG;
+  }
+  if (method == BCMG_METHOD_LUSGS && c->precision == BCMG_PRECISION_SPLIT) {
+    set_err("LU-SGS is available on the FP64 path only");
+    return BCMG_ERR_ARG;
+  }
+  c->method = method;
+  c->lu_cfl = cfl;
+  c->lu_omega = omega;
+  if (c->graph) cudaGraphExecDestroy(c->graph);  // the captured step changes
+  c->graph = nullptr;
+  c->graph_subiters = -1;
+  return BCMG_OK;
 }
 
 int bcmg_case_ncase(const bcmg_case *c) { return c ? c->ncase : 0; }

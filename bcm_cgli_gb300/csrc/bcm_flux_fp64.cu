@@ -270,7 +270,10 @@ __global__ void __launch_bounds__(T *T *T, 1) k_flux_fp64(FluxArgs a) {
     Rk[v] = v == 0 ? Rp + Rf : Rp + Rf + vF[v];
   }
   double *rk = a.Rku1 + 5 * go;
-  if (IF == kFluid) {
+  if (IF == kFluid && a.raw) {
+#pragma unroll
+    for (int r = 0; r < 5; ++r) rk[r] = Rk[r];
+  } else if (IF == kFluid) {
     const double K = BCMG_K;
     const double rho = __ldg(u);
     const double Uc = c.U, Vc = c.V, Wc = c.W;

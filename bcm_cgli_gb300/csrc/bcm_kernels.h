@@ -37,6 +37,7 @@ struct FluxArgs {
   const double *U1_, *U1, *U1q;
   double *Rku1, *Residual1;
   Batch bt;
+  int raw = 0;  // 1: write the residual R itself (LU-SGS right-hand side)
 };
 
 // FP64 residual + increment (bit-exact with the reference).
@@ -103,6 +104,23 @@ cudaError_t launch_norms_batch(int n, const CaseConst *cases, const int *case_bl
                                const double *partials, double *er, cudaStream_t s);
 // Batch form of launch_rk over an explicit block table (nblocks blocks).
 cudaError_t launch_rk_table(const RkArgs &a, int nblocks, cudaStream_t s);
+
+// LU-SGS sub-iteration (bcm_lusgs.cu; no reference counterpart): per cube,
+// forward and backward Gauss-Seidel sweeps over the planes i+j+k = const,
+// then Q += dq on fluid cells with per-cube norm/force partial sums.
+struct LusgsArgs {
+  Phys ph;
+  double dT, cfl, omega;
+  const int *FWS;
+  const double *cube_size;
+  double *U1_;             // updated in place on fluid cells
+  double *Rku1;            // in: residual; out: increment
+  double *coefA, *coefB;   // [ncell][5] each: scratch for the cell coefficients
+  const double *Residual1; // force integrands (summed into the partials)
+  double *partials;        // [ncube-1][7]
+  Batch bt;
+};
+cudaError_t launch_lusgs(const LusgsArgs &a, int ncubes, cudaStream_t s);
 
 // Interface: face-copy tasks (destination cube, source cube, axis, side) built
 // on the host, then the ordered three-phase edge fill of every cube.

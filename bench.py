@@ -256,6 +256,8 @@ def measure(api, case, precision_name, args, dist, clocks_on=True):
     kernel's launches are bracketed by events for its average duration."""
     precision = api.PRECISION_SPLIT if precision_name == "split" else api.PRECISION_FP64
     ctx = make_context(api, case, precision)
+    if getattr(args, "method", "rk3") == "lusgs" and precision_name == "fp64":
+        ctx.set_method(api.METHOD_LUSGS, cfl=0.0, omega=1.5)
     ctx.set_state(case.U, case.U, case.U)
     for _ in range(args.warmup):
         ctx.advance(1, SUBITERS, use_graph=False)
@@ -452,6 +454,8 @@ def main():
     ap.add_argument("--flux-only", action="store_true",
                     help="time the flux kernel alone on a smaller case (profiling target)")
     ap.add_argument("--ncx", type=int, default=6, help="cubes per edge for --flux-only")
+    ap.add_argument("--method", default="rk3", choices=["rk3", "lusgs"],
+                    help="sub-iteration method of the FP64 path (lusgs: LU-SGS sweeps)")
     ap.add_argument("--workload", default="tgv", choices=sorted(WORKLOADS),
                     help="tgv (default, the metric's configuration), vortex, sphere, tgv32, "
                          "batch")

@@ -217,6 +217,19 @@ int bcmg_case_profile(const bcmg_case *c, double *flux_ms_total, long long *flux
  * normalisers).  Each case's state evolves exactly as it would in a context
  * of its own. */
 int bcmg_batch_create(int ncase, const bcmg_case_desc *descs, bcmg_case **out);
+
+/* Sub-iteration method of bcmg_case_advance.  BCMG_METHOD_RK3 (default) is
+ * the reference's three-stage preconditioned RK (bit-exact).  BCMG_METHOD_LUSGS
+ * has no counterpart in the reference (BCM_LUSGS.h there holds no solver):
+ * one matrix-free LU-SGS step per sub-iteration for the same residual
+ * (split Jacobians with relaxation omega in [1, 4], scalar viscous term, a
+ * local pseudo-time term when cfl > 0, none when cfl == 0), swept per cube
+ * over the planes i+j+k = const.  It converges to the state the RK
+ * sub-iterations converge to, in fewer sub-iterations; er and emax keep
+ * their meaning (change norms of each update).  FP64 path only. */
+#define BCMG_METHOD_RK3 0
+#define BCMG_METHOD_LUSGS 1
+int bcmg_case_set_method(bcmg_case *c, int method, double cfl, double omega);
 int bcmg_case_ncase(const bcmg_case *c);
 /* First flat cube of case q and the case's own cube-slot count (ncube of
  * its descriptor, unused slot 0 included). */

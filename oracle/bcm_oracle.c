@@ -369,7 +369,10 @@ void bcmo_flux_stage(const bcmo_phys *ph, int ncube, int RK, double deltaT, doub
           d[4][3] = (-4 * H * W * temp2) / temp;
           d[4][4] = (2 * deltaT * (2 * H * (KG - 1) * (beta - 1) * deltaT + KG * T * (2 * deltaT + 3 * beta * deltaTau))) / temp;
           double *rk = Rku1 + 5 * o;
-          if (IF == IFLUID) {
+          if (IF == IFLUID && RK == 0) {
+            /* residual only (the LU-SGS sub-iteration's right-hand side) */
+            for (int a = 0; a < 5; ++a) rk[a] = Rk[a];
+          } else if (IF == IFLUID) {
             for (int a = 0; a < 5; ++a)
               rk[a] = deltaTau * (d[a][0] * Rk[0] + d[a][1] * Rk[1] + d[a][2] * Rk[2] +
                                   d[a][3] * Rk[3] + d[a][4] * Rk[4]);

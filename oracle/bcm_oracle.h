@@ -20,6 +20,8 @@ typedef struct bcmo_phys {
   double P0;      /* prm.h:37 */
 } bcmo_phys;
 
+/* RK 1..3: one stage; RK 0: the raw residual R into Rku1 (fluid cells) and
+ * the force integrands, no update. */
 void bcmo_flux_stage(const bcmo_phys *ph, int ncube, int RK, double deltaT, double deltaTau,
                      double e, const int *FWS, const double *cube_size, double *U1_,
                      const double *U1, const double *U1q, double *U1p1, double *U1p2,
@@ -43,6 +45,20 @@ void bcmo_run(const bcmo_phys *ph, int ncube, int steps, int subiters, double de
               const int *zl, const int *zu, int nminus, const double *wm, const int *gm,
               const int *im, int nplus, const double *wp, const int *gp, const int *ip,
               double *er, double *Emax);
+/* LU-SGS sub-iteration (bcm_oracle_lusgs.c; no reference counterpart).
+ * Rku1 holds the residual (bcmo_flux_stage with RK = 0) on entry and the
+ * increment on return; U1_ is updated on fluid cells and er[1..7] set. */
+void bcmo_lusgs(const bcmo_phys *ph, int ncube, double deltaT, double cfl, double omega,
+                const int *FWS, const double *cube_size, double *U1_, double *Rku1,
+                const double *Residual1, double *er);
+void bcmo_run_lusgs(const bcmo_phys *ph, int ncube, int steps, int subiters, double deltaT,
+                    double cfl, double omega, double e, const int *FWS, const int *adj,
+                    const int *csl, const double *cube_size, double *U1_, double *U1,
+                    double *U1q, double *Rku1, double *Residual1, int nxl, int nxu,
+                    const int *xl, const int *xu, int nyl, int nyu, const int *yl,
+                    const int *yu, int nzl, int nzu, const int *zl, const int *zu, int nminus,
+                    const double *wm, const int *gm, const int *im, int nplus,
+                    const double *wp, const int *gp, const int *ip, double *er, double *Emax);
 void bcmo_set_threads(int n);
 
 #ifdef __cplusplus

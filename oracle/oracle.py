@@ -32,13 +32,13 @@ def build_port(force: bool = False) -> str:
     """Compile the C restatement; returns the .so path."""
     os.makedirs(BUILD_DIR, exist_ok=True)
     out = os.path.join(BUILD_DIR, "libbcm_oracle.so")
-    src = os.path.join(HERE, "bcm_oracle.c")
+    srcs = [os.path.join(HERE, "bcm_oracle.c"), os.path.join(HERE, "bcm_oracle_lusgs.c")]
     hdr = os.path.join(HERE, "bcm_oracle.h")
-    if (not force and os.path.isfile(out)
-            and os.path.getmtime(out) >= max(os.path.getmtime(src), os.path.getmtime(hdr))):
+    if (not force and os.path.isfile(out) and os.path.getmtime(out) >= max(
+            [os.path.getmtime(x) for x in srcs] + [os.path.getmtime(hdr)])):
         return out
     cmd = ["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-std=c11",
-           src, "-o", out + ".tmp", "-lm"]
+           *srcs, "-o", out + ".tmp", "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + r.stderr[-4000:])
@@ -101,6 +101,13 @@ class Port:
                                _dp, C.c_int, C.c_int, _ip, _ip, C.c_int, C.c_int, _ip, _ip,
                                C.c_int, C.c_int, _ip, _ip, C.c_int, _dp, _ip, _ip, C.c_int,
                                _dp, _ip, _ip, _dp, _dp]
+        L.bcmo_run_lusgs.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                     C.c_double, C.c_double, _ip, _ip, _ip, _dp, _dp, _dp,
+                                     _dp, _dp, _dp, C.c_int, C.c_int, _ip, _ip, C.c_int,
+                                     C.c_int, _ip, _ip, C.c_int, C.c_int, _ip, _ip, C.c_int,
+                                     _dp, _ip, _ip, C.c_int, _dp, _ip, _ip, _dp, _dp]
+        L.bcmo_lusgs.argtypes = [P, C.c_int, C.c_double, C.c_double, C.c_double, _ip, _dp,
+                                 _dp, _dp, _dp, _dp]
         L.bcmo_set_threads.argtypes = [C.c_int]
 
     @staticmethod
@@ -131,6 +138,25 @@ class Port:
 
     def time_shift(self, case, st: State):
         self.lib.bcmo_time_shift(self.phys(case), case.ncube, st.U1_, st.U1, st.U1q)
+
+    def run_lusgs(self, case, st: State, steps: int, subiters: int, cfl: float = 0.0,
+                  omega: float = 1.5):
+        """bcmo_run with one LU-SGS update per sub-iteration (no reference
+        counterpart; see bcm_oracle_lusgs.c)."""
+        xl, xu, yl, yu, zl, zu = case.bc_lists()
+        nm, Wm, Gm, Im = _ibm(case, -1)
+        npl, Wp, Gp, Ip = _ibm(case, 1)
+        self.lib.bcmo_run_lusgs(self.phys(case), case.ncube, steps, subiters, case.dT, cfl,
+                                omega, case.e, case.fws, _adj(case), case.csl, case.cube_size,
+                                st.U1_, st.U1, st.U1q, st.Rku1, st.Residual1, len(xl), len(xu),
+                                _nz(xl), _nz(xu), len(yl), len(yu), _nz(yl), _nz(yu), len(zl),
+                                len(zu), _nz(zl), _nz(zu), nm, Wm, Gm, Im, npl, Wp, Gp, Ip,
+                                st.er, st.Emax)
+
+    def residual(self, case, st: State):
+        """The raw residual R(U1_) into st.Rku1 (fluid cells) and the force
+        integrands into st.Residual1 (bcmo_flux_stage with RK = 0)."""
+        self.flux_stage(case, st, 0)
 
     def run(self, case, st: State, steps: int, subiters: int):
         xl, xu, yl, yu, zl, zu = case.bc_lists()
@@ -214,6 +240,25 @@ class Ref:
 
     def interface(self, case, U):
         self.lib.ref_interface(U)
+
+    def run_lusgs(self, case, st: State, steps: int, subiters: int, cfl: float = 0.0,
+                  omega: float = 1.5):
+        """bcmo_run with one LU-SGS update per sub-iteration (no reference
+        counterpart; see bcm_oracle_lusgs.c)."""
+        xl, xu, yl, yu, zl, zu = case.bc_lists()
+        nm, Wm, Gm, Im = _ibm(case, -1)
+        npl, Wp, Gp, Ip = _ibm(case, 1)
+        self.lib.bcmo_run_lusgs(self.phys(case), case.ncube, steps, subiters, case.dT, cfl,
+                                omega, case.e, case.fws, _adj(case), case.csl, case.cube_size,
+                                st.U1_, st.U1, st.U1q, st.Rku1, st.Residual1, len(xl), len(xu),
+                                _nz(xl), _nz(xu), len(yl), len(yu), _nz(yl), _nz(yu), len(zl),
+                                len(zu), _nz(zl), _nz(zu), nm, Wm, Gm, Im, npl, Wp, Gp, Ip,
+                                st.er, st.Emax)
+
+    def residual(self, case, st: State):
+        """The raw residual R(U1_) into st.Rku1 (fluid cells) and the force
+        integrands into st.Residual1 (bcmo_flux_stage with RK = 0)."""
+        self.flux_stage(case, st, 0)
 
     def run(self, case, st: State, steps: int, subiters: int):
         xl, xu, yl, yu, zl, zu = (_one_based(a) for a in case.bc_lists())
