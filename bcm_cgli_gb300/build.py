@@ -31,6 +31,7 @@ UNITS = [
     ("bcm_capi.cu", ["--fmad=false"]),
     ("bcm_noalloc.cu", ["--fmad=false"]),
     ("bcm_lusgs.cu", ["--fmad=false"]),
+    ("bcm_lusgs_split.cu", ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"]),
     ("bcm_tables.cpp", []),
 ]
 

@@ -240,10 +240,6 @@ int case_flux(bcmg_case *c, int RK) {
   a.Residual1 = c->Residual1;
   a.bt = c->bt();
   a.raw = RK == 0;  // residual only (LU-SGS)
-  if (RK == 0 && c->precision == BCMG_PRECISION_SPLIT) {
-    set_err("LU-SGS residual mode is not available for the split-precision path");
-    return BCMG_ERR_ARG;
-  }
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (c->profile) {
     while (c->ev.size() < c->ev_used + 2) {
@@ -283,6 +279,9 @@ int case_flux(bcmg_case *c, int RK) {
     sa.U1q = c->U1q;
     sa.D2 = c->D2;
     sa.RK = RK;
+    // RK 0 (LU-SGS): FP32 residual into the Rku1 buffer, which the split
+    // path does not otherwise use
+    sa.R32 = reinterpret_cast<float *>(c->Rku1);
     sa.partials = c->partials;
     sa.Residual1 = c->Residual1;
     sa.bt = c->bt();
@@ -335,6 +334,27 @@ int case_lusgs(bcmg_case *c) {
   int r;
   if ((r = case_prologue(c))) return r;
   if ((r = case_flux(c, 0))) return r;
+  if (c->precision == BCMG_PRECISION_SPLIT) {
+    LusgsSplitArgs l;
+    l.ph = c->ph;
+    l.dTf = (float)c->dT;
+    l.cflf = (float)c->lu_cfl;
+    l.omegaf = (float)c->lu_omega;
+    l.rho0f = (float)c->ph.rho0;
+    l.P0f = (float)c->ph.P0;
+    l.T0f = (float)(c->ph.P0 / c->ph.rho0 / BCMG_R);
+    l.mu_Lf = (float)c->ph.mu_L;
+    l.FWS = c->FWS;
+    l.inv_dx = c->inv_dx;
+    l.M = c->M;
+    l.U1_ = c->U1_;
+    l.R32 = reinterpret_cast<float *>(c->Rku1);
+    l.coef = reinterpret_cast<float *>(c->U1p1);  // 10 floats per cell
+    l.Residual1 = c->Residual1;
+    l.partials = c->partials;
+    l.bt = c->bt();
+    CK(launch_lusgs_split(l, c->ncube - 1, c->stream));
+  } else {
   LusgsArgs l;
   l.ph = c->ph;
   l.dT = c->dT;
@@ -350,6 +370,7 @@ int case_lusgs(bcmg_case *c) {
   l.partials = c->partials;
   l.bt = c->bt();
   CK(launch_lusgs(l, c->ncube - 1, c->stream));
+  }
   ++c->launches;
   if (c->batched)
     CK(launch_norms_batch(c->ph.n, c->cases, c->case_blk_cube, c->ncase, c->partials, c->er,
@@ -1047,10 +1068,6 @@ int bcmg_case_set_method(bcmg_case *c, int method, double cfl, double omega) {
   }
   if (method == BCMG_METHOD_LUSGS && !(cfl >= 0 && omega >= 1 && omega <= 4)) {
     set_err("LU-SGS needs cfl >= 0 (0: no pseudo-time term) and 1 <= omega <= 4");
-    return BCMG_ERR_ARG;
-  }
-  if (method == BCMG_METHOD_LUSGS && c->precision == BCMG_PRECISION_SPLIT) {
-    set_err("LU-SGS is available on the FP64 path only");
     return BCMG_ERR_ARG;
   }
   c->method = method;

@@ -445,7 +445,11 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
     const float Rp = -(3.0f * d1 - d2) * i2dt;
     Rk[v] = Rp - acc[v] + vF[v];
   }
-  if (IF == kFluid) {
+  if (IF == kFluid && a.RK == 0) {
+    // residual only: the LU-SGS right-hand side
+#pragma unroll
+    for (int v = 0; v < 5; ++v) a.R32[5 * go + v] = Rk[v];
+  } else if (IF == kFluid) {
     const float K = 1.4f, Km1 = 0.4f;
     const float dT = dTc, dTau = dTauc;
     const float *qm = BX(mi, mj, mk);

@@ -61,7 +61,9 @@ struct FluxSplitArgs {
   double *U1_;     // updated in place for the CTA's own cells
   const double *U1, *U1q;
   const float *D2;  // FP32 of the FP64 difference U1 - U1q (k_level_diff)
-  int RK;              // stage 1..3: the kernel applies the stage update
+  int RK;              // stage 1..3: the kernel applies the stage update;
+                       // 0: it writes the FP32 residual to R32 instead
+  float *R32 = nullptr;  // [ncell][5] (RK == 0)
   double *partials;    // [blocks][7] norm/force partial sums (stage 3)
   double *Residual1;
   Batch bt;
@@ -121,6 +123,24 @@ struct LusgsArgs {
   Batch bt;
 };
 cudaError_t launch_lusgs(const LusgsArgs &a, int ncubes, cudaStream_t s);
+
+// Split-precision LU-SGS: FP32 sweeps on the FP32 mirror of the state (deltas
+// from the case's reference state), FP64 update and norm sums.
+struct LusgsSplitArgs {
+  Phys ph;
+  float dTf, cflf, omegaf;
+  float rho0f, P0f, T0f, mu_Lf;
+  const int *FWS;
+  const float *inv_dx;     // [ncube] n / cube_size
+  const float *M;          // FP32 deltas of the state
+  double *U1_;             // updated in place on fluid cells
+  float *R32;              // in: residual; out: increment
+  float *coef;             // [ncell][10] scratch
+  const double *Residual1;
+  double *partials;        // [ncube-1][7]
+  Batch bt;
+};
+cudaError_t launch_lusgs_split(const LusgsSplitArgs &a, int ncubes, cudaStream_t s);
 
 // Interface: face-copy tasks (destination cube, source cube, axis, side) built
 // on the host, then the ordered three-phase edge fill of every cube.

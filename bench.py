@@ -256,7 +256,7 @@ def measure(api, case, precision_name, args, dist, clocks_on=True):
     kernel's launches are bracketed by events for its average duration."""
     precision = api.PRECISION_SPLIT if precision_name == "split" else api.PRECISION_FP64
     ctx = make_context(api, case, precision)
-    if getattr(args, "method", "rk3") == "lusgs" and precision_name == "fp64":
+    if getattr(args, "method", "rk3") == "lusgs":
         ctx.set_method(api.METHOD_LUSGS, cfl=0.0, omega=1.5)
     ctx.set_state(case.U, case.U, case.U)
     for _ in range(args.warmup):
@@ -455,7 +455,7 @@ def main():
                     help="time the flux kernel alone on a smaller case (profiling target)")
     ap.add_argument("--ncx", type=int, default=6, help="cubes per edge for --flux-only")
     ap.add_argument("--method", default="rk3", choices=["rk3", "lusgs"],
-                    help="sub-iteration method of the FP64 path (lusgs: LU-SGS sweeps)")
+                    help="sub-iteration method (rk3: the reference's RK; lusgs: LU-SGS sweeps)")
     ap.add_argument("--workload", default="tgv", choices=sorted(WORKLOADS),
                     help="tgv (default, the metric's configuration), vortex, sphere, tgv32, "
                          "batch")

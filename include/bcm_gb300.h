@@ -226,7 +226,9 @@ int bcmg_batch_create(int ncase, const bcmg_case_desc *descs, bcmg_case **out);
  * local pseudo-time term when cfl > 0, none when cfl == 0), swept per cube
  * over the planes i+j+k = const.  It converges to the state the RK
  * sub-iterations converge to, in fewer sub-iterations; er and emax keep
- * their meaning (change norms of each update).  FP64 path only. */
+ * their meaning (change norms of each update).  On the split-precision
+ * path the sweeps run in FP32 on the FP32 mirror of the state, the update
+ * and norm sums in FP64. */
 #define BCMG_METHOD_RK3 0
 #define BCMG_METHOD_LUSGS 1
 int bcmg_case_set_method(bcmg_case *c, int method, double cfl, double omega);

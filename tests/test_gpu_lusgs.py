@@ -113,3 +113,50 @@ def test_lusgs_rejects_bad_settings():
     with pytest.raises(api.BcmgError):
         ctx.set_method(7)
     ctx.close()
+
+
+def _rel_l2_scaled(a, b, n):
+    ai = a[1:, 2:n + 2, 2:n + 2, 2:n + 2].reshape(-1, 5)
+    bi = b[1:, 2:n + 2, 2:n + 2, 2:n + 2].reshape(-1, 5)
+    d = np.linalg.norm(ai - bi, axis=0)
+    own = d / np.maximum(np.linalg.norm(bi, axis=0), 1e-300)
+    mom = np.linalg.norm(bi[:, 1:4])
+    return np.array([own[0], d[1] / mom, d[2] / mom, d[3] / mom, own[4]])
+
+
+@pytest.mark.parametrize("make", [lambda: cases.taylor_green(ncx=2, n=8),
+                                  lambda: cases.sphere_cubes(64, n=8, mach=0.2, reynolds=150.0,
+                                                             seed=11)])
+def test_split_lusgs_close_to_fp64_lusgs(make):
+    """FP32 sweeps on the FP32 mirror: after a dual-time step of LU-SGS
+    sub-iterations the state is within the split path's 1e-5 bound of the
+    FP64 LU-SGS state (relative L2, momentum scaled by its magnitude)."""
+    case = make()
+    out = {}
+    for prec in (api.PRECISION_FP64, api.PRECISION_SPLIT):
+        ctx = api.CaseContext(case, precision=prec)
+        ctx.set_method(api.METHOD_LUSGS)
+        ctx.set_state(case.U, case.U, case.U)
+        out[prec] = (ctx.advance(2, 8), ctx.get_state()[0])
+        ctx.close()
+    err = _rel_l2_scaled(out[api.PRECISION_SPLIT][1], out[api.PRECISION_FP64][1], case.n)
+    assert err.max() < 1e-5, err
+
+
+def test_split_lusgs_batch_equals_single():
+    cs = [cases.taylor_green(ncx=2, n=8), cases.random_two_level_case(seed=6, n=8, periodic=False)]
+    b = api.BatchContext(cs, precision=api.PRECISION_SPLIT)
+    b.set_method(api.METHOD_LUSGS, omega=1.5)
+    for q, c in enumerate(cs):
+        b.set_case_state(q, c.U, c.U, c.U)
+    eb = b.advance(1, 4)
+    for q, c in enumerate(cs):
+        s = api.CaseContext(c, precision=api.PRECISION_SPLIT)
+        s.set_method(api.METHOD_LUSGS, omega=1.5)
+        s.set_state(c.U, c.U, c.U)
+        es = s.advance(1, 4)
+        for x, y in zip(s.get_state(), b.get_case_state(q)):
+            assert np.array_equal(x[1:], y[1:])
+        assert np.array_equal(es[1:], eb[q, 1:])
+        s.close()
+    b.close()
