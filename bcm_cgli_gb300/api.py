@@ -258,6 +258,19 @@ class CaseContext:
                                       er.ctypes.data, self.emax.ctypes.data))
         return er.reshape(self.ncase, 8) if isinstance(self, BatchContext) else er
 
+    def advance_converged(self, steps, max_subiters, tol=0.02, use_graph=True):
+        """Steps with the reference's convergence test (main.cpp:1249-1271);
+        returns (er, sub-iterations per step [steps] or [steps, ncase])."""
+        er = np.zeros(8 * self.ncase)
+        its = np.zeros(max(1, steps) * self.ncase, np.int32)
+        check(lib().bcmg_case_advance_converged(
+            self.h, int(steps), int(max_subiters), float(tol), int(bool(use_graph)),
+            its.ctypes.data, er.ctypes.data, self.emax.ctypes.data))
+        its = its[:steps * self.ncase]
+        if isinstance(self, BatchContext):
+            return er.reshape(self.ncase, 8), its.reshape(steps, self.ncase)
+        return er, its
+
     def sync(self):
         check(lib().bcmg_case_sync(self.h))
 

@@ -67,9 +67,10 @@ __global__ void k_time_shift(int n, long long total, const double *U1_, double *
   }
 }
 
-__global__ void k_emax(double *er, double *emax) {
+__global__ void k_emax(double *er, double *emax, const int *active) {
   // main.cpp:1249-1259: E_k = max(E_k, er_k); er_k /= E_k.  One block per
-  // case: er[8q..], emax[6q..].
+  // case: er[8q..], emax[6q..]; converged cases keep theirs.
+  if (active && !active[blockIdx.x]) return;
   er += 8 * (size_t)blockIdx.x;
   emax += 6 * (size_t)blockIdx.x;
   const int v = threadIdx.x + 1;
@@ -78,6 +79,42 @@ __global__ void k_emax(double *er, double *emax) {
     emax[v] = E;
     er[v] = er[v] / E;
   }
+}
+
+// Convergence-driven sub-iterations (main.cpp:1249-1271): before a step
+// every case is active with zero sub-iterations; after each sub-iteration
+// (and its E normalisation) a case whose normalised change norms er[1..5]
+// are all below tol, or that reached max_subiters, becomes inactive; the
+// loop continues while any case is active.  With a graph handle the
+// decision drives the step graph's while node on the device.
+__global__ void k_conv_reset(int *active, int *iters, int ncase) {
+  for (int q = threadIdx.x; q < ncase; q += blockDim.x) {
+    active[q] = 1;
+    iters[q] = 0;
+  }
+}
+
+__global__ void k_conv_check(const double *er, int *active, int *iters, int ncase, double tol,
+                             int max_subiters, int *cont, cudaGraphConditionalHandle h,
+                             int use_handle) {
+  if (threadIdx.x != 0) return;
+  int any = 0;
+  for (int q = 0; q < ncase; ++q) {
+    if (!active[q]) continue;
+    const double *e = er + 8 * (size_t)q;
+    const int it = ++iters[q];
+    const bool conv = e[1] < tol && e[2] < tol && e[3] < tol && e[4] < tol && e[5] < tol;
+    if (conv || it >= max_subiters)
+      active[q] = 0;
+    else
+      any = 1;
+  }
+  *cont = any;
+  if (use_handle) cudaGraphSetConditional(h, any ? 1u : 0u);
+}
+
+__global__ void k_store_iters(const int *iters, int *dst, int ncase) {
+  for (int q = threadIdx.x; q < ncase; q += blockDim.x) dst[q] = iters[q];
 }
 
 struct Ibm {
@@ -184,12 +221,19 @@ struct bcmg_case {
   // LU-SGS with its pseudo-time CFL (0: none) and relaxation factor.
   int method = BCMG_METHOD_RK3;
   double lu_cfl = 0.0, lu_omega = 1.5;
+  // Convergence-driven stepping (bcmg_case_advance_converged)
+  bool conv = false;                 // kernels see the active masks
+  int *active = nullptr, *iters = nullptr, *cont = nullptr;  // device
+  cudaGraphExec_t cgraph = nullptr;  // step graph with the while node
+  int cgraph_max = -1, cgraph_method = -1;
+  double cgraph_tol = -1;
   Batch bt() const {
     Batch b;
     if (batched) {
       b.cube_case = cube_case;
       b.cases = cases;
     }
+    if (conv) b.active = active;
     return b;
   }
   cudaGraphExec_t graph = nullptr;
@@ -208,6 +252,9 @@ struct bcmg_case {
     marks.clear();
     if (graph) cudaGraphExecDestroy(graph);
     graph = nullptr;
+    if (cgraph) cudaGraphExecDestroy(cgraph);
+    cgraph = nullptr;
+    dfree(active); dfree(iters); dfree(cont);
     for (auto x : ev) cudaEventDestroy(x);
     ev.clear();
     dfree(U1_); dfree(U1); dfree(U1q); dfree(U1p1); dfree(U1p2); dfree(Rku1); dfree(Residual1);
@@ -301,6 +348,7 @@ int case_interface(bcmg_case *c) {
   ia.task_cube = c->task_cube;
   ia.tasks = c->tasks;
   ia.U1_ = c->U1_;
+  ia.bt = c->bt();
   CK(launch_interface(ia, c->ncube, c->stream));
   c->launches += c->ntasks > 0 ? 2 : 1;
   return BCMG_OK;
@@ -374,9 +422,9 @@ int case_lusgs(bcmg_case *c) {
   ++c->launches;
   if (c->batched)
     CK(launch_norms_batch(c->ph.n, c->cases, c->case_blk_cube, c->ncase, c->partials, c->er,
-                          c->stream));
+                          c->stream, c->bt().active));
   else
-    CK(launch_norms(c->ph, c->partials, c->ncube - 1, c->er, c->stream));
+    CK(launch_norms(c->ph, c->partials, c->ncube - 1, c->er, c->stream, c->bt().active));
   ++c->launches;
   return case_interface(c);
 }
@@ -392,9 +440,9 @@ int case_stage(bcmg_case *c, int RK) {
     if (RK == 3) {
       if (c->batched)
         CK(launch_norms_batch(c->ph.n, c->cases, c->case_blk_flux, c->ncase, c->partials, c->er,
-                              c->stream));
+                              c->stream, c->bt().active));
       else
-        CK(launch_norms(c->ph, c->partials, nb, c->er, c->stream));
+        CK(launch_norms(c->ph, c->partials, nb, c->er, c->stream, c->bt().active));
       ++c->launches;
     }
     return case_interface(c);
@@ -410,6 +458,7 @@ int case_stage(bcmg_case *c, int RK) {
   k.Rku1 = c->Rku1;
   k.Residual1 = c->Residual1;
   k.partials = c->partials;
+  k.bt = c->bt();
   if (c->batched) {
     k.blk_beg = c->rk_blk;
     CK(launch_rk_table(k, c->nrk, c->stream));
@@ -420,27 +469,32 @@ int case_stage(bcmg_case *c, int RK) {
   if (RK == 3) {
     if (c->batched)
       CK(launch_norms_batch(c->ph.n, c->cases, c->case_blk_rk, c->ncase, c->partials, c->er,
-                            c->stream));
+                            c->stream, c->bt().active));
     else
-      CK(launch_norms(c->ph, c->partials, nb, c->er, c->stream));
+      CK(launch_norms(c->ph, c->partials, nb, c->er, c->stream, c->bt().active));
     ++c->launches;
   }
   return case_interface(c);
 }
 
-int case_step(bcmg_case *c, int subiters) {
+// One sub-iteration (three RK stages or one LU-SGS update) and the E
+// normalisation of its norms (main.cpp:1249-1259).
+int case_subiter(bcmg_case *c) {
   int r;
-  for (int it = 0; it < subiters; ++it) {
-    if (c->method == BCMG_METHOD_LUSGS) {
-      if ((r = case_lusgs(c))) return r;
-    } else {
-      for (int RK = 1; RK <= 3; ++RK)
-        if ((r = case_stage(c, RK))) return r;
-    }
-    k_emax<<<c->ncase, 32, 0, c->stream>>>(c->er, c->emax);
-    CK(cudaGetLastError());
-    ++c->launches;
+  if (c->method == BCMG_METHOD_LUSGS) {
+    if ((r = case_lusgs(c))) return r;
+  } else {
+    for (int RK = 1; RK <= 3; ++RK)
+      if ((r = case_stage(c, RK))) return r;
   }
+  k_emax<<<c->ncase, 32, 0, c->stream>>>(c->er, c->emax, c->bt().active);
+  CK(cudaGetLastError());
+  ++c->launches;
+  return BCMG_OK;
+}
+
+// Time-level shift at the end of a dual-time step (main.cpp:1292-1315).
+int case_shift(bcmg_case *c) {
   const long long total = (long long)(c->ncube - 1) * c->ph.n * c->ph.n * c->ph.n;
   if (total > 0) {
     int blocks = (int)std::min<long long>((total + 255) / 256, 152 * 8);
@@ -452,6 +506,67 @@ int case_step(bcmg_case *c, int subiters) {
       ++c->launches;
     }
   }
+  return BCMG_OK;
+}
+
+int case_step(bcmg_case *c, int subiters) {
+  int r;
+  for (int it = 0; it < subiters; ++it)
+    if ((r = case_subiter(c))) return r;
+  return case_shift(c);
+}
+
+// The step graph of convergence-driven stepping: reset of the masks, a
+// while node whose body is one sub-iteration plus the convergence check
+// (which sets the node's condition on the device), then the time shift.
+int build_conv_graph(bcmg_case *c, int max_subiters, double tol) {
+  if (c->cgraph) cudaGraphExecDestroy(c->cgraph);
+  c->cgraph = nullptr;
+  const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+  cudaGraph_t g = nullptr;
+  CK(cudaGraphCreate(&g, 0));
+  struct Guard {
+    cudaGraph_t *g;
+    ~Guard() { if (*g) cudaGraphDestroy(*g); }
+  } guard{&g};
+  cudaGraphConditionalHandle h;
+  CK(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+  CK(cudaStreamBeginCaptureToGraph(c->stream, g, nullptr, nullptr, 0, mode));
+  k_conv_reset<<<1, 128, 0, c->stream>>>(c->active, c->iters, c->ncase);
+  cudaError_t le = cudaGetLastError();
+  CK(cudaStreamEndCapture(c->stream, &g));
+  CK(le);
+  cudaGraphNode_t reset;
+  size_t nn = 1;
+  CK(cudaGraphGetNodes(g, &reset, &nn));
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.size = 1;
+  cudaGraphNode_t wnode;
+  CK(cudaGraphAddNode(&wnode, g, &reset, nullptr, 1, &p));
+  cudaGraph_t body = p.conditional.phGraph_out[0];
+  CK(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, mode));
+  int r = case_subiter(c);
+  if (!r) {
+    k_conv_check<<<1, 32, 0, c->stream>>>(c->er, c->active, c->iters, c->ncase, tol,
+                                          max_subiters, c->cont, h, 1);
+    le = cudaGetLastError();
+  }
+  cudaError_t ce = cudaStreamEndCapture(c->stream, &body);
+  if (r) return r;
+  CK(le);
+  CK(ce);
+  CK(cudaStreamBeginCaptureToGraph(c->stream, g, &wnode, nullptr, 1, mode));
+  r = case_shift(c);
+  ce = cudaStreamEndCapture(c->stream, &g);
+  if (r) return r;
+  CK(ce);
+  CK(cudaGraphInstantiate(&c->cgraph, g, 0));
+  c->cgraph_max = max_subiters;
+  c->cgraph_tol = tol;
+  c->cgraph_method = c->method;
   return BCMG_OK;
 }
 
@@ -1076,6 +1191,95 @@ int bcmg_case_set_method(bcmg_case *c, int method, double cfl, double omega) {
   if (c->graph) cudaGraphExecDestroy(c->graph);  // the captured step changes
   c->graph = nullptr;
   c->graph_subiters = -1;
+  return BCMG_OK;
+}
+
+int bcmg_case_advance_converged(bcmg_case *c, int steps, int max_subiters, double tol,
+                                int use_graph, int *subiters_out, double *er, double *emax) {
+  clear_err();
+  if (!c || steps < 0 || max_subiters < 1 || !(tol > 0)) {
+    set_err("bad arguments");
+    return BCMG_ERR_ARG;
+  }
+  if (!c->active) {
+    CK(dalloc(&c->active, (size_t)c->ncase));
+    CK(dalloc(&c->iters, (size_t)c->ncase));
+    CK(dalloc(&c->cont, 1));
+  }
+  int *hist = nullptr;
+  CK(dalloc(&hist, (size_t)std::max(1, steps) * c->ncase));
+  struct Restore {
+    bcmg_case *c;
+    int *hist;
+    ~Restore() {
+      c->conv = false;
+      if (hist) cudaFree(hist);
+    }
+  } restore{c, hist};
+  if (emax)
+    CK(cudaMemcpyAsync(c->emax, emax, 6 * sizeof(double) * c->ncase, cudaMemcpyHostToDevice,
+                       c->stream));
+  c->conv = true;
+  c->launches = 0;
+  c->ev_used = 0;
+  int r;
+  if (use_graph && !c->profile) {
+    if (!c->cgraph || c->cgraph_max != max_subiters || c->cgraph_tol != tol ||
+        c->cgraph_method != c->method) {
+      long long saved = c->launches;
+      if ((r = build_conv_graph(c, max_subiters, tol))) return r;
+      c->launches = saved;
+    }
+    for (int st = 0; st < steps; ++st) {
+      CK(cudaGraphLaunch(c->cgraph, c->stream));
+      k_store_iters<<<1, 128, 0, c->stream>>>(c->iters, hist + (size_t)st * c->ncase, c->ncase);
+      CK(cudaGetLastError());
+    }
+  } else {
+    for (int st = 0; st < steps; ++st) {
+      k_conv_reset<<<1, 128, 0, c->stream>>>(c->active, c->iters, c->ncase);
+      CK(cudaGetLastError());
+      for (int it = 0; it < max_subiters; ++it) {
+        if ((r = case_subiter(c))) return r;
+        k_conv_check<<<1, 32, 0, c->stream>>>(c->er, c->active, c->iters, c->ncase, tol,
+                                              max_subiters, c->cont, 0, 0);
+        CK(cudaGetLastError());
+        int more = 0;
+        CK(cudaMemcpyAsync(&more, c->cont, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        if (!more) break;
+      }
+      if ((r = case_shift(c))) return r;
+      k_store_iters<<<1, 128, 0, c->stream>>>(c->iters, hist + (size_t)st * c->ncase, c->ncase);
+      CK(cudaGetLastError());
+    }
+  }
+  std::vector<int> h((size_t)std::max(1, steps) * c->ncase, 0);
+  CK(cudaMemcpyAsync(h.data(), hist, sizeof(int) * h.size(), cudaMemcpyDeviceToHost, c->stream));
+  if (er)
+    CK(cudaMemcpyAsync(er, c->er, 8 * sizeof(double) * c->ncase, cudaMemcpyDeviceToHost,
+                       c->stream));
+  if (emax)
+    CK(cudaMemcpyAsync(emax, c->emax, 6 * sizeof(double) * c->ncase, cudaMemcpyDeviceToHost,
+                       c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (subiters_out) std::copy(h.begin(), h.begin() + (size_t)steps * c->ncase, subiters_out);
+  if (use_graph && !c->profile) {
+    // kernel launches of the replayed graphs: per sub-iteration as in
+    // bcmg_case_advance, plus reset, check and shift
+    const int L = (int)(c->ibm.level_off.size() > 0 ? c->ibm.level_off.size() - 1 : 0);
+    const long long ifl = c->ntasks > 0 ? 2 : 1;
+    const long long stage = (c->nbc > 0) + L + ifl + 1 + 1 + ifl;
+    const long long lu = (c->nbc > 0) + L + ifl + 1 + 1 + 1 + ifl;
+    const long long sub = (c->method == BCMG_METHOD_LUSGS ? lu : 3 * stage) + 1 + 1;
+    long long tot = 0;
+    for (int st = 0; st < steps; ++st) {
+      int mx = 0;
+      for (int q = 0; q < c->ncase; ++q) mx = std::max(mx, h[(size_t)st * c->ncase + q]);
+      tot += mx * sub + 2 + (c->precision == BCMG_PRECISION_SPLIT ? 1 : 0);
+    }
+    c->launches = tot;
+  }
   return BCMG_OK;
 }
 

@@ -134,6 +134,7 @@ __global__ void __launch_bounds__(T *T *T, 1) k_flux_fp64(FluxArgs a) {
   const int tid = threadIdx.x;
   const int tiles = nt * nt * nt;
   const int cube = a.cube0 + blockIdx.x / tiles;
+  if (!case_active(a.bt, cube)) return;  // converged case (uniform per CTA)
   const int tl = blockIdx.x % tiles;
   const int bi = 2 + (tl / (nt * nt)) * T, bj = 2 + ((tl / nt) % nt) * T, bk = 2 + (tl % nt) * T;
   const double *__restrict__ U = a.U1_;

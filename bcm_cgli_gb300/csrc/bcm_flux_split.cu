@@ -266,6 +266,7 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
   const int tid = threadIdx.x;
   const int tiles = nt * nt * nt;
   const int cube = a.cube0 + blockIdx.x / tiles;
+  if (!case_active(a.bt, cube)) return;  // converged case (uniform per CTA)
   const int tl = blockIdx.x % tiles;
   const int bi = 2 + (tl / (nt * nt)) * T, bj = 2 + ((tl / nt) % nt) * T, bk = 2 + (tl % nt) * T;
   const float *__restrict__ M = a.M;

@@ -89,6 +89,7 @@ __global__ void __launch_bounds__(kHaloThreads) k_iface_faces(InterfaceArgs a) {
   const int n = a.n, S = n + 4;
   const int t = blockIdx.x;
   const int c = a.task_cube[t];
+  if (!case_active(a.bt, c)) return;
   const FaceTask ft = a.tasks[t];
   const int ax = ft.axis;
   const int dbase = ft.side == 0 ? 0 : n + 2;
@@ -124,6 +125,7 @@ __global__ void __launch_bounds__(kHaloThreads) k_iface_faces(InterfaceArgs a) {
 __global__ void __launch_bounds__(kHaloThreads) k_iface_edges(InterfaceArgs a) {
   const int n = a.n, S = n + 4, nx = n + 1, nyy = n + 2;
   const int c = blockIdx.x + 1;
+  if (!case_active(a.bt, c)) return;
   double *U = a.U1_;
   auto Q = [&](int i, int j, int k) { return U + 5 * cell_index(S, c, i, j, k); };
   // Phase 1: i-edges, i = 2..nx.
@@ -182,6 +184,7 @@ cudaError_t launch_interface(const InterfaceArgs &a, int ncubes_total, cudaStrea
 __global__ void __launch_bounds__(kHaloThreads) k_bc(BcArgs a) {
   const int n = a.n, S = n + 4, nx = n + 1, nxx = n + 2, nxxx = n + 3;
   const int c = a.cubes[blockIdx.x];
+  if (!case_active(a.bt, c)) return;
   const int m = a.masks[blockIdx.x];
   double *U = a.U1_;
   auto Q = [&](int i, int j, int k) { return U + 5 * cell_index(S, c, i, j, k); };
@@ -265,6 +268,7 @@ __global__ void k_ghost(GhostArgs a, int count) {
   const int S = a.n + 4;
   const int b = (e - 1) * 4;
   const int c = a.IPsur[b + 1], i = a.IPsur[b + 2], j = a.IPsur[b + 3], k = a.IPsur[b + 4];
+  if (!case_active(a.bt, c)) return;
   double rho0 = a.rho0, P0 = a.P0;
   if (a.bt.cube_case) {  // the case of the stencil's cube
     const CaseConst &cq = a.bt.cases[a.bt.cube_case[c]];

@@ -26,7 +26,17 @@ struct CaseConst {
 struct Batch {
   const int *cube_case = nullptr;    // [ncube] case of each cube (slot 0 unused)
   const CaseConst *cases = nullptr;  // [ncase]
+  // Convergence-driven sub-iterations: active[q] == 0 once case q met the
+  // convergence test; kernels then leave its cubes alone.  nullptr: all
+  // cases active.
+  const int *active = nullptr;
 };
+__device__ __forceinline__ int case_of(const Batch &bt, int cube) {
+  return bt.cube_case ? bt.cube_case[cube] : 0;
+}
+__device__ __forceinline__ bool case_active(const Batch &bt, int cube) {
+  return !bt.active || bt.active[case_of(bt, cube)] != 0;
+}
 
 struct FluxArgs {
   Phys ph;
@@ -88,6 +98,7 @@ struct RkArgs {
   // flat numbering (c-1)*n^3 + r, so no block straddles two cases.  nullptr:
   // equal chunks over all cubes.
   const long long *blk_beg = nullptr;
+  Batch bt;
 };
 
 // Stage combination (BCM_Flux...cpp:2417-2599) and, at RK 3, the per-block
@@ -99,11 +110,12 @@ int rk_partial_blocks(const RkArgs &a);
 cudaError_t launch_rk_chunked(const RkArgs &a, long long chunk, int nblocks, cudaStream_t s);
 // Deterministic final reduction of partials -> er[1..7] (device, 8 doubles).
 cudaError_t launch_norms(const Phys &ph, const double *partials, int nblocks, double *er,
-                         cudaStream_t s);
+                         cudaStream_t s, const int *active = nullptr);
 // Batches: case q reduces partial blocks [case_blk[q], case_blk[q+1]) into
 // er[8q .. 8q+7] with its own normalisers.
 cudaError_t launch_norms_batch(int n, const CaseConst *cases, const int *case_blk, int ncase,
-                               const double *partials, double *er, cudaStream_t s);
+                               const double *partials, double *er, cudaStream_t s,
+                               const int *active = nullptr);
 // Batch form of launch_rk over an explicit block table (nblocks blocks).
 cudaError_t launch_rk_table(const RkArgs &a, int nblocks, cudaStream_t s);
 
@@ -157,6 +169,7 @@ struct InterfaceArgs {
   const int *task_cube;   // [ntasks] destination cube of each task
   const FaceTask *tasks;  // [ntasks]
   double *U1_;
+  Batch bt;
 };
 cudaError_t launch_interface(const InterfaceArgs &a, int ndst, cudaStream_t s);
 

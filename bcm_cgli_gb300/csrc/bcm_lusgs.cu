@@ -109,6 +109,7 @@ __global__ void __launch_bounds__(kLuMaxThreads) k_lusgs(LusgsArgs a) {
   extern __shared__ double buf[];  // [2][n*n][5] increments of the previous plane
   const int n = a.ph.n, S = n + 4, nn = n * n;
   const int cube = 1 + blockIdx.x;
+  if (!case_active(a.bt, cube)) return;  // converged case
   double dT = a.dT, mu_L = a.ph.mu_L, rho0 = a.ph.rho0, P0 = a.ph.P0;
   if (a.bt.cube_case) {
     const CaseConst *q = a.bt.cases + a.bt.cube_case[cube];

@@ -79,6 +79,7 @@ __global__ void __launch_bounds__(kLuMaxThreads) k_lusgs_split(LusgsSplitArgs a)
   extern __shared__ __align__(16) float fbuf[];  // [2][n*n][5]; later the reduction's doubles
   const int n = a.ph.n, S = n + 4, nn = n * n;
   const int cube = 1 + blockIdx.x;
+  if (!case_active(a.bt, cube)) return;  // converged case
   float dT = a.dTf, mu_L = a.mu_Lf, rho0 = a.rho0f, P0 = a.P0f, T0 = a.T0f;
   if (a.bt.cube_case) {
     const CaseConst *q = a.bt.cases + a.bt.cube_case[cube];

@@ -24,6 +24,7 @@ __global__ void __launch_bounds__(kRkThreads) k_rk(RkArgs a, long long total, lo
     beg = a.blk_beg[blockIdx.x];
     end = a.blk_beg[blockIdx.x + 1];
   }
+  if (beg < end && !case_active(a.bt, 1 + (int)(beg / ((long long)n * n * n)))) return;
   double s[7] = {0, 0, 0, 0, 0, 0, 0};
   for (long long t = beg + threadIdx.x; t < end; t += kRkThreads) {
     const int c = 1 + (int)(t / ((long long)n * n * n));
@@ -125,7 +126,9 @@ __device__ void write_norms(int n, int mpi_ncube, double rho0, double U0, const 
   er[7] = tot[6] / (0.5 * rho0 * U0 * U0 * 2.602);
 }
 
-__global__ void k_norms(Phys ph, const double *partials, int nblocks, double *er) {
+__global__ void k_norms(Phys ph, const double *partials, int nblocks, double *er,
+                        const int *active) {
+  if (active && !active[0]) return;
   __shared__ double tot[7];
   sum_partials(partials, 0, nblocks, tot);
   if (threadIdx.x == 0) write_norms(ph.n, ph.mpi_ncube, ph.rho0, ph.U0, tot, er);
@@ -133,9 +136,10 @@ __global__ void k_norms(Phys ph, const double *partials, int nblocks, double *er
 
 // One CTA per case of a batch.
 __global__ void k_norms_batch(int n, const CaseConst *cases, const int *case_blk,
-                              const double *partials, double *er) {
+                              const double *partials, double *er, const int *active) {
   __shared__ double tot[7];
   const int q = blockIdx.x;
+  if (active && !active[q]) return;
   sum_partials(partials, case_blk[q], case_blk[q + 1], tot);
   if (threadIdx.x == 0) {
     const CaseConst &c = cases[q];
@@ -170,15 +174,16 @@ cudaError_t launch_rk(const RkArgs &a, int *nblocks_out, cudaStream_t s) {
 }
 
 cudaError_t launch_norms(const Phys &ph, const double *partials, int nblocks, double *er,
-                         cudaStream_t s) {
-  k_norms<<<1, 7 * 32, 0, s>>>(ph, partials, nblocks, er);
+                         cudaStream_t s, const int *active) {
+  k_norms<<<1, 7 * 32, 0, s>>>(ph, partials, nblocks, er, active);
   return cudaGetLastError();
 }
 
 cudaError_t launch_norms_batch(int n, const CaseConst *cases, const int *case_blk, int ncase,
-                               const double *partials, double *er, cudaStream_t s) {
+                               const double *partials, double *er, cudaStream_t s,
+                               const int *active) {
   if (ncase <= 0) return cudaSuccess;
-  k_norms_batch<<<ncase, 7 * 32, 0, s>>>(n, cases, case_blk, partials, er);
+  k_norms_batch<<<ncase, 7 * 32, 0, s>>>(n, cases, case_blk, partials, er, active);
   return cudaGetLastError();
 }
 

@@ -182,6 +182,20 @@ int bcmg_case_stage(bcmg_case *c, int RK);
 int bcmg_case_advance(bcmg_case *c, int steps, int subiters, int use_graph, double *er,
                       double *emax);
 
+/* `steps` dual-time steps with the reference's convergence test
+ * (main.cpp:1249-1271): each step sub-iterates until every normalised
+ * change norm er[1..5] (E-normalised as in bcmg_case_advance) is below tol
+ * (the reference uses 0.02) or max_subiters sub-iterations ran (the
+ * reference's iteration_end_step), then shifts the time levels.  With
+ * use_graph != 0 each step is one CUDA graph launch whose sub-iteration loop
+ * is a device-side while node: no host round trip per sub-iteration.  In a
+ * batch each case stops on its own test (the kernels skip converged cases),
+ * so every case evolves as it would alone; the step ends when all cases
+ * have.  subiters_out[step * ncase + q] receives the sub-iterations case q
+ * took in each step (may be NULL); er and emax as in bcmg_case_advance. */
+int bcmg_case_advance_converged(bcmg_case *c, int steps, int max_subiters, double tol,
+                                int use_graph, int *subiters_out, double *er, double *emax);
+
 /* Waits for all work of the context. */
 int bcmg_case_sync(bcmg_case *c);
 

@@ -59,6 +59,16 @@ void bcmo_run_lusgs(const bcmo_phys *ph, int ncube, int steps, int subiters, dou
                     const int *yu, int nzl, int nzu, const int *zl, const int *zu, int nminus,
                     const double *wm, const int *gm, const int *im, int nplus,
                     const double *wp, const int *gp, const int *ip, double *er, double *Emax);
+void bcmo_run_converged(const bcmo_phys *ph, int ncube, int steps, int max_subiters, double tol,
+                        int method, double deltaT, double deltaTau, double cfl, double omega,
+                        double e, const int *FWS, const int *adj, const int *csl,
+                        const double *cube_size, double *U1_, double *U1, double *U1q,
+                        double *U1p1, double *U1p2, double *Rku1, double *Residual1, int nxl,
+                        int nxu, const int *xl, const int *xu, int nyl, int nyu, const int *yl,
+                        const int *yu, int nzl, int nzu, const int *zl, const int *zu,
+                        int nminus, const double *wm, const int *gm, const int *im, int nplus,
+                        const double *wp, const int *gp, const int *ip, double *er, double *Emax,
+                        int *iters_out);
 void bcmo_set_threads(int n);
 
 #ifdef __cplusplus

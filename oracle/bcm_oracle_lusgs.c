@@ -213,3 +213,47 @@ void bcmo_run_lusgs(const bcmo_phys *ph, int ncube, int steps, int subiters, dou
     bcmo_time_shift(ph, ncube, U1_, U1, U1q);
   }
 }
+
+/* The reference time loop with its convergence test (main.cpp:1146-1357):
+ * per step, sub-iterations (method 0: three RK stages as in bcmo_run;
+ * method 1: one LU-SGS update) until every normalised change norm er[1..5]
+ * is below tol or max_subiters ran (the reference's iteration_end_step),
+ * then the time shift.  iters_out[step] receives the sub-iteration counts. */
+void bcmo_run_converged(const bcmo_phys *ph, int ncube, int steps, int max_subiters, double tol,
+                        int method, double deltaT, double deltaTau, double cfl, double omega,
+                        double e, const int *FWS, const int *adj, const int *csl,
+                        const double *cube_size, double *U1_, double *U1, double *U1q,
+                        double *U1p1, double *U1p2, double *Rku1, double *Residual1, int nxl,
+                        int nxu, const int *xl, const int *xu, int nyl, int nyu, const int *yl,
+                        const int *yu, int nzl, int nzu, const int *zl, const int *zu,
+                        int nminus, const double *wm, const int *gm, const int *im, int nplus,
+                        const double *wp, const int *gp, const int *ip, double *er, double *Emax,
+                        int *iters_out) {
+  for (int step = 1; step <= steps; ++step) {
+    int it;
+    for (it = 1; it <= max_subiters; ++it) {
+      for (int RK = 1; RK <= (method == 1 ? 1 : 3); ++RK) {
+        bcmo_bc(ph, nxl, nxu, xl, xu, nyl, nyu, yl, yu, nzl, nzu, zl, zu, U1_);
+        if (nminus > 0) bcmo_ghost(ph, nminus, wm, gm, im, U1_);
+        if (nplus > 0) bcmo_ghost(ph, nplus, wp, gp, ip, U1_);
+        bcmo_interface(ph, ncube, adj, csl, U1_);
+        if (method == 1) {
+          bcmo_flux_stage(ph, ncube, 0, deltaT, deltaT, e, FWS, cube_size, U1_, U1, U1q, U1p1,
+                          U1p2, Rku1, Residual1, er);
+          bcmo_lusgs(ph, ncube, deltaT, cfl, omega, FWS, cube_size, U1_, Rku1, Residual1, er);
+        } else {
+          bcmo_flux_stage(ph, ncube, RK, deltaT, deltaTau, e, FWS, cube_size, U1_, U1, U1q, U1p1,
+                          U1p2, Rku1, Residual1, er);
+        }
+        bcmo_interface(ph, ncube, adj, csl, U1_);
+      }
+      for (int v = 1; v <= 5; ++v) {
+        Emax[v] = er[v] > Emax[v] ? er[v] : Emax[v];
+        er[v] = er[v] / Emax[v];
+      }
+      if (er[1] < tol && er[2] < tol && er[3] < tol && er[4] < tol && er[5] < tol) break;
+    }
+    iters_out[step - 1] = it > max_subiters ? max_subiters : it;
+    bcmo_time_shift(ph, ncube, U1_, U1, U1q);
+  }
+}

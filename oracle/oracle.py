@@ -108,6 +108,12 @@ class Port:
                                      _dp, _ip, _ip, C.c_int, _dp, _ip, _ip, _dp, _dp]
         L.bcmo_lusgs.argtypes = [P, C.c_int, C.c_double, C.c_double, C.c_double, _ip, _dp,
                                  _dp, _dp, _dp, _dp]
+        L.bcmo_run_converged.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int,
+                                         C.c_double, C.c_double, C.c_double, C.c_double,
+                                         C.c_double, _ip, _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp,
+                                         _dp, _dp, C.c_int, C.c_int, _ip, _ip, C.c_int, C.c_int,
+                                         _ip, _ip, C.c_int, C.c_int, _ip, _ip, C.c_int, _dp, _ip,
+                                         _ip, C.c_int, _dp, _ip, _ip, _dp, _dp, _ip]
         L.bcmo_set_threads.argtypes = [C.c_int]
 
     @staticmethod
@@ -152,6 +158,22 @@ class Port:
                                 _nz(xl), _nz(xu), len(yl), len(yu), _nz(yl), _nz(yu), len(zl),
                                 len(zu), _nz(zl), _nz(zu), nm, Wm, Gm, Im, npl, Wp, Gp, Ip,
                                 st.er, st.Emax)
+
+    def run_converged(self, case, st: State, steps: int, max_subiters: int, tol: float,
+                      method: int = 0, cfl: float = 0.0, omega: float = 1.5):
+        """The reference loop with its convergence test (main.cpp:1249-1271);
+        returns the sub-iteration count of each step."""
+        xl, xu, yl, yu, zl, zu = case.bc_lists()
+        nm, Wm, Gm, Im = _ibm(case, -1)
+        npl, Wp, Gp, Ip = _ibm(case, 1)
+        iters = np.zeros(max(1, steps), np.int32)
+        self.lib.bcmo_run_converged(
+            self.phys(case), case.ncube, steps, max_subiters, tol, method, case.dT, case.dTau,
+            cfl, omega, case.e, case.fws, _adj(case), case.csl, case.cube_size, st.U1_, st.U1,
+            st.U1q, st.U1p1, st.U1p2, st.Rku1, st.Residual1, len(xl), len(xu), _nz(xl), _nz(xu),
+            len(yl), len(yu), _nz(yl), _nz(yu), len(zl), len(zu), _nz(zl), _nz(zu), nm, Wm, Gm,
+            Im, npl, Wp, Gp, Ip, st.er, st.Emax, iters)
+        return iters[:steps]
 
     def residual(self, case, st: State):
         """The raw residual R(U1_) into st.Rku1 (fluid cells) and the force
@@ -254,6 +276,22 @@ class Ref:
                                 _nz(xl), _nz(xu), len(yl), len(yu), _nz(yl), _nz(yu), len(zl),
                                 len(zu), _nz(zl), _nz(zu), nm, Wm, Gm, Im, npl, Wp, Gp, Ip,
                                 st.er, st.Emax)
+
+    def run_converged(self, case, st: State, steps: int, max_subiters: int, tol: float,
+                      method: int = 0, cfl: float = 0.0, omega: float = 1.5):
+        """The reference loop with its convergence test (main.cpp:1249-1271);
+        returns the sub-iteration count of each step."""
+        xl, xu, yl, yu, zl, zu = case.bc_lists()
+        nm, Wm, Gm, Im = _ibm(case, -1)
+        npl, Wp, Gp, Ip = _ibm(case, 1)
+        iters = np.zeros(max(1, steps), np.int32)
+        self.lib.bcmo_run_converged(
+            self.phys(case), case.ncube, steps, max_subiters, tol, method, case.dT, case.dTau,
+            cfl, omega, case.e, case.fws, _adj(case), case.csl, case.cube_size, st.U1_, st.U1,
+            st.U1q, st.U1p1, st.U1p2, st.Rku1, st.Residual1, len(xl), len(xu), _nz(xl), _nz(xu),
+            len(yl), len(yu), _nz(yl), _nz(yu), len(zl), len(zu), _nz(zl), _nz(zu), nm, Wm, Gm,
+            Im, npl, Wp, Gp, Ip, st.er, st.Emax, iters)
+        return iters[:steps]
 
     def residual(self, case, st: State):
         """The raw residual R(U1_) into st.Rku1 (fluid cells) and the force
