@@ -16,6 +16,7 @@ Every call goes to the CUDA library; there is no CPU fallback.
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -270,6 +271,20 @@ class CaseContext:
         if isinstance(self, BatchContext):
             return er.reshape(self.ncase, 8), its.reshape(steps, self.ncase)
         return er, its
+
+    def output_q(self, path, q=-1, ncube_out=0):
+        """PLOT3D solution file of the current state (BCM_Output); returns once
+        the device snapshot is queued.  output_wait() waits for the file."""
+        check(lib().bcmg_case_output_q(self.h, int(q), int(ncube_out), os.fsencode(path)))
+
+    def output_wait(self):
+        check(lib().bcmg_case_output_wait(self.h))
+
+    def output_x(self, path, origin, q=-1, ncube_out=0):
+        """PLOT3D grid file from the cube corners origin[ncube][3]."""
+        o = np.ascontiguousarray(origin, dtype=np.float64)
+        check(lib().bcmg_case_output_x(self.h, int(q), int(ncube_out), os.fsencode(path),
+                                       o.ctypes.data))
 
     def sync(self):
         check(lib().bcmg_case_sync(self.h))

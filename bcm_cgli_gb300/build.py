@@ -32,6 +32,7 @@ UNITS = [
     ("bcm_noalloc.cu", ["--fmad=false"]),
     ("bcm_lusgs.cu", ["--fmad=false"]),
     ("bcm_lusgs_split.cu", ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"]),
+    ("bcm_output.cu", ["--fmad=false"]),
     ("bcm_tables.cpp", []),
 ]
 

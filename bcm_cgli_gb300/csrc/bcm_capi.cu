@@ -8,6 +8,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/bcm_gb300.h"
@@ -227,6 +228,17 @@ struct bcmg_case {
   cudaGraphExec_t cgraph = nullptr;  // step graph with the while node
   int cgraph_max = -1, cgraph_method = -1;
   double cgraph_tol = -1;
+  // PLOT3D output (bcmg_case_output_*): device byte image, a side stream for
+  // the copies, two pinned chunks and the writer thread.
+  int device = 0;
+  double *out_dev = nullptr;
+  size_t out_cap = 0;  // doubles
+  cudaStream_t out_stream = nullptr;
+  cudaEvent_t out_ready = nullptr, out_chunk[2] = {nullptr, nullptr};
+  char *out_host[2] = {nullptr, nullptr};
+  std::thread out_thread;
+  int out_status = 0;
+  std::string out_err;
   Batch bt() const {
     Batch b;
     if (batched) {
@@ -246,7 +258,23 @@ struct bcmg_case {
   long long flux_launches = 0;
   std::vector<cudaEvent_t> marks;  // bcmg_case_timer_mark slots
 
+  void join_output() {
+    if (out_thread.joinable()) out_thread.join();
+  }
   void release() {
+    join_output();
+    if (out_dev) cudaFree(out_dev);
+    out_dev = nullptr;
+    for (int i = 0; i < 2; ++i) {
+      if (out_host[i]) cudaFreeHost(out_host[i]);
+      out_host[i] = nullptr;
+      if (out_chunk[i]) cudaEventDestroy(out_chunk[i]);
+      out_chunk[i] = nullptr;
+    }
+    if (out_ready) cudaEventDestroy(out_ready);
+    out_ready = nullptr;
+    if (out_stream) cudaStreamDestroy(out_stream);
+    out_stream = nullptr;
     for (auto x : marks)
       if (x) cudaEventDestroy(x);
     marks.clear();
@@ -673,6 +701,7 @@ int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out)
   c->e = d->e;
   c->precision = d->precision;
   c->ncell = (size_t)d->ncube * c->S * c->S * c->S;
+  cudaGetDevice(&c->device);
   if (bi) {
     c->batched = true;
     c->ncase = (int)bi->cases.size();
@@ -1281,6 +1310,153 @@ int bcmg_case_advance_converged(bcmg_case *c, int steps, int max_subiters, doubl
     c->launches = tot;
   }
   return BCMG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// PLOT3D output (BCM_Output.cpp:16-300).  The byte image is formed on the
+// device on the context's stream (a snapshot: later solver work may proceed
+// at once); a writer thread copies it to the host in pinned chunks on a side
+// stream and writes the file, so the copy and the disk write overlap the
+// solver.  Only one output is in flight: the next output call (or
+// bcmg_case_output_wait / destroy) waits for it.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kOutChunk = (size_t)32 << 20;  // bytes per pinned chunk
+
+int out_range(bcmg_case *c, int q, int *g0, int *ng) {
+  if (q < 0) {
+    *g0 = 1;
+    *ng = c->ncube - 1;
+    return BCMG_OK;
+  }
+  int nq = 0;
+  int r = bcmg_case_case_cubes(c, q, g0, &nq);
+  *ng = nq - 1;
+  return r;
+}
+
+int out_prepare(bcmg_case *c, size_t ndoubles) {
+  c->join_output();
+  if (!c->out_stream) {
+    CK(cudaStreamCreateWithFlags(&c->out_stream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&c->out_ready, cudaEventDisableTiming));
+    for (int i = 0; i < 2; ++i) {
+      CK(cudaEventCreateWithFlags(&c->out_chunk[i], cudaEventDisableTiming));
+      CK(cudaMallocHost((void **)&c->out_host[i], kOutChunk));
+    }
+  }
+  if (ndoubles > c->out_cap) {
+    if (c->out_dev) cudaFree(c->out_dev);
+    c->out_dev = nullptr;
+    c->out_cap = 0;
+    CK(cudaMalloc((void **)&c->out_dev, ndoubles * sizeof(double)));
+    c->out_cap = ndoubles;
+  }
+  return BCMG_OK;
+}
+
+// Writer thread body: header, then the device image in pinned chunks.
+void out_write(bcmg_case *c, std::string path, std::vector<int> header, size_t bytes) {
+  auto fail = [&](const std::string &m) {
+    c->out_status = BCMG_ERR_CUDA;
+    c->out_err = m;
+  };
+  cudaSetDevice(c->device);
+  FILE *f = std::fopen(path.c_str(), "wb");
+  if (!f) {
+    c->out_status = BCMG_ERR_ARG;
+    c->out_err = "cannot open " + path;
+    return;
+  }
+  bool ok = std::fwrite(header.data(), sizeof(int), header.size(), f) == header.size();
+  const char *src = reinterpret_cast<const char *>(c->out_dev);
+  auto issue = [&](size_t off, int slot) {
+    const size_t len = std::min(kOutChunk, bytes - off);
+    cudaError_t e = cudaMemcpyAsync(c->out_host[slot], src + off, len, cudaMemcpyDeviceToHost,
+                                    c->out_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(c->out_chunk[slot], c->out_stream);
+    return e;
+  };
+  cudaError_t e = cudaSuccess;
+  if (bytes > 0) e = issue(0, 0);
+  int slot = 0;
+  for (size_t off = 0; ok && e == cudaSuccess && off < bytes; off += kOutChunk, slot ^= 1) {
+    if (off + kOutChunk < bytes) e = issue(off + kOutChunk, slot ^ 1);
+    if (e != cudaSuccess) break;
+    e = cudaEventSynchronize(c->out_chunk[slot]);
+    if (e != cudaSuccess) break;
+    const size_t len = std::min(kOutChunk, bytes - off);
+    ok = std::fwrite(c->out_host[slot], 1, len, f) == len;
+  }
+  if (std::fclose(f) != 0) ok = false;
+  if (e != cudaSuccess)
+    fail(std::string("output copy: ") + cudaGetErrorString(e));
+  else if (!ok)
+    fail("write failed: " + path);
+  else
+    c->out_status = BCMG_OK;
+}
+
+int out_launch(bcmg_case *c, const char *path, int ncube_out, int ng, size_t ndoubles) {
+  std::vector<int> header(1 + 3 * (size_t)ncube_out, c->ph.n + 2);
+  header[0] = ncube_out;
+  CK(cudaEventRecord(c->out_ready, c->stream));
+  CK(cudaStreamWaitEvent(c->out_stream, c->out_ready, 0));
+  c->out_status = BCMG_OK;
+  c->out_err.clear();
+  c->out_thread = std::thread(out_write, c, std::string(path), std::move(header),
+                              ndoubles * sizeof(double));
+  (void)ng;
+  return BCMG_OK;
+}
+
+}  // namespace
+
+int bcmg_case_output_q(bcmg_case *c, int q, int ncube_out, const char *path) {
+  clear_err();
+  if (!c || !path) { set_err("null argument"); return BCMG_ERR_ARG; }
+  int g0 = 0, ng = 0, r;
+  if ((r = out_range(c, q, &g0, &ng))) return r;
+  if (ncube_out <= 0) ncube_out = ng;
+  const size_t m = c->ph.n + 2;
+  const size_t nd = (4 + 5 * m * m * m) * (size_t)ng;
+  if ((r = out_prepare(c, nd))) return r;
+  CK(launch_plot3d_q(c->U1_, c->out_dev, c->ph.n, g0, ng, c->stream));
+  return out_launch(c, path, ncube_out, ng, nd);
+}
+
+int bcmg_case_output_x(bcmg_case *c, int q, int ncube_out, const char *path,
+                       const double *origin) {
+  clear_err();
+  if (!c || !path || !origin) { set_err("null argument"); return BCMG_ERR_ARG; }
+  int g0 = 0, ng = 0, r;
+  if ((r = out_range(c, q, &g0, &ng))) return r;
+  if (ncube_out <= 0) ncube_out = ng;
+  const size_t m = c->ph.n + 2;
+  const size_t nd = 3 * m * m * m * (size_t)ng;
+  if ((r = out_prepare(c, nd))) return r;
+  double *dorig = nullptr;
+  CK(dalloc(&dorig, 3 * (size_t)std::max(ng, 1)));
+  // origin rows of the written cubes: the case's own cubes 1.. (q >= 0) or
+  // the flat list's cubes 1.. (q < 0)
+  cudaError_t e = cudaMemcpyAsync(dorig, origin + 3, 3 * sizeof(double) * ng,
+                                  cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess)
+    e = launch_plot3d_x(c->cube_size, dorig, c->out_dev, c->ph.n, g0, ng, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(dorig);
+  CK(e);
+  if ((r = out_launch(c, path, ncube_out, ng, nd))) return r;
+  return bcmg_case_output_wait(c);
+}
+
+int bcmg_case_output_wait(bcmg_case *c) {
+  clear_err();
+  if (!c) { set_err("null context"); return BCMG_ERR_ARG; }
+  c->join_output();
+  if (c->out_status) set_err(c->out_err);
+  return c->out_status;
 }
 
 int bcmg_case_ncase(const bcmg_case *c) { return c ? c->ncase : 0; }

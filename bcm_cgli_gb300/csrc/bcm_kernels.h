@@ -154,6 +154,14 @@ struct LusgsSplitArgs {
 };
 cudaError_t launch_lusgs_split(const LusgsSplitArgs &a, int ncubes, cudaStream_t s);
 
+// PLOT3D byte images of BCM_Output (bcm_output.cu) for cubes
+// [cube0, cube0 + ncubes): solution (4 + 5 (n+2)^3 doubles per cube) and
+// grid (3 (n+2)^3 doubles per cube; origin [ncubes][3] of those cubes).
+cudaError_t launch_plot3d_q(const double *U, double *out, int n, int cube0, int ncubes,
+                            cudaStream_t s);
+cudaError_t launch_plot3d_x(const double *cube_size, const double *origin, double *out, int n,
+                            int cube0, int ncubes, cudaStream_t s);
+
 // Interface: face-copy tasks (destination cube, source cube, axis, side) built
 // on the host, then the ordered three-phase edge fill of every cube.
 struct FaceTask {

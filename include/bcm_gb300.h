@@ -196,6 +196,28 @@ int bcmg_case_advance(bcmg_case *c, int steps, int subiters, int use_graph, doub
 int bcmg_case_advance_converged(bcmg_case *c, int steps, int max_subiters, double tol,
                                 int use_graph, int *subiters_out, double *er, double *emax);
 
+/* PLOT3D output of BCM_Output (BCM_Output.cpp:16-300), byte-compatible:
+ * raw native-endian files, header int32 ncube_out then (n+2, n+2, n+2) for
+ * each of ncube_out cubes (the reference writes MPI_Ncube; <= 0 here means
+ * the number of cubes written), then per cube the padded indices 1..n+2
+ * with the first array index fastest.  Case q of a batch (q < 0: every cube
+ * of the context).
+ * bcmg_case_output_q writes the solution file (four 1.0 doubles and the
+ * five variables of the current state U1_ per cube, main.cpp:1348)
+ * asynchronously: it returns once the device snapshot is queued on the
+ * context's stream, so solver calls may follow at once; the host copy and
+ * the file write proceed on a side stream and a writer thread.
+ * bcmg_case_output_wait waits for that write and returns its status (a
+ * following output call or bcmg_case_destroy also waits).
+ * bcmg_case_output_x writes the grid file synchronously: cell centres
+ * origin + (i - 1.5) dx (BCM_Grid.cpp:124-148) from origin[ncube][3] (the
+ * cube corners Xcube, Ycube, Zcube; rows of the case's own numbering, row 0
+ * unused). */
+int bcmg_case_output_q(bcmg_case *c, int q, int ncube_out, const char *path);
+int bcmg_case_output_x(bcmg_case *c, int q, int ncube_out, const char *path,
+                       const double *origin);
+int bcmg_case_output_wait(bcmg_case *c);
+
 /* Waits for all work of the context. */
 int bcmg_case_sync(bcmg_case *c);
 

@@ -232,6 +232,7 @@ class Ref:
         L.ref_interface.argtypes = [_dp]
         L.ref_interface_list.argtypes = [C.c_int, _ip]
         L.ref_set_threads.argtypes = [C.c_int]
+        L.ref_output.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp]
         L.ref_run.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                               _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.c_int,
                               C.c_int, _ip, _ip, C.c_int, C.c_int, _ip, _ip, C.c_int, C.c_int,
@@ -263,40 +264,18 @@ class Ref:
     def interface(self, case, U):
         self.lib.ref_interface(U)
 
-    def run_lusgs(self, case, st: State, steps: int, subiters: int, cfl: float = 0.0,
-                  omega: float = 1.5):
-        """bcmo_run with one LU-SGS update per sub-iteration (no reference
-        counterpart; see bcm_oracle_lusgs.c)."""
-        xl, xu, yl, yu, zl, zu = case.bc_lists()
-        nm, Wm, Gm, Im = _ibm(case, -1)
-        npl, Wp, Gp, Ip = _ibm(case, 1)
-        self.lib.bcmo_run_lusgs(self.phys(case), case.ncube, steps, subiters, case.dT, cfl,
-                                omega, case.e, case.fws, _adj(case), case.csl, case.cube_size,
-                                st.U1_, st.U1, st.U1q, st.Rku1, st.Residual1, len(xl), len(xu),
-                                _nz(xl), _nz(xu), len(yl), len(yu), _nz(yl), _nz(yu), len(zl),
-                                len(zu), _nz(zl), _nz(zu), nm, Wm, Gm, Im, npl, Wp, Gp, Ip,
-                                st.er, st.Emax)
-
-    def run_converged(self, case, st: State, steps: int, max_subiters: int, tol: float,
-                      method: int = 0, cfl: float = 0.0, omega: float = 1.5):
-        """The reference loop with its convergence test (main.cpp:1249-1271);
-        returns the sub-iteration count of each step."""
-        xl, xu, yl, yu, zl, zu = case.bc_lists()
-        nm, Wm, Gm, Im = _ibm(case, -1)
-        npl, Wp, Gp, Ip = _ibm(case, 1)
-        iters = np.zeros(max(1, steps), np.int32)
-        self.lib.bcmo_run_converged(
-            self.phys(case), case.ncube, steps, max_subiters, tol, method, case.dT, case.dTau,
-            cfl, omega, case.e, case.fws, _adj(case), case.csl, case.cube_size, st.U1_, st.U1,
-            st.U1q, st.U1p1, st.U1p2, st.Rku1, st.Residual1, len(xl), len(xu), _nz(xl), _nz(xu),
-            len(yl), len(yu), _nz(yl), _nz(yu), len(zl), len(zu), _nz(zl), _nz(zu), nm, Wm, Gm,
-            Im, npl, Wp, Gp, Ip, st.er, st.Emax, iters)
-        return iters[:steps]
-
-    def residual(self, case, st: State):
-        """The raw residual R(U1_) into st.Rku1 (fluid cells) and the force
-        integrands into st.Residual1 (bcmo_flux_stage with RK = 0)."""
-        self.flux_stage(case, st, 0)
+    def output(self, case, U, step: int, directory: str):
+        """The reference's BCM_Output of U into `directory` (BCMdata00001.x and
+        qBCMdata<step>.q)."""
+        cwd = os.getcwd()
+        os.chdir(directory)
+        try:
+            o = np.ascontiguousarray(case.origin, dtype=np.float64)
+            self.lib.ref_output(case.ncube, step, U, case.cube_size,
+                                np.ascontiguousarray(o[:, 0]), np.ascontiguousarray(o[:, 1]),
+                                np.ascontiguousarray(o[:, 2]))
+        finally:
+            os.chdir(cwd)
 
     def run(self, case, st: State, steps: int, subiters: int):
         xl, xu, yl, yu, zl, zu = (_one_based(a) for a in case.bc_lists())

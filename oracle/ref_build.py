@@ -45,6 +45,7 @@ REF_SOURCES = [
     "BCM_X_boundary_condition.cpp",
     "BCM_Y_boundary_condition.cpp",
     "BCM_Z_boundary_condition.cpp",
+    "BCM_Output.cpp",
 ]
 
 

@@ -179,4 +179,28 @@ void ref_run(int ncube, int steps, int subiters, double dT, double dTau, double 
   }
 }
 
+/* BCM_Output (BCM_Output.cpp:16-300) on one rank: the PLOT3D grid file
+ * BCMdata00001.x and solution file qBCMdata<step>.q of U1 in the current
+ * directory.  Cell-centre coordinates as BCM_Grid.cpp:124-148 forms them
+ * from the cube origins. */
+void ref_output(int ncube, int step, double *U1, double *cube_size, const double *Xcube,
+                const double *Ycube, const double *Zcube) {
+  Ncube = ncube;
+  int (*rank_map)[MPI_Ncube] = (int (*)[MPI_Ncube])calloc(2 * (size_t)MPI_Ncube, sizeof(int));
+  double (*Xcnt)[X_size] = (double (*)[X_size])calloc((size_t)ncube * X_size, sizeof(double));
+  double (*Ycnt)[Y_size] = (double (*)[Y_size])calloc((size_t)ncube * Y_size, sizeof(double));
+  double (*Zcnt)[Z_size] = (double (*)[Z_size])calloc((size_t)ncube * Z_size, sizeof(double));
+  for (int c = 1; c < ncube; ++c) {
+    double dx = cube_size[c] / NcubeX, dy = cube_size[c] / NcubeY, dz = cube_size[c] / NcubeZ;
+    for (int i = 0; i < X_size; ++i) Xcnt[c][i] = Xcube[c] + (i - 1.5) * dx;
+    for (int j = 0; j < Y_size; ++j) Ycnt[c][j] = Ycube[c] + (j - 1.5) * dy;
+    for (int k = 0; k < Z_size; ++k) Zcnt[c][k] = Zcube[c] + (k - 1.5) * dz;
+  }
+  BCM_Output(0, ncube, step, rank_map, (Cell *)U1, (Cell *)U1, cube_size, Xcnt, Ycnt, Zcnt);
+  free(rank_map);
+  free(Xcnt);
+  free(Ycnt);
+  free(Zcnt);
+}
+
 }  // extern "C"

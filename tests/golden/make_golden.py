@@ -11,6 +11,7 @@ import hashlib
 import json
 import os
 import sys
+import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
@@ -55,6 +56,12 @@ def main():
         rec["run_er"] = [repr(float(x)) for x in st.er]
         rec["run_emax"] = [repr(float(x)) for x in st.Emax]
         rec["run_sum"] = [repr(float(x)) for x in st.U1_.reshape(-1, 5).sum(axis=0)]
+        # the reference's PLOT3D writer (BCM_Output.cpp) on the final state
+        with tempfile.TemporaryDirectory() as d:
+            ref.output(case, st.U1_, 7, d)
+            for key, fn in (("plot3d_x", "BCMdata00001.x"), ("plot3d_q", "qBCMdata00007.q")):
+                with open(os.path.join(d, fn), "rb") as f:
+                    rec[key] = hashlib.sha256(f.read()).hexdigest()
         out[name] = rec
         print(name, "done", file=sys.stderr)
     with open(os.path.join(HERE, "golden.json"), "w") as f:

@@ -87,3 +87,33 @@ def test_oracle_thread_count_invariant():
         out.append((st.U1_.copy(), st.er.copy()))
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("name", sorted(GOLD["cases"]))
+def test_plot3d_restatement_matches_reference_writer(port, name):
+    """oracle/plot3d.py reproduces the bytes of the reference's BCM_Output
+    (grid and solution files of the final state of the golden run)."""
+    import plot3d
+    case = G.golden_cases()[name]
+    rec = GOLD["cases"][name]
+    st = O.State(case)
+    port.run(case, st, GOLD["steps"], GOLD["subiters"])
+    x = plot3d.grid_bytes(case.n, case.ncube, case.cube_size, case.origin, case.phys.mpi_ncube)
+    q = plot3d.solution_bytes(case.n, st.U1_, case.phys.mpi_ncube)
+    assert hashlib.sha256(x).hexdigest() == rec["plot3d_x"]
+    assert hashlib.sha256(q).hexdigest() == rec["plot3d_q"]
+
+
+@pytest.mark.skipif(not O.reference_available(), reason="reference sources not present")
+def test_plot3d_restatement_equals_reference_writer_directly(tmp_path):
+    """A larger two-level case through the reference's own BCM_Output."""
+    import plot3d
+    from bcm_cgli_gb300 import cases
+    case = cases.random_two_level_case(seed=21, n=8, periodic=False)
+    ref = O.Ref(case)
+    ref.output(case, case.U.copy(), 12, str(tmp_path))
+    x = (tmp_path / "BCMdata00001.x").read_bytes()
+    q = (tmp_path / "qBCMdata00012.q").read_bytes()
+    assert x == plot3d.grid_bytes(case.n, case.ncube, case.cube_size, case.origin,
+                                  case.phys.mpi_ncube)
+    assert q == plot3d.solution_bytes(case.n, case.U, case.phys.mpi_ncube)
