@@ -107,16 +107,26 @@ def workload_config(case, precision):
 # distributed helpers (timing only)
 # ---------------------------------------------------------------------------
 class Dist:
-    def __init__(self, gpus: int):
+    """Rank bookkeeping of a torchrun launch.  Every rank advances its own
+    replica of the case (the path has no data exchange between replicas);
+    the process group only brackets the timed region with barriers and takes
+    the maximum time over ranks.  NCCL on GPUs, gloo where there is none."""
+
+    def __init__(self, gpus: int, backend: str | None = None):
         self.world = int(os.environ.get("WORLD_SIZE", "1"))
         self.rank = int(os.environ.get("RANK", "0"))
         self.local = int(os.environ.get("LOCAL_RANK", "0"))
         self.pg = None
+        self.device = "cpu"
         if self.world > 1:
             import torch
             import torch.distributed as dist
-            torch.cuda.set_device(self.local)
-            dist.init_process_group("nccl")
+            if backend is None:
+                backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local)
+                self.device = "cuda"
+            dist.init_process_group(backend)
             self.pg = dist
             self.torch = torch
 
@@ -127,9 +137,14 @@ class Dist:
     def max(self, x: float) -> float:
         if not self.pg:
             return x
-        t = self.torch.tensor([x], dtype=self.torch.float64, device="cuda")
+        t = self.torch.tensor([x], dtype=self.torch.float64, device=self.device)
         self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
         return float(t.item())
+
+    def throughput(self, units_per_rank: float, ms: float) -> float:
+        """Whole-job rate: the units all ranks processed over the slowest
+        rank's time (ms already max-reduced)."""
+        return units_per_rank * self.world / (ms * 1e-3)
 
     def close(self):
         if self.pg:
@@ -280,7 +295,8 @@ def measure(api, case, precision_name, args, dist, clocks_on=True):
     flux_ms, flux_n = ctx.profile()
     ctx.set_profiling(False)
     cell_subiters = case.n_cells * SUBITERS * args.steps * dist.world
-    out = {"value": cell_subiters / (ms * 1e-3), "ms_per_step": ms / args.steps,
+    out = {"value": dist.throughput(case.n_cells * SUBITERS * args.steps, ms),
+           "ms_per_step": ms / args.steps,
            "launches": launches, "flux_ms_avg": flux_ms / max(1, flux_n), "flux_launches": flux_n,
            "clocks": clk, "ctx": ctx}
     return out
@@ -307,6 +323,33 @@ def measure_e2e(ctx, case, args, dist, cell_subiters):
     dist.barrier()
     ms_e2e = dist.max(ctx.timer_elapsed(2, 3))
     return cell_subiters / (ms_e2e * 1e-3)
+
+
+def measure_converged(api, case, precision_name, method, args, dist, steps=2, max_subiters=50,
+                      tol=0.02):
+    """Physical steps with the reference's convergence test (main.cpp:1249-
+    1271: every E-normalised change norm below tol, else max_subiters), one
+    graph launch per step with the sub-iteration loop on the device; from
+    the initial state, after one untimed step that builds the graph."""
+    precision = api.PRECISION_SPLIT if precision_name == "split" else api.PRECISION_FP64
+    ctx = make_context(api, case, precision)
+    ctx.set_method(api.METHOD_LUSGS if method == "lusgs" else api.METHOD_RK3)
+    ctx.set_state(case.U, case.U, case.U)
+    ctx.advance_converged(1, max_subiters, tol)
+    ctx.set_state(case.U, case.U, case.U)
+    ctx.emax[...] = 0
+    dist.barrier()
+    ctx.sync()
+    ctx.timer_mark(4)
+    _, its = ctx.advance_converged(steps, max_subiters, tol)
+    ctx.timer_mark(5)
+    ctx.sync()
+    ms = dist.max(ctx.timer_elapsed(4, 5))
+    ctx.close()
+    its = np.asarray(its).reshape(steps, -1)
+    return {"ms_per_physical_step": ms / steps,
+            "subiters_per_step": its.max(axis=1).tolist(),
+            "converged": bool((its < max_subiters).all())}
 
 
 def rel_l2(a, b, n):
@@ -413,6 +456,16 @@ def run_gpu_arm(args, dist):
                                          else m_other["value"] / line["value"])
     if acc is not None:
         line["accuracy"] = acc
+    if not args.no_converged and not args.quick:
+        conv = {m: measure_converged(api, case, head, m, args, dist) for m in ("rk3", "lusgs")}
+        conv["tol"] = 0.02
+        conv["max_subiters"] = 50
+        conv["precision"] = head
+        conv["note"] = ("physical steps with the reference's convergence test "
+                        "(main.cpp:1249-1271); RK3 at the reference's dTau=dT/200")
+        conv["lusgs_speedup_per_physical_step"] = (conv["rk3"]["ms_per_physical_step"] /
+                                                   conv["lusgs"]["ms_per_physical_step"])
+        line["converged_step"] = conv
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample(case, subiters=1)
     for m in (m_head, m_other):
@@ -449,6 +502,8 @@ def main():
                          "reported beside it)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end measurement")
+    ap.add_argument("--no-converged", action="store_true",
+                    help="skip the convergence-test (RK3 vs LU-SGS) physical-step timing")
     ap.add_argument("--quick", action="store_true",
                     help="headline path only (no second precision, no accuracy check)")
     ap.add_argument("--flux-only", action="store_true",
