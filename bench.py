@@ -491,6 +491,27 @@ def run_flux_only(args):
                       "cell_stages_per_s": case.n_cells / (ms * 1e-3)}), flush=True)
 
 
+def run_lusgs_only(args):
+    """Profiling target: LU-SGS sub-iterations (residual + sweeps) on a
+    Taylor-Green case of ncx^3 cubes of 24^3 cells, `steps` sub-iterations
+    after one warm-up step."""
+    from bcm_cgli_gb300 import api, cases
+    case = cases.taylor_green(ncx=args.ncx, n=24)
+    prec = api.PRECISION_SPLIT if args.precision == "split" else api.PRECISION_FP64
+    ctx = api.CaseContext(case, precision=prec)
+    ctx.set_method(api.METHOD_LUSGS)
+    ctx.set_state(case.U, case.U, case.U)
+    ctx.advance(1, 1, use_graph=False)
+    ctx.sync()
+    ctx.timer_mark(0)
+    ctx.advance(1, max(1, args.steps), use_graph=False)
+    ctx.timer_mark(1)
+    ms = ctx.timer_elapsed(0, 1)
+    ctx.close()
+    print(json.dumps({"lusgs_only": args.precision, "cells": case.n_cells,
+                      "ms_per_subiter": ms / max(1, args.steps)}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -508,7 +529,10 @@ def main():
                     help="headline path only (no second precision, no accuracy check)")
     ap.add_argument("--flux-only", action="store_true",
                     help="time the flux kernel alone on a smaller case (profiling target)")
-    ap.add_argument("--ncx", type=int, default=6, help="cubes per edge for --flux-only")
+    ap.add_argument("--lusgs-only", action="store_true",
+                    help="LU-SGS sub-iterations alone on a smaller case (profiling target)")
+    ap.add_argument("--ncx", type=int, default=6,
+                    help="cubes per edge for --flux-only / --lusgs-only")
     ap.add_argument("--method", default="rk3", choices=["rk3", "lusgs"],
                     help="sub-iteration method (rk3: the reference's RK; lusgs: LU-SGS sweeps)")
     ap.add_argument("--workload", default="tgv", choices=sorted(WORKLOADS),
@@ -519,6 +543,9 @@ def main():
     WORKLOAD = args.workload
     if args.flux_only:
         run_flux_only(args)
+        return
+    if args.lusgs_only:
+        run_lusgs_only(args)
         return
     if args.impl == "reference":
         # Rank 0 alone times the CPU implementation; other ranks exit at once.
