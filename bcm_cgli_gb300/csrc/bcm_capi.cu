@@ -228,6 +228,7 @@ struct bcmg_case {
   cudaGraphExec_t cgraph = nullptr;  // step graph with the while node
   int cgraph_max = -1, cgraph_method = -1;
   double cgraph_tol = -1;
+  float *lu_scr = nullptr;  // split LU-SGS sweep scratch
   // PLOT3D output (bcmg_case_output_*): device byte image, a side stream for
   // the copies, two pinned chunks and the writer thread.
   int device = 0;
@@ -282,7 +283,7 @@ struct bcmg_case {
     graph = nullptr;
     if (cgraph) cudaGraphExecDestroy(cgraph);
     cgraph = nullptr;
-    dfree(active); dfree(iters); dfree(cont);
+    dfree(active); dfree(iters); dfree(cont); dfree(lu_scr);
     for (auto x : ev) cudaEventDestroy(x);
     ev.clear();
     dfree(U1_); dfree(U1); dfree(U1q); dfree(U1p1); dfree(U1p2); dfree(Rku1); dfree(Residual1);
@@ -424,8 +425,8 @@ int case_lusgs(bcmg_case *c) {
     l.inv_dx = c->inv_dx;
     l.M = c->M;
     l.U1_ = c->U1_;
-    l.R32 = reinterpret_cast<float *>(c->Rku1);
-    l.coef = reinterpret_cast<float *>(c->U1p1);  // 10 floats per cell
+    l.R32 = reinterpret_cast<const float *>(c->Rku1);
+    l.scr = c->lu_scr;
     l.Residual1 = c->Residual1;
     l.partials = c->partials;
     l.bt = c->bt();
@@ -1214,6 +1215,12 @@ int bcmg_case_set_method(bcmg_case *c, int method, double cfl, double omega) {
     set_err("LU-SGS needs cfl >= 0 (0: no pseudo-time term) and 1 <= omega <= 4");
     return BCMG_ERR_ARG;
   }
+  if (method == BCMG_METHOD_LUSGS && c->ph.n * c->ph.n > 1024) {
+    set_err("LU-SGS needs n <= 32 (one thread per cube column)");
+    return BCMG_ERR_ARG;
+  }
+  if (method == BCMG_METHOD_LUSGS && c->precision == BCMG_PRECISION_SPLIT && !c->lu_scr)
+    CK(dalloc(&c->lu_scr, lusgs_split_scratch(c->ph.n) * (size_t)(c->ncube - 1)));
   c->method = method;
   c->lu_cfl = cfl;
   c->lu_omega = omega;

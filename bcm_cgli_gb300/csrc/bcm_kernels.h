@@ -146,13 +146,15 @@ struct LusgsSplitArgs {
   const float *inv_dx;     // [ncube] n / cube_size
   const float *M;          // FP32 deltas of the state
   double *U1_;             // updated in place on fluid cells
-  float *R32;              // in: residual; out: increment
-  float *coef;             // [ncell][10] scratch
+  const float *R32;        // residual (FP32) of every cell
+  float *scr;              // [ncube-1][11][n^3] sweep scratch (lusgs_split_scratch)
   const double *Residual1;
   double *partials;        // [ncube-1][7]
   Batch bt;
 };
 cudaError_t launch_lusgs_split(const LusgsSplitArgs &a, int ncubes, cudaStream_t s);
+// Floats of that scratch per cube.
+size_t lusgs_split_scratch(int n);
 
 // PLOT3D byte images of BCM_Output (bcm_output.cu) for cubes
 // [cube0, cube0 + ncubes): solution (4 + 5 (n+2)^3 doubles per cube) and

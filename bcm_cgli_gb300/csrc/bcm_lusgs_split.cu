@@ -1,8 +1,11 @@
 // Split-precision LU-SGS sub-iteration: the sweeps in FP32, the update and
 // norm sums in FP64.  Same scheme and parallel form as the FP64 kernel
 // (bcm_lusgs.cu): per cube, forward and backward sweeps over the planes
-// i+j+k = const, thread column (a, b) owning cells (a, b, h-a-b), the
-// previous plane's increments double-buffered in shared memory.  The sweep
+// i+j+k = const, the previous plane's values double-buffered in shared memory.  The cube's
+// inputs are first packed into a scratch in plane order, so the cells of a
+// plane are consecutive: they go to consecutive threads (full warps) and the
+// sequential sweeps read and write consecutive words; the update runs
+// afterwards slab by slab in memory order.  The sweep
 // is a preconditioner of the dual-time iteration (the FP32 residual it is
 // fed decides the converged state), so its coefficients come from the FP32
 // mirror of the state: deltas from the case's reference state (rho0, 0, 0,
@@ -11,16 +14,14 @@
 // in FP64, as in the split RK path.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "bcm_common.cuh"
 #include "bcm_kernels.h"
 
 namespace bcmg {
 
-int lusgs_threads(int n);
-
 namespace {
-
-constexpr int kLuMaxThreads = 288;
 
 // Cell coefficients U, V, W, VV, H, r_x, r_y, r_z, nu, dg from the FP32
 // deltas m (rho' = m0, rho u = m1.., E' = m4).
@@ -66,18 +67,26 @@ __device__ __forceinline__ void luf_off(const float *k, float idx, float omega, 
     s[m] += LOWER ? h * (a[m] + w * dq[m]) + v * dq[m] : h * (a[m] - w * dq[m]) - v * dq[m];
 }
 
-template <int D, bool LOWER>
-__device__ __forceinline__ void addf_nb(const float *coef, size_t on, const float *dqn, float idx,
-                                        float omega, float *s) {
-  float kn[10];
-#pragma unroll
-  for (int m = 0; m < 10; ++m) kn[m] = coef[10 * on + m];  // written in this launch
-  luf_off<D, LOWER>(kn, idx, omega, dqn, s);
+// Per-cube scratch in plane order: the cells of plane h = i+j+k, i then j
+// ascending, at positions pos = P[h] + Q[h][i] + (j - jlo(h, i)), one array
+// per value (mirror 0..4, residual / increment 5..9, fluid flag 10).  The
+// threads of a sweep plane (consecutive columns) and of a packing pass
+// (consecutive cells of a slab's anti-diagonal) touch consecutive words, so
+// every global access of the kernel is coalesced.
+constexpr int kScr = 11;
+// Shared slots of the previous plane, value-major [kSlot][n*n]: coefficients
+// 0..9, increment 10..14, fluid flag 15.
+constexpr int kSlot = 16;
+
+__device__ __forceinline__ int jlo_of(int h, int i, int n) {
+  const int x = h - i - (n - 1);
+  return x > 0 ? x : 0;
 }
 
-__global__ void __launch_bounds__(kLuMaxThreads) k_lusgs_split(LusgsSplitArgs a) {
-  extern __shared__ __align__(16) float fbuf[];  // [2][n*n][5]; later the reduction's doubles
-  const int n = a.ph.n, S = n + 4, nn = n * n;
+template <int MAXT>
+__global__ void __launch_bounds__(MAXT, MAXT <= 576 ? 2 : 1) k_lusgs_split(LusgsSplitArgs a) {
+  extern __shared__ __align__(16) float fbuf[];
+  const int n = a.ph.n, S = n + 4, nn = n * n, n3 = nn * n, np = 3 * n - 2;
   const int cube = 1 + blockIdx.x;
   if (!case_active(a.bt, cube)) return;  // converged case
   float dT = a.dTf, mu_L = a.mu_Lf, rho0 = a.rho0f, P0 = a.P0f, T0 = a.T0f;
@@ -88,94 +97,212 @@ __global__ void __launch_bounds__(kLuMaxThreads) k_lusgs_split(LusgsSplitArgs a)
   const float omega = a.omegaf, cfl = a.cflf;
   const float idx = a.inv_dx[cube];
   const size_t cb = cell_index(S, cube, 0, 0, 0);
-  auto cell = [&](int i, int j, int k) -> size_t {
-    return cb + ((size_t)(i + 2) * S + (j + 2)) * S + (k + 2);
-  };
-  const int *F = a.FWS;
+  float *scr = a.scr + (size_t)blockIdx.x * kScr * n3;
 
-  for (int h = 0; h <= 3 * (n - 1); ++h) {
-    float *cur = fbuf + (size_t)(h & 1) * nn * 5;
-    const float *prv = fbuf + (size_t)((h + 1) & 1) * nn * 5;
-    for (int col = threadIdx.x; col < nn; col += blockDim.x) {
-      const int ci = col / n, cj = col - (col / n) * n, ck = h - ci - cj;
-      if (ck < 0 || ck >= n) continue;
-      const size_t o = cell(ci, cj, ck);
-      float *slot = cur + 5 * col;
-      if (F[o] != kFluid) {
+  // Shared memory: slots (also the slab staging area), then the tables.
+  float *slots = fbuf;                                   // [2][kSlot][nn]
+  int *Pt = reinterpret_cast<int *>(fbuf + 2 * kSlot * nn);  // [np + 1]
+  int *Qt = Pt + np + 1;                                 // [np][n]
+  int *At = Qt + np * n;                                 // [2n] anti-diagonal starts
+  int *sorder = At + 2 * n;                              // [nn] slab cells by anti-diagonal
+  unsigned short *dec = reinterpret_cast<unsigned short *>(sorder + nn);  // [n3] column of a position
+  const int tid = threadIdx.x, NT = blockDim.x;
+  for (int h = tid; h < np; h += NT) {
+    const int ilo = h - 2 * (n - 1) > 0 ? h - 2 * (n - 1) : 0, ihi = h < n - 1 ? h : n - 1;
+    int acc = 0;
+    for (int i = 0; i < n; ++i) {
+      Qt[h * n + i] = acc;
+      if (i >= ilo && i <= ihi) acc += (h - i < n - 1 ? h - i : n - 1) - jlo_of(h, i, n) + 1;
+    }
+  }
+  if (tid == 0) {
+    int acc = 0;
+    for (int h = 0; h < np; ++h) {
+      Pt[h] = acc;
+      const int ilo = h - 2 * (n - 1) > 0 ? h - 2 * (n - 1) : 0, ihi = h < n - 1 ? h : n - 1;
+      for (int i = ilo; i <= ihi; ++i)
+        acc += (h - i < n - 1 ? h - i : n - 1) - jlo_of(h, i, n) + 1;
+    }
+    Pt[np] = acc;
+    int d0 = 0;
+    for (int d = 0; d <= 2 * n - 2; ++d) {
+      At[d] = d0;
+      d0 += (d < 2 * n - 2 - d ? d : 2 * n - 2 - d) + 1;
+    }
+  }
+  __syncthreads();
+  for (int jk = tid; jk < nn; jk += NT) {
+    const int j = jk / n, k = jk - j * n, d = j + k;
+    sorder[At[d] + j - (d - (n - 1) > 0 ? d - (n - 1) : 0)] = jk;
+  }
+  auto pos = [&](int h, int i, int j) { return Pt[h] + Qt[h * n + i] + (j - jlo_of(h, i, n)); };
+  auto SV = [&](int v, int p) -> float & { return scr[(size_t)v * n3 + p]; };
+  __syncthreads();
+  for (int c = tid; c < n3; c += NT) {
+    const int i = c / nn, j = (c / n) % n, k = c % n;
+    dec[pos(i + j + k, i, j)] = (unsigned short)(i * n + j);
+  }
+  __syncthreads();
+
+  // Pack, slab by slab (i fixed): coalesced loads in memory order into
+  // shared memory, coalesced stores in plane order.
+  float *stage = slots;  // [kScr][nn]
+  for (int i = 0; i < n; ++i) {
+    for (int jk = tid; jk < nn; jk += NT) {
+      const int j = jk / n, k = jk - j * n;
+      const size_t o = cb + ((size_t)(i + 2) * S + (j + 2)) * S + (k + 2);
 #pragma unroll
-        for (int m = 0; m < 5; ++m) slot[m] = 0.f;
-        continue;
+      for (int v = 0; v < 5; ++v) {
+        stage[v * nn + jk] = a.M[5 * o + v];
+        stage[(5 + v) * nn + jk] = a.R32[5 * o + v];
       }
-      float k[10];
-      luf_coef(a.M + 5 * o, rho0, P0, T0, mu_L, idx, dT, cfl, omega, k);
+      stage[10 * nn + jk] = a.FWS[o] == kFluid ? 1.f : 0.f;
+    }
+    __syncthreads();
+    for (int t = tid; t < nn; t += NT) {
+      const int jk = sorder[t], j = jk / n, k = jk - j * n;
+      const int p = pos(i + j + k, i, j);
 #pragma unroll
-      for (int m = 0; m < 10; ++m) a.coef[10 * o + m] = k[m];
-      float s[5];
-#pragma unroll
-      for (int m = 0; m < 5; ++m) s[m] = a.R32[5 * o + m];
-      if (ci > 0 && F[cell(ci - 1, cj, ck)] == kFluid)
-        addf_nb<0, true>(a.coef, cell(ci - 1, cj, ck), prv + 5 * (col - n), idx, omega, s);
-      if (cj > 0 && F[cell(ci, cj - 1, ck)] == kFluid)
-        addf_nb<1, true>(a.coef, cell(ci, cj - 1, ck), prv + 5 * (col - 1), idx, omega, s);
-      if (ck > 0 && F[cell(ci, cj, ck - 1)] == kFluid)
-        addf_nb<2, true>(a.coef, cell(ci, cj, ck - 1), prv + 5 * col, idx, omega, s);
-      const float idg = 1.0f / k[9];
-#pragma unroll
-      for (int m = 0; m < 5; ++m) {
-        const float x = s[m] * idg;
-        a.R32[5 * o + m] = x;
-        slot[m] = x;
-      }
+      for (int v = 0; v < kScr; ++v) SV(v, p) = stage[v * nn + jk];
     }
     __syncthreads();
   }
 
+  // Sweeps: the cells of plane h (positions Pt[h] .. Pt[h+1]) go to
+  // consecutive threads, so every active warp is full; each cell finds its
+  // neighbours' previous-plane values in the shared slot of their column.
+  auto nb = [&](const float *prv, int c, float *kk, float *dd) {
+#pragma unroll
+    for (int v = 0; v < 10; ++v) kk[v] = prv[v * nn + c];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) dd[v] = prv[(10 + v) * nn + c];
+  };
+  float m[5], r[5], fl = 0.f;
+  auto fetch = [&](int pp) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      m[v] = SV(v, pp);
+      r[v] = SV(5 + v, pp);
+    }
+    fl = SV(10, pp);
+  };
+
+  // Forward sweep: dq* = (R + sum of lower A+ terms) / dg.
+  if (tid < Pt[1] - Pt[0]) fetch(Pt[0] + tid);
+  for (int h = 0; h < np; ++h) {
+    float *cur = slots + (size_t)(h & 1) * kSlot * nn;
+    const float *prv = slots + (size_t)((h + 1) & 1) * kSlot * nn;
+    const int cnt = Pt[h + 1] - Pt[h];
+    for (int t = tid; t < cnt; t += NT) {
+      const int pp = Pt[h] + t;
+      if (t != tid) fetch(pp);  // further cells of a wide plane
+      const int col = dec[pp], ci = col / n, cj = col - ci * n, k = h - ci - cj;
+      cur[15 * nn + col] = fl;
+      if (fl != 0.f) {
+        float kc[10], kk[10], dd[5];
+        luf_coef(m, rho0, P0, T0, mu_L, idx, dT, cfl, omega, kc);
+        if (ci > 0 && prv[15 * nn + col - n] != 0.f) {
+          nb(prv, col - n, kk, dd);
+          luf_off<0, true>(kk, idx, omega, dd, r);
+        }
+        if (cj > 0 && prv[15 * nn + col - 1] != 0.f) {
+          nb(prv, col - 1, kk, dd);
+          luf_off<1, true>(kk, idx, omega, dd, r);
+        }
+        if (k > 0 && prv[15 * nn + col] != 0.f) {  // the column's previous cell
+          nb(prv, col, kk, dd);
+          luf_off<2, true>(kk, idx, omega, dd, r);
+        }
+        const float idg = 1.0f / kc[9];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          const float x = r[v] * idg;
+          SV(5 + v, pp) = x;
+          cur[(10 + v) * nn + col] = x;
+        }
+#pragma unroll
+        for (int v = 0; v < 10; ++v) cur[v * nn + col] = kc[v];
+      }
+    }
+    if (h + 1 < np && tid < Pt[h + 2] - Pt[h + 1]) fetch(Pt[h + 1] + tid);  // next plane
+    __syncthreads();
+  }
+
+  // Backward sweep: dq = dq* - (sum of upper A- terms) / dg.
+  if (tid < Pt[np] - Pt[np - 1]) fetch(Pt[np - 1] + tid);
+  for (int h = np - 1; h >= 0; --h) {
+    float *cur = slots + (size_t)(h & 1) * kSlot * nn;
+    const float *prv = slots + (size_t)((h + 1) & 1) * kSlot * nn;
+    const int cnt = Pt[h + 1] - Pt[h];
+    for (int t = tid; t < cnt; t += NT) {
+      const int pp = Pt[h] + t;
+      if (t != tid) fetch(pp);
+      const int col = dec[pp], ci = col / n, cj = col - ci * n, k = h - ci - cj;
+      cur[15 * nn + col] = fl;
+      if (fl != 0.f) {
+        float kc[10], kk[10], dd[5], s[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+        luf_coef(m, rho0, P0, T0, mu_L, idx, dT, cfl, omega, kc);
+        if (ci + 1 < n && prv[15 * nn + col + n] != 0.f) {
+          nb(prv, col + n, kk, dd);
+          luf_off<0, false>(kk, idx, omega, dd, s);
+        }
+        if (cj + 1 < n && prv[15 * nn + col + 1] != 0.f) {
+          nb(prv, col + 1, kk, dd);
+          luf_off<1, false>(kk, idx, omega, dd, s);
+        }
+        if (k + 1 < n && prv[15 * nn + col] != 0.f) {
+          nb(prv, col, kk, dd);
+          luf_off<2, false>(kk, idx, omega, dd, s);
+        }
+        const float idg = 1.0f / kc[9];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          const float x = r[v] - s[v] * idg;
+          SV(5 + v, pp) = x;
+          cur[(10 + v) * nn + col] = x;
+        }
+#pragma unroll
+        for (int v = 0; v < 10; ++v) cur[v * nn + col] = kc[v];
+      }
+    }
+    if (h > 0 && tid < Pt[h] - Pt[h - 1]) fetch(Pt[h - 1] + tid);
+    __syncthreads();
+  }
+
+  // Update, slab by slab: increments gathered in plane order (coalesced)
+  // into shared memory, then Q += dq on fluid cells in memory order (FP64),
+  // change norms of p, u, v, w, T from the FP32 increment (the split RK
+  // path's third-stage formulas) and the force integrands of every cell.
   double e[7] = {0, 0, 0, 0, 0, 0, 0};
-  for (int h = 3 * (n - 1); h >= 0; --h) {
-    float *cur = fbuf + (size_t)(h & 1) * nn * 5;
-    const float *prv = fbuf + (size_t)((h + 1) & 1) * nn * 5;
-    for (int col = threadIdx.x; col < nn; col += blockDim.x) {
-      const int ci = col / n, cj = col - (col / n) * n, ck = h - ci - cj;
-      if (ck < 0 || ck >= n) continue;
-      const size_t o = cell(ci, cj, ck);
-      float *slot = cur + 5 * col;
+  for (int i = 0; i < n; ++i) {
+    for (int t = tid; t < nn; t += NT) {
+      const int jk = sorder[t], j = jk / n, k = jk - j * n;
+      const int pp = pos(i + j + k, i, j);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) stage[v * nn + jk] = SV(5 + v, pp);
+    }
+    __syncthreads();
+    for (int jk = tid; jk < nn; jk += NT) {
+      const int j = jk / n, k = jk - j * n;
+      const size_t o = cb + ((size_t)(i + 2) * S + (j + 2)) * S + (k + 2);
       e[5] += a.Residual1[5 * o + 0];
       e[6] += a.Residual1[5 * o + 1];
-      if (F[o] != kFluid) {
-#pragma unroll
-        for (int m = 0; m < 5; ++m) slot[m] = 0.f;
-        continue;
-      }
-      float s[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-      if (ci + 1 < n && F[cell(ci + 1, cj, ck)] == kFluid)
-        addf_nb<0, false>(a.coef, cell(ci + 1, cj, ck), prv + 5 * (col + n), idx, omega, s);
-      if (cj + 1 < n && F[cell(ci, cj + 1, ck)] == kFluid)
-        addf_nb<1, false>(a.coef, cell(ci, cj + 1, ck), prv + 5 * (col + 1), idx, omega, s);
-      if (ck + 1 < n && F[cell(ci, cj, ck + 1)] == kFluid)
-        addf_nb<2, false>(a.coef, cell(ci, cj, ck + 1), prv + 5 * col, idx, omega, s);
-      const float idg = 1.0f / a.coef[10 * o + 9];
+      if (a.FWS[o] != kFluid) continue;
       float dq[5];
 #pragma unroll
-      for (int m = 0; m < 5; ++m) {
-        dq[m] = a.R32[5 * o + m] - s[m] * idg;
-        a.R32[5 * o + m] = dq[m];
-        slot[m] = dq[m];
-      }
-      // FP64 update; change norms of p, u, v, w, T from the FP32 increment
-      // (same formulas as the split RK path's third stage).
-      double *q = a.U1_ + 5 * o;
+      for (int v = 0; v < 5; ++v) dq[v] = stage[v * nn + jk];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) a.U1_[5 * o + v] = a.U1_[5 * o + v] + (double)dq[v];
       const float *mm_ = a.M + 5 * o;
       const float rf = rho0 + mm_[0];
       const float m1 = mm_[1], m2 = mm_[2], m3 = mm_[3];
-      const float Pc = P0 + (mm_[4] - 0.5f * (m1 * m1 + m2 * m2 + m3 * m3) / rf) * 0.4f;
-#pragma unroll
-      for (int m = 0; m < 5; ++m) q[m] = q[m] + (double)dq[m];
+      const float mm = m1 * m1 + m2 * m2 + m3 * m3;
+      const float Pc = P0 + (mm_[4] - 0.5f * mm / rf) * 0.4f;
       const float dr = dq[0], e1 = dq[1], e2 = dq[2], e3 = dq[3], dE = dq[4];
       const float den = 1.0f / (rf * (rf + dr));
       const float dU = (e1 * rf - m1 * dr) * den;
       const float dVv = (e2 * rf - m2 * dr) * den;
       const float dW = (e3 * rf - m3 * dr) * den;
-      const float mm = m1 * m1 + m2 * m2 + m3 * m3;
       const float dKE =
           0.5f * ((2.f * (m1 * e1 + m2 * e2 + m3 * e3) + e1 * e1 + e2 * e2 + e3 * e3) * rf - mm * dr) * den;
       const float dP = 0.4f * (dE - dKE);
@@ -190,35 +317,70 @@ __global__ void __launch_bounds__(kLuMaxThreads) k_lusgs_split(LusgsSplitArgs a)
   }
 
   double *red = reinterpret_cast<double *>(fbuf);  // [warps][7]
-  const int nw = (blockDim.x + 31) / 32;
+  const int nw = (NT + 31) / 32;
 #pragma unroll
-  for (int m = 0; m < 7; ++m) {
-    double v = e[m];
+  for (int v = 0; v < 7; ++v) {
+    double x = e[v];
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-    if ((threadIdx.x & 31) == 0) red[(threadIdx.x >> 5) * 7 + m] = v;
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+    if ((tid & 31) == 0) red[(tid >> 5) * 7 + v] = x;
   }
   __syncthreads();
-  if (threadIdx.x < 7) {
-    double v = 0;
-    for (int w = 0; w < nw; ++w) v += red[w * 7 + threadIdx.x];
-    a.partials[(size_t)blockIdx.x * 7 + threadIdx.x] = v;
+  if (tid < 7) {
+    double x = 0;
+    for (int w = 0; w < nw; ++w) x += red[w * 7 + tid];
+    a.partials[(size_t)blockIdx.x * 7 + tid] = x;
   }
 }
 
 }  // namespace
 
+size_t lusgs_split_scratch(int n) { return (size_t)kScr * n * n * n; }
+
+// Threads of the split LU-SGS kernel: the widest plane of a cube, in whole
+// warps (every plane then takes one pass).
+static int lusgs_split_threads(int n) {
+  int mx = 0;
+  for (int h = 0; h <= 3 * n - 3; ++h) {
+    int c = 0;
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        const int k = h - i - j;
+        c += k >= 0 && k < n;
+      }
+    mx = c > mx ? c : mx;
+  }
+  return (mx + 31) / 32 * 32;
+}
+
 cudaError_t launch_lusgs_split(const LusgsSplitArgs &a, int ncubes, cudaStream_t s) {
   if (ncubes <= 0) return cudaSuccess;
   const int n = a.ph.n;
-  const int threads = lusgs_threads(n);
-  size_t smem = (size_t)2 * n * n * 5 * sizeof(float);
+  if (n * n > 1024) return cudaErrorInvalidValue;  // columns are 16-bit shared indices
+  static std::atomic<int> cache[33];  // threads per n (0: not yet computed)
+  int threads = cache[n].load(std::memory_order_relaxed);
+  if (threads == 0) {
+    threads = lusgs_split_threads(n);
+    cache[n].store(threads, std::memory_order_relaxed);
+  }
+  const int np = 3 * n - 2;
+  size_t smem = (size_t)2 * n * n * kSlot * sizeof(float) +
+                (size_t)(np + 1 + np * n + 2 * n + n * n) * sizeof(int) +
+                (size_t)n * n * n * sizeof(unsigned short);
   const size_t red = (size_t)(threads / 32) * 7 * sizeof(double);
   if (smem < red) smem = red;
-  cudaError_t e = cudaFuncSetAttribute(k_lusgs_split,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  k_lusgs_split<<<ncubes, threads, smem, s>>>(a);
+  cudaError_t e;
+  if (threads <= 576) {
+    e = cudaFuncSetAttribute(k_lusgs_split<576>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    if (e != cudaSuccess) return e;
+    k_lusgs_split<576><<<ncubes, threads, smem, s>>>(a);
+  } else {
+    e = cudaFuncSetAttribute(k_lusgs_split<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    if (e != cudaSuccess) return e;
+    k_lusgs_split<1024><<<ncubes, threads, smem, s>>>(a);
+  }
   return cudaGetLastError();
 }
 
