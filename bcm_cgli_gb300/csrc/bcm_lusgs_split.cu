@@ -84,7 +84,7 @@ __device__ __forceinline__ int jlo_of(int h, int i, int n) {
 }
 
 template <int MAXT>
-__global__ void __launch_bounds__(MAXT, MAXT <= 576 ? 2 : 1) k_lusgs_split(LusgsSplitArgs a) {
+__global__ void __launch_bounds__(MAXT, MAXT <= 448 ? 2 : 1) k_lusgs_split(LusgsSplitArgs a) {
   extern __shared__ __align__(16) float fbuf[];
   const int n = a.ph.n, S = n + 4, nn = n * n, n3 = nn * n, np = 3 * n - 2;
   const int cube = 1 + blockIdx.x;
@@ -177,7 +177,8 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 576 ? 2 : 1) k_lusgs_split(Lusgs
 #pragma unroll
     for (int v = 0; v < 5; ++v) dd[v] = prv[(10 + v) * nn + c];
   };
-  float m[5], r[5], fl = 0.f;
+  float m[5], r[5], fl = 0.f;     // this plane's cell
+  float m2[5], r2[5], fl2 = 0.f;  // the next plane's, loaded a plane ahead
   auto fetch = [&](int pp) {
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
@@ -186,13 +187,31 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 576 ? 2 : 1) k_lusgs_split(Lusgs
     }
     fl = SV(10, pp);
   };
+  auto fetch2 = [&](int pp) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      m2[v] = SV(v, pp);
+      r2[v] = SV(5 + v, pp);
+    }
+    fl2 = SV(10, pp);
+  };
+  auto take2 = [&]() {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      m[v] = m2[v];
+      r[v] = r2[v];
+    }
+    fl = fl2;
+  };
 
   // Forward sweep: dq* = (R + sum of lower A+ terms) / dg.
-  if (tid < Pt[1] - Pt[0]) fetch(Pt[0] + tid);
+  if (tid < Pt[1] - Pt[0]) fetch2(Pt[0] + tid);
   for (int h = 0; h < np; ++h) {
     float *cur = slots + (size_t)(h & 1) * kSlot * nn;
     const float *prv = slots + (size_t)((h + 1) & 1) * kSlot * nn;
     const int cnt = Pt[h + 1] - Pt[h];
+    take2();
+    if (h + 1 < np && tid < Pt[h + 2] - Pt[h + 1]) fetch2(Pt[h + 1] + tid);  // next plane
     for (int t = tid; t < cnt; t += NT) {
       const int pp = Pt[h] + t;
       if (t != tid) fetch(pp);  // further cells of a wide plane
@@ -224,16 +243,17 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 576 ? 2 : 1) k_lusgs_split(Lusgs
         for (int v = 0; v < 10; ++v) cur[v * nn + col] = kc[v];
       }
     }
-    if (h + 1 < np && tid < Pt[h + 2] - Pt[h + 1]) fetch(Pt[h + 1] + tid);  // next plane
     __syncthreads();
   }
 
   // Backward sweep: dq = dq* - (sum of upper A- terms) / dg.
-  if (tid < Pt[np] - Pt[np - 1]) fetch(Pt[np - 1] + tid);
+  if (tid < Pt[np] - Pt[np - 1]) fetch2(Pt[np - 1] + tid);
   for (int h = np - 1; h >= 0; --h) {
     float *cur = slots + (size_t)(h & 1) * kSlot * nn;
     const float *prv = slots + (size_t)((h + 1) & 1) * kSlot * nn;
     const int cnt = Pt[h + 1] - Pt[h];
+    take2();
+    if (h > 0 && tid < Pt[h] - Pt[h - 1]) fetch2(Pt[h - 1] + tid);
     for (int t = tid; t < cnt; t += NT) {
       const int pp = Pt[h] + t;
       if (t != tid) fetch(pp);
@@ -265,7 +285,6 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 576 ? 2 : 1) k_lusgs_split(Lusgs
         for (int v = 0; v < 10; ++v) cur[v * nn + col] = kc[v];
       }
     }
-    if (h > 0 && tid < Pt[h] - Pt[h - 1]) fetch(Pt[h - 1] + tid);
     __syncthreads();
   }
 
@@ -370,11 +389,11 @@ cudaError_t launch_lusgs_split(const LusgsSplitArgs &a, int ncubes, cudaStream_t
   const size_t red = (size_t)(threads / 32) * 7 * sizeof(double);
   if (smem < red) smem = red;
   cudaError_t e;
-  if (threads <= 576) {
-    e = cudaFuncSetAttribute(k_lusgs_split<576>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if (threads <= 448) {
+    e = cudaFuncSetAttribute(k_lusgs_split<448>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
     if (e != cudaSuccess) return e;
-    k_lusgs_split<576><<<ncubes, threads, smem, s>>>(a);
+    k_lusgs_split<448><<<ncubes, threads, smem, s>>>(a);
   } else {
     e = cudaFuncSetAttribute(k_lusgs_split<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
