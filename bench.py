@@ -265,13 +265,13 @@ def pinned_like(a):
         return np.ascontiguousarray(a.copy()), None
 
 
-def measure(api, case, precision_name, args, dist, clocks_on=True):
+def measure(api, case, precision_name, args, dist, clocks_on=True, method=None):
     """Timed region for one precision: args.steps dual-time steps resident in
     HBM, device-timed with CUDA events on the context's stream; the flux
     kernel's launches are bracketed by events for its average duration."""
     precision = api.PRECISION_SPLIT if precision_name == "split" else api.PRECISION_FP64
     ctx = make_context(api, case, precision)
-    if getattr(args, "method", "rk3") == "lusgs":
+    if (method or getattr(args, "method", "rk3")) == "lusgs":
         ctx.set_method(api.METHOD_LUSGS, cfl=0.0, omega=1.5)
     ctx.set_state(case.U, case.U, case.U)
     for _ in range(args.warmup):
@@ -456,6 +456,16 @@ def run_gpu_arm(args, dist):
                                          else m_other["value"] / line["value"])
     if acc is not None:
         line["accuracy"] = acc
+    line["method"] = args.method
+    if args.method == "rk3" and not args.quick:
+        # the same workload with LU-SGS sub-iterations (no reference
+        # counterpart; converges further per sub-iteration)
+        m_lu = measure(api, case, head, args, dist, clocks_on=False, method="lusgs")
+        line["lusgs"] = {"value": m_lu["value"], "ms_per_step": m_lu["ms_per_step"],
+                         "precision": head, "gpu_launches": m_lu["launches"],
+                         "note": "LU-SGS sub-iterations (hyperplane sweeps) instead of the "
+                                 "reference's 3-stage RK, same residual and workload"}
+        m_lu["ctx"].close()
     if not args.no_converged and not args.quick:
         conv = {m: measure_converged(api, case, head, m, args, dist) for m in ("rk3", "lusgs")}
         conv["tol"] = 0.02
