@@ -88,6 +88,7 @@ def _declare(L):
     L.bcmg_case_timer_elapsed.argtypes = [P, C.c_int, C.c_int, C.POINTER(C.c_double)]
     L.bcmg_batch_create.argtypes = [C.c_int, C.POINTER(CaseDesc), C.POINTER(P)]
     L.bcmg_case_set_method.argtypes = [P, C.c_int, C.c_double, C.c_double]
+    L.bcmg_case_mirror.argtypes = [P, P]
     L.bcmg_case_output_q.argtypes = [P, C.c_int, C.c_int, C.c_char_p]
     L.bcmg_case_output_x.argtypes = [P, C.c_int, C.c_int, C.c_char_p, P]
     L.bcmg_case_output_wait.argtypes = [P]

@@ -286,6 +286,12 @@ class CaseContext:
         check(lib().bcmg_case_output_x(self.h, int(q), int(ncube_out), os.fsencode(path),
                                        o.ctypes.data))
 
+    def mirror(self):
+        """FP32 mirror of the current state (split-precision path)."""
+        out = np.empty(self.shape, np.float32)
+        check(lib().bcmg_case_mirror(self.h, out.ctypes.data))
+        return out
+
     def sync(self):
         check(lib().bcmg_case_sync(self.h))
 

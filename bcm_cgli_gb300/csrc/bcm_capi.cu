@@ -1466,6 +1466,19 @@ int bcmg_case_output_wait(bcmg_case *c) {
   return c->out_status;
 }
 
+int bcmg_case_mirror(bcmg_case *c, float *M) {
+  clear_err();
+  if (!c || !M) { set_err("null argument"); return BCMG_ERR_ARG; }
+  if (c->precision != BCMG_PRECISION_SPLIT) {
+    set_err("the FP32 mirror exists on the split-precision path only");
+    return BCMG_ERR_ARG;
+  }
+  CK(launch_mirror(c->U1_, c->M, c->ph.n, c->ncube, c->ph.rho0, c->ph.P0, c->bt(), c->stream));
+  CK(cudaMemcpyAsync(M, c->M, c->ncell * 5 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return BCMG_OK;
+}
+
 int bcmg_case_ncase(const bcmg_case *c) { return c ? c->ncase : 0; }
 
 int bcmg_case_case_cubes(const bcmg_case *c, int q, int *cube0, int *ncube) {

@@ -26,36 +26,68 @@ namespace bcmg {
 
 // ---------------------------------------------------------------------------
 // FP64 -> FP32 deltas of the state, all cells of all cubes (ghosts included).
+// The state is taken as a flat array of doubles two at a time (16-byte loads,
+// 8-byte stores, consecutive for consecutive threads); component v of a
+// double is its index mod 5 (a cube holds 5 S^3 doubles, S even, so a pair
+// never straddles two cubes).  One block row per cube, 32-bit indices.
 // ---------------------------------------------------------------------------
-__global__ void k_mirror(const double *__restrict__ U, float *__restrict__ M, size_t ncell_from,
-                         size_t ncell_to, double rho0_, double E0_, Batch bt, size_t cube_cells) {
-  for (size_t c = ncell_from + blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < ncell_to;
-       c += (size_t)gridDim.x * blockDim.x) {
+// double -> float, round to nearest even (IEEE 754), on the integer pipes:
+// this part's FP64 pipe, where the hardware conversion runs, is its
+// narrowest (1/64 of FP32) and would otherwise bound this memory-bound pass.
+// Results outside the normal float range (|x| < 2^-126, overflow, zero,
+// inf/nan) take the hardware conversion.
+__device__ __forceinline__ float to_float_rn(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const int e = (int)((hi >> 20) & 0x7FF) - 1023 + 127;  // float exponent field
+  if (e <= 0 || e >= 255) return (float)x;
+  const unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);  // top 23 fraction bits
+  const unsigned rem = lo & 0x1FFFFFFFu, half = 0x10000000u;
+  unsigned r = ((unsigned)e << 23) | m;
+  r += (rem > half || (rem == half && (m & 1u))) ? 1u : 0u;  // a carry may raise the exponent
+  return __uint_as_float((hi & 0x80000000u) | r);
+}
+
+__device__ __forceinline__ float mirror_component(double x, int v, double rho0, double E0) {
+  return to_float_rn(v == 0 ? x - rho0 : (v == 4 ? x - E0 : x));
+}
+
+__global__ void __launch_bounds__(256) k_mirror(const double2 *__restrict__ U,
+                                                float2 *__restrict__ M, double rho0_,
+                                                double E0_, Batch bt, int cube_pairs,
+                                                int ncubes) {
+  for (int cube = 1 + blockIdx.y; cube <= ncubes; cube += gridDim.y) {
     double rho0 = rho0_, E0 = E0_;
-    if (bt.cube_case) {  // the reference state of the cell's case
-      const CaseConst *cq = bt.cases + __ldg(bt.cube_case + c / cube_cells);
+    if (bt.cube_case) {  // the reference state of the cube's case
+      const CaseConst *cq = bt.cases + bt.cube_case[cube];
       rho0 = cq->rho0;
       E0 = cq->P0 / (BCMG_K - 1);
     }
-    const double *q = U + 5 * c;
-    float *m = M + 5 * c;
-    m[0] = (float)(q[0] - rho0);
-    m[1] = (float)q[1];
-    m[2] = (float)q[2];
-    m[3] = (float)q[3];
-    m[4] = (float)(q[4] - E0);
+    const double2 *u = U + (size_t)cube * cube_pairs;
+    float2 *m = M + (size_t)cube * cube_pairs;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int q = (blockIdx.x * 4 + r) * 256 + threadIdx.x;
+      if (q < cube_pairs) {
+        const double2 x = u[q];
+        const int v0 = (2 * q) % 5;  // a cube holds a multiple of 5 doubles
+        const int v1 = v0 == 4 ? 0 : v0 + 1;
+        m[q] = make_float2(mirror_component(x.x, v0, rho0, E0),
+                           mirror_component(x.y, v1, rho0, E0));
+      }
+    }
   }
 }
 
 cudaError_t launch_mirror(const double *U, float *M, int n, int ncube, double rho0, double P0,
                           const Batch &bt, cudaStream_t s) {
-  const size_t S = n + 4;
-  const size_t from = S * S * S, to = (size_t)ncube * S * S * S;  // skip cube slot 0
-  if (to <= from) return cudaSuccess;
-  const size_t cnt = to - from;
-  int blocks = (int)((cnt + 255) / 256);
-  if (blocks > 152 * 16) blocks = 152 * 16;
-  k_mirror<<<blocks, 256, 0, s>>>(U, M, from, to, rho0, P0 / (BCMG_K - 1), bt, S * S * S);
+  if (ncube <= 1) return cudaSuccess;  // cube slot 0 is unused
+  const int S = n + 4;
+  const int cube_pairs = 5 * S * S * S / 2;  // S is even
+  const dim3 grid((cube_pairs + 1023) / 1024, ncube - 1 < 65535 ? ncube - 1 : 65535);
+  k_mirror<<<grid, 256, 0, s>>>(reinterpret_cast<const double2 *>(U),
+                               reinterpret_cast<float2 *>(M), rho0, P0 / (BCMG_K - 1), bt,
+                               cube_pairs, ncube - 1);
   return cudaGetLastError();
 }
 

@@ -99,23 +99,27 @@ __global__ void __launch_bounds__(kHaloThreads) k_iface_faces(InterfaceArgs a) {
     level_face(a, c, ft);
     return;
   }
+  // Copies move 16-byte pairs of doubles: S is even, so every row below
+  // starts at an even cell index (an even double index) and is 5n or 10
+  // doubles long (n is a multiple of 4).
+  double2 *U2 = reinterpret_cast<double2 *>(U);
   if (ax < 2) {
     // rows: (layer l, transverse index p); each row = 5n doubles along k
-    const int rowlen = 5 * n;
+    const int rowlen = 5 * n / 2;
     for (int w = threadIdx.x; w < 2 * n * rowlen; w += kHaloThreads) {
       const int row = w / rowlen, e = w - row * rowlen;
       const int l = row / n, p = 2 + (row - l * n);
       int di, dj, si, sj;
       if (ax == 0) { di = dbase + l; si = sbase + l; dj = sj = p; }
       else { dj = dbase + l; sj = sbase + l; di = si = p; }
-      U[5 * cell_index(S, c, di, dj, 2) + e] = U[5 * cell_index(S, ft.src, si, sj, 2) + e];
+      U2[5 * cell_index(S, c, di, dj, 2) / 2 + e] = U2[5 * cell_index(S, ft.src, si, sj, 2) / 2 + e];
     }
   } else {
     // z faces: per (i, j) the two layers are 10 contiguous doubles
-    for (int w = threadIdx.x; w < n * n * 10; w += kHaloThreads) {
-      const int col = w / 10, e = w - col * 10;
+    for (int w = threadIdx.x; w < n * n * 5; w += kHaloThreads) {
+      const int col = w / 5, e = w - col * 5;
       const int i = 2 + col / n, j = 2 + (col - (col / n) * n);
-      U[5 * cell_index(S, c, i, j, dbase) + e] = U[5 * cell_index(S, ft.src, i, j, sbase) + e];
+      U2[5 * cell_index(S, c, i, j, dbase) / 2 + e] = U2[5 * cell_index(S, ft.src, i, j, sbase) / 2 + e];
     }
   }
 }

@@ -218,6 +218,11 @@ int bcmg_case_output_x(bcmg_case *c, int q, int ncube_out, const char *path,
                        const double *origin);
 int bcmg_case_output_wait(bcmg_case *c);
 
+/* Split-precision path: forms the FP32 mirror of the current state U1_ (the
+ * deltas from each case's reference state (rho0, 0, 0, 0, P0/(K-1)) that the
+ * flux kernel reads) and copies it to M[ncell][5] on the host, for checks. */
+int bcmg_case_mirror(bcmg_case *c, float *M);
+
 /* Waits for all work of the context. */
 int bcmg_case_sync(bcmg_case *c);
 

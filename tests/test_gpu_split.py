@@ -72,3 +72,40 @@ def test_split_sphere_forces_within_bound():
     err = rel_l2(b, a, case.n)
     assert max(err) <= SPLIT_BOUND, err
     assert abs(er_b[6] - er_a[6]) <= 1e-3 * abs(er_a[6]), (er_a[6], er_b[6])
+
+
+def _mirror_ref(U, rho0, P0):
+    d = U.copy()
+    d[..., 0] -= rho0
+    d[..., 4] -= P0 / (1.4 - 1)
+    return d.astype(np.float32)  # IEEE round to nearest even
+
+
+def test_mirror_is_the_ieee_rounding_of_the_deltas():
+    """The FP32 mirror (formed with an integer round-to-nearest-even
+    conversion) equals numpy's IEEE conversion of the FP64 deltas, bit for
+    bit, for values spread over many binades and for per-case reference
+    states in a batch."""
+    a = cases.random_case(seed=31, n=8, periodic=True)
+    b = cases.random_case(seed=32, n=8, periodic=False)
+    b.phys.rho0, b.phys.P0 = 0.93, 87000.0
+    rng = np.random.default_rng(5)
+    for c in (a, b):  # momentum spread over many binades, some exact zeros
+        c.U[..., 2] *= 10.0 ** rng.integers(-12, 6, size=c.U.shape[:-1])
+        c.U[..., 3][rng.random(c.U.shape[:-1]) < 0.05] = 0.0
+    ctx = api.CaseContext(a, precision=api.PRECISION_SPLIT)
+    ctx.set_state(a.U, a.U, a.U)
+    M = ctx.mirror()
+    ref = _mirror_ref(a.U, a.phys.rho0, a.phys.P0)
+    assert np.array_equal(M[1:].view(np.uint32), ref[1:].view(np.uint32))
+    ctx.close()
+    bt = api.BatchContext([a, b], precision=api.PRECISION_SPLIT)
+    for q, c in enumerate((a, b)):
+        bt.set_case_state(q, c.U, c.U, c.U)
+    M = bt.mirror()
+    g = 1
+    for c in (a, b):
+        ref = _mirror_ref(c.U, c.phys.rho0, c.phys.P0)[1:]
+        assert np.array_equal(M[g:g + c.ncube - 1].view(np.uint32), ref.view(np.uint32))
+        g += c.ncube - 1
+    bt.close()
