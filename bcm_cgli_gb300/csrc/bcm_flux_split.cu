@@ -26,10 +26,8 @@ namespace bcmg {
 
 // ---------------------------------------------------------------------------
 // FP64 -> FP32 deltas of the state, all cells of all cubes (ghosts included).
-// The state is taken as a flat array of doubles two at a time (16-byte loads,
-// 8-byte stores, consecutive for consecutive threads); component v of a
-// double is its index mod 5 (a cube holds 5 S^3 doubles, S even, so a pair
-// never straddles two cubes).  One block row per cube, 32-bit indices.
+// 16-byte loads and 8-byte stores (a cube holds S^3 cells, S even, so cells
+// pair up within a cube); 32-bit indices within a cube.
 // ---------------------------------------------------------------------------
 // double -> float, round to nearest even (IEEE 754), on the integer pipes:
 // this part's FP64 pipe, where the hardware conversion runs, is its
@@ -48,13 +46,12 @@ __device__ __forceinline__ float to_float_rn(double x) {
   return __uint_as_float((hi & 0x80000000u) | r);
 }
 
-__device__ __forceinline__ float mirror_component(double x, int v, double rho0, double E0) {
-  return to_float_rn(v == 0 ? x - rho0 : (v == 4 ? x - E0 : x));
-}
-
+// One block row per cube (blockIdx.y); a thread converts two cells, i.e.
+// five 16-byte pairs whose components are known at compile time, so only
+// the density and energy components take an FP64 subtraction.
 __global__ void __launch_bounds__(256) k_mirror(const double2 *__restrict__ U,
                                                 float2 *__restrict__ M, double rho0_,
-                                                double E0_, Batch bt, int cube_pairs,
+                                                double E0_, Batch bt, int cube_cell_pairs,
                                                 int ncubes) {
   for (int cube = 1 + blockIdx.y; cube <= ncubes; cube += gridDim.y) {
     double rho0 = rho0_, E0 = E0_;
@@ -63,17 +60,20 @@ __global__ void __launch_bounds__(256) k_mirror(const double2 *__restrict__ U,
       rho0 = cq->rho0;
       E0 = cq->P0 / (BCMG_K - 1);
     }
-    const double2 *u = U + (size_t)cube * cube_pairs;
-    float2 *m = M + (size_t)cube * cube_pairs;
+    const size_t base = (size_t)cube * cube_cell_pairs * 5;  // in 16-byte pairs
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const int q = (blockIdx.x * 4 + r) * 256 + threadIdx.x;
-      if (q < cube_pairs) {
-        const double2 x = u[q];
-        const int v0 = (2 * q) % 5;  // a cube holds a multiple of 5 doubles
-        const int v1 = v0 == 4 ? 0 : v0 + 1;
-        m[q] = make_float2(mirror_component(x.x, v0, rho0, E0),
-                           mirror_component(x.y, v1, rho0, E0));
+    for (int r = 0; r < 2; ++r) {
+      const int q = (blockIdx.x * 2 + r) * 256 + threadIdx.x;  // cell pair in the cube
+      if (q < cube_cell_pairs) {
+        const double2 *u = U + base + 5 * (size_t)q;
+        float2 *m = M + base + 5 * (size_t)q;
+        const double2 a = u[0], b = u[1], c = u[2], d = u[3], e = u[4];
+        // doubles: rho, mx, my, mz, E | rho, mx, my, mz, E
+        m[0] = make_float2(to_float_rn(a.x - rho0), to_float_rn(a.y));
+        m[1] = make_float2(to_float_rn(b.x), to_float_rn(b.y));
+        m[2] = make_float2(to_float_rn(c.x - E0), to_float_rn(c.y - rho0));
+        m[3] = make_float2(to_float_rn(d.x), to_float_rn(d.y));
+        m[4] = make_float2(to_float_rn(e.x), to_float_rn(e.y - E0));
       }
     }
   }
@@ -83,11 +83,11 @@ cudaError_t launch_mirror(const double *U, float *M, int n, int ncube, double rh
                           const Batch &bt, cudaStream_t s) {
   if (ncube <= 1) return cudaSuccess;  // cube slot 0 is unused
   const int S = n + 4;
-  const int cube_pairs = 5 * S * S * S / 2;  // S is even
-  const dim3 grid((cube_pairs + 1023) / 1024, ncube - 1 < 65535 ? ncube - 1 : 65535);
+  const int cube_cell_pairs = S * S * S / 2;  // S is even
+  const dim3 grid((cube_cell_pairs + 511) / 512, ncube - 1 < 65535 ? ncube - 1 : 65535);
   k_mirror<<<grid, 256, 0, s>>>(reinterpret_cast<const double2 *>(U),
                                reinterpret_cast<float2 *>(M), rho0, P0 / (BCMG_K - 1), bt,
-                               cube_pairs, ncube - 1);
+                               cube_cell_pairs, ncube - 1);
   return cudaGetLastError();
 }
 
