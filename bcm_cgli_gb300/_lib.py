@@ -43,6 +43,11 @@ class CaseDesc(C.Structure):
     ]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("flux_tile", C.c_int), ("lusgs_threads", C.c_int),
+                ("flux_ms", C.c_double * 2), ("lusgs_ms", C.c_double * 2)]
+
+
 class RefConfig(C.Structure):
     _fields_ = [("ncube_x", C.c_int), ("mpi_ncube", C.c_int), ("mu_L", C.c_double),
                 ("rho0", C.c_double), ("U0", C.c_double), ("Uin", C.c_double),
@@ -89,6 +94,8 @@ def _declare(L):
     L.bcmg_batch_create.argtypes = [C.c_int, C.POINTER(CaseDesc), C.POINTER(P)]
     L.bcmg_case_set_method.argtypes = [P, C.c_int, C.c_double, C.c_double]
     L.bcmg_case_mirror.argtypes = [P, P]
+    L.bcmg_case_set_tuning.argtypes = [P, C.POINTER(Tuning)]
+    L.bcmg_case_autotune.argtypes = [P, C.c_int, C.POINTER(Tuning)]
     L.bcmg_case_output_q.argtypes = [P, C.c_int, C.c_int, C.c_char_p]
     L.bcmg_case_output_x.argtypes = [P, C.c_int, C.c_int, C.c_char_p, P]
     L.bcmg_case_output_wait.argtypes = [P]

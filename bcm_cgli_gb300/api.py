@@ -286,6 +286,21 @@ class CaseContext:
         check(lib().bcmg_case_output_x(self.h, int(q), int(ncube_out), os.fsencode(path),
                                        o.ctypes.data))
 
+    def set_tuning(self, flux_tile=0, lusgs_threads=0):
+        """Launch shapes: flux tile edge (0, 4 or 8) and threads per cube of the
+        split LU-SGS sweep (0: the widest plane)."""
+        t = _lib.Tuning(int(flux_tile), int(lusgs_threads))
+        check(lib().bcmg_case_set_tuning(self.h, C.byref(t)))
+
+    def autotune(self, reps=3):
+        """Times the launch-shape candidates on this context's state, applies the
+        fastest and returns the choice with the measured milliseconds."""
+        t = _lib.Tuning()
+        check(lib().bcmg_case_autotune(self.h, int(reps), C.byref(t)))
+        return {"flux_tile": t.flux_tile, "lusgs_threads": t.lusgs_threads,
+                "flux_ms": {"8": t.flux_ms[0], "4": t.flux_ms[1]},
+                "lusgs_ms": {"widest": t.lusgs_ms[0], "half": t.lusgs_ms[1]}}
+
     def mirror(self):
         """FP32 mirror of the current state (split-precision path)."""
         out = np.empty(self.shape, np.float32)

@@ -221,6 +221,9 @@ struct bcmg_case {
   // Sub-iteration method (bcmg_case_set_method): RK3 (the reference's) or
   // LU-SGS with its pseudo-time CFL (0: none) and relaxation factor.
   int method = BCMG_METHOD_RK3;
+  // Launch shapes (bcmg_case_set_tuning / bcmg_case_autotune): flux tile
+  // edge (0: default) and threads per cube of the split LU-SGS sweep.
+  int tile = 0, lu_threads = 0;
   double lu_cfl = 0.0, lu_omega = 1.5;
   // Convergence-driven stepping (bcmg_case_advance_converged)
   bool conv = false;                 // kernels see the active masks
@@ -316,6 +319,7 @@ int case_flux(bcmg_case *c, int RK) {
   a.Residual1 = c->Residual1;
   a.bt = c->bt();
   a.raw = RK == 0;  // residual only (LU-SGS)
+  a.tile = c->tile;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (c->profile) {
     while (c->ev.size() < c->ev_used + 2) {
@@ -358,6 +362,7 @@ int case_flux(bcmg_case *c, int RK) {
     // RK 0 (LU-SGS): FP32 residual into the Rku1 buffer, which the split
     // path does not otherwise use
     sa.R32 = reinterpret_cast<float *>(c->Rku1);
+    sa.tile = c->tile;
     sa.partials = c->partials;
     sa.Residual1 = c->Residual1;
     sa.bt = c->bt();
@@ -407,46 +412,51 @@ int case_prologue(bcmg_case *c) {
 
 // One LU-SGS sub-iteration: prologue, residual, sweeps with the update and
 // per-cube norm partials, norms, interface.
+LusgsSplitArgs lusgs_split_args(bcmg_case *c) {
+  LusgsSplitArgs l;
+  l.ph = c->ph;
+  l.dTf = (float)c->dT;
+  l.cflf = (float)c->lu_cfl;
+  l.omegaf = (float)c->lu_omega;
+  l.rho0f = (float)c->ph.rho0;
+  l.P0f = (float)c->ph.P0;
+  l.T0f = (float)(c->ph.P0 / c->ph.rho0 / BCMG_R);
+  l.mu_Lf = (float)c->ph.mu_L;
+  l.FWS = c->FWS;
+  l.inv_dx = c->inv_dx;
+  l.M = c->M;
+  l.U1_ = c->U1_;
+  l.R32 = reinterpret_cast<const float *>(c->Rku1);
+  l.scr = c->lu_scr;
+  l.Residual1 = c->Residual1;
+  l.partials = c->partials;
+  l.bt = c->bt();
+  l.threads = c->lu_threads;
+  return l;
+}
+
 int case_lusgs(bcmg_case *c) {
   int r;
   if ((r = case_prologue(c))) return r;
   if ((r = case_flux(c, 0))) return r;
   if (c->precision == BCMG_PRECISION_SPLIT) {
-    LusgsSplitArgs l;
+    CK(launch_lusgs_split(lusgs_split_args(c), c->ncube - 1, c->stream));
+  } else {
+    LusgsArgs l;
     l.ph = c->ph;
-    l.dTf = (float)c->dT;
-    l.cflf = (float)c->lu_cfl;
-    l.omegaf = (float)c->lu_omega;
-    l.rho0f = (float)c->ph.rho0;
-    l.P0f = (float)c->ph.P0;
-    l.T0f = (float)(c->ph.P0 / c->ph.rho0 / BCMG_R);
-    l.mu_Lf = (float)c->ph.mu_L;
+    l.dT = c->dT;
+    l.cfl = c->lu_cfl;
+    l.omega = c->lu_omega;
     l.FWS = c->FWS;
-    l.inv_dx = c->inv_dx;
-    l.M = c->M;
+    l.cube_size = c->cube_size;
     l.U1_ = c->U1_;
-    l.R32 = reinterpret_cast<const float *>(c->Rku1);
-    l.scr = c->lu_scr;
+    l.Rku1 = c->Rku1;
+    l.coefA = c->U1p1;
+    l.coefB = c->U1p2;
     l.Residual1 = c->Residual1;
     l.partials = c->partials;
     l.bt = c->bt();
-    CK(launch_lusgs_split(l, c->ncube - 1, c->stream));
-  } else {
-  LusgsArgs l;
-  l.ph = c->ph;
-  l.dT = c->dT;
-  l.cfl = c->lu_cfl;
-  l.omega = c->lu_omega;
-  l.FWS = c->FWS;
-  l.cube_size = c->cube_size;
-  l.U1_ = c->U1_;
-  l.Rku1 = c->Rku1;
-  l.coefA = c->U1p1;
-  l.coefB = c->U1p2;
-  l.Residual1 = c->Residual1;
-  l.partials = c->partials;
-  l.bt = c->bt();
-  CK(launch_lusgs(l, c->ncube - 1, c->stream));
+    CK(launch_lusgs(l, c->ncube - 1, c->stream));
   }
   ++c->launches;
   if (c->batched)
@@ -465,7 +475,7 @@ int case_stage(bcmg_case *c, int RK) {
   int nb = 0;
   if (c->precision == BCMG_PRECISION_SPLIT) {
     // the split flux kernel applied the stage update and wrote the partials
-    nb = flux_split_blocks(c->ph.n, c->ncube - 1);
+    nb = flux_split_blocks(c->ph.n, c->ncube - 1, c->tile);
     if (RK == 3) {
       if (c->batched)
         CK(launch_norms_batch(c->ph.n, c->cases, c->case_blk_flux, c->ncase, c->partials, c->er,
@@ -769,8 +779,8 @@ int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out)
   probe.ph = c->ph;
   probe.ncube = c->ncube;
   c->nparts = rk_partial_blocks(probe);
-  if (d->precision == BCMG_PRECISION_SPLIT)
-    c->nparts = std::max(c->nparts, flux_split_blocks(d->n, d->ncube - 1));
+  if (d->precision == BCMG_PRECISION_SPLIT)  // room for either tile edge
+    c->nparts = std::max(c->nparts, flux_split_blocks(d->n, d->ncube - 1, 4));
   c->nparts = std::max(c->nparts, d->ncube - 1);  // LU-SGS: one block per cube
   if (c->batched) {
     // Stage-update blocks of about equal size that never straddle two cases
@@ -1476,6 +1486,116 @@ int bcmg_case_mirror(bcmg_case *c, float *M) {
   CK(launch_mirror(c->U1_, c->M, c->ph.n, c->ncube, c->ph.rho0, c->ph.P0, c->bt(), c->stream));
   CK(cudaMemcpyAsync(M, c->M, c->ncell * 5 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  return BCMG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Launch-shape tuning.  The choices change how work is split across CTAs,
+// never the arithmetic of a cell: the FP64 path stays bit-identical to the
+// reference with either tile edge (each cell's operations are the same), the
+// split path's results change only by where a CTA boundary falls in its
+// fixed-order norm sums.
+// ---------------------------------------------------------------------------
+int bcmg_case_set_tuning(bcmg_case *c, const bcmg_tuning *t) {
+  clear_err();
+  if (!c || !t) { set_err("null argument"); return BCMG_ERR_ARG; }
+  const int n = c->ph.n;
+  if (!(t->flux_tile == 0 || ((t->flux_tile == 4 || t->flux_tile == 8) && n % t->flux_tile == 0))) {
+    set_err("flux_tile must be 0, or 4 or 8 dividing n");
+    return BCMG_ERR_ARG;
+  }
+  if (t->lusgs_threads != 0 &&
+      (n * n > 1024 || t->lusgs_threads % 32 != 0 || t->lusgs_threads < 32 ||
+       t->lusgs_threads > lusgs_split_default_threads(n))) {
+    set_err("lusgs_threads must be 0 or a multiple of 32 up to the widest plane of a cube");
+    return BCMG_ERR_ARG;
+  }
+  const int old_tiles = flux_split_blocks(n, 1, c->tile);
+  c->tile = t->flux_tile;
+  c->lu_threads = t->lusgs_threads;
+  const int tiles = flux_split_blocks(n, 1, c->tile);
+  if (c->batched && tiles != old_tiles) {
+    std::vector<int> cbf(c->ncase + 1);
+    for (int q = 0; q <= c->ncase; ++q) cbf[q] = (c->case_cube0[q] - 1) * tiles;
+    CK(cudaMemcpy(c->case_blk_flux, cbf.data(), sizeof(int) * cbf.size(), cudaMemcpyHostToDevice));
+  }
+  if (c->graph) cudaGraphExecDestroy(c->graph);  // captured steps hold the old shapes
+  c->graph = nullptr;
+  c->graph_subiters = -1;
+  if (c->cgraph) cudaGraphExecDestroy(c->cgraph);
+  c->cgraph = nullptr;
+  return BCMG_OK;
+}
+
+int bcmg_case_autotune(bcmg_case *c, int reps, bcmg_tuning *out) {
+  clear_err();
+  if (!c || reps < 1) { set_err("bad arguments"); return BCMG_ERR_ARG; }
+  const int n = c->ph.n;
+  bcmg_tuning best{};
+  best.flux_tile = c->tile;
+  best.lusgs_threads = c->lu_threads;
+  // Flux: tile edges 8 and 4 (8 only when it divides n), timed on the
+  // context's own state (bcmg_case_time_flux restores it).
+  const int tiles[2] = {8, 4};
+  double best_ms = 1e300;
+  for (int v = 0; v < 2; ++v) {
+    if (n % tiles[v] != 0) continue;
+    bcmg_tuning t = best;
+    t.flux_tile = tiles[v];
+    int r = bcmg_case_set_tuning(c, &t);
+    if (r) return r;
+    double ms = 0;
+    if ((r = bcmg_case_time_flux(c, reps, &ms))) return r;
+    best.flux_ms[v] = ms;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best.flux_tile = tiles[v];
+    }
+  }
+  // Split LU-SGS sweep: the widest plane's threads or half of them (wide
+  // planes then take two passes), timed on the residual of the current
+  // state; the state is restored afterwards.
+  if (c->precision == BCMG_PRECISION_SPLIT && c->method == BCMG_METHOD_LUSGS && c->lu_scr) {
+    const int full = lusgs_split_default_threads(n);
+    const int cand[2] = {full, ((full / 2) + 31) / 32 * 32};
+    const size_t bytes = c->ncell * 5 * sizeof(double);
+    CK(cudaMemcpyAsync(c->U1p1, c->U1_, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    int r = case_flux(c, 0);  // residual and mirror of the current state
+    if (r) return r;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    double lbest = 1e300;
+    for (int v = 0; v < 2; ++v) {
+      c->lu_threads = cand[v];
+      LusgsSplitArgs l = lusgs_split_args(c);
+      cudaError_t e = launch_lusgs_split(l, c->ncube - 1, c->stream);  // warm-up
+      if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
+      for (int i = 0; i < reps && e == cudaSuccess; ++i)
+        e = launch_lusgs_split(l, c->ncube - 1, c->stream);
+      if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      float ms = 0;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (e != cudaSuccess) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        CK(e);
+      }
+      best.lusgs_ms[v] = ms / reps;
+      if (ms / reps < lbest) {
+        lbest = ms / reps;
+        best.lusgs_threads = v == 0 ? 0 : cand[v];
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CK(cudaMemcpyAsync(c->U1_, c->U1p1, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  int r = bcmg_case_set_tuning(c, &best);
+  if (r) return r;
+  if (out) *out = best;
   return BCMG_OK;
 }
 

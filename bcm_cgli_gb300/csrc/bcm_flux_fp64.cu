@@ -351,9 +351,9 @@ static cudaError_t launch_t(const FluxArgs &a, int ncubes, cudaStream_t s) {
 
 // Cubes [a.cube0, a.cube0 + ncubes) of the flat list.
 cudaError_t launch_flux_fp64(const FluxArgs &a, int ncubes, cudaStream_t s) {
-  if (a.ph.n % 8 == 0) return launch_t<8>(a, ncubes, s);
-  if (a.ph.n % 4 == 0) return launch_t<4>(a, ncubes, s);
-  return cudaErrorInvalidValue;
+  if (a.ph.n % 4 != 0) return cudaErrorInvalidValue;
+  if (flux_tile(a.ph.n, a.tile) == 8) return launch_t<8>(a, ncubes, s);
+  return launch_t<4>(a, ncubes, s);
 }
 
 }  // namespace bcmg

@@ -610,16 +610,22 @@ static cudaError_t launch_split_t(const FluxSplitArgs &a, int ncubes, cudaStream
   return cudaGetLastError();
 }
 
-int flux_split_blocks(int n, int ncubes) {
-  const int T = n % 8 == 0 ? 8 : 4;
+int flux_tile(int n, int tile) {
+  if (tile == 8 && n % 8 == 0) return 8;
+  if (tile == 4 && n % 4 == 0) return 4;
+  return n % 8 == 0 ? 8 : 4;
+}
+
+int flux_split_blocks(int n, int ncubes, int tile) {
+  const int T = flux_tile(n, tile);
   const int nt = n / T;
   return ncubes * nt * nt * nt;
 }
 
 cudaError_t launch_flux_split(const FluxSplitArgs &a, int ncubes, cudaStream_t s) {
-  if (a.ph.n % 8 == 0) return launch_split_t<8>(a, ncubes, s);
-  if (a.ph.n % 4 == 0) return launch_split_t<4>(a, ncubes, s);
-  return cudaErrorInvalidValue;
+  if (a.ph.n % 4 != 0) return cudaErrorInvalidValue;
+  if (flux_tile(a.ph.n, a.tile) == 8) return launch_split_t<8>(a, ncubes, s);
+  return launch_split_t<4>(a, ncubes, s);
 }
 
 }  // namespace bcmg

@@ -48,6 +48,7 @@ struct FluxArgs {
   double *Rku1, *Residual1;
   Batch bt;
   int raw = 0;  // 1: write the residual R itself (LU-SGS right-hand side)
+  int tile = 0;  // tile edge 8 or 4 (0: 8 when n is a multiple of 8, else 4)
 };
 
 // FP64 residual + increment (bit-exact with the reference).
@@ -74,12 +75,15 @@ struct FluxSplitArgs {
   int RK;              // stage 1..3: the kernel applies the stage update;
                        // 0: it writes the FP32 residual to R32 instead
   float *R32 = nullptr;  // [ncell][5] (RK == 0)
+  int tile = 0;          // tile edge 8 or 4 (0: 8 when n is a multiple of 8, else 4)
   double *partials;    // [blocks][7] norm/force partial sums (stage 3)
   double *Residual1;
   Batch bt;
 };
+// Tile edge a flux launch uses (tile: 0 default, else 8 or 4 when it divides n).
+int flux_tile(int n, int tile);
 // Blocks of one split flux launch over ncubes cubes (one per tile).
-int flux_split_blocks(int n, int ncubes);
+int flux_split_blocks(int n, int ncubes, int tile = 0);
 cudaError_t launch_mirror(const double *U, float *M, int n, int ncube, double rho0, double P0,
                           const Batch &bt, cudaStream_t s);
 cudaError_t launch_flux_split(const FluxSplitArgs &a, int ncubes, cudaStream_t s);
@@ -148,6 +152,7 @@ struct LusgsSplitArgs {
   double *U1_;             // updated in place on fluid cells
   const float *R32;        // residual (FP32) of every cell
   float *scr;              // [ncube-1][11][n^3] sweep scratch (lusgs_split_scratch)
+  int threads = 0;         // threads per cube (0: the widest plane, in whole warps)
   const double *Residual1;
   double *partials;        // [ncube-1][7]
   Batch bt;
@@ -155,6 +160,8 @@ struct LusgsSplitArgs {
 cudaError_t launch_lusgs_split(const LusgsSplitArgs &a, int ncubes, cudaStream_t s);
 // Floats of that scratch per cube.
 size_t lusgs_split_scratch(int n);
+// Default threads per cube of the split LU-SGS kernel (the widest plane).
+int lusgs_split_default_threads(int n);
 
 // PLOT3D byte images of BCM_Output (bcm_output.cu) for cubes
 // [cube0, cube0 + ncubes): solution (4 + 5 (n+2)^3 doubles per cube) and

@@ -372,15 +372,21 @@ static int lusgs_split_threads(int n) {
   return (mx + 31) / 32 * 32;
 }
 
+int lusgs_split_default_threads(int n) { return lusgs_split_threads(n); }
+
 cudaError_t launch_lusgs_split(const LusgsSplitArgs &a, int ncubes, cudaStream_t s) {
   if (ncubes <= 0) return cudaSuccess;
   const int n = a.ph.n;
   if (n * n > 1024) return cudaErrorInvalidValue;  // columns are 16-bit shared indices
-  static std::atomic<int> cache[33];  // threads per n (0: not yet computed)
+  static std::atomic<int> cache[33];  // widest plane per n (0: not yet computed)
   int threads = cache[n].load(std::memory_order_relaxed);
   if (threads == 0) {
     threads = lusgs_split_threads(n);
     cache[n].store(threads, std::memory_order_relaxed);
+  }
+  if (a.threads > 0) {
+    if (a.threads % 32 != 0 || a.threads > threads) return cudaErrorInvalidValue;
+    threads = a.threads;  // fewer threads: wide planes take several passes
   }
   const int np = 3 * n - 2;
   size_t smem = (size_t)2 * n * n * kSlot * sizeof(float) +

@@ -271,8 +271,14 @@ def measure(api, case, precision_name, args, dist, clocks_on=True, method=None):
     kernel's launches are bracketed by events for its average duration."""
     precision = api.PRECISION_SPLIT if precision_name == "split" else api.PRECISION_FP64
     ctx = make_context(api, case, precision)
-    if (method or getattr(args, "method", "rk3")) == "lusgs":
+    meth = method or getattr(args, "method", "rk3")
+    if meth == "lusgs":
         ctx.set_method(api.METHOD_LUSGS, cfl=0.0, omega=1.5)
+    # launch shapes from the committed autotuner table (bcm_cgli_gb300/autotune.py)
+    from bcm_cgli_gb300 import autotune
+    shape = autotune.lookup(case.n, precision_name, meth)
+    if shape:
+        ctx.set_tuning(shape["flux_tile"], shape["lusgs_threads"])
     ctx.set_state(case.U, case.U, case.U)
     for _ in range(args.warmup):
         ctx.advance(1, SUBITERS, use_graph=False)
@@ -295,7 +301,9 @@ def measure(api, case, precision_name, args, dist, clocks_on=True, method=None):
     flux_ms, flux_n = ctx.profile()
     ctx.set_profiling(False)
     cell_subiters = case.n_cells * SUBITERS * args.steps * dist.world
-    out = {"value": dist.throughput(case.n_cells * SUBITERS * args.steps, ms),
+    out = {"tuning": ({"flux_tile": shape["flux_tile"], "lusgs_threads": shape["lusgs_threads"],
+                       "from": "bcm_cgli_gb300/tuning_gb300.json"} if shape else None),
+           "value": dist.throughput(case.n_cells * SUBITERS * args.steps, ms),
            "ms_per_step": ms / args.steps,
            "launches": launches, "flux_ms_avg": flux_ms / max(1, flux_n), "flux_launches": flux_n,
            "clocks": clk, "ctx": ctx}
@@ -447,6 +455,7 @@ def run_gpu_arm(args, dist):
             "e2e": ({"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 3 * case.U.nbytes,
                      "d2h_bytes_per_step": 3 * case.U.nbytes} if e2e is not None else None),
             "gpu_launches": m_head["launches"], "clocks": m_head["clocks"],
+            "launch_shapes": m_head["tuning"],
             "fp64_alu": {"measured_fma_gflops": fp64_gflops,
                          "note": "FP64 FMA rate of this GPU, measured by bcmg_probe_fp64_rate"}}
     if m_other is not None:

@@ -223,6 +223,26 @@ int bcmg_case_output_wait(bcmg_case *c);
  * flux kernel reads) and copies it to M[ncell][5] on the host, for checks. */
 int bcmg_case_mirror(bcmg_case *c, float *M);
 
+/* Launch shapes.  flux_tile: edge of the cube tile one flux CTA works on,
+ * 8 or 4 (0: 8 when it divides n, else 4); lusgs_threads: threads per cube
+ * of the split-precision LU-SGS sweep, a multiple of 32 up to the widest
+ * plane of a cube (0: the widest plane; fewer threads take wide planes in
+ * several passes).  The shapes change how work is spread over the GPU, not
+ * any cell's arithmetic (the FP64 path stays bit-identical to the
+ * reference).  bcmg_case_autotune times the candidates on the context's own
+ * state with CUDA events (`reps` launches each, state restored), applies the
+ * fastest and reports every time in `out` (flux_ms: tiles 8 and 4;
+ * lusgs_ms: widest plane, half of it; 0 where not measured).  The LU-SGS
+ * candidates are timed only on the split path with LU-SGS selected. */
+typedef struct bcmg_tuning {
+  int flux_tile;
+  int lusgs_threads;
+  double flux_ms[2];
+  double lusgs_ms[2];
+} bcmg_tuning;
+int bcmg_case_set_tuning(bcmg_case *c, const bcmg_tuning *t);
+int bcmg_case_autotune(bcmg_case *c, int reps, bcmg_tuning *out);
+
 /* Waits for all work of the context. */
 int bcmg_case_sync(bcmg_case *c);
 

@@ -218,3 +218,41 @@ def test_sphere_ibm_two_level_bitwise(port, graph):
     assert abs(er[6] - a.er[6]) <= 1e-12 * max(abs(a.er[6]), scale)
     assert abs(er[7] - a.er[7]) <= 1e-12 * max(abs(a.er[7]), scale)
     ctx.close()
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_tile_shape_keeps_fp64_bitwise(port, graph):
+    """Tile edge 4 instead of 8: the same per-cell arithmetic, so the FP64
+    state after whole dual-time steps still equals the oracle's bit for bit."""
+    case = _cases()["two_level_open_n8"]
+    a = O.State(case)
+    port.run(case, a, G.RUN_STEPS, G.RUN_SUBITERS)
+    ctx = api.CaseContext(case)
+    ctx.set_tuning(flux_tile=4)
+    ctx.set_state(case.U, case.U, case.U)
+    er = ctx.advance(G.RUN_STEPS, G.RUN_SUBITERS, use_graph=graph)
+    U1_, U1, U1q = ctx.get_state()
+    assert np.array_equal(U1_, a.U1_) and np.array_equal(U1, a.U1) and np.array_equal(U1q, a.U1q)
+    assert np.allclose(er[1:6], a.er[1:6], rtol=1e-12, atol=0)
+    with pytest.raises(api.BcmgError):
+        ctx.set_tuning(flux_tile=6)
+    ctx.close()
+
+
+def test_autotune_applies_a_valid_shape(port):
+    case = cases.taylor_green(ncx=2, n=16)
+    for prec in (api.PRECISION_FP64, api.PRECISION_SPLIT):
+        ctx = api.CaseContext(case, precision=prec)
+        ctx.set_method(api.METHOD_LUSGS)
+        ctx.set_state(case.U, case.U, case.U)
+        before = ctx.get_state()
+        res = ctx.autotune(2)
+        assert res["flux_tile"] in (4, 8)
+        assert res["flux_ms"]["8"] > 0 and res["flux_ms"]["4"] > 0
+        if prec == api.PRECISION_SPLIT:
+            assert res["lusgs_ms"]["widest"] > 0 and res["lusgs_ms"]["half"] > 0
+        after = ctx.get_state()  # the tuner restores the state it timed on
+        for x, y in zip(before, after):
+            assert np.array_equal(x, y)
+        ctx.advance(1, 2)
+        ctx.close()
