@@ -107,6 +107,52 @@ def BCM_Ghostcell_plus(myid, NNBC, weight, GCindex, IPsur, FWS, U1_):
     _raise_if_failed("BCM_Ghostcell_plus")
 
 
+def _fws_inplace(FWS):
+    if FWS.dtype != np.int32 or not FWS.flags.c_contiguous:
+        raise BcmgError("FWS must be a C-contiguous int32 array (updated in place)")
+    return FWS
+
+
+def BCM_Immersed_boundary(myid, ncube, n_wallcube, NBC, Xmin, Xmax, Ymin, Ymax, Zmin, Zmax,
+                          cube_size, csl, Xcube, Ycube, Zcube, Xcnt, Ycnt, Zcnt, FWS, wallcube):
+    """BCM_Immersed_boundary.cpp:127-1081 on the GPU: reads BCM_STL_fine.stl
+    in the working directory, updates FWS in place and writes
+    IBM_minus<myid>.dat / IBM_plus<myid>.dat.  Xcnt/Ycnt/Zcnt may be None
+    (centres formed from the cube corners).  NBC, n_wallcube, the domain
+    bounds and wallcube are unused, as in the reference."""
+    cen = [None if a is None else _dp(a) for a in (Xcnt, Ycnt, Zcnt)]
+    lib().BCM_Immersed_boundary(int(myid), int(ncube), int(n_wallcube), None, float(Xmin),
+                                float(Xmax), float(Ymin), float(Ymax), float(Zmin), float(Zmax),
+                                _dp(cube_size), _ip(csl), _dp(Xcube), _dp(Ycube), _dp(Zcube),
+                                *(None if a is None else a.ctypes.data for a in cen),
+                                _fws_inplace(FWS), None)
+    _raise_if_failed("BCM_Immersed_boundary")
+
+
+def ibm_preprocess(case, tris, fws=None):
+    """The IBM preprocessing of BCM_Immersed_boundary in memory, on the GPU:
+    tris[ntri, 3, 3] in STL facet order; fws (default case.fws) updated in
+    place.  Returns the minus and plus tables, each (GCindex[m,4],
+    IPsur[m,4], weight[m,8]) with 0-based rows and unrounded weights."""
+    fws = _fws_inplace(case.fws if fws is None else fws)
+    tri = np.ascontiguousarray(np.asarray(tris, np.float64).reshape(-1, 9))
+    cap = int((fws == 0).sum()) + 1
+    o = np.ascontiguousarray(case.origin, dtype=np.float64)
+    out = [np.zeros(4 * cap, np.int32), np.zeros(4 * cap, np.int32), np.zeros(8 * cap),
+           np.zeros(4 * cap, np.int32), np.zeros(4 * cap, np.int32), np.zeros(8 * cap)]
+    nm, npl = C.c_int(), C.c_int()
+    check(lib().bcmg_ibm_preprocess(
+        int(case.n), int(case.ncube), np.ascontiguousarray(case.cube_size, np.float64),
+        _ip(case.csl), np.ascontiguousarray(o[:, 0]), np.ascontiguousarray(o[:, 1]),
+        np.ascontiguousarray(o[:, 2]), fws, tri.shape[0], tri if tri.size else np.zeros(9),
+        cap, C.byref(nm), out[0], out[1], out[2], C.byref(npl), out[3], out[4], out[5]))
+    m, p = nm.value, npl.value
+    return ((out[0][:4 * m].reshape(m, 4), out[1][:4 * m].reshape(m, 4),
+             out[2][:8 * m].reshape(m, 8)),
+            (out[3][:4 * p].reshape(p, 4), out[4][:4 * p].reshape(p, 4),
+             out[5][:8 * p].reshape(p, 8)))
+
+
 def interface_lists(case):
     """The 15 neighbour lists of BCM_Interface_table.cpp:96-308 (1-based
     arrays): per axis x, y, z the same-level, big->small (+), small->big (+),

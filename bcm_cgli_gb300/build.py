@@ -33,6 +33,7 @@ UNITS = [
     ("bcm_lusgs.cu", ["--fmad=false"]),
     ("bcm_lusgs_split.cu", ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"]),
     ("bcm_output.cu", ["--fmad=false"]),
+    ("bcm_ibm.cu", ["--fmad=false"]),
     ("bcm_tables.cpp", []),
 ]
 

@@ -422,22 +422,105 @@ def random_two_level_case(seed=1, ncx=2, ncy=2, ncz=2, n=4, periodic=True, visco
                 name=name)
 
 
+def icosphere(levels: int = 5, radius: float = 0.5, center=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """Triangles [20 * 4**levels, 3, 3] of a sphere: an icosahedron whose faces
+    are split into four `levels` times, new vertices pushed onto the sphere;
+    counter-clockwise seen from outside (outward normals).  levels=5 gives the
+    20,480 triangles of the sphere benchmark."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    verts = [np.array(v, np.float64) for v in (
+        (-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t),
+        (0, -1, -t), (0, 1, -t), (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1))]
+    verts = [v / np.linalg.norm(v) for v in verts]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4),
+             (11, 10, 2), (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8),
+             (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    tris = np.array([[verts[a], verts[b], verts[c]] for a, b, c in faces])
+    for _ in range(levels):
+        a, b, c = tris[:, 0], tris[:, 1], tris[:, 2]
+        ab, bc, ca = a + b, b + c, c + a
+        ab /= np.linalg.norm(ab, axis=1)[:, None]
+        bc /= np.linalg.norm(bc, axis=1)[:, None]
+        ca /= np.linalg.norm(ca, axis=1)[:, None]
+        tris = np.concatenate([np.stack([a, ab, ca], 1), np.stack([b, bc, ab], 1),
+                               np.stack([c, ca, bc], 1), np.stack([ab, bc, ca], 1)])
+    return tris * radius + np.asarray(center, np.float64)
+
+
+def write_stl(path: str, tris: np.ndarray, name: str = "body") -> None:
+    """ASCII STL (the format BCM_Immersed_boundary.cpp:197-270 reads), every
+    coordinate written so that it reads back exactly."""
+    lines = [f"solid {name}"]
+    for t in tris:
+        nrm = np.cross(t[1] - t[0], t[2] - t[0])
+        nrm = nrm / max(np.linalg.norm(nrm), 1e-300)
+        lines.append("  facet normal %r %r %r" % tuple(float(x) for x in nrm))
+        lines.append("    outer loop")
+        for v in t:
+            lines.append("      vertex %r %r %r" % tuple(float(x) for x in v))
+        lines.append("    endloop")
+        lines.append("  endfacet")
+    lines.append(f"endsolid {name}")
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def read_stl(path: str) -> np.ndarray:
+    """Triangles [ntri, 3, 3] of an ASCII STL, in file order."""
+    vals = []
+    with open(path) as f:
+        for line in f:
+            tok = line.split()
+            if tok and tok[0] == "vertex":
+                vals.append([float(x) for x in tok[1:4]])
+    return np.asarray(vals, np.float64).reshape(-1, 3, 3)
+
+
+def _pack_tables(gc, ip, w):
+    """0-based [m,4] / [m,8] tables -> the 1-based packed arrays of
+    BCM_Reading_IBM (weight[8m+1], GCindex[4m+1], IPsur[4m+1])."""
+    m = len(gc)
+    GC = np.zeros(4 * m + 1, np.int32)
+    IP = np.zeros(4 * m + 1, np.int32)
+    W = np.zeros(8 * m + 1)
+    GC[1:] = np.asarray(gc, np.int32).reshape(-1)
+    IP[1:] = np.asarray(ip, np.int32).reshape(-1)
+    W[1:] = np.asarray(w, np.float64).reshape(-1)
+    return W, GC, IP
+
+
+def quantize_weights(w: np.ndarray) -> np.ndarray:
+    """Weights as the reference's text files carry them (printed with %f, six
+    decimals, then read back)."""
+    return np.array([float("%f" % x) for x in np.asarray(w, np.float64).reshape(-1)]).reshape(
+        np.shape(w))
+
+
 def sphere_ibm(n=16, coarse=2.0, box=((-10.0, 20.0), (-10.0, 10.0), (-10.0, 10.0)),
                refine_box=((-2.0, 4.0), (-2.0, 2.0), (-2.0, 2.0)), diameter=1.0, mach=0.3,
-               reynolds=300.0, noise=1e-4, seed=7, dT=1e-4, sub_ratio=200.0, name="sphere"):
+               reynolds=300.0, noise=1e-4, seed=7, dT=1e-4, sub_ratio=200.0, name="sphere",
+               preprocess=None, stl_levels=5):
     """Flow past a sphere with immersed-boundary ghost cells on a two-level grid.
 
     Coarse cubes of edge `coarse` tile `box`; those inside `refine_box` are
-    split into 2x2x2 fine cubes (2:1).  Flags from the analytic sphere
-    (BCM.h:6-8): cells whose centre lies inside are solid, solid cells with a
-    fluid face neighbour are IBM ghost cells.  Each ghost cell gets the image
-    point mirrored across the surface, the 8 cells around it in its own cube
-    (IPsur) and trilinear weights in the reference's 000,100,010,001,110,101,
-    011,111 order rounded to 6 decimals (BCM_Immersed_boundary.cpp writes them
-    with %f); ghosts with x < 0 go to the "minus" list, the rest to "plus".
-    Free stream at `mach`, Re on the diameter, seeded density noise; solid
-    cells at rest (BCM_Initial_condition.cpp).  Domain faces carry the
-    reference's X/Y/Z boundary conditions.
+    split into 2x2x2 fine cubes (2:1).  Flags in the reference's convention
+    (BCM.h:6-8): cells whose centre lies inside the sphere are solid; fluid
+    cells with a solid face neighbour are IBM ghost cells, whose value the
+    ghost fill sets halfway between the wall and an image point in the fluid
+    (BCM_Ghostcell_minus.cpp:172-189 halves the velocity).
+
+    IBM tables: with `preprocess` (a callable (case, triangles) -> (minus,
+    plus), each (GCindex[m,4], IPsur[m,4], weight[m,8]) 0-based, updating
+    case.fws in place like BCM_Immersed_boundary.cpp, e.g. the GPU
+    preprocessing) they come from the icosphere of 20 * 4**stl_levels
+    triangles (meta["triangles"]); without it, an analytic stand-in in the
+    same convention: boundary point = the ghost centre's radial projection
+    onto the sphere, image point = 2 centre - boundary point, trilinear
+    weights of its 8 surrounding cells in the ghost's cube.  Weights are
+    quantised to six decimals like the reference's files.  Free stream at
+    `mach`, Re on the diameter, seeded density noise; solid cells at rest
+    (BCM_Initial_condition.cpp).  Domain faces carry the reference's X/Y/Z
+    boundary conditions.
     """
     (x0, x1), (y0, y1), (z0, z1) = box
     ncx, ncy, ncz = (int(round((x1 - x0) / coarse)), int(round((y1 - y0) / coarse)),
@@ -463,51 +546,17 @@ def sphere_ibm(n=16, coarse=2.0, box=((-10.0, 20.0), (-10.0, 10.0), (-10.0, 10.0
     r = np.sqrt(X * X + Y * Y + Z * Z)
     solid = r < R
     fws = np.where(solid, ISOLID, IFLUID).astype(np.int32)
-    # ghost = solid with a fluid face neighbour (inside the padded cube)
+    # ghost = fluid cell with a solid face neighbour (inside the padded cube)
     ghost = np.zeros_like(solid)
     for ax in (1, 2, 3):
         for sh in (1, -1):
-            nb = np.roll(~solid, sh, axis=ax)
+            nb = np.roll(solid, sh, axis=ax)
             edge = [slice(None)] * 4
             edge[ax] = 0 if sh == 1 else S - 1
             nb[tuple(edge)] = False
-            ghost |= solid & nb
+            ghost |= (~solid) & nb
     fws[ghost] = IGHOST
     fws[0] = IFLUID
-    # IBM tables for interior ghost cells
-    entries = {"minus": [], "plus": []}
-    idx = np.argwhere(ghost[1:, 2:n + 2, 2:n + 2, 2:n + 2])
-    for cc, ii, jj, kk in idx:
-        c, i, j, k = int(cc) + 1, int(ii) + 2, int(jj) + 2, int(kk) + 2
-        dx = cube_size[c] / n
-        xg = np.array([X[c, i, j, k], Y[c, i, j, k], Z[c, i, j, k]])
-        rg = np.linalg.norm(xg)
-        xs = xg * (R / max(rg, 1e-12))
-        xi = 2 * xs - xg
-        # base cell of the 8-cell box containing the image point, kept inside
-        # the padded cube: centre of cell m is origin + (m - 1.5) dx
-        f = (xi - origin[c]) / dx + 1.5
-        base = np.clip(np.floor(f).astype(int), 1, S - 2)
-        t = np.clip(f - base, 0.0, 1.0)
-        wx, wy, wz = t
-        w = np.array([(1 - wx) * (1 - wy) * (1 - wz), wx * (1 - wy) * (1 - wz),
-                      (1 - wx) * wy * (1 - wz), (1 - wx) * (1 - wy) * wz, wx * wy * (1 - wz),
-                      wx * (1 - wy) * wz, (1 - wx) * wy * wz, wx * wy * wz])
-        w = np.round(w, 6)
-        e = (c, i, j, k, c, int(base[0]), int(base[1]), int(base[2]), w)
-        entries["minus" if xg[0] < 0 else "plus"].append(e)
-
-    def pack(lst):
-        m = len(lst)
-        GC = np.zeros(4 * m + 1, np.int32)
-        IP = np.zeros(4 * m + 1, np.int32)
-        W = np.zeros(8 * m + 1)
-        for q, (c, i, j, k, ic, bi, bj, bk, w) in enumerate(lst):
-            GC[4 * q + 1:4 * q + 5] = (c, i, j, k)
-            IP[4 * q + 1:4 * q + 5] = (ic, bi, bj, bk)
-            W[8 * q + 1:8 * q + 9] = w
-        return W, GC, IP
-
     cnt = ncube * S ** 3
     rnd = splitmix_uniform(seed, cnt).reshape(ncube, S, S, S)
     rho = ph.rho0 * (1 + noise * (rnd - 0.5))
@@ -519,19 +568,58 @@ def sphere_ibm(n=16, coarse=2.0, box=((-10.0, 20.0), (-10.0, 10.0), (-10.0, 10.0
     U = np.where(solid[..., None], rest, U)
     case = Case(n=n, ncube=ncube, phys=ph, cube_size=cube_size, csl=csl, origin=origin, adj=adj,
                 fws=fws, U=np.ascontiguousarray(U), dT=dT, dTau=dT / sub_ratio, name=name)
-    case.ibm_minus = pack(entries["minus"])
-    case.ibm_plus = pack(entries["plus"])
-    case.meta.update(area_ratio=2.602 / (np.pi / 4 * diameter ** 2), ghosts=int(ghost[1:].sum()))
+    if preprocess is not None:
+        tris = icosphere(stl_levels, R)
+        minus, plus = preprocess(case, tris)
+        case.meta["triangles"] = len(tris)
+    else:
+        minus, plus = _analytic_sphere_tables(case, X, Y, Z, R)
+    case.ibm_minus = _pack_tables(minus[0], minus[1], quantize_weights(minus[2]))
+    case.ibm_plus = _pack_tables(plus[0], plus[1], quantize_weights(plus[2]))
+    case.meta.update(area_ratio=2.602 / (np.pi / 4 * diameter ** 2),
+                     ghosts=int((case.fws[1:] == IGHOST).sum()))
     return case
 
 
+def _analytic_sphere_tables(case, X, Y, Z, R):
+    """Analytic stand-in for the preprocessing in the reference convention
+    (all entries on the minus side, as outward-facing geometry gives)."""
+    n, S = case.n, case.n + 4
+    gc, ip, ws = [], [], []
+    idx = np.argwhere(case.fws[1:, 2:n + 2, 2:n + 2, 2:n + 2] == IGHOST)
+    for cc, ii, jj, kk in idx:
+        c, i, j, k = int(cc) + 1, int(ii) + 2, int(jj) + 2, int(kk) + 2
+        dx = case.cube_size[c] / n
+        xg = np.array([X[c, i, j, k], Y[c, i, j, k], Z[c, i, j, k]])
+        bi = xg * (R / max(np.linalg.norm(xg), 1e-12))
+        xi = 2 * xg - bi
+        f = (xi - case.origin[c]) / dx + 1.5  # centre of cell m is origin + (m - 1.5) dx
+        base = np.floor(f).astype(int)
+        if np.any(base < 0) or np.any(base > S - 2):
+            continue
+        t = f - base
+        wx, wy, wz = t
+        w = np.array([(1 - wx) * (1 - wy) * (1 - wz), wx * (1 - wy) * (1 - wz),
+                      (1 - wx) * wy * (1 - wz), (1 - wx) * (1 - wy) * wz, wx * wy * (1 - wz),
+                      wx * (1 - wy) * wz, (1 - wx) * wy * wz, wx * wy * wz])
+        gc.append((c, i, j, k))
+        ip.append((c, int(base[0]), int(base[1]), int(base[2])))
+        ws.append(w)
+    m = len(gc)
+    minus = (np.array(gc, np.int32).reshape(m, 4), np.array(ip, np.int32).reshape(m, 4),
+             np.array(ws).reshape(m, 8))
+    empty = (np.zeros((0, 4), np.int32), np.zeros((0, 4), np.int32), np.zeros((0, 8)))
+    return minus, empty
+
+
 def sphere_cubes(target, n=16, mach=0.3, reynolds=300.0, seed=7, dT=None, sub_ratio=200.0,
-                 name=None):
+                 name=None, preprocess=None, stl_levels=5):
     """Sphere flow (D = 1, IBM ghost cells, two levels) with about `target`
     cubes: coarse cubes of edge 1 tile an mx x my x mz box (x about 1.5
     times y and z); the 2x2x2 coarse cubes around the sphere are split into
     64 fine cubes of edge 0.5, so the count is mx*my*mz + 56 (64 at least).
-    dT defaults to a convective CFL of 0.5 on the fine cells."""
+    dT defaults to a convective CFL of 0.5 on the fine cells.  preprocess,
+    stl_levels: as sphere_ibm."""
     m = max(target - 56, 8)
     my = max(2, int(round((m / 1.5) ** (1.0 / 3.0))))
     mx = max(2, int(round(m / (my * my))))
@@ -544,14 +632,16 @@ def sphere_cubes(target, n=16, mach=0.3, reynolds=300.0, seed=7, dT=None, sub_ra
     return sphere_ibm(n=n, coarse=1.0, box=((x0, x0 + mx), (y0, y0 + my), (y0, y0 + my)),
                       refine_box=((-1.0, 1.0), (-1.0, 1.0), (-1.0, 1.0)), mach=mach,
                       reynolds=reynolds, seed=seed, dT=dT, sub_ratio=sub_ratio,
-                      name=name or f"sphere{mx}x{my}x{my}")
+                      name=name or f"sphere{mx}x{my}x{my}", preprocess=preprocess,
+                      stl_levels=stl_levels)
 
 
-def sphere_batch(ncase=16, seed=2024, n=16, lo=64, hi=2048):
+def sphere_batch(ncase=16, seed=2024, n=16, lo=64, hi=2048, preprocess=None, stl_levels=5):
     """Independent sphere flows for one batched context: cube counts drawn
     from the seed in [lo, hi] (realised to the nearest mx*my*mz + 56), Mach
     uniform in [0.1, 0.6], Re uniform in [100, 1000], per-case dT (CFL 0.5 on
-    the fine cells) and per-case density-noise seeds."""
+    the fine cells) and per-case density-noise seeds.  preprocess,
+    stl_levels: as sphere_ibm."""
     r = splitmix_uniform(seed, 3 * ncase).reshape(ncase, 3)
     out = []
     for q in range(ncase):
@@ -559,7 +649,8 @@ def sphere_batch(ncase=16, seed=2024, n=16, lo=64, hi=2048):
         mach = 0.1 + 0.5 * float(r[q, 1])
         re = 100.0 + 900.0 * float(r[q, 2])
         out.append(sphere_cubes(min(target, hi), n=n, mach=mach, reynolds=re, seed=seed + 1 + q,
-                                name=f"sphere{q}"))
+                                name=f"sphere{q}", preprocess=preprocess,
+                                stl_levels=stl_levels))
     return out
 
 

@@ -62,17 +62,42 @@ WORKLOADS = {
 WORKLOAD = "tgv"
 
 
-def workload_case():
+class TimedPreprocess:
+    """IBM preprocessing of the sphere workloads (the 20,480-triangle
+    icosphere through BCM_Immersed_boundary's algorithm), with its wall time
+    summed over the cases it builds."""
+
+    def __init__(self, fn, where):
+        self.fn, self.where, self.seconds, self.calls = fn, where, 0.0, 0
+
+    def __call__(self, case, tris):
+        t0 = time.perf_counter()
+        out = self.fn(case, tris)
+        self.seconds += time.perf_counter() - t0
+        self.calls += 1
+        return out
+
+
+def workload_case(preprocess=None):
+    """The workload's case; preprocess (a TimedPreprocess) builds the IBM
+    tables of the sphere workloads from the triangulated body."""
     from bcm_cgli_gb300 import cases
     if WORKLOAD == "vortex":
         return cases.isentropic_vortex(ncx=4, n=16)
     if WORKLOAD == "sphere":
-        return cases.sphere_ibm()
-    if WORKLOAD == "tgv32":
+        case = cases.sphere_ibm(preprocess=preprocess)
+    elif WORKLOAD == "batch":
+        case = cases.CaseBatch(cases.sphere_batch(ncase=16, seed=2024, n=16,
+                                                  preprocess=preprocess), name="batch")
+    elif WORKLOAD == "tgv32":
         return cases.taylor_green(ncx=16, n=32)
-    if WORKLOAD == "batch":
-        return cases.CaseBatch(cases.sphere_batch(ncase=16, seed=2024, n=16), name="batch")
-    return cases.taylor_green(ncx=8, n=24)
+    else:
+        return cases.taylor_green(ncx=8, n=24)
+    if preprocess is not None:
+        case.meta["ibm_preprocess"] = {
+            "triangles": 20 * 4 ** 5, "cases": preprocess.calls, "where": preprocess.where,
+            "seconds": round(preprocess.seconds, 4)}
+    return case
 
 
 def is_batch(case):
@@ -91,7 +116,9 @@ def workload_config(case, precision):
         extra = {"cases": len(case.cases), "cubes": [c.ncube - 1 for c in case.cases],
                  "mach": [round(c.phys.U0 / np.sqrt(1.4 * c.phys.P0 / c.phys.rho0), 4)
                           for c in case.cases]}
-    return {**extra, 
+    if "ibm_preprocess" in getattr(case, "meta", {}):
+        extra["ibm_preprocess"] = case.meta["ibm_preprocess"]
+    return {**extra,
         "workload": WORKLOADS[WORKLOAD] + f"; {SUBITERS} sub-iterations x 3 RK stages per "
                                           "dual-time step",
         "cells": int(case.n_cells),
@@ -210,6 +237,16 @@ class Clocks:
 # CPU arm: the reference's algorithm on the host cores (oracle port here,
 # since the reference sources are not present on the GPU host)
 # ---------------------------------------------------------------------------
+def _oracle_preprocess():
+    """The reference arm builds its sphere tables with the oracle's C
+    restatement of BCM_Immersed_boundary (the same tables as the GPU)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    port = O.Port()
+    return TimedPreprocess(lambda case, tris: port.ibm(case, case.fws, tris),
+                           "CPU, C restatement of BCM_Immersed_boundary (1 thread)")
+
+
 def cpu_sample(case, subiters=1, threads=None):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
@@ -233,7 +270,7 @@ def cpu_sample(case, subiters=1, threads=None):
 def run_reference_arm(args, dist):
     if dist.rank != 0:
         return
-    case = workload_case()
+    case = workload_case(_oracle_preprocess())
     for _ in range(max(0, args.warmup)):
         pass  # the CPU sample needs no warm-up; kept for the launch contract
     vals, t_total = [], 0.0
@@ -375,7 +412,7 @@ def rel_l2(a, b, n):
 
 def run_gpu_arm(args, dist):
     from bcm_cgli_gb300 import api
-    case = workload_case()
+    case = workload_case(TimedPreprocess(api.ibm_preprocess, "GPU, bcmg_ibm_preprocess"))
     head = args.precision
     other = "fp64" if head == "split" else "split"
     m_head = measure(api, case, head, args, dist, clocks_on=True)

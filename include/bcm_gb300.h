@@ -126,6 +126,37 @@ void BCM_Interface(int myid, int ncube, int mPI_Nadj, int ncpu_bs, int ncpu_eq, 
                    int *adjZ_bs_plus, int *adjZ_sb_plus, int *adjZ_bs_minus,
                    int *adjZ_sb_minus, double *U1_);
 
+/* Replaces BCM_Immersed_boundary (main.h:113-144, BCM_Immersed_boundary.cpp
+ * :127-1081; called once before the time loop, main.cpp:811).  Reads the
+ * ASCII STL BCM_STL_fine.stl from the working directory, finds on the GPU
+ * the boundary point, image point and trilinear weights of every IBM ghost
+ * cell (FWS == 0) of the finest cubes, turns ghost cells farther than
+ * sqrt(2) cells from the surface into fluid (FWS = 1) and writes
+ * IBM_minus<myid>.dat / IBM_plus<myid>.dat byte for byte as the reference
+ * does.  Cube resolution: bcmg_set_reference_config's ncube_x.  Xcnt, Ycnt,
+ * Zcnt: cell centres [ncube][ncube_x+4] (NULL: formed from the corners).
+ * n_wallcube, NBC, X/Y/Zmin/max and wallcube are accepted and unused, as in
+ * the reference.  Errors (missing STL file, CUDA): bcmg_last_error(). */
+void BCM_Immersed_boundary(int myid, int ncube, int n_wallcube, int *NBC, double Xmin,
+                           double Xmax, double Ymin, double Ymax, double Zmin, double Zmax,
+                           double *cube_size, int *csl, double *Xcube, double *Ycube,
+                           double *Zcube, double *Xcnt, double *Ycnt, double *Zcnt, int *FWS,
+                           int *wallcube);
+
+/* The same preprocessing in memory.  tri: ntri triangles x 3 vertices x
+ * (x, y, z), in STL facet order.  Cell centres are formed from the cube
+ * corners (BCM_Grid.cpp:124-148).  FWS ([ncube][n+4]^3) is updated in
+ * place.  Tables (0-based arrays, up to `cap` entries each): gc_* = ghost
+ * cell (cube, i, j, k), ip_* = the image point's base cell (cube, i, j, k),
+ * w_* = eight weights, unrounded (the files hold them with six decimals);
+ * minus = entries with dotp >= 0 (IBM_minus), plus = the others.  Returns
+ * BCMG_ERR_ARG when an output table would exceed cap (FWS then untouched). */
+int bcmg_ibm_preprocess(int n, int ncube, const double *cube_size, const int *csl,
+                        const double *Xcube, const double *Ycube, const double *Zcube, int *FWS,
+                        int ntri, const double *tri, int cap, int *nminus, int *gc_minus,
+                        int *ip_minus, double *w_minus, int *nplus, int *gc_plus, int *ip_plus,
+                        double *w_plus);
+
 /* ----------------------------------------------------------------------- */
 /* 2. Device-resident case context                                         */
 /* ----------------------------------------------------------------------- */

@@ -69,6 +69,14 @@ void bcmo_run_converged(const bcmo_phys *ph, int ncube, int steps, int max_subit
                         int nminus, const double *wm, const int *gm, const int *im, int nplus,
                         const double *wp, const int *gp, const int *ip, double *er, double *Emax,
                         int *iters_out);
+/* IBM preprocessing (bcm_oracle_ibm.c): triangles tri_in[ntri][9], FWS
+ * updated in place, entries 0-based packed (GCindex / IPsur 4 ints, weight 8
+ * doubles per entry), tri_scratch holds ntri*9 doubles.  Returns 0, or -1
+ * when an output table would exceed cap entries. */
+int bcmo_ibm(int n, int ncube, const double *cube_size, const int *csl, const double *Xcube,
+             const double *Ycube, const double *Zcube, int *FWS, int ntri_in, const double *tri_in,
+             int cap, int *nminus, int *gc_m, int *ip_m, double *w_m, int *nplus, int *gc_p,
+             int *ip_p, double *w_p, double *tri_scratch);
 void bcmo_set_threads(int n);
 
 #ifdef __cplusplus

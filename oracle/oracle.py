@@ -32,7 +32,8 @@ def build_port(force: bool = False) -> str:
     """Compile the C restatement; returns the .so path."""
     os.makedirs(BUILD_DIR, exist_ok=True)
     out = os.path.join(BUILD_DIR, "libbcm_oracle.so")
-    srcs = [os.path.join(HERE, "bcm_oracle.c"), os.path.join(HERE, "bcm_oracle_lusgs.c")]
+    srcs = [os.path.join(HERE, "bcm_oracle.c"), os.path.join(HERE, "bcm_oracle_lusgs.c"),
+            os.path.join(HERE, "bcm_oracle_ibm.c")]
     hdr = os.path.join(HERE, "bcm_oracle.h")
     if (not force and os.path.isfile(out) and os.path.getmtime(out) >= max(
             [os.path.getmtime(x) for x in srcs] + [os.path.getmtime(hdr)])):
@@ -114,6 +115,9 @@ class Port:
                                          _dp, _dp, C.c_int, C.c_int, _ip, _ip, C.c_int, C.c_int,
                                          _ip, _ip, C.c_int, C.c_int, _ip, _ip, C.c_int, _dp, _ip,
                                          _ip, C.c_int, _dp, _ip, _ip, _dp, _dp, _ip]
+        L.bcmo_ibm.argtypes = [C.c_int, C.c_int, _dp, _ip, _dp, _dp, _dp, _ip, C.c_int, _dp,
+                               C.c_int, C.POINTER(C.c_int), _ip, _ip, _dp, C.POINTER(C.c_int),
+                               _ip, _ip, _dp, _dp]
         L.bcmo_set_threads.argtypes = [C.c_int]
 
     @staticmethod
@@ -175,6 +179,32 @@ class Port:
             Im, npl, Wp, Gp, Ip, st.er, st.Emax, iters)
         return iters[:steps]
 
+    def ibm(self, case, fws, tris):
+        """IBM preprocessing (restatement of BCM_Immersed_boundary) for the
+        triangles tris[ntri, 3, 3]; fws updated in place.  Returns the minus
+        and plus tables as (GCindex[m,4], IPsur[m,4], weight[m,8])."""
+        tri = np.ascontiguousarray(np.asarray(tris, np.float64).reshape(-1, 9))
+        ntri = tri.shape[0]
+        cap = int((fws == 0).sum()) + 1
+        o = np.ascontiguousarray(case.origin, dtype=np.float64)
+        out = [np.zeros(4 * cap, np.int32), np.zeros(4 * cap, np.int32), np.zeros(8 * cap),
+               np.zeros(4 * cap, np.int32), np.zeros(4 * cap, np.int32), np.zeros(8 * cap)]
+        nm, npl = C.c_int(), C.c_int()
+        r = self.lib.bcmo_ibm(case.n, case.ncube, np.ascontiguousarray(case.cube_size, np.float64),
+                              np.ascontiguousarray(case.csl, np.int32),
+                              np.ascontiguousarray(o[:, 0]), np.ascontiguousarray(o[:, 1]),
+                              np.ascontiguousarray(o[:, 2]), fws, ntri,
+                              tri if ntri else np.zeros(9), cap, C.byref(nm), out[0], out[1],
+                              out[2], C.byref(npl), out[3], out[4], out[5],
+                              np.zeros(max(9 * ntri, 9)))
+        if r != 0:
+            raise RuntimeError("bcmo_ibm: table capacity exceeded")
+        m, p = nm.value, npl.value
+        return ((out[0][:4 * m].reshape(m, 4), out[1][:4 * m].reshape(m, 4),
+                 out[2][:8 * m].reshape(m, 8)),
+                (out[3][:4 * p].reshape(p, 4), out[4][:4 * p].reshape(p, 4),
+                 out[5][:8 * p].reshape(p, 8)))
+
     def residual(self, case, st: State):
         """The raw residual R(U1_) into st.Rku1 (fluid cells) and the force
         integrands into st.Residual1 (bcmo_flux_stage with RK = 0)."""
@@ -233,6 +263,7 @@ class Ref:
         L.ref_interface_list.argtypes = [C.c_int, _ip]
         L.ref_set_threads.argtypes = [C.c_int]
         L.ref_output.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp]
+        L.ref_ibm.argtypes = [C.c_int, _dp, _ip, _dp, _dp, _dp, _ip]
         L.ref_run.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                               _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.c_int,
                               C.c_int, _ip, _ip, C.c_int, C.c_int, _ip, _ip, C.c_int, C.c_int,
@@ -274,6 +305,20 @@ class Ref:
             self.lib.ref_output(case.ncube, step, U, case.cube_size,
                                 np.ascontiguousarray(o[:, 0]), np.ascontiguousarray(o[:, 1]),
                                 np.ascontiguousarray(o[:, 2]))
+        finally:
+            os.chdir(cwd)
+
+    def ibm(self, case, fws, directory: str):
+        """The reference's BCM_Immersed_boundary in `directory` (which holds
+        BCM_STL_fine.stl); fws (the case's flags) is updated in place."""
+        cwd = os.getcwd()
+        os.chdir(directory)
+        try:
+            o = np.ascontiguousarray(case.origin, dtype=np.float64)
+            self.lib.ref_ibm(case.ncube, np.ascontiguousarray(case.cube_size, dtype=np.float64),
+                             np.ascontiguousarray(case.csl, dtype=np.int32),
+                             np.ascontiguousarray(o[:, 0]), np.ascontiguousarray(o[:, 1]),
+                             np.ascontiguousarray(o[:, 2]), fws)
         finally:
             os.chdir(cwd)
 

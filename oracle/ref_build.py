@@ -46,6 +46,7 @@ REF_SOURCES = [
     "BCM_Y_boundary_condition.cpp",
     "BCM_Z_boundary_condition.cpp",
     "BCM_Output.cpp",
+    "BCM_Immersed_boundary.cpp",
 ]
 
 
@@ -155,12 +156,15 @@ def build(c: RefConfig, force: bool = False, verbose: bool = False) -> str | Non
                 f.write(text)
             changed = True
     driver = os.path.join(HERE, "ref_driver.cpp")
+    recipe = [driver, os.path.abspath(__file__), os.path.join(HERE, "mpi_stub", "mpi.h")]
     if os.path.isfile(out) and not (force or changed):
-        if os.path.getmtime(out) >= os.path.getmtime(driver):
+        if os.path.getmtime(out) >= max(os.path.getmtime(x) for x in recipe):
             return out
     srcs = [os.path.join(REF_DIR, s) for s in REF_SOURCES] + [driver]
     cmd = [
-        "g++", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-w",
+        # C++14: the reference is C++98-style code, and a C++17 <algorithm>
+        # pulls in parallel-STL headers whose quoted includes -I- would hide
+        "g++", "-std=gnu++14", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-w",
         "-I", cfg_dir, "-I-", "-I", os.path.join(HERE, "mpi_stub"), "-I", REF_DIR,
         *srcs, "-o", out + ".tmp",
     ]

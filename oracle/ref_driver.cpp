@@ -203,4 +203,30 @@ void ref_output(int ncube, int step, double *U1, double *cube_size, const double
   free(Zcnt);
 }
 
+/* BCM_Immersed_boundary (BCM_Immersed_boundary.cpp:127-1081) on one rank:
+ * reads BCM_STL_fine.stl and writes IBM_minus00000.dat / IBM_plus00000.dat
+ * in the current directory; FWS is updated in place (ghost cells whose
+ * boundary point lies too far become fluid).  Cell centres as
+ * BCM_Grid.cpp:124-148 forms them. */
+void ref_ibm(int ncube, double *cube_size, int *csl, double *Xcube, double *Ycube,
+             double *Zcube, int *FWS) {
+  Ncube = ncube;
+  double (*Xcnt)[X_size] = (double (*)[X_size])calloc((size_t)ncube * X_size, sizeof(double));
+  double (*Ycnt)[Y_size] = (double (*)[Y_size])calloc((size_t)ncube * Y_size, sizeof(double));
+  double (*Zcnt)[Z_size] = (double (*)[Z_size])calloc((size_t)ncube * Z_size, sizeof(double));
+  for (int c = 1; c < ncube; ++c) {
+    double dx = cube_size[c] / NcubeX, dy = cube_size[c] / NcubeY, dz = cube_size[c] / NcubeZ;
+    for (int i = 0; i < X_size; ++i) Xcnt[c][i] = Xcube[c] + (i - 1.5) * dx;
+    for (int j = 0; j < Y_size; ++j) Ycnt[c][j] = Ycube[c] + (j - 1.5) * dy;
+    for (int k = 0; k < Z_size; ++k) Zcnt[c][k] = Zcube[c] + (k - 1.5) * dz;
+  }
+  int NBC = 0;
+  int wallcube[2] = {0, 0};
+  BCM_Immersed_boundary(0, ncube, 1, &NBC, 0., 0., 0., 0., 0., 0., cube_size, csl, Xcube, Ycube,
+                        Zcube, Xcnt, Ycnt, Zcnt, (Flag *)FWS, wallcube);
+  free(Xcnt);
+  free(Ycnt);
+  free(Zcnt);
+}
+
 }  // extern "C"

@@ -36,3 +36,20 @@ def golden_cases():
 
 RUN_STEPS = 2
 RUN_SUBITERS = 2
+
+
+def ibm_cases():
+    """(case, triangles) pairs for the IBM preprocessing fixtures: a sphere of
+    diameter 1 on a two-level grid of n=8 cubes (fine cubes of edge 1, cells
+    of 1/8), as icospheres of 80, 1,280 and 20,480 triangles.  The coarse
+    80-triangle body and the off-centre sphere leave many ghost cells
+    without any ray hit (closest-point fallback, carried side test)."""
+    def grid():
+        return cases.sphere_ibm(n=8, coarse=2.0, box=((-2.0, 4.0), (-2.0, 2.0), (-2.0, 2.0)),
+                                refine_box=((-2.0, 2.0), (-2.0, 2.0), (-2.0, 2.0)))
+    return {
+        "sphere_n8_l1": (grid(), cases.icosphere(1, 0.5)),
+        "sphere_n8_l3": (grid(), cases.icosphere(3, 0.5)),
+        "sphere_n8_l5": (grid(), cases.icosphere(5, 0.5)),
+        "sphere_n8_l2_offset": (grid(), cases.icosphere(2, 0.45, center=(0.13, -0.07, 0.05))),
+    }

@@ -5,7 +5,8 @@ BCM_*.cpp compiled from /root/reference by oracle/ref_build.py, one OpenMP
 thread so its norm sums are serial) and records SHA-256 digests of every
 output array plus the norms.  Run here, where the reference sources exist:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # everything
+    python tests/golden/make_golden.py --ibm-only # the IBM preprocessing records
 """
 import hashlib
 import json
@@ -20,14 +21,43 @@ sys.path[:0] = [ROOT, os.path.join(ROOT, "oracle"), HERE]
 import numpy as np  # noqa: E402
 
 import oracle as O  # noqa: E402
-from golden_cases import RUN_STEPS, RUN_SUBITERS, canonical, golden_cases  # noqa: E402
+from golden_cases import RUN_STEPS, RUN_SUBITERS, canonical, golden_cases, ibm_cases  # noqa: E402
+from bcm_cgli_gb300 import cases as _cases  # noqa: E402
 
 
 def digest(a):
     return hashlib.sha256(canonical(a)).hexdigest()
 
 
+def ibm_records():
+    """Digests of the reference's BCM_Immersed_boundary outputs: the two
+    table files (text) and the flags after it."""
+    out = {}
+    for name, (case, tris) in ibm_cases().items():
+        fws = case.fws.copy()
+        with tempfile.TemporaryDirectory() as d:
+            _cases.write_stl(os.path.join(d, "BCM_STL_fine.stl"), tris)
+            O.Ref(case).ibm(case, fws, d)
+            rec = {"fws": digest(fws), "fws_changed": int((fws != case.fws).sum())}
+            for side in ("minus", "plus"):
+                with open(os.path.join(d, f"IBM_{side}00000.dat"), "rb") as f:
+                    txt = f.read()
+                rec[side] = hashlib.sha256(txt).hexdigest()
+                rec[side + "_count"] = int(txt.rsplit(b"\n", 1)[-1])
+        out[name] = rec
+        print(name, "done", file=sys.stderr)
+    return out
+
+
 def main():
+    path = os.path.join(HERE, "golden.json")
+    if "--ibm-only" in sys.argv:
+        with open(path) as f:
+            doc = json.load(f)
+        doc["ibm"] = ibm_records()
+        with open(path, "w") as f:
+            json.dump(doc, f, indent=1)
+        return
     out = {}
     for name, case in golden_cases().items():
         ref = O.Ref(case)
@@ -67,7 +97,8 @@ def main():
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py (reference compiled by "
                                 "oracle/ref_build.py, OMP_NUM_THREADS=1)",
-                   "steps": RUN_STEPS, "subiters": RUN_SUBITERS, "cases": out}, f, indent=1)
+                   "steps": RUN_STEPS, "subiters": RUN_SUBITERS, "cases": out,
+                   "ibm": ibm_records()}, f, indent=1)
 
 
 if __name__ == "__main__":
