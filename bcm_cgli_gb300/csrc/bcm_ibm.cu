@@ -7,11 +7,13 @@
 // The reference loops ghost cells x triangles on one core.  Here:
 //  * k_ibm_keep: one thread per triangle tests its three vertices against
 //    every cube's box widened by 1.5 cells (:330-430);
-//  * k_ibm_search: one thread per ghost cell sweeps the kept triangles,
-//    staged through shared memory in chunks every thread of the CTA reads:
-//    the ray along each triangle's normal (first closest hit) and, for a
-//    cell without any hit, the last closest point over all triangles
-//    (:686-720, :1086-1405);
+//  * k_ibm_tri_prep: the ray invariants of every kept triangle, once;
+//  * k_ibm_ray_part / k_ibm_ray_combine: ghost cells x triangle ranges
+//    (triangles staged through shared memory, read by every thread of the
+//    CTA), then per cell the first closest hit of a ray along each
+//    triangle's normal over all ranges (:686-720, :1409-1450);
+//  * k_ibm_closest_part / k_ibm_closest_combine: the same split for the
+//    cells without any hit, the last closest point (:1290-1405);
 //  * the side test of a cell uses the dotp of the last hit cell at or before
 //    it in the reference's (cube, i, j, k) order, because the reference never
 //    resets it; that carry is a short sequential pass on the host;
@@ -23,6 +25,7 @@
 // is built with --fmad=false, so the tables equal the reference's.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -142,77 +145,164 @@ __global__ void k_ibm_tri_prep(int ntri, const double *__restrict__ tri,
   r[21] = 0.0;
 }
 
-// Per ghost cell over the kept triangles in order: the number of ray hits
-// (Moller-Trumbore, :1409-1450, det below 1e-7 rejected, both directions
-// accepted), and of the first closest hit |t|, its direction and
-// dotp = nu . (v0 - centre); with no hit, the last closest point over all
-// triangles.  out[g*8 + 0..5] = hits, |t|, d0, d1, d2 (the closest point
-// when there is no hit), dotp.
-__global__ void __launch_bounds__(256) k_ibm_search(int ng, const double *__restrict__ cen,
-                                                    int ntri, const double *__restrict__ rec,
-                                                    const double *__restrict__ tri,
-                                                    double *__restrict__ out) {
+// Ray test of ghost centre o against triangle record r (Moller-Trumbore,
+// :1409-1450: det below 1e-7 rejected, both directions accepted); on a hit
+// returns 1 with tt = t.
+__device__ __forceinline__ int ray_hit(const double *o, const double *r, double *tt) {
+  if (r[18] < kMinimum) return 0;
+  const double tv[3] = {o[0] - r[0], o[1] - r[1], o[2] - r[2]};
+  const double u = tv[0] * r[12] + tv[1] * r[13] + tv[2] * r[14];
+  if (u < 0.0 || u > r[18]) return 0;
+  const double q[3] = {tv[1] * r[5] - tv[2] * r[4], tv[2] * r[3] - tv[0] * r[5],
+                       tv[0] * r[4] - tv[1] * r[3]};
+  const double w = r[9] * q[0] + r[10] * q[1] + r[11] * q[2];
+  if (w < 0.0 || u + w > r[18]) return 0;
+  *tt = (r[6] * q[0] + r[7] * q[1] + r[8] * q[2]) * r[19];
+  return 1;
+}
+
+// Search over the kept triangles, split over CTAs: blockIdx.x picks 128
+// ghost cells, blockIdx.y one of gridDim.y contiguous triangle ranges.  Per
+// (range, ghost): the number of ray hits and the first triangle with the
+// smallest |t| (dir . dir), the reference's strict `<` over its serial loop.
+// Cells are a list (cell < 0: skipped) so the closest-point pass below can
+// reuse the layout.
+constexpr int kGhostBlock = 128;
+__global__ void __launch_bounds__(kGhostBlock)
+    k_ibm_ray_part(int ng, const double *__restrict__ cen, int ntri, int per,
+                   const double *__restrict__ rec, int *__restrict__ hits_p,
+                   int *__restrict__ best_p, double *__restrict__ nd_p) {
   __shared__ double st[kTriChunk * kRec];
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   const bool has = g < ng;
   double o[3] = {0, 0, 0};
   if (has) { o[0] = cen[3 * g]; o[1] = cen[3 * g + 1]; o[2] = cen[3 * g + 2]; }
-  int hits = 0;
-  double tmin = kBig, dmin = kBig, d0 = 0, d1 = 0, d2 = 0, dotp = 0;
-  for (int base = 0; base < ntri; base += kTriChunk) {
-    const int cnt = ntri - base < kTriChunk ? ntri - base : kTriChunk;
+  const int t0 = blockIdx.y * per, t1 = min(ntri, t0 + per);
+  int hits = 0, best = -1;
+  double dmin = kBig;
+  for (int base = t0; base < t1; base += kTriChunk) {
+    const int cnt = min(kTriChunk, t1 - base);
     __syncthreads();
     for (int e = threadIdx.x; e < cnt * kRec; e += blockDim.x)
       st[e] = rec[kRec * (size_t)base + e];
     __syncthreads();
     if (!has) continue;
     for (int t = 0; t < cnt; ++t) {
-      const double *r = st + kRec * t;
-      if (r[18] < kMinimum) continue;
-      const double tv[3] = {o[0] - r[0], o[1] - r[1], o[2] - r[2]};
-      const double u = tv[0] * r[12] + tv[1] * r[13] + tv[2] * r[14];
-      if (u < 0.0 || u > r[18]) continue;
-      const double q[3] = {tv[1] * r[5] - tv[2] * r[4], tv[2] * r[3] - tv[0] * r[5],
-                           tv[0] * r[4] - tv[1] * r[3]};
-      const double w = r[9] * q[0] + r[10] * q[1] + r[11] * q[2];
-      if (w < 0.0 || u + w > r[18]) continue;
-      const double tt = (r[6] * q[0] + r[7] * q[1] + r[8] * q[2]) * r[19];
-      const double nd = fabs(tt) * r[20];
+      double tt;
+      if (!ray_hit(o, st + kRec * t, &tt)) continue;
+      const double nd = fabs(tt) * st[kRec * t + 20];
       ++hits;
-      if (nd < dmin) {
-        dmin = nd;
-        tmin = fabs(tt);
-        d0 = r[9]; d1 = r[10]; d2 = r[11];
-        dotp = r[15] * (r[0] - o[0]) + r[16] * (r[1] - o[1]) + r[17] * (r[2] - o[2]);
-      }
+      if (nd < dmin) { dmin = nd; best = base + t; }
     }
-  }
-  // Cells without any hit: closest point over all triangles (the CTA walks
-  // the triangles again only if one of its cells needs it).
-  const int need = __syncthreads_or(has && hits == 0);
-  if (need) {
-    double bp[3] = {0, 0, 0};
-    double *sv = st;  // raw vertices, 9 per triangle
-    constexpr int kRaw = kTriChunk * kRec / 9;
-    for (int base = 0; base < ntri; base += kRaw) {
-      const int cnt = ntri - base < kRaw ? ntri - base : kRaw;
-      __syncthreads();
-      for (int e = threadIdx.x; e < cnt * 9; e += blockDim.x) sv[e] = tri[9 * (size_t)base + e];
-      __syncthreads();
-      if (!has || hits != 0) continue;
-      for (int t = 0; t < cnt; ++t) {
-        double p[3];
-        closest(sv + 9 * t, o[0], o[1], o[2], p);
-        const double nd = (p[0] - o[0]) * (p[0] - o[0]) + (p[1] - o[1]) * (p[1] - o[1]) +
-                          (p[2] - o[2]) * (p[2] - o[2]);
-        if (nd <= dmin) { bp[0] = p[0]; bp[1] = p[1]; bp[2] = p[2]; dmin = nd; }
-      }
-    }
-    if (has && hits == 0) { d0 = bp[0]; d1 = bp[1]; d2 = bp[2]; }
   }
   if (!has) return;
-  double *r = out + 8 * (size_t)g;
-  r[0] = hits; r[1] = tmin; r[2] = d0; r[3] = d1; r[4] = d2; r[5] = dotp;
+  const size_t at = (size_t)blockIdx.y * ng + g;
+  hits_p[at] = hits;
+  best_p[at] = best;
+  nd_p[at] = dmin;
+}
+
+// Per ghost cell: total hits; of the closest hit (smallest |t| dir.dir, the
+// lowest triangle on ties) |t|, direction and dotp = nu . (v0 - centre),
+// recomputed from that triangle with the same arithmetic.  out[g*8 + 0..5] =
+// hits, |t|, d0, d1, d2, dotp.
+__global__ void k_ibm_ray_combine(int ng, int nsplit, const double *__restrict__ cen,
+                                  const double *__restrict__ rec,
+                                  const int *__restrict__ hits_p, const int *__restrict__ best_p,
+                                  const double *__restrict__ nd_p, double *__restrict__ out) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ng) return;
+  int hits = 0, best = -1;
+  double dmin = kBig;
+  for (int sp = 0; sp < nsplit; ++sp) {
+    const size_t at = (size_t)sp * ng + g;
+    hits += hits_p[at];
+    if (best_p[at] >= 0 && nd_p[at] < dmin) { dmin = nd_p[at]; best = best_p[at]; }
+  }
+  double tmin = kBig, d0 = 0, d1 = 0, d2 = 0, dotp = 0;
+  if (best >= 0) {
+    const double o[3] = {cen[3 * g], cen[3 * g + 1], cen[3 * g + 2]};
+    const double *r = rec + kRec * (size_t)best;
+    double tt = 0;
+    ray_hit(o, r, &tt);
+    tmin = fabs(tt);
+    d0 = r[9]; d1 = r[10]; d2 = r[11];
+    dotp = r[15] * (r[0] - o[0]) + r[16] * (r[1] - o[1]) + r[17] * (r[2] - o[2]);
+  }
+  double *w = out + 8 * (size_t)g;
+  w[0] = hits; w[1] = tmin; w[2] = d0; w[3] = d1; w[4] = d2; w[5] = dotp;
+}
+
+// Closest-point search for the ghost cells without any hit (list[m] ghost
+// numbers), split like the ray search: per (range, cell) the LAST triangle
+// with the smallest squared distance (the reference's `<=`).
+constexpr int kRawChunk = kTriChunk * kRec / 9;
+__global__ void __launch_bounds__(kGhostBlock)
+    k_ibm_closest_part(int m, const int *__restrict__ list, const double *__restrict__ cen,
+                       int ntri, int per, const double *__restrict__ tri,
+                       int *__restrict__ best_p, double *__restrict__ nd_p) {
+  __shared__ double sv[kRawChunk * 9];
+  const int e0 = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool has = e0 < m;
+  double o[3] = {0, 0, 0};
+  if (has) {
+    const int g = list[e0];
+    o[0] = cen[3 * g]; o[1] = cen[3 * g + 1]; o[2] = cen[3 * g + 2];
+  }
+  const int t0 = blockIdx.y * per, t1 = min(ntri, t0 + per);
+  int best = -1;
+  double dmin = kBig;
+  for (int base = t0; base < t1; base += kRawChunk) {
+    const int cnt = min(kRawChunk, t1 - base);
+    __syncthreads();
+    for (int e = threadIdx.x; e < cnt * 9; e += blockDim.x) sv[e] = tri[9 * (size_t)base + e];
+    __syncthreads();
+    if (!has) continue;
+    for (int t = 0; t < cnt; ++t) {
+      double p[3];
+      closest(sv + 9 * t, o[0], o[1], o[2], p);
+      const double nd = (p[0] - o[0]) * (p[0] - o[0]) + (p[1] - o[1]) * (p[1] - o[1]) +
+                        (p[2] - o[2]) * (p[2] - o[2]);
+      if (nd <= dmin) { dmin = nd; best = base + t; }
+    }
+  }
+  if (!has) return;
+  const size_t at = (size_t)blockIdx.y * m + e0;
+  best_p[at] = best;
+  nd_p[at] = dmin;
+}
+
+// The closest point of those cells (the highest triangle on ties) into
+// out[g*8 + 2..4]; 0 when no triangle is within the search distance.
+__global__ void k_ibm_closest_combine(int m, int nsplit, const int *__restrict__ list,
+                                      const double *__restrict__ cen,
+                                      const double *__restrict__ tri,
+                                      const int *__restrict__ best_p,
+                                      const double *__restrict__ nd_p, double *__restrict__ out) {
+  const int e0 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e0 >= m) return;
+  int best = -1;
+  double dmin = kBig;
+  for (int sp = 0; sp < nsplit; ++sp) {
+    const size_t at = (size_t)sp * m + e0;
+    if (best_p[at] >= 0 && nd_p[at] <= dmin) { dmin = nd_p[at]; best = best_p[at]; }
+  }
+  const int g = list[e0];
+  double p[3] = {0, 0, 0};
+  if (best >= 0) closest(tri + 9 * (size_t)best, cen[3 * g], cen[3 * g + 1], cen[3 * g + 2], p);
+  double *w = out + 8 * (size_t)g;
+  w[2] = p[0]; w[3] = p[1]; w[4] = p[2];
+}
+
+// Triangle ranges per ghost block so that a search launch fills the GPU
+// (about 8 CTAs per SM), each range at least 64 triangles.
+int ibm_splits(int nblocks, int ntri) {
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int want = (8 * sms + nblocks - 1) / nblocks;
+  const int most = (ntri + 63) / 64;
+  return std::max(1, std::min(want, most));
 }
 
 // In-place inverse of the 8x8 row-major matrix m (:1504-1576).
@@ -432,15 +522,50 @@ int ibm_run(int n, int ncube, const double *cube_size, const int *csl, const dou
   CKI(dsrch.alloc((size_t)ng * 8));
   CKI(cudaMemcpy(dcen.p, cen.data(), sizeof(double) * cen.size(), cudaMemcpyHostToDevice));
   CKI(cudaMemcpy(dg.p, gidx.data(), sizeof(int) * gidx.size(), cudaMemcpyHostToDevice));
-  k_ibm_search<<<(ng + 255) / 256, 256>>>(ng, dcen.p, nk, drec.p, dtri.p, dsrch.p);
-  CKI(cudaGetLastError());
+  {
+    const int gb = (ng + kGhostBlock - 1) / kGhostBlock;
+    const int ns = ibm_splits(gb, nk), per = (nk + ns - 1) / ns;
+    DevBuf<int> hp, bp;
+    DevBuf<double> np_;
+    CKI(hp.alloc((size_t)ns * ng));
+    CKI(bp.alloc((size_t)ns * ng));
+    CKI(np_.alloc((size_t)ns * ng));
+    k_ibm_ray_part<<<dim3(gb, ns), kGhostBlock>>>(ng, dcen.p, nk, per, drec.p, hp.p, bp.p,
+                                                  np_.p);
+    CKI(cudaGetLastError());
+    k_ibm_ray_combine<<<(ng + 127) / 128, 128>>>(ng, ns, dcen.p, drec.p, hp.p, bp.p, np_.p,
+                                                 dsrch.p);
+    CKI(cudaGetLastError());
+  }
   // The side test's dotp carries over cells without a hit (in order).
   std::vector<double> srch((size_t)ng * 8), deff(ng);
   CKI(cudaMemcpy(srch.data(), dsrch.p, sizeof(double) * srch.size(), cudaMemcpyDeviceToHost));
   double carry = 0.0;
+  std::vector<int> nohit;
   for (int g = 0; g < ng; ++g) {
-    if (srch[8 * (size_t)g] > 0) carry = srch[8 * (size_t)g + 5];
+    if (srch[8 * (size_t)g] > 0)
+      carry = srch[8 * (size_t)g + 5];
+    else
+      nohit.push_back(g);
     deff[g] = carry;
+  }
+  // Closest points of the cells without a hit.
+  if (!nohit.empty()) {
+    const int m = (int)nohit.size();
+    const int gb = (m + kGhostBlock - 1) / kGhostBlock;
+    const int ns = ibm_splits(gb, nk), per = (nk + ns - 1) / ns;
+    DevBuf<int> dl, bp;
+    DevBuf<double> np_;
+    CKI(dl.alloc(m));
+    CKI(bp.alloc((size_t)ns * m));
+    CKI(np_.alloc((size_t)ns * m));
+    CKI(cudaMemcpy(dl.p, nohit.data(), sizeof(int) * m, cudaMemcpyHostToDevice));
+    k_ibm_closest_part<<<dim3(gb, ns), kGhostBlock>>>(m, dl.p, dcen.p, nk, per, dtri.p, bp.p,
+                                                      np_.p);
+    CKI(cudaGetLastError());
+    k_ibm_closest_combine<<<(m + 127) / 128, 128>>>(m, ns, dl.p, dcen.p, dtri.p, bp.p, np_.p,
+                                                    dsrch.p);
+    CKI(cudaGetLastError());
   }
   CKI(dctr.alloc((size_t)3 * ncube * S));
   CKI(ddot.alloc(ng));

@@ -412,6 +412,9 @@ def rel_l2(a, b, n):
 
 def run_gpu_arm(args, dist):
     from bcm_cgli_gb300 import api
+    # the FP64 probe also creates the CUDA context, which the preprocessing
+    # time below should not include
+    fp64_gflops = api.probe_fp64_gflops()
     case = workload_case(TimedPreprocess(api.ibm_preprocess, "GPU, bcmg_ibm_preprocess"))
     head = args.precision
     other = "fp64" if head == "split" else "split"
@@ -464,7 +467,6 @@ def run_gpu_arm(args, dist):
     except Exception:
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    fp64_gflops = api.probe_fp64_gflops()
 
     def roofline(m, prec):
         alg_bytes = BYTES_PER_CELL_STAGE * case.n_cells
