@@ -6,7 +6,7 @@
 //
 // The reference loops ghost cells x triangles on one core.  Here:
 //  * k_ibm_keep: one thread per triangle tests its three vertices against
-//    every cube's box widened by 1.5 cells (:330-430);
+//    every cube's box widened by 1.5 cells (k_ibm_cube_box, :330-430);
 //  * k_ibm_tri_prep: the ray invariants of every kept triangle, once;
 //  * k_ibm_ray_part / k_ibm_ray_combine: ghost cells x triangle ranges
 //    (triangles staged through shared memory, read by every thread of the
@@ -43,26 +43,48 @@ constexpr double kMinimum = 0.0000001;  // prm.h `minimum`
 constexpr double kBig = 100000000;       // prm.h `MAX`
 constexpr int kTriChunk = 128;           // triangles staged per CTA pass
 
-__global__ void k_ibm_keep(int ntri, const double *__restrict__ tri, int ncube, int n,
-                           const double *__restrict__ cube_size, const double *__restrict__ X,
-                           const double *__restrict__ Y, const double *__restrict__ Z,
-                           int *__restrict__ keep) {
+// Box of every cube widened by 1.5 cells, box[c*6 + 0..5] = x lo, x hi,
+// y lo, y hi, z lo, z hi (the reference's bounds expressions, :330-430).
+__global__ void k_ibm_cube_box(int ncube, int n, const double *__restrict__ cube_size,
+                               const double *__restrict__ X, const double *__restrict__ Y,
+                               const double *__restrict__ Z, double *__restrict__ box) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncube) return;
+  const double dx = cube_size[c] / n;
+  double *b = box + 6 * (size_t)c;
+  b[0] = X[c] - 1.5 * dx; b[1] = X[c] + cube_size[c] + 1.5 * dx;
+  b[2] = Y[c] - 1.5 * dx; b[3] = Y[c] + cube_size[c] + 1.5 * dx;
+  b[4] = Z[c] - 1.5 * dx; b[5] = Z[c] + cube_size[c] + 1.5 * dx;
+}
+
+// keep[t] = 1 when a vertex of triangle t lies in some cube's widened box
+// (cubes 1..ncube-1, staged through shared memory).
+constexpr int kBoxChunk = 512;
+__global__ void __launch_bounds__(256) k_ibm_keep(int ntri, const double *__restrict__ tri,
+                                                  int ncube, const double *__restrict__ box,
+                                                  int *__restrict__ keep) {
+  __shared__ double sb[kBoxChunk * 6];
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ntri) return;
-  const double *v = tri + 9 * (size_t)t;
+  double v[9];
+  for (int e = 0; e < 9; ++e) v[e] = t < ntri ? tri[9 * (size_t)t + e] : 0.0;
   int k = 0;
-  for (int q = 0; q < 3 && !k; ++q)
-    for (int c = 1; c < ncube; ++c) {
-      const double dx = cube_size[c] / n;
-      const double px = v[3 * q], py = v[3 * q + 1], pz = v[3 * q + 2];
-      if (px >= X[c] - 1.5 * dx && px <= X[c] + cube_size[c] + 1.5 * dx &&
-          py >= Y[c] - 1.5 * dx && py <= Y[c] + cube_size[c] + 1.5 * dx &&
-          pz >= Z[c] - 1.5 * dx && pz <= Z[c] + cube_size[c] + 1.5 * dx) {
-        k = 1;
-        break;
-      }
+  for (int c0 = 1; c0 < ncube; c0 += kBoxChunk) {
+    const int cnt = min(kBoxChunk, ncube - c0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < cnt * 6; e += blockDim.x) sb[e] = box[6 * (size_t)c0 + e];
+    __syncthreads();
+    if (k || t >= ntri) continue;
+    for (int c = 0; c < cnt && !k; ++c) {
+      const double *b = sb + 6 * c;
+      for (int q = 0; q < 3; ++q)
+        if (v[3 * q] >= b[0] && v[3 * q] <= b[1] && v[3 * q + 1] >= b[2] &&
+            v[3 * q + 1] <= b[3] && v[3 * q + 2] >= b[4] && v[3 * q + 2] <= b[5]) {
+          k = 1;
+          break;
+        }
     }
-  keep[t] = k;
+  }
+  if (t < ntri) keep[t] = k;
 }
 
 // Closest point of a triangle (:1290-1405), with the interior weight formed
@@ -503,9 +525,14 @@ int ibm_run(int n, int ncube, const double *cube_size, const int *csl, const dou
   CKI(cudaMemcpy(dX.p, Xcube, sizeof(double) * ncube, cudaMemcpyHostToDevice));
   CKI(cudaMemcpy(dY.p, Ycube, sizeof(double) * ncube, cudaMemcpyHostToDevice));
   CKI(cudaMemcpy(dZ.p, Zcube, sizeof(double) * ncube, cudaMemcpyHostToDevice));
-  k_ibm_keep<<<(ntri + 127) / 128, 128>>>(ntri, dtri.p, ncube, n, dsize.p, dX.p, dY.p, dZ.p,
-                                          dkeep.p);
-  CKI(cudaGetLastError());
+  {
+    DevBuf<double> dbox;
+    CKI(dbox.alloc((size_t)6 * ncube));
+    k_ibm_cube_box<<<(ncube + 127) / 128, 128>>>(ncube, n, dsize.p, dX.p, dY.p, dZ.p, dbox.p);
+    CKI(cudaGetLastError());
+    k_ibm_keep<<<(ntri + 255) / 256, 256>>>(ntri, dtri.p, ncube, dbox.p, dkeep.p);
+    CKI(cudaGetLastError());
+  }
   std::vector<int> keep(ntri);
   CKI(cudaMemcpy(keep.data(), dkeep.p, sizeof(int) * ntri, cudaMemcpyDeviceToHost));
   std::vector<double> kept;
