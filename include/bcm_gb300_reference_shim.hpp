@@ -5,8 +5,9 @@
 // [Z_size][Ndim]`.  Including this header in exactly ONE translation unit of
 // the host program (after Resolution.h, so X_size/Ndim are defined), and
 // dropping the reference's BCM_Flux_XYZ_Viscous_Runge_kutta.cpp,
-// BCM_Interface.cpp, BCM_Ghostcell_minus.cpp, BCM_Ghostcell_plus.cpp and
-// BCM_X/Y/Z_boundary_condition.cpp from the link, gives main.cpp the same
+// BCM_Interface.cpp, BCM_Ghostcell_minus.cpp, BCM_Ghostcell_plus.cpp,
+// BCM_X/Y/Z_boundary_condition.cpp and BCM_Immersed_boundary.cpp from the
+// link, gives main.cpp the same
 // C++ symbols, now running on the GPU through the C ABI of bcm_gb300.h.
 // Call bcmg_set_reference_config() once at start-up with the values of
 // Resolution.h / prm.h.
@@ -101,4 +102,15 @@ void BCM_Interface(int myid, int ncube, int mPI_Nadj, int ncpu_bs, int ncpu_eq, 
                   adjY_eq, adjZ_eq, adjX_bs_plus, adjX_sb_plus, adjX_bs_minus, adjX_sb_minus,
                   adjY_bs_plus, adjY_sb_plus, adjY_bs_minus, adjY_sb_minus, adjZ_bs_plus,
                   adjZ_sb_plus, adjZ_bs_minus, adjZ_sb_minus, (double *)U1_);
+}
+
+// main.h:113-144 (setup, called once at main.cpp:811)
+void BCM_Immersed_boundary(int myid, int ncube, int n_wallcube, int *NBC, double Xmin,
+                           double Xmax, double Ymin, double Ymax, double Zmin, double Zmax,
+                           double *cube_size, int *csl, double *Xcube, double *Ycube,
+                           double *Zcube, double (*Xcnt)[X_size], double (*Ycnt)[Y_size],
+                           double (*Zcnt)[Z_size], bcmg_shim_flag_t *FWS, int *wallcube) {
+  ::BCM_Immersed_boundary(myid, ncube, n_wallcube, NBC, Xmin, Xmax, Ymin, Ymax, Zmin, Zmax,
+                          cube_size, csl, Xcube, Ycube, Zcube, (double *)Xcnt, (double *)Ycnt,
+                          (double *)Zcnt, (int *)FWS, wallcube);
 }
