@@ -5,7 +5,9 @@ this GPU and writes the table the benchmark applies.
 
 For every cube resolution n of the benchmark workloads (16, 24, 32) and each
 path (FP64 / split precision, RK / LU-SGS sub-iterations) it builds a
-Taylor-Green case of 4^3 cubes (n = 16, 24) or 3^3 cubes (n = 32), lets
+Taylor-Green case of 2-3 million cells (8^3 cubes of 16^3, 6^3 of 24^3, 4^3
+of 32^3: many waves of CTAs, as in the benchmark workloads; a case of a
+wave or two favours the smaller tile through its tail alone), lets
 bcmg_case_autotune time the flux tile edges (8, 4) and, for split LU-SGS,
 the sweep's thread counts (widest plane, half of it), and records the
 fastest shape with the measured times.  The shapes change how work is
@@ -37,7 +39,7 @@ def lookup(n: int, precision: str, method: str, path: str = DEFAULT_TABLE):
 def tune(reps: int = 3):
     from . import api, cases
     shapes = {}
-    for n, ncx in ((16, 4), (24, 4), (32, 3)):
+    for n, ncx in ((16, 8), (24, 6), (32, 4)):
         case = cases.taylor_green(ncx=ncx, n=n)
         for precision in ("fp64", "split"):
             for method in ("rk3", "lusgs"):
