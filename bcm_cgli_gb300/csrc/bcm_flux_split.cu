@@ -121,6 +121,19 @@ struct PrimF {
   float U, V, W, Tp;  // velocity, T - T0
 };
 
+// Asynchronous 4-byte global -> shared copy (cp.async) and the wait for all
+// of a thread's copies; an L2 prefetch hint.
+__device__ __forceinline__ void cp_async4(void *smem_dst, const void *gmem_src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+__device__ __forceinline__ void prefetch_l2(const void *p) {
+  asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p));
+}
+
 template <int T>
 struct SplitSmem {
   static constexpr int B = T + 2;      // primitive box edge (tile + 1 halo)
@@ -314,12 +327,30 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
   }
   const float iR = 1.0f / 287.0f;
 
+  // The FP64 state, the previous level and the level difference of the
+  // tile's own cells are read at the end of the stage: start moving their
+  // rows (8 cells: 320 B, 320 B, 160 B) into L2 now.
+  for (int r = tid; r < T * T * 4; r += NT) {
+    const int row = r >> 2, part = r & 3;
+    const size_t go = cb + ((size_t)(bi + row / T) * S + (bj + row % T)) * S + bk;
+    const int od = part == 3 ? 5 * T - 1 : 16 * part;  // doubles
+    const int of = part == 3 ? 5 * T - 1 : (part == 2 ? 32 : 0);  // floats
+    prefetch_l2(a.U1_ + 5 * go + od);
+    prefetch_l2(a.U1 + 5 * go + od);
+    prefetch_l2(a.D2 + 5 * go + of);
+  }
+
   // Phase 0: stage the stencil box (tile +- 3 cells, clipped to the padded
-  // cube) of FP32 deltas and flags into shared memory.  Each box row along k
-  // is a contiguous run of 5*X floats in the cube's AoS layout, so the loads
-  // are coalesced and many are in flight per thread.  Box cells outside the
-  // padded cube are never read by the stencil (the reconstruction order falls
-  // back before reaching them) and are left unset.
+  // cube) of FP32 deltas and flags into shared memory with asynchronous
+  // 4-byte copies (the rows of the AoS layout start at any 4-byte boundary),
+  // all in flight at once and waited for once.  Each box row along k is a
+  // contiguous run of 5*X floats, so the copies are coalesced.  The flags go
+  // as ints into the face buffers (unused until the face passes) and are
+  // narrowed to bytes below.  Box cells outside the padded cube are never
+  // read by the stencil (the reconstruction order falls back before reaching
+  // them) and are left unset.
+  int *ftmp = reinterpret_cast<int *>(Fb);
+  static_assert(SM::nBox <= 19 * SM::nCell, "int flags fit the face buffers");
   {
     const int k0 = bk - 3;
     const int klo = k0 < 0 ? -k0 : 0;                 // first valid column
@@ -334,13 +365,15 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
       const size_t g = cb + ((size_t)gi * S + gj) * S + (k0 + klo);
       const float *src = M + 5 * g;
       float *dst = box + (row * X + klo) * 5;
-      for (int e = lane; e < 5 * ncol; e += 32) dst[e] = __ldg(src + e);
+      for (int e = lane; e < 5 * ncol; e += 32) cp_async4(dst + e, src + e);
       const int *fsrc = F + g;
-      signed char *fdst = fbox + row * X + klo;
-      for (int e = lane; e < ncol; e += 32) fdst[e] = (signed char)__ldg(fsrc + e);
+      int *fdst = ftmp + row * X + klo;
+      for (int e = lane; e < ncol; e += 32) cp_async4(fdst + e, fsrc + e);
     }
+    cp_async_wait_all();
   }
   __syncthreads();
+  for (int p = tid; p < SM::nBox; p += NT) fbox[p] = (signed char)ftmp[p];
   auto BX = [&](int li, int lj, int lk) -> const float * {  // li.. relative to tile origin
     return box + (((li + 3) * X + (lj + 3)) * X + (lk + 3)) * 5;
   };
@@ -363,6 +396,7 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
     pr.Tp = (pp - r * RT0) * ir * iR;  // T - T0 = (p' - rho' R T0) / (rho R)
     prim[p] = pr;
   }
+  __syncthreads();  // byte flags complete; the face buffers are free again
 
   const float inv = a.inv_dx[cube];
 
