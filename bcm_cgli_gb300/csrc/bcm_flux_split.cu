@@ -141,13 +141,33 @@ struct SplitSmem {
   static constexpr int nPrim = B * B * B;
   static constexpr int nCell = T * T * T;
   static constexpr int nBox = X * X * X;
-  static constexpr size_t bytes = sizeof(float) * 5 * nBox /*state deltas*/ +
+  // Box pitches in floats: a row of X cells along k (5 floats each), a plane
+  // of X rows.  For 8^3 tiles the pitches are padded (72 = 8 mod 32, 1011
+  // odd) so that the stencil reads of a warp hit 32 distinct banks for x- and
+  // z-faces (2 ways for y-faces) instead of 2 and 4 ways.
+  static constexpr int RP = T == 8 ? 72 : 5 * X;
+  static constexpr int PP = T == 8 ? 1011 : X * RP;
+  static constexpr int nBoxF = X * PP;
+  static constexpr size_t bytes = sizeof(float) * nBoxF /*state deltas*/ +
                                   sizeof(PrimF) * nPrim + 2 * sizeof(float) * 5 * nCell +
                                   2 * sizeof(float) * nCell /*dPb, dPf*/ +
                                   sizeof(float) * 5 * nCell /*flux balance*/ +
                                   2 * sizeof(float) * nCell /*x, z pressure differences*/ +
                                   ((nBox + 15) / 16) * 16 /*flags*/;
+  static_assert(RP >= 5 * X && PP >= X * RP, "box pitches hold the rows");
+  static_assert(T != 8 || bytes + 1024 <= 233472 / 2, "two CTAs per SM");
 };
+
+// Slot of tile cell (li, lj, lk) in the value-major face buffers.  For 8^3
+// tiles an XOR swizzle: the 32 faces of a warp (4 x 8 or 8 x 4 cells of one
+// face plane, any of the three orientations) and 32 consecutive cells in
+// (i, j, k) order all land in distinct banks.
+template <int T>
+__device__ __forceinline__ int face_slot(int li, int lj, int lk) {
+  if (T == 8)
+    return ((li * 2 + (lj >> 2)) << 5) | (((lj + li) & 3) << 3) | (lk ^ (lj & 3) ^ (li & 4));
+  return (li * T + lj) * T + lk;
+}
 
 // Delta-form preconditioned Roe flux (same formulas as face_flux in
 // bcm_common.cuh, evaluated on deltas from the reference state).  Returns the
@@ -295,13 +315,13 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
   constexpr int X = SM::X;
   constexpr int NT = split_threads<T>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float *box = reinterpret_cast<float *>(smem_raw);  // [X][X][X][5] deltas
-  PrimF *prim = reinterpret_cast<PrimF *>(box + 5 * SM::nBox);
+  float *box = reinterpret_cast<float *>(smem_raw);  // [X][X][X][5] deltas, pitches RP, PP
+  PrimF *prim = reinterpret_cast<PrimF *>(box + SM::nBoxF);
   float *Fb = reinterpret_cast<float *>(prim + SM::nPrim);
   float *Ff = Fb + 5 * SM::nCell;
   float *dPb = Ff + 5 * SM::nCell;
   float *dPf = dPb + SM::nCell;
-  float *accS = dPf + SM::nCell;        // [nCell][5] Rfx/dx + Rfy/dy + Rfz/dz
+  float *accS = dPf + SM::nCell;        // [5][nCell] Rfx/dx + Rfy/dy + Rfz/dz
   float *dPxS = accS + 5 * SM::nCell;   // [nCell] x-face pressure difference
   float *dPzS = dPxS + SM::nCell;       // [nCell] z-face pressure difference
   signed char *fbox = reinterpret_cast<signed char *>(dPzS + SM::nCell);  // [X][X][X] flags
@@ -364,7 +384,7 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
       if (gi < 0 || gi >= S || gj < 0 || gj >= S) continue;
       const size_t g = cb + ((size_t)gi * S + gj) * S + (k0 + klo);
       const float *src = M + 5 * g;
-      float *dst = box + (row * X + klo) * 5;
+      float *dst = box + bi_ * SM::PP + bj_ * SM::RP + klo * 5;
       for (int e = lane; e < 5 * ncol; e += 32) cp_async4(dst + e, src + e);
       const int *fsrc = F + g;
       int *fdst = ftmp + row * X + klo;
@@ -375,7 +395,7 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
   __syncthreads();
   for (int p = tid; p < SM::nBox; p += NT) fbox[p] = (signed char)ftmp[p];
   auto BX = [&](int li, int lj, int lk) -> const float * {  // li.. relative to tile origin
-    return box + (((li + 3) * X + (lj + 3)) * X + (lk + 3)) * 5;
+    return box + (li + 3) * SM::PP + (lj + 3) * SM::RP + (lk + 3) * 5;
   };
   auto FL = [&](int li, int lj, int lk) -> int {
     return fbox[((li + 3) * X + (lj + 3)) * X + (lk + 3)];
@@ -404,10 +424,10 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
   for (int ax = 0; ax < 3; ++ax) {
     for (int f = tid; f < (T + 1) * T * T; f += NT) {
       const int fa = f / (T * T), p = (f / T) % T, q = f % T;
-      int li, lj, lk;
+      int li, lj, lk;  // a warp covers 4 x 8 faces of a plane (8 x 4 for z-faces)
       if (ax == 0) { li = fa; lj = p; lk = q; }
       else if (ax == 1) { li = p; lj = fa; lk = q; }
-      else { li = p; lj = q; lk = fa; }
+      else { li = q; lj = p; lk = fa; }
       const int g = (ax == 0 ? bi + li : (ax == 1 ? bj + lj : bk + lk));
       const int di = ax == 0, dj = ax == 1, dk = ax == 2;
       const int fm2 = FL(li - 2 * di, lj - 2 * dj, lk - 2 * dk),
@@ -416,15 +436,15 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
       const bool needB = fa < T, needF = fa > 0;
       const int ob = order_backward(g, fm2, fm1, fp1);
       const int of = order_forward(g, nx, fm2, f0, fp1);
-      const int slotB = (li * T + lj) * T + lk;
-      const int slotF = slotB - (ax == 0 ? T * T : (ax == 1 ? T : 1));
+      const int slotB = face_slot<T>(li, lj, lk);
+      const int slotF = face_slot<T>(li - di, lj - dj, lk - dk);
       int nviews, ord0, ord1 = 0, dst0, dst1 = 0;
       if (needB && needF && ob == of) { nviews = 1; ord0 = ob; dst0 = 3; }
       else if (needB && needF) { nviews = 2; ord0 = ob; dst0 = 1; ord1 = of; dst1 = 2; }
       else if (needB) { nviews = 1; ord0 = ob; dst0 = 1; }
       else { nviews = 1; ord0 = of; dst0 = 2; }
       const float *base = BX(li, lj, lk);
-      const int sstride = 5 * (ax == 0 ? X * X : (ax == 1 ? X : 1));
+      const int sstride = ax == 0 ? SM::PP : (ax == 1 ? SM::RP : 5);
       auto ld = [&](int d, int v) -> float { return base[sstride * d + v]; };
 #pragma unroll 1
       for (int w = 0; w < nviews; ++w) {
@@ -437,25 +457,26 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
         else face_flux_delta<2>(ML, MR, ef, rho0, P0, Fx, dP);
         if (dst & 1) {
 #pragma unroll
-          for (int v = 0; v < 5; ++v) Fb[5 * slotB + v] = Fx[v];
+          for (int v = 0; v < 5; ++v) Fb[v * SM::nCell + slotB] = Fx[v];
           dPb[slotB] = dP;
         }
         if (dst & 2) {
 #pragma unroll
-          for (int v = 0; v < 5; ++v) Ff[5 * slotF + v] = Fx[v];
+          for (int v = 0; v < 5; ++v) Ff[v * SM::nCell + slotF] = Fx[v];
           dPf[slotF] = dP;
         }
       }
     }
     __syncthreads();
     for (int cl = tid; cl < SM::nCell; cl += NT) {
+      const int sl = face_slot<T>(cl / (T * T), (cl / T) % T, cl % T);
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
-        float t = (Ff[5 * cl + v] - Fb[5 * cl + v]) * inv;
-        accS[5 * cl + v] = ax == 0 ? t : accS[5 * cl + v] + t;
+        float t = (Ff[v * SM::nCell + sl] - Fb[v * SM::nCell + sl]) * inv;
+        accS[v * SM::nCell + cl] = ax == 0 ? t : accS[v * SM::nCell + cl] + t;
       }
-      if (ax == 0) dPxS[cl] = dPf[cl] - dPb[cl];
-      if (ax == 2) dPzS[cl] = dPf[cl] - dPb[cl];
+      if (ax == 0) dPxS[cl] = dPf[sl] - dPb[sl];
+      if (ax == 2) dPzS[cl] = dPf[sl] - dPb[sl];
     }
     __syncthreads();
   }
@@ -467,7 +488,7 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
   const int mi = cl / (T * T), mj = (cl / T) % T, mk = cl % T;
   float acc[5];
 #pragma unroll
-  for (int v = 0; v < 5; ++v) acc[v] = accS[5 * cl + v];
+  for (int v = 0; v < 5; ++v) acc[v] = accS[v * SM::nCell + cl];
   const float dPdx = dPxS[cl], dPdz = dPzS[cl];
   auto P = [&](int di, int dj, int dk) -> const PrimF & {
     return prim[((mi + 1 + di) * B + (mj + 1 + dj)) * B + (mk + 1 + dk)];
