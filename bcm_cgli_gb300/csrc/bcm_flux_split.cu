@@ -46,6 +46,17 @@ __device__ __forceinline__ float to_float_rn(double x) {
   return __uint_as_float((hi & 0x80000000u) | r);
 }
 
+// float -> double (exact) on the integer pipes, for the same reason; zero,
+// subnormal, inf and nan inputs take the hardware conversion.
+__device__ __forceinline__ double to_double_exact(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xFFu;
+  if ((b & 0x7FFFFFFFu) == 0) return __hiloint2double((int)(b & 0x80000000u), 0);
+  if (e == 0 || e == 255) return (double)f;
+  const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7FFFFFu) >> 3);
+  return __hiloint2double((int)hi, (int)(b << 29));
+}
+
 // One block row per cube (blockIdx.y); a thread converts two cells, i.e.
 // five 16-byte pairs whose components are known at compile time, so only
 // the density and energy components take an FP64 subtraction.
@@ -420,7 +431,10 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
 
   const float inv = a.inv_dx[cube];
 
-#pragma unroll 1
+  // The three axes are unrolled: every axis-dependent index, stride and
+  // flux variant is then a compile-time choice (6% of the launch on the
+  // 7 M-cell TGV case, measured).
+#pragma unroll
   for (int ax = 0; ax < 3; ++ax) {
     for (int f = tid; f < (T + 1) * T * T; f += NT) {
       const int fa = f / (T * T), p = (f / T) % T, q = f % T;
@@ -529,7 +543,7 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
   for (int v = 0; v < 5; ++v) {
     const double x = u[v], y = __ldg(uu + v);
     xq[v] = x;
-    const float d1 = (float)(x - y), d2 = __ldg(d2p + v);
+    const float d1 = to_float_rn(x - y), d2 = __ldg(d2p + v);
     const float Rp = -(3.0f * d1 - d2) * i2dt;
     Rk[v] = Rp - acc[v] + vF[v];
   }
@@ -590,12 +604,13 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
     for (int r = 0; r < 5; ++r) {
       dq[r] = w * dTau * (d[r][0] * Rk[0] + d[r][1] * Rk[1] + d[r][2] * Rk[2] +
                           d[r][3] * Rk[3] + d[r][4] * Rk[4]);
-      u[r] = xq[r] + (double)dq[r];
+      u[r] = xq[r] + to_double_exact(dq[r]);
     }
     if (a.RK == 3) {
       // Change norms of p, u, v, w, T from the increment, in FP32; summed
       // in FP64 (BCM_Flux...cpp:2530-2566).
-      const float rf = rho, m1 = (float)xq[1], m2 = (float)xq[2], m3 = (float)xq[3];
+      const float rf = rho, m1 = to_float_rn(xq[1]), m2 = to_float_rn(xq[2]),
+                  m3 = to_float_rn(xq[3]);
       const float dr = dq[0], e1 = dq[1], e2 = dq[2], e3 = dq[3], dE = dq[4];
       const float den = 1.0f / (rf * (rf + dr));
       const float dU = (e1 * rf - m1 * dr) * den;
@@ -606,11 +621,11 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
           0.5f * ((2.f * (m1 * e1 + m2 * e2 + m3 * e3) + e1 * e1 + e2 * e2 + e3 * e3) * rf - mm * dr) * den;
       const float dP = Km1 * (dE - dKE);
       const float dTt = (dP * rf - Pc * dr) * den;
-      s5[0] += (double)(dP * dP);
-      s5[1] += (double)(dU * dU);
-      s5[2] += (double)(dVv * dVv);
-      s5[3] += (double)(dW * dW);
-      s5[4] += (double)(dTt * dTt);
+      s5[0] += to_double_exact(dP * dP);
+      s5[1] += to_double_exact(dU * dU);
+      s5[2] += to_double_exact(dVv * dVv);
+      s5[3] += to_double_exact(dW * dW);
+      s5[4] += to_double_exact(dTt * dTt);
     }
   } else {
     // Force integrands on non-fluid cells (:2395-2398); their sum over the
