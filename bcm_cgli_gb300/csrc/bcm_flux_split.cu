@@ -318,6 +318,37 @@ __host__ __device__ constexpr int split_threads() {
 template <int T>
 __host__ __device__ constexpr int split_ctas_per_sm() { return T == 8 ? 2 : 1; }
 
+// Reconstruction of the split path: the stencils of recon() (bcm_common.cuh)
+// with the 1/60 and 1/6 factors folded into the coefficients (one multiply
+// fewer per value; the FP64 path keeps the reference's form).
+template <typename Ld>
+__device__ __forceinline__ void recon_split(int ord, Ld ld, float *ML, float *MR) {
+  if (ord == 5) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const float a = ld(-3, v), b = ld(-2, v), c = ld(-1, v), d = ld(0, v), f = ld(1, v),
+                  g = ld(2, v);
+      ML[v] = (2.f / 60) * a - (13.f / 60) * b + (47.f / 60) * c + (27.f / 60) * d -
+              (3.f / 60) * f;
+      MR[v] = (-3.f / 60) * b + (27.f / 60) * c + (47.f / 60) * d - (13.f / 60) * f +
+              (2.f / 60) * g;
+    }
+  } else if (ord == 3) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const float b = ld(-2, v), c = ld(-1, v), d = ld(0, v), f = ld(1, v);
+      ML[v] = (-1.f / 6) * b + (5.f / 6) * c + (2.f / 6) * d;
+      MR[v] = (2.f / 6) * c + (5.f / 6) * d - (1.f / 6) * f;
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      ML[v] = ld(-1, v);
+      MR[v] = ld(0, v);
+    }
+  }
+}
+
 template <int T, bool VISCOUS>
 __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
     k_flux_split(FluxSplitArgs a) {
@@ -460,12 +491,11 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
       const float *base = BX(li, lj, lk);
       const int sstride = ax == 0 ? SM::PP : (ax == 1 ? SM::RP : 5);
       auto ld = [&](int d, int v) -> float { return base[sstride * d + v]; };
-#pragma unroll 1
-      for (int w = 0; w < nviews; ++w) {
-        const int ord = w == 0 ? ord0 : ord1;
-        const int dst = w == 0 ? dst0 : dst1;
+      // One view (reconstruction order, destination slots) of the face; a
+      // second view only where the two cells use different orders.
+      auto view = [&](const int ord, const int dst) {
         float ML[5], MR[5], Fx[5], dP;
-        recon<float>(ord, ld, ML, MR);
+        recon_split(ord, ld, ML, MR);
         if (ax == 0) face_flux_delta<0>(ML, MR, ef, rho0, P0, Fx, dP);
         else if (ax == 1) face_flux_delta<1>(ML, MR, ef, rho0, P0, Fx, dP);
         else face_flux_delta<2>(ML, MR, ef, rho0, P0, Fx, dP);
@@ -479,7 +509,9 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
           for (int v = 0; v < 5; ++v) Ff[v * SM::nCell + slotF] = Fx[v];
           dPf[slotF] = dP;
         }
-      }
+      };
+      view(ord0, dst0);
+      if (nviews == 2) view(ord1, dst1);
     }
     __syncthreads();
     for (int cl = tid; cl < SM::nCell; cl += NT) {
@@ -497,7 +529,7 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
   // Norm / force partial sums of this CTA (stage 3), reduced below by all
   // threads.
   double s5[7] = {0, 0, 0, 0, 0, 0, 0};
-#pragma unroll 1
+#pragma unroll 2
   for (int cl = tid; cl < SM::nCell; cl += NT) {
   const int mi = cl / (T * T), mj = (cl / T) % T, mk = cl % T;
   float acc[5];
