@@ -103,24 +103,48 @@ __global__ void __launch_bounds__(kHaloThreads) k_iface_faces(InterfaceArgs a) {
   // starts at an even cell index (an even double index) and is 5n or 10
   // doubles long (n is a multiple of 4).
   double2 *U2 = reinterpret_cast<double2 *>(U);
+  // Source (the neighbour's interior) and destination (this cube's ghost
+  // layers) never overlap: each thread issues its loads for kBatch items
+  // before storing them, so the copies are not a chain of round trips.
+  constexpr int kBatch = 4;
+  auto copy = [&](int total, auto index) {
+    for (int w0 = threadIdx.x; w0 < total; w0 += kBatch * kHaloThreads) {
+      double2 u[kBatch];
+      size_t od[kBatch];
+#pragma unroll
+      for (int b = 0; b < kBatch; ++b) {
+        const int w = w0 + b * kHaloThreads;
+        if (w < total) {
+          size_t os;
+          index(w, od[b], os);
+          u[b] = U2[os];
+        }
+      }
+#pragma unroll
+      for (int b = 0; b < kBatch; ++b)
+        if (w0 + b * kHaloThreads < total) U2[od[b]] = u[b];
+    }
+  };
   if (ax < 2) {
     // rows: (layer l, transverse index p); each row = 5n doubles along k
     const int rowlen = 5 * n / 2;
-    for (int w = threadIdx.x; w < 2 * n * rowlen; w += kHaloThreads) {
+    copy(2 * n * rowlen, [&](int w, size_t &od, size_t &os) {
       const int row = w / rowlen, e = w - row * rowlen;
       const int l = row / n, p = 2 + (row - l * n);
       int di, dj, si, sj;
       if (ax == 0) { di = dbase + l; si = sbase + l; dj = sj = p; }
       else { dj = dbase + l; sj = sbase + l; di = si = p; }
-      U2[5 * cell_index(S, c, di, dj, 2) / 2 + e] = U2[5 * cell_index(S, ft.src, si, sj, 2) / 2 + e];
-    }
+      od = 5 * cell_index(S, c, di, dj, 2) / 2 + e;
+      os = 5 * cell_index(S, ft.src, si, sj, 2) / 2 + e;
+    });
   } else {
     // z faces: per (i, j) the two layers are 10 contiguous doubles
-    for (int w = threadIdx.x; w < n * n * 5; w += kHaloThreads) {
+    copy(n * n * 5, [&](int w, size_t &od, size_t &os) {
       const int col = w / 5, e = w - col * 5;
       const int i = 2 + col / n, j = 2 + (col - (col / n) * n);
-      U2[5 * cell_index(S, c, i, j, dbase) / 2 + e] = U2[5 * cell_index(S, ft.src, i, j, sbase) / 2 + e];
-    }
+      od = 5 * cell_index(S, c, i, j, dbase) / 2 + e;
+      os = 5 * cell_index(S, ft.src, i, j, sbase) / 2 + e;
+    });
   }
 }
 
