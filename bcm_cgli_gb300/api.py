@@ -285,6 +285,17 @@ class CaseContext:
         check(lib().bcmg_case_get_state(self.h, *(a.ctypes.data for a in out)))
         return out
 
+    def get_result(self, out=None):
+        """The state U1_ alone copied to host (the result of an advance);
+        `out` may supply the array (e.g. a pinned buffer)."""
+        if out is None:
+            out = np.empty(self.shape)
+        _dp(out)
+        if out.shape != tuple(self.shape):
+            raise BcmgError("output array has the wrong shape")
+        check(lib().bcmg_case_get_state(self.h, out.ctypes.data, None, None))
+        return out
+
     def get_scratch(self):
         out = [np.empty(self.shape) for _ in range(4)]
         check(lib().bcmg_case_get_scratch(self.h, *(a.ctypes.data for a in out)))
