@@ -37,6 +37,7 @@ namespace bcmg {
 __device__ __forceinline__ float to_float_rn(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  if ((b << 1) == 0) return __uint_as_float(hi);  // signed zero (common: rest momenta)
   const int e = (int)((hi >> 20) & 0x7FF) - 1023 + 127;  // float exponent field
   if (e <= 0 || e >= 255) return (float)x;
   const unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);  // top 23 fraction bits
@@ -55,6 +56,46 @@ __device__ __forceinline__ double to_double_exact(float f) {
   if (e == 0 || e == 255) return (double)f;
   const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7FFFFFu) >> 3);
   return __hiloint2double((int)hi, (int)(b << 29));
+}
+
+// (float)(x - r) without FP64 arithmetic when x and r have the same sign and
+// binade: their difference is then exact in FP64 (Sterbenz), so the integer
+// difference of the 53-bit significands, rounded once to nearest even, is
+// bit for bit the FP64 subtraction followed by the conversion.  Other inputs
+// take that subtraction.
+__device__ __forceinline__ float delta_rn(double x, double r) {
+  const unsigned long long bx = (unsigned long long)__double_as_longlong(x),
+                           br = (unsigned long long)__double_as_longlong(r);
+  const int ex = (int)((bx >> 52) & 0x7FF);
+  if (ex != (int)((br >> 52) & 0x7FF) || ex == 0 || ex == 0x7FF || ((bx ^ br) >> 63))
+    return to_float_rn(x - r);
+  const long long mx = (long long)((bx & 0xFFFFFFFFFFFFFull) | (1ull << 52));
+  const long long mr = (long long)((br & 0xFFFFFFFFFFFFFull) | (1ull << 52));
+  long long d = mx - mr;  // value = d * 2^(ex - 1075)
+  if (bx >> 63) d = -d;
+  if (d == 0) return 0.0f;  // x - x is +0 when rounding to nearest
+  const unsigned sign = d < 0 ? 0x80000000u : 0u;
+  const unsigned long long a = d < 0 ? (unsigned long long)(-d) : (unsigned long long)d;
+  const int bl = 64 - __clzll((long long)a);  // bit length, at most 53
+  int fe = (bl - 1) + (ex - 1075) + 127;     // float exponent field
+  if (fe <= 0) return to_float_rn(x - r);    // subnormal float: hardware path
+  unsigned m;
+  if (bl <= 24) {
+    m = (unsigned)(a << (24 - bl));
+  } else {
+    const int sh = bl - 24;
+    const unsigned long long keep = a >> sh, rem = a & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    m = (unsigned)keep;
+    if (rem > half || (rem == half && (keep & 1))) {
+      m += 1;
+      if (m == (1u << 24)) {  // the carry raises the exponent
+        m >>= 1;
+        fe += 1;
+      }
+    }
+  }
+  if (fe >= 255) return to_float_rn(x - r);
+  return __uint_as_float(sign | ((unsigned)fe << 23) | (m & 0x7FFFFFu));
 }
 
 // One block row per cube (blockIdx.y); a thread converts two cells, i.e.
@@ -80,11 +121,11 @@ __global__ void __launch_bounds__(256) k_mirror(const double2 *__restrict__ U,
         float2 *m = M + base + 5 * (size_t)q;
         const double2 a = u[0], b = u[1], c = u[2], d = u[3], e = u[4];
         // doubles: rho, mx, my, mz, E | rho, mx, my, mz, E
-        m[0] = make_float2(to_float_rn(a.x - rho0), to_float_rn(a.y));
+        m[0] = make_float2(delta_rn(a.x, rho0), to_float_rn(a.y));
         m[1] = make_float2(to_float_rn(b.x), to_float_rn(b.y));
-        m[2] = make_float2(to_float_rn(c.x - E0), to_float_rn(c.y - rho0));
+        m[2] = make_float2(delta_rn(c.x, E0), delta_rn(c.y, rho0));
         m[3] = make_float2(to_float_rn(d.x), to_float_rn(d.y));
-        m[4] = make_float2(to_float_rn(e.x), to_float_rn(e.y - E0));
+        m[4] = make_float2(to_float_rn(e.x), delta_rn(e.y, E0));
       }
     }
   }
