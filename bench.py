@@ -304,8 +304,9 @@ def pinned_like(a):
 
 def measure(api, case, precision_name, args, dist, clocks_on=True, method=None):
     """Timed region for one precision: args.steps dual-time steps resident in
-    HBM, device-timed with CUDA events on the context's stream; the flux
-    kernel's launches are bracketed by events for its average duration."""
+    HBM, each one captured-graph launch, device-timed with CUDA events on the
+    context's stream; then two eager profiled steps bracket every flux launch
+    with events for the kernel's average duration."""
     precision = api.PRECISION_SPLIT if precision_name == "split" else api.PRECISION_FP64
     ctx = make_context(api, case, precision)
     meth = method or getattr(args, "method", "rk3")
@@ -317,9 +318,8 @@ def measure(api, case, precision_name, args, dist, clocks_on=True, method=None):
     if shape:
         ctx.set_tuning(shape["flux_tile"], shape["lusgs_threads"])
     ctx.set_state(case.U, case.U, case.U)
-    for _ in range(args.warmup):
-        ctx.advance(1, SUBITERS, use_graph=False)
-    ctx.set_profiling(True)
+    for _ in range(args.warmup):  # the last warm-up step captures the step graph
+        ctx.advance(1, SUBITERS, use_graph=True)
     clocks = Clocks(dist.local) if clocks_on else None
     if clocks:
         clocks.start()
@@ -327,14 +327,19 @@ def measure(api, case, precision_name, args, dist, clocks_on=True, method=None):
     dist.barrier()
     ctx.sync()
     ctx.timer_mark(0)
-    for _ in range(args.steps):
-        ctx.advance(1, SUBITERS, use_graph=False)
+    for _ in range(args.steps):  # one graph launch per dual-time step
+        ctx.advance(1, SUBITERS, use_graph=True)
         launches += ctx.launch_count()
     ctx.timer_mark(1)
     ctx.sync()
     dist.barrier()
     ms = dist.max(ctx.timer_elapsed(0, 1))
     clk = clocks.stop() if clocks else None
+    # flux kernel duration: events around each flux launch in eager profiled
+    # steps of the same kind (graphs are not profiled)
+    ctx.set_profiling(True)
+    for _ in range(min(2, args.steps)):
+        ctx.advance(1, SUBITERS, use_graph=False)
     flux_ms, flux_n = ctx.profile()
     ctx.set_profiling(False)
     cell_subiters = case.n_cells * SUBITERS * args.steps * dist.world
