@@ -200,25 +200,31 @@ struct SplitSmem {
   static constexpr int RP = T == 8 ? 72 : 5 * X;
   static constexpr int PP = T == 8 ? 1011 : X * RP;
   static constexpr int nBoxF = X * PP;
+  static constexpr int nFace = (T + 1) * T * T;  // faces of one axis
+  static constexpr int nBits = (3 * nFace + 31) / 32;
   static constexpr size_t bytes = sizeof(float) * nBoxF /*state deltas*/ +
-                                  sizeof(PrimF) * nPrim + 2 * sizeof(float) * 5 * nCell +
-                                  2 * sizeof(float) * nCell /*dPb, dPf*/ +
-                                  sizeof(float) * 5 * nCell /*flux balance*/ +
-                                  2 * sizeof(float) * nCell /*x, z pressure differences*/ +
+                                  sizeof(PrimF) * nPrim +
+                                  sizeof(float) * 15 * nFace /*face fluxes, 3 axes*/ +
+                                  sizeof(float) * 2 * nFace /*x, z face pressure halves*/ +
+                                  sizeof(unsigned) * ((nBits + 3) / 4) * 4 /*second views*/ +
                                   ((nBox + 15) / 16) * 16 /*flags*/;
   static_assert(RP >= 5 * X && PP >= X * RP, "box pitches hold the rows");
   static_assert(T != 8 || bytes + 1024 <= 233472 / 2, "two CTAs per SM");
 };
 
-// Slot of tile cell (li, lj, lk) in the value-major face buffers.  For 8^3
-// tiles an XOR swizzle: the 32 faces of a warp (4 x 8 or 8 x 4 cells of one
-// face plane, any of the three orientations) and 32 consecutive cells in
-// (i, j, k) order all land in distinct banks.
+// Index of face fa (0..T along axis ax) at in-plane position (p, q) in the
+// value-major face arrays.  The in-plane coordinates are (j, k) for x-faces,
+// (i, k) for y-faces and (j, i) for z-faces.  For 8^3 tiles the plane index
+// is rotated per face (by 8 fa for y-faces, by fa for z-faces) so that the
+// 32 faces a warp stores (4 x 8 of one plane) and the faces 32 consecutive
+// cells read (i, j, k order) land in distinct banks for every axis.
 template <int T>
-__device__ __forceinline__ int face_slot(int li, int lj, int lk) {
-  if (T == 8)
-    return ((li * 2 + (lj >> 2)) << 5) | (((lj + li) & 3) << 3) | (lk ^ (lj & 3) ^ (li & 4));
-  return (li * T + lj) * T + lk;
+__device__ __forceinline__ int face_idx(int ax, int fa, int p, int q) {
+  if (T == 8) {
+    const int in = 8 * p + q;
+    return fa * 64 + (ax == 0 ? in : ((in + (ax == 1 ? 8 * fa : fa)) & 63));
+  }
+  return (fa * T + p) * T + q;
 }
 
 // Delta-form preconditioned Roe flux (same formulas as face_flux in
@@ -400,14 +406,16 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float *box = reinterpret_cast<float *>(smem_raw);  // [X][X][X][5] deltas, pitches RP, PP
   PrimF *prim = reinterpret_cast<PrimF *>(box + SM::nBoxF);
-  float *Fb = reinterpret_cast<float *>(prim + SM::nPrim);
-  float *Ff = Fb + 5 * SM::nCell;
-  float *dPb = Ff + 5 * SM::nCell;
-  float *dPf = dPb + SM::nCell;
-  float *accS = dPf + SM::nCell;        // [5][nCell] Rfx/dx + Rfy/dy + Rfz/dz
-  float *dPxS = accS + 5 * SM::nCell;   // [nCell] x-face pressure difference
-  float *dPzS = dPxS + SM::nCell;       // [nCell] z-face pressure difference
-  signed char *fbox = reinterpret_cast<signed char *>(dPzS + SM::nCell);  // [X][X][X] flags
+  // Face fluxes stored once per face: [3 axes][5][nFace], the x- and z-face
+  // pressure halves [2][nFace], and one bit per face whose minus-side cell
+  // takes a different reconstruction order (that cell recomputes its view).
+  constexpr int NF = SM::nFace;
+  float *FF = reinterpret_cast<float *>(prim + SM::nPrim);
+  float *FdP = FF + 15 * NF;
+  unsigned *dbits = reinterpret_cast<unsigned *>(FdP + 2 * NF);
+  signed char *fbox =
+      reinterpret_cast<signed char *>(dbits + ((SM::nBits + 3) / 4) * 4);  // [X][X][X] flags
+  float *Fb = FF;  // staging area of the int flags (before the face pass)
 
   const int n = a.ph.n, S = n + 4, nx = n + 1;
   const int nt = n / T;
@@ -453,7 +461,8 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
   // read by the stencil (the reconstruction order falls back before reaching
   // them) and are left unset.
   int *ftmp = reinterpret_cast<int *>(Fb);
-  static_assert(SM::nBox <= 19 * SM::nCell, "int flags fit the face buffers");
+  static_assert(SM::nBox <= 17 * SM::nFace, "int flags fit the face buffers");
+  for (int w = tid; w < SM::nBits; w += NT) dbits[w] = 0u;
   {
     const int k0 = bk - 3;
     const int klo = k0 < 0 ? -k0 : 0;                 // first valid column
@@ -522,61 +531,76 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
       const bool needB = fa < T, needF = fa > 0;
       const int ob = order_backward(g, fm2, fm1, fp1);
       const int of = order_forward(g, nx, fm2, f0, fp1);
-      const int slotB = face_slot<T>(li, lj, lk);
-      const int slotF = face_slot<T>(li - di, lj - dj, lk - dk);
-      int nviews, ord0, ord1 = 0, dst0, dst1 = 0;
-      if (needB && needF && ob == of) { nviews = 1; ord0 = ob; dst0 = 3; }
-      else if (needB && needF) { nviews = 2; ord0 = ob; dst0 = 1; ord1 = of; dst1 = 2; }
-      else if (needB) { nviews = 1; ord0 = ob; dst0 = 1; }
-      else { nviews = 1; ord0 = of; dst0 = 2; }
       const float *base = BX(li, lj, lk);
       const int sstride = ax == 0 ? SM::PP : (ax == 1 ? SM::RP : 5);
       auto ld = [&](int d, int v) -> float { return base[sstride * d + v]; };
-      // One view (reconstruction order, destination slots) of the face; a
-      // second view only where the two cells use different orders.
-      auto view = [&](const int ord, const int dst) {
-        float ML[5], MR[5], Fx[5], dP;
-        recon_split(ord, ld, ML, MR);
-        if (ax == 0) face_flux_delta<0>(ML, MR, ef, rho0, P0, Fx, dP);
-        else if (ax == 1) face_flux_delta<1>(ML, MR, ef, rho0, P0, Fx, dP);
-        else face_flux_delta<2>(ML, MR, ef, rho0, P0, Fx, dP);
-        if (dst & 1) {
+      // The stored view is the plus-side cell's (the minus-side cell's for
+      // the last face, which has no plus cell in the tile); where the
+      // minus-side cell's order differs it recomputes its own view.
+      float ML[5], MR[5], Fx[5], dP;
+      recon_split(needB ? ob : of, ld, ML, MR);
+      if (ax == 0) face_flux_delta<0>(ML, MR, ef, rho0, P0, Fx, dP);
+      else if (ax == 1) face_flux_delta<1>(ML, MR, ef, rho0, P0, Fx, dP);
+      else face_flux_delta<2>(ML, MR, ef, rho0, P0, Fx, dP);
+      const int fi = face_idx<T>(ax, fa, p, q);
 #pragma unroll
-          for (int v = 0; v < 5; ++v) Fb[v * SM::nCell + slotB] = Fx[v];
-          dPb[slotB] = dP;
-        }
-        if (dst & 2) {
-#pragma unroll
-          for (int v = 0; v < 5; ++v) Ff[v * SM::nCell + slotF] = Fx[v];
-          dPf[slotF] = dP;
-        }
-      };
-      view(ord0, dst0);
-      if (nviews == 2) view(ord1, dst1);
-    }
-    __syncthreads();
-    for (int cl = tid; cl < SM::nCell; cl += NT) {
-      const int sl = face_slot<T>(cl / (T * T), (cl / T) % T, cl % T);
-#pragma unroll
-      for (int v = 0; v < 5; ++v) {
-        float t = (Ff[v * SM::nCell + sl] - Fb[v * SM::nCell + sl]) * inv;
-        accS[v * SM::nCell + cl] = ax == 0 ? t : accS[v * SM::nCell + cl] + t;
+      for (int v = 0; v < 5; ++v) FF[(5 * ax + v) * NF + fi] = Fx[v];
+      if (ax != 1) FdP[(ax == 2) * NF + fi] = dP;
+      if (needB && needF && ob != of) {
+        const int bit = ax * NF + fi;
+        atomicOr(dbits + (bit >> 5), 1u << (bit & 31));
       }
-      if (ax == 0) dPxS[cl] = dPf[sl] - dPb[sl];
-      if (ax == 2) dPzS[cl] = dPf[sl] - dPb[sl];
     }
-    __syncthreads();
   }
+  __syncthreads();
   // Norm / force partial sums of this CTA (stage 3), reduced below by all
   // threads.
   double s5[7] = {0, 0, 0, 0, 0, 0, 0};
 #pragma unroll 2
   for (int cl = tid; cl < SM::nCell; cl += NT) {
   const int mi = cl / (T * T), mj = (cl / T) % T, mk = cl % T;
-  float acc[5];
+  // Flux balance of the cell from its six faces, axis by axis.
+  float acc[5], dPdx = 0.f, dPdz = 0.f;
 #pragma unroll
-  for (int v = 0; v < 5; ++v) acc[v] = accS[v * SM::nCell + cl];
-  const float dPdx = dPxS[cl], dPdz = dPzS[cl];
+  for (int ax = 0; ax < 3; ++ax) {
+    const int m = ax == 0 ? mi : (ax == 1 ? mj : mk);
+    const int p = ax == 2 ? mj : (ax == 0 ? mj : mi), q = ax == 2 ? mi : mk;
+    const int fb = face_idx<T>(ax, m, p, q), ff = face_idx<T>(ax, m + 1, p, q);
+    float Fbv[5], Ffv[5], dPbv = 0.f, dPfv = 0.f;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      Fbv[v] = FF[(5 * ax + v) * NF + fb];
+      Ffv[v] = FF[(5 * ax + v) * NF + ff];
+    }
+    if (ax != 1) {
+      dPbv = FdP[(ax == 2) * NF + fb];
+      dPfv = FdP[(ax == 2) * NF + ff];
+    }
+    const int bit = ax * NF + ff;
+    if (m + 1 < T && ((dbits[bit >> 5] >> (bit & 31)) & 1u)) {
+      // the forward face's stored view is the next cell's: form this cell's
+      const int li = mi + (ax == 0), lj = mj + (ax == 1), lk = mk + (ax == 2);
+      const int g = (ax == 0 ? bi + li : (ax == 1 ? bj + lj : bk + lk));
+      const int di = ax == 0, dj = ax == 1, dk = ax == 2;
+      const int of = order_forward(g, nx, FL(li - 2 * di, lj - 2 * dj, lk - 2 * dk),
+                                   FL(li, lj, lk), FL(li + di, lj + dj, lk + dk));
+      const float *base = BX(li, lj, lk);
+      const int sstride = ax == 0 ? SM::PP : (ax == 1 ? SM::RP : 5);
+      auto ld = [&](int d, int v) -> float { return base[sstride * d + v]; };
+      float ML[5], MR[5];
+      recon_split(of, ld, ML, MR);
+      if (ax == 0) face_flux_delta<0>(ML, MR, ef, rho0, P0, Ffv, dPfv);
+      else if (ax == 1) face_flux_delta<1>(ML, MR, ef, rho0, P0, Ffv, dPfv);
+      else face_flux_delta<2>(ML, MR, ef, rho0, P0, Ffv, dPfv);
+    }
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const float t = (Ffv[v] - Fbv[v]) * inv;
+      acc[v] = ax == 0 ? t : acc[v] + t;
+    }
+    if (ax == 0) dPdx = dPfv - dPbv;
+    if (ax == 2) dPdz = dPfv - dPbv;
+  }
   auto P = [&](int di, int dj, int dk) -> const PrimF & {
     return prim[((mi + 1 + di) * B + (mj + 1 + dj)) * B + (mk + 1 + dk)];
   };
