@@ -100,17 +100,39 @@ __global__ void __launch_bounds__(kRkThreads) k_rk(RkArgs a, long long total, lo
   }
 }
 
-// Sum of partial blocks [b0, b1) per quantity into tot[0..6] (block of 7
-// warps).  One warp per quantity: lane l sums blocks b0+l, b0+l+32, ... in
-// order, then a fixed shuffle tree; the result does not depend on timing.
+// Deterministic sum of partials[b][0..6] over blocks [b0, b1) into tot[7]
+// (shared).  kNormWarps warps per quantity; lane l of warp w takes blocks
+// b0 + 32 w + l, then every 32 kNormWarps-th, into four accumulators in turn
+// (loads in flight), combined as (v0 + v1) + (v2 + v3); a fixed shuffle tree
+// per warp and the warps' results in warp order.  The order depends only on
+// b1 - b0, never on timing, so a batch's case and the same case alone sum
+// identically.  Launch with 7 * kNormWarps warps.
+constexpr int kNormWarps = 4;
 __device__ void sum_partials(const double *partials, int b0, int b1, double *tot) {
-  const int m = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __shared__ double part[7][kNormWarps];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m = w / kNormWarps, sub = w % kNormWarps;
+  constexpr int kStride = 32 * kNormWarps;
   if (m < 7) {
-    double v = 0;
-    for (int b = b0 + lane; b < b1; b += 32) v += partials[(size_t)b * 7 + m];
+    double v0 = 0, v1 = 0, v2 = 0, v3 = 0;
+    int b = b0 + sub * 32 + lane;
+    for (; b + 3 * kStride < b1; b += 4 * kStride) {
+      v0 += partials[(size_t)b * 7 + m];
+      v1 += partials[(size_t)(b + kStride) * 7 + m];
+      v2 += partials[(size_t)(b + 2 * kStride) * 7 + m];
+      v3 += partials[(size_t)(b + 3 * kStride) * 7 + m];
+    }
+    for (; b < b1; b += kStride) v0 += partials[(size_t)b * 7 + m];
+    double v = (v0 + v1) + (v2 + v3);
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-    if (lane == 0) tot[m] = v;
+    if (lane == 0) part[m][sub] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 7) {
+    double t = part[threadIdx.x][0];
+    for (int q = 1; q < kNormWarps; ++q) t += part[threadIdx.x][q];
+    tot[threadIdx.x] = t;
   }
   __syncthreads();
 }
@@ -175,7 +197,7 @@ cudaError_t launch_rk(const RkArgs &a, int *nblocks_out, cudaStream_t s) {
 
 cudaError_t launch_norms(const Phys &ph, const double *partials, int nblocks, double *er,
                          cudaStream_t s, const int *active) {
-  k_norms<<<1, 7 * 32, 0, s>>>(ph, partials, nblocks, er, active);
+  k_norms<<<1, 7 * 32 * kNormWarps, 0, s>>>(ph, partials, nblocks, er, active);
   return cudaGetLastError();
 }
 
@@ -183,7 +205,7 @@ cudaError_t launch_norms_batch(int n, const CaseConst *cases, const int *case_bl
                                const double *partials, double *er, cudaStream_t s,
                                const int *active) {
   if (ncase <= 0) return cudaSuccess;
-  k_norms_batch<<<ncase, 7 * 32, 0, s>>>(n, cases, case_blk, partials, er, active);
+  k_norms_batch<<<ncase, 7 * 32 * kNormWarps, 0, s>>>(n, cases, case_blk, partials, er, active);
   return cudaGetLastError();
 }
 
