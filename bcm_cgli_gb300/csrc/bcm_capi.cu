@@ -50,22 +50,20 @@ void dfree(T *&p) {
   p = nullptr;
 }
 
-__global__ void k_time_shift(int n, long long total, const double *U1_, double *U1,
-                             double *U1q) {
-  // main.cpp:1292-1315: U1q <- U1, U1 <- U1_ on interior cells.
-  const int S = n + 4;
-  const long long n3 = (long long)n * n * n;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
-    const int c = 1 + (int)(t / n3);
-    const int r = (int)(t % n3);
-    const size_t o = 5 * cell_index(S, c, 2 + r / (n * n), 2 + (r / n) % n, 2 + r % n);
-#pragma unroll
-    for (int v = 0; v < 5; ++v) {
-      U1q[o + v] = U1[o + v];
-      U1[o + v] = U1_[o + v];
+__global__ void k_time_shift(int n, int ncubes, const double2 *__restrict__ U1_,
+                             double2 *__restrict__ U1, double2 *__restrict__ U1q) {
+  // main.cpp:1292-1315: U1q <- U1, U1 <- U1_ on interior cells.  An interior
+  // row (cube, i, j) is 5n contiguous doubles starting at an even cell index
+  // (S even), so it moves as 5n/2 aligned 16-byte pairs; cubes on blockIdx.y.
+  const int S = n + 4, rl = 5 * n / 2, per = n * n * rl;
+  for (int cube = 1 + blockIdx.y; cube <= ncubes; cube += gridDim.y)
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < per; w += gridDim.x * blockDim.x) {
+      const int row = w / rl, e = w - row * rl;
+      const size_t o = 5 * cell_index(S, cube, 2 + row / n, 2 + row % n, 2) / 2 + e;
+      const double2 a = U1[o], b = U1_[o];
+      U1q[o] = a;
+      U1[o] = b;
     }
-  }
 }
 
 __global__ void k_emax(double *er, double *emax, const int *active) {
@@ -539,8 +537,12 @@ int case_subiter(bcmg_case *c) {
 int case_shift(bcmg_case *c) {
   const long long total = (long long)(c->ncube - 1) * c->ph.n * c->ph.n * c->ph.n;
   if (total > 0) {
-    int blocks = (int)std::min<long long>((total + 255) / 256, 152 * 8);
-    k_time_shift<<<blocks, 256, 0, c->stream>>>(c->ph.n, total, c->U1_, c->U1, c->U1q);
+    const int n = c->ph.n, per = n * n * (5 * n / 2);
+    const dim3 grid((per + 255) / 256, std::min(c->ncube - 1, 65535));
+    k_time_shift<<<grid, 256, 0, c->stream>>>(n, c->ncube - 1,
+                                              reinterpret_cast<const double2 *>(c->U1_),
+                                              reinterpret_cast<double2 *>(c->U1),
+                                              reinterpret_cast<double2 *>(c->U1q));
     CK(cudaGetLastError());
     ++c->launches;
     if (c->precision == BCMG_PRECISION_SPLIT) {
