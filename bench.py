@@ -428,7 +428,7 @@ def run_gpu_arm(args, dist):
     m_other = measure(api, case, other, args, dist, clocks_on=False) if not args.quick else None
 
     # Accuracy of the split form against the FP64 path after one dual-time
-    # step from the same initial state (spec bound: 1e-5 relative L2).
+    # step from the same initial state (bound: 1e-5 relative L2).
     acc = None
     if m_other is not None:
         states = {}

@@ -35,7 +35,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.environ.get("BCM_REFERENCE_DIR", "/root/reference")
 OUT_DIR = os.path.join(HERE, "_ref")
 
-# The reference translation units on the hot path (SURVEY-mapped in the design doc).
+# The reference translation units on the hot path.
 REF_SOURCES = [
     "BCM_Flux_XYZ_Viscous_Runge_kutta.cpp",
     "BCM_Interface.cpp",

@@ -3,8 +3,8 @@
 The FP64 path is bit-identical to the reference, so state arrays are
 compared with exact equality (signed zeros compare equal).  The residual
 norms are sums whose order differs from the reference's serial loop, so they
-are compared with a relative tolerance of 1e-12 (the benchmark spec's tolerance for
-the FP64 path)."""
+are compared with a relative tolerance of 1e-12 (the FP64 path's stated
+tolerance)."""
 import numpy as np
 import pytest
 
