@@ -175,12 +175,17 @@ def test_full_size_tgv_sampled_cubes(port):
     assert np.array_equal(a.U1_[1:], b.U1_[pick])
 
 
-def test_full_size_sphere_loop_bitwise(port):
-    """Config-3 size (1,584 cubes of 16^3 on two levels, 6.5 M cells, IBM
-    tables from the GPU preprocessing of the 20,480-triangle body, open-domain
+@pytest.mark.parametrize("workload", ["tgv", "sphere"])
+def test_full_size_loop_bitwise(port, workload):
+    """Full benchmark sizes: config 2 (TGV, 8^3 cubes of 24^3, 7.1 M cells)
+    and config 3 (1,584 cubes of 16^3 on two levels, 6.5 M cells, IBM tables
+    from the GPU preprocessing of the 20,480-triangle body, open-domain
     boundaries): one FP64 dual-time step of two sub-iterations, replayed as one
     graph, equals the oracle's loop bit for bit in every state array."""
-    case = cases.sphere_ibm(preprocess=api.ibm_preprocess)
+    if workload == "tgv":
+        case = cases.taylor_green(ncx=8, n=24)
+    else:
+        case = cases.sphere_ibm(preprocess=api.ibm_preprocess)
     a = O.State(case)
     port.run(case, a, 1, 2)
     ctx = api.CaseContext(case)
@@ -190,7 +195,7 @@ def test_full_size_sphere_loop_bitwise(port):
     for k, y in (("U1_", U1_), ("U1", U1), ("U1q", U1q)):
         bad = np.argwhere(getattr(a, k) != y)
         assert bad.size == 0, f"{k}: {len(bad)} mismatches, first {bad[:3]}"
-    # The norms are ratios of sums over 6.5 M cells taken in different orders
+    # The norms are ratios of sums over ~7 M cells taken in different orders
     # (fixed GPU blocks against the oracle's thread chunks); the rounding bound
     # of such a sum is about n * 2^-53 = 7e-10 relative (observed: 1.3e-12).
     rel = np.max(np.abs(er[1:6] - a.er[1:6]) / np.abs(a.er[1:6]))
