@@ -74,6 +74,40 @@ def test_split_sphere_forces_within_bound():
     assert abs(er_b[6] - er_a[6]) <= 1e-3 * abs(er_a[6]), (er_a[6], er_b[6])
 
 
+@pytest.mark.parametrize("workload", ["tgv", "sphere", "batch"])
+def test_split_full_size_within_bound(workload):
+    """Benchmark sizes (config 2 TGV 7.1 M cells, config 3 sphere 6.5 M cells
+    with the GPU-built IBM tables, config 4 batch of 16 spheres): one
+    dual-time step of 10 sub-iterations, split against FP64 within 1e-5
+    relative L2 per variable, and every case's drag within 0.1%."""
+    if workload == "tgv":
+        cs = [cases.taylor_green(ncx=8, n=24)]
+    elif workload == "sphere":
+        cs = [cases.sphere_ibm(preprocess=api.ibm_preprocess)]
+    else:
+        cs = cases.sphere_batch(ncase=16, seed=2024, n=16, preprocess=api.ibm_preprocess)
+    states, ers = {}, {}
+    for prec in (api.PRECISION_FP64, api.PRECISION_SPLIT):
+        ctx = (api.BatchContext(cs, precision=prec) if len(cs) > 1
+               else api.CaseContext(cs[0], precision=prec))
+        if len(cs) > 1:
+            for q, c in enumerate(cs):
+                ctx.set_case_state(q, c.U, c.U, c.U)
+        else:
+            ctx.set_state(cs[0].U, cs[0].U, cs[0].U)
+        er = ctx.advance(1, 10)
+        states[prec] = ([ctx.get_case_state(q)[0] for q in range(len(cs))] if len(cs) > 1
+                        else [ctx.get_state()[0]])
+        ers[prec] = np.asarray(er).reshape(len(cs), 8)
+        ctx.close()
+    for q, c in enumerate(cs):
+        err = rel_l2(states[api.PRECISION_SPLIT][q], states[api.PRECISION_FP64][q], c.n)
+        assert max(err) <= SPLIT_BOUND, (q, err)
+        if workload != "tgv":
+            a, b = ers[api.PRECISION_FP64][q, 6], ers[api.PRECISION_SPLIT][q, 6]
+            assert abs(b - a) <= 1e-3 * abs(a), (q, a, b)
+
+
 def _mirror_ref(U, rho0, P0):
     d = U.copy()
     d[..., 0] -= rho0
