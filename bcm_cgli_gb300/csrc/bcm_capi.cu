@@ -198,6 +198,16 @@ struct bcmg_case {
   int *task_cube = nullptr;  // destination cube of each face task
   FaceTask *tasks = nullptr;
   int ntasks = 0;
+  // The face tasks a stage's first interface call must repeat after the
+  // previous stage's last one (main.cpp:1161-1204 runs the interface before
+  // and after every update): level jumps, faces the boundary fill writes and
+  // faces whose source or destination layers hold IBM ghost cells.  The
+  // other copies would write the values already there: between the two
+  // calls only the boundary fill (its own ghost faces) and the IBM ghost
+  // fill (its listed cells) write the state.
+  int *task_cube_p = nullptr;
+  FaceTask *tasks_p = nullptr;
+  int ntasks_p = 0;
   int *bc_cubes = nullptr, *bc_masks = nullptr;
   int nbc = 0;
   Ibm ibm;  // minus entries then plus entries, one combined schedule
@@ -289,7 +299,8 @@ struct bcmg_case {
     ev.clear();
     dfree(U1_); dfree(U1); dfree(U1q); dfree(U1p1); dfree(U1p2); dfree(Rku1); dfree(Residual1);
     dfree(M); dfree(D2); dfree(inv_dx);
-    dfree(FWS); dfree(cube_size); dfree(task_cube); dfree(tasks); dfree(bc_cubes);
+    dfree(FWS); dfree(cube_size); dfree(task_cube); dfree(tasks); dfree(task_cube_p);
+    dfree(tasks_p); dfree(bc_cubes);
     dfree(bc_masks); dfree(partials); dfree(er); dfree(emax);
     dfree(cases); dfree(cube_case); dfree(rk_blk); dfree(case_blk_rk); dfree(case_blk_flux);
     dfree(case_blk_cube);
@@ -376,22 +387,23 @@ int case_flux(bcmg_case *c, int RK) {
   return BCMG_OK;
 }
 
-int case_interface(bcmg_case *c) {
+int case_interface(bcmg_case *c, bool full = true) {
   InterfaceArgs ia;
   ia.n = c->ph.n;
-  ia.ntasks = c->ntasks;
-  ia.task_cube = c->task_cube;
-  ia.tasks = c->tasks;
+  ia.ntasks = full ? c->ntasks : c->ntasks_p;
+  ia.task_cube = full ? c->task_cube : c->task_cube_p;
+  ia.tasks = full ? c->tasks : c->tasks_p;
   ia.U1_ = c->U1_;
   ia.bt = c->bt();
   CK(launch_interface(ia, c->ncube, c->stream));
-  c->launches += c->ntasks > 0 ? 2 : 1;
+  c->launches += ia.ntasks > 0 ? 2 : 1;
   return BCMG_OK;
 }
 
 // Boundary conditions, IBM ghost cells and interface ahead of each update
-// (main.cpp:1161-1204).
-int case_prologue(bcmg_case *c) {
+// (main.cpp:1161-1204).  full == false: the stage follows another stage's
+// closing interface call, so only the face copies that can change run.
+int case_prologue(bcmg_case *c, bool full = true) {
   int r;
   if (c->nbc > 0) {
     BcArgs b;
@@ -408,7 +420,7 @@ int case_prologue(bcmg_case *c) {
   if ((r = ibm_run(c->ibm, c->ph.n, c->ph.rho0, c->ph.P0, c->U1_, c->stream, &c->launches,
                    c->bt())))
     return r;
-  return case_interface(c);
+  return case_interface(c, full);
 }
 
 // One LU-SGS sub-iteration: prologue, residual, sweeps with the update and
@@ -436,9 +448,9 @@ LusgsSplitArgs lusgs_split_args(bcmg_case *c) {
   return l;
 }
 
-int case_lusgs(bcmg_case *c) {
+int case_lusgs(bcmg_case *c, bool full = true) {
   int r;
-  if ((r = case_prologue(c))) return r;
+  if ((r = case_prologue(c, full))) return r;
   if ((r = case_flux(c, 0))) return r;
   if (c->precision == BCMG_PRECISION_SPLIT) {
     CK(launch_lusgs_split(lusgs_split_args(c), c->ncube - 1, c->stream));
@@ -469,9 +481,9 @@ int case_lusgs(bcmg_case *c) {
   return case_interface(c);
 }
 
-int case_stage(bcmg_case *c, int RK) {
+int case_stage(bcmg_case *c, int RK, bool full = true) {
   int r;
-  if ((r = case_prologue(c))) return r;
+  if ((r = case_prologue(c, full))) return r;
   if ((r = case_flux(c, RK))) return r;
   int nb = 0;
   if (c->precision == BCMG_PRECISION_SPLIT) {
@@ -519,13 +531,13 @@ int case_stage(bcmg_case *c, int RK) {
 
 // One sub-iteration (three RK stages or one LU-SGS update) and the E
 // normalisation of its norms (main.cpp:1249-1259).
-int case_subiter(bcmg_case *c) {
+int case_subiter(bcmg_case *c, bool full = true) {
   int r;
   if (c->method == BCMG_METHOD_LUSGS) {
-    if ((r = case_lusgs(c))) return r;
+    if ((r = case_lusgs(c, full))) return r;
   } else {
     for (int RK = 1; RK <= 3; ++RK)
-      if ((r = case_stage(c, RK))) return r;
+      if ((r = case_stage(c, RK, full && RK == 1))) return r;
   }
   k_emax<<<c->ncase, 32, 0, c->stream>>>(c->er, c->emax, c->bt().active);
   CK(cudaGetLastError());
@@ -555,8 +567,8 @@ int case_shift(bcmg_case *c) {
 
 int case_step(bcmg_case *c, int subiters) {
   int r;
-  for (int it = 0; it < subiters; ++it)
-    if ((r = case_subiter(c))) return r;
+  for (int it = 0; it < subiters; ++it)  // the step's first stage runs every face copy
+    if ((r = case_subiter(c, it == 0))) return r;
   return case_shift(c);
 }
 
@@ -883,6 +895,52 @@ int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out)
     int r = ibm_upload(c->ibm, nm + np, w.data(), gc.data(), ip.data(), d->n, d->ncube, s);
     if (r) return fail(r);
   }
+  // Reduced face-task list of the prologue interface calls.  Per cube, bits
+  // 0..5: its ghost face (axis, side) is written by the boundary fill or
+  // holds an IBM ghost cell; bits 6..11: the two interior layers that face
+  // (axis, side) of a neighbour copies from hold an IBM ghost cell.
+  {
+    const int n = d->n;
+    std::vector<uint16_t> hot((size_t)d->ncube, 0);
+    for (size_t q = 0; q < bcc.size(); ++q) hot[bcc[q]] |= (uint16_t)(bcm[q] & 63);
+    auto mark = [&](const int *G, int cnt) {
+      for (int e = 0; e < cnt; ++e) {
+        const int g = G[1 + 4 * e];
+        const int x[3] = {G[2 + 4 * e], G[3 + 4 * e], G[4 + 4 * e]};
+        if (g <= 0 || g >= d->ncube) continue;
+        for (int ax = 0; ax < 3; ++ax) {
+          const int a = x[(ax + 1) % 3], b = x[(ax + 2) % 3];
+          if (a < 2 || a > n + 1 || b < 2 || b > n + 1) continue;
+          const int l = x[ax];
+          if (l == 0 || l == 1) hot[g] |= (uint16_t)(1 << (2 * ax));
+          if (l == n + 2 || l == n + 3) hot[g] |= (uint16_t)(1 << (2 * ax + 1));
+          if (l == n || l == n + 1) hot[g] |= (uint16_t)(1 << (6 + 2 * ax));
+          if (l == 2 || l == 3) hot[g] |= (uint16_t)(1 << (6 + 2 * ax + 1));
+        }
+      }
+    };
+    if (nm) mark(d->gc_minus, nm);
+    if (np) mark(d->gc_plus, np);
+    std::vector<FaceTask> tp;
+    std::vector<int> cp;
+    for (size_t t = 0; t < tasks.size(); ++t) {
+      const FaceTask &f = tasks[t];
+      const int face = 2 * f.axis + f.side;
+      if (f.kind != 0 || (hot[task_cube[t]] >> face & 1) || (hot[f.src] >> (6 + face) & 1)) {
+        tp.push_back(f);
+        cp.push_back(task_cube[t]);
+      }
+    }
+    c->ntasks_p = (int)tp.size();
+    if (!tp.empty() &&
+        !(ck(dalloc(&c->tasks_p, tp.size()), "alloc") &&
+          ck(dalloc(&c->task_cube_p, cp.size()), "alloc") &&
+          ck(cudaMemcpy(c->tasks_p, tp.data(), sizeof(FaceTask) * tp.size(),
+                        cudaMemcpyHostToDevice), "copy") &&
+          ck(cudaMemcpy(c->task_cube_p, cp.data(), sizeof(int) * cp.size(),
+                        cudaMemcpyHostToDevice), "copy")))
+      return fail(BCMG_ERR_CUDA);
+  }
   *out = c;
   return BCMG_OK;
 }
@@ -978,12 +1036,14 @@ int bcmg_case_advance(bcmg_case *c, int steps, int subiters, int use_graph, doub
       int L = (int)(c->ibm.level_off.size() > 0 ? c->ibm.level_off.size() - 1 : 0);
       // bc, IBM levels, interface (faces + edges), [mirror], flux, [rk],
       // interface (faces + edges)
-      const long long ifl = c->ntasks > 0 ? 2 : 1;
-      long long stage = (c->nbc > 0) + L + ifl + 1 + 1 + ifl;
+      const long long ifl = c->ntasks > 0 ? 2 : 1, ifp = c->ntasks_p > 0 ? 2 : 1;
+      // stages after the first of a step run the reduced prologue copies
+      const long long stage = (c->nbc > 0) + L + ifp + 1 + 1 + ifl;
       // LU-SGS: prologue, residual, sweeps, norms, interface
-      long long lu = (c->nbc > 0) + L + ifl + 1 + 1 + 1 + ifl;
-      long long sub = c->method == BCMG_METHOD_LUSGS ? lu : 3 * stage + 1;
-      per = subiters * (sub + 1) + 1 + (c->precision == BCMG_PRECISION_SPLIT ? 1 : 0);
+      const long long lu = (c->nbc > 0) + L + ifp + 1 + 1 + 1 + ifl;
+      const long long sub = c->method == BCMG_METHOD_LUSGS ? lu : 3 * stage + 1;
+      per = subiters * (sub + 1) + (ifl - ifp) + 1 +
+            (c->precision == BCMG_PRECISION_SPLIT ? 1 : 0);
     }
     for (int s = 0; s < steps; ++s) CK(cudaGraphLaunch(c->graph, c->stream));
     c->launches = per * steps;
@@ -1319,10 +1379,12 @@ int bcmg_case_advance_converged(bcmg_case *c, int steps, int max_subiters, doubl
     // kernel launches of the replayed graphs: per sub-iteration as in
     // bcmg_case_advance, plus reset, check and shift
     const int L = (int)(c->ibm.level_off.size() > 0 ? c->ibm.level_off.size() - 1 : 0);
-    const long long ifl = c->ntasks > 0 ? 2 : 1;
-    const long long stage = (c->nbc > 0) + L + ifl + 1 + 1 + ifl;
+    const long long ifl = c->ntasks > 0 ? 2 : 1, ifp = c->ntasks_p > 0 ? 2 : 1;
+    // RK: the second and third stages run the reduced prologue copies
+    const long long stage = (c->nbc > 0) + L + 1 + 1 + ifl;
     const long long lu = (c->nbc > 0) + L + ifl + 1 + 1 + 1 + ifl;
-    const long long sub = (c->method == BCMG_METHOD_LUSGS ? lu : 3 * stage) + 1 + 1;
+    const long long sub =
+        (c->method == BCMG_METHOD_LUSGS ? lu : 3 * stage + ifl + 2 * ifp) + 1 + 1;
     long long tot = 0;
     for (int st = 0; st < steps; ++st) {
       int mx = 0;

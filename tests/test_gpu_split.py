@@ -52,6 +52,36 @@ def test_split_graph_replay_is_identical():
     assert np.array_equal(a, b) and np.array_equal(a1, b1) and np.array_equal(a2, b2)
 
 
+def _prologue_cases():
+    cs = dict(G.golden_cases())
+    cs["sphere_two_level"] = cases.sphere_ibm(n=8, coarse=2.0, box=((-2, 4), (-2, 2), (-2, 2)),
+                                              refine_box=((-2, 2), (-2, 2), (-2, 2)))
+    return cs
+
+
+@pytest.mark.parametrize("name", sorted(_prologue_cases()))
+@pytest.mark.parametrize("precision", [api.PRECISION_FP64, api.PRECISION_SPLIT])
+def test_reduced_prologue_copies_change_no_cell(name, precision):
+    """advance() runs only the face copies that can change a cell in the
+    interface call ahead of every stage but a step's first; single stage()
+    calls run all of them.  Two sub-iterations both ways end in the same
+    state, bit for bit."""
+    case = _prologue_cases()[name]
+    states = []
+    for stepped in (False, True):
+        ctx = api.CaseContext(case, precision=precision)
+        ctx.set_state(case.U, case.U, case.U)
+        if stepped:
+            for _ in range(2):
+                for RK in (1, 2, 3):
+                    ctx.stage(RK)
+        else:
+            ctx.advance(1, 2, use_graph=False)
+        states.append(ctx.get_state()[0])
+        ctx.close()
+    assert np.array_equal(states[0].view(np.uint64), states[1].view(np.uint64))
+
+
 def test_split_vortex_config1_size():
     """Config-1 size (4x4x4 cubes of 16^3, inviscid vortex, M 0.5): 3 dual-time
     steps of 10 sub-iterations, split vs FP64."""
