@@ -7,6 +7,8 @@
 // reference's results exactly.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "bcm_common.cuh"
 #include "bcm_kernels.h"
 
@@ -149,15 +151,17 @@ __global__ void __launch_bounds__(kHaloThreads) k_iface_faces(InterfaceArgs a) {
 }
 
 // Edge fill after all face copies (BCM_Interface.cpp:5640-5732): three
-// ordered phases per cube with CTA barriers in between.
-__global__ void __launch_bounds__(kHaloThreads) k_iface_edges(InterfaceArgs a) {
+// ordered phases per cube with CTA barriers in between.  The block has one
+// thread per item of the largest phase (20 (n + 2) values, up to 1,024), so
+// each phase is one round of loads and stores.
+__global__ void __launch_bounds__(1024) k_iface_edges(InterfaceArgs a) {
   const int n = a.n, S = n + 4, nx = n + 1, nyy = n + 2;
   const int c = blockIdx.x + 1;
   if (!case_active(a.bt, c)) return;
   double *U = a.U1_;
   auto Q = [&](int i, int j, int k) { return U + 5 * cell_index(S, c, i, j, k); };
   // Phase 1: i-edges, i = 2..nx.
-  for (int w = threadIdx.x; w < 4 * n * 5; w += kHaloThreads) {
+  for (int w = threadIdx.x; w < 4 * n * 5; w += blockDim.x) {
     const int v = w % 5, e = (w / 5) % 4, i = 2 + (w / 20);
     double *d;
     const double *x, *y;
@@ -169,7 +173,7 @@ __global__ void __launch_bounds__(kHaloThreads) k_iface_edges(InterfaceArgs a) {
   }
   __syncthreads();
   // Phase 2: j-edges, j = 1..nyy.
-  for (int w = threadIdx.x; w < 4 * (n + 2) * 5; w += kHaloThreads) {
+  for (int w = threadIdx.x; w < 4 * (n + 2) * 5; w += blockDim.x) {
     const int v = w % 5, e = (w / 5) % 4, j = 1 + (w / 20);
     double *d;
     const double *x, *y;
@@ -181,7 +185,7 @@ __global__ void __launch_bounds__(kHaloThreads) k_iface_edges(InterfaceArgs a) {
   }
   __syncthreads();
   // Phase 3: k-edges, k = 1..nyy.
-  for (int w = threadIdx.x; w < 4 * (n + 2) * 5; w += kHaloThreads) {
+  for (int w = threadIdx.x; w < 4 * (n + 2) * 5; w += blockDim.x) {
     const int v = w % 5, e = (w / 5) % 4, k = 1 + (w / 20);
     double *d;
     const double *x, *y;
@@ -200,25 +204,61 @@ cudaError_t launch_interface(const InterfaceArgs &a, int ncubes_total, cudaStrea
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
-  k_iface_edges<<<ncubes_total - 1, kHaloThreads, 0, s>>>(a);
+  const int et = std::min(1024, (20 * (a.n + 2) + 31) / 32 * 32);
+  k_iface_edges<<<ncubes_total - 1, et, 0, s>>>(a);
   return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
-// Boundary conditions (BCM_X/Y/Z_boundary_condition.cpp), one CTA per cube,
-// phases x -> y -> z with barriers: y reads x ghosts and z reads y ghosts of
-// the same cube (main.cpp:1161-1165 order).
+// Boundary conditions (BCM_X/Y/Z_boundary_condition.cpp), phases x -> y -> z
+// with barriers: y reads x ghosts and z reads y ghosts of the same cube
+// (main.cpp:1161-1165 order).  A cube's work is split into slabs of whole
+// i-planes (blockIdx.y), each of at least three planes: an x face and the
+// interior plane it reads lie in one slab, and a y or z item of plane i
+// reads only cells of plane i, so every dependency stays inside one CTA.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kHaloThreads) k_bc(BcArgs a) {
+constexpr int kBcThreads = 512, kBcBatch = 4;
+
+__global__ void __launch_bounds__(kBcThreads) k_bc(BcArgs a) {
   const int n = a.n, S = n + 4, nx = n + 1, nxx = n + 2, nxxx = n + 3;
   const int c = a.cubes[blockIdx.x];
   if (!case_active(a.bt, c)) return;
   const int m = a.masks[blockIdx.x];
+  const int T = (S + gridDim.y - 1) / gridDim.y, i0 = blockIdx.y * T, i1 = min(S, i0 + T);
   double *U = a.U1_;
   auto Q = [&](int i, int j, int k) { return U + 5 * cell_index(S, c, i, j, k); };
+  auto at = [&](int i, int j, int k) { return (size_t)5 * cell_index(S, c, i, j, k); };
+  // Zero-gradient and slip faces: both ghost layers take one interior value.
+  // No item of a phase reads a cell another item of that phase writes, so a
+  // thread issues the loads of kBcBatch items before their stores and the
+  // phase is a few memory round trips rather than one per item.
+  // index(w, src, dst1, dst0, negate) describes item w.
+  auto pairs = [&](int total, auto index) {
+    for (int w0 = threadIdx.x; w0 < total; w0 += kBcBatch * kBcThreads) {
+      double x[kBcBatch];
+      size_t d1[kBcBatch], d0[kBcBatch];
+#pragma unroll
+      for (int b = 0; b < kBcBatch; ++b) {
+        const int w = w0 + b * kBcThreads;
+        if (w < total) {
+          size_t src;
+          bool neg;
+          index(w, src, d1[b], d0[b], neg);
+          x[b] = U[src];
+          if (neg) x[b] = -x[b];
+        }
+      }
+#pragma unroll
+      for (int b = 0; b < kBcBatch; ++b)
+        if (w0 + b * kBcThreads < total) {
+          U[d1[b]] = x[b];
+          U[d0[b]] = x[b];
+        }
+    }
+  };
   if (a.axes & 1) {
-    if (m & 1) {  // x lower: inflow, rho and p from cell 2, u = Uin (:43-80)
-      for (int w = threadIdx.x; w < n * n; w += kHaloThreads) {
+    if ((m & 1) && i0 == 0) {  // x lower: inflow, rho and p from cell 2, u = Uin (:43-80)
+      for (int w = threadIdx.x; w < n * n; w += kBcThreads) {
         const int j = 2 + w / n, k = 2 + w % n;
         const double *q = Q(2, j, k);
         double rho = q[0];
@@ -233,53 +273,51 @@ __global__ void __launch_bounds__(kHaloThreads) k_bc(BcArgs a) {
         for (int v = 0; v < 5; ++v) { d1[v] = o[v]; d0[v] = o[v]; }
       }
     }
-    if (m & 2) {  // x upper: zero gradient (:85-118)
-      for (int w = threadIdx.x; w < n * n * 5; w += kHaloThreads) {
+    if ((m & 2) && i1 == S)  // x upper: zero gradient (:85-118)
+      pairs(n * n * 5, [&](int w, size_t &src, size_t &d1, size_t &d0, bool &neg) {
         const int v = w % 5, j = 2 + (w / 5) / n, k = 2 + (w / 5) % n;
-        double x = Q(nx, j, k)[v];
-        Q(nxx, j, k)[v] = x;
-        Q(nxxx, j, k)[v] = x;
-      }
-    }
+        src = at(nx, j, k) + v;
+        d1 = at(nxx, j, k) + v;
+        d0 = at(nxxx, j, k) + v;
+        neg = false;
+      });
     __syncthreads();
   }
-  if (a.axes & 2) {
-    for (int w = threadIdx.x; w < (n + 4) * n * 5; w += kHaloThreads) {
-      const int v = w % 5, i = (w / 5) / n, k = 2 + (w / 5) % n;
-      if (m & 4) {  // y lower (:36-59)
-        double x = Q(i, 2, k)[v];
-        Q(i, 1, k)[v] = x;
-        Q(i, 0, k)[v] = x;
-      }
-      if (m & 8) {  // y upper (:62-85)
-        double x = Q(i, nx, k)[v];
-        Q(i, nxx, k)[v] = x;
-        Q(i, nxxx, k)[v] = x;
-      }
-    }
-    __syncthreads();
+  if ((a.axes & 2) && (m & 12)) {
+    // y lower (:36-59) and upper (:62-85) over the slab's planes (x ghosts too)
+    const int per = (i1 - i0) * n * 5;
+    const int lo = (m & 4) ? 1 : 0, cnt = lo + ((m & 8) ? 1 : 0);
+    pairs(cnt * per, [&](int w, size_t &src, size_t &d1, size_t &d0, bool &neg) {
+      const bool lower = lo && w < per;
+      if (w >= per) w -= per;
+      const int v = w % 5, i = i0 + (w / 5) / n, k = 2 + (w / 5) % n;
+      src = at(i, lower ? 2 : nx, k) + v;
+      d1 = at(i, lower ? 1 : nxx, k) + v;
+      d0 = at(i, lower ? 0 : nxxx, k) + v;
+      neg = false;
+    });
   }
-  if (a.axes & 4) {
-    for (int w = threadIdx.x; w < (n + 4) * (n + 4) * 5; w += kHaloThreads) {
-      const int v = w % 5, i = (w / 5) / (n + 4), j = (w / 5) % (n + 4);
-      if (m & 16) {  // z lower: slip wall, rho*w negated (:42-65)
-        double x = Q(i, j, 2)[v];
-        if (v == 3) x = -x;
-        Q(i, j, 1)[v] = x;
-        Q(i, j, 0)[v] = x;
-      }
-      if (m & 32) {  // z upper (:70-92)
-        double x = Q(i, j, nx)[v];
-        Q(i, j, nxx)[v] = x;
-        Q(i, j, nxxx)[v] = x;
-      }
-    }
+  if (a.axes & 2) __syncthreads();
+  if ((a.axes & 4) && (m & 48)) {
+    // z lower: slip wall, rho*w negated (:42-65); z upper (:70-92)
+    const int per = (i1 - i0) * (n + 4) * 5;
+    const int lo = (m & 16) ? 1 : 0, cnt = lo + ((m & 32) ? 1 : 0);
+    pairs(cnt * per, [&](int w, size_t &src, size_t &d1, size_t &d0, bool &neg) {
+      const bool lower = lo && w < per;
+      if (w >= per) w -= per;
+      const int v = w % 5, i = i0 + (w / 5) / (n + 4), j = (w / 5) % (n + 4);
+      src = at(i, j, lower ? 2 : nx) + v;
+      d1 = at(i, j, lower ? 1 : nxx) + v;
+      d0 = at(i, j, lower ? 0 : nxxx) + v;
+      neg = lower && v == 3;
+    });
   }
 }
 
 cudaError_t launch_bc(const BcArgs &a, int ncubes, cudaStream_t s) {
   if (ncubes <= 0) return cudaSuccess;
-  k_bc<<<ncubes, kHaloThreads, 0, s>>>(a);
+  const int S = a.n + 4, slabs = std::max(1, std::min(4, S / 3));  // >= 3 planes each
+  k_bc<<<dim3(ncubes, slabs), kBcThreads, 0, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -346,13 +384,22 @@ __global__ void k_ghost(GhostArgs a, int count) {
   const bool self = (gi - i == 0 || gi - i == 1) && (gj - j == 0 || gj - j == 1) &&
                     (gk - k == 0 || gk - k == 1);
   if (self) {
-    // bit pattern (di,dj,dk) -> stencil slot in the 000,100,010,001,... order
-    const int slot_of[8] = {0, 1, 2, 4, 3, 5, 6, 7};
-    const int sl = slot_of[s];
+    // bit pattern (di,dj,dk) -> stencil slot in the 000,100,010,001,...
+    // order (patterns 3 and 4 swap); the slot's values picked by selects so
+    // the arrays stay in registers
+    const int sl = s == 3 ? 4 : (s == 4 ? 3 : s);
+    double wsl = 0, rsl = 0, psl = 0;
+#pragma unroll
+    for (int m = 0; m < 8; ++m)
+      if (m == sl) {
+        wsl = wl[m];
+        rsl = rh[m];
+        psl = Pp[m];
+      }
     double r2, p2;
-    if (wl[sl] > 0.9999) {
-      r2 = rh[sl];
-      p2 = Pp[sl];
+    if (wsl > 0.9999) {
+      r2 = rsl;
+      p2 = psl;
     } else {
       double ar = 0, ap = 0;
       bool first = true;
@@ -363,8 +410,8 @@ __global__ void k_ghost(GhostArgs a, int count) {
         if (first) { ar = tr; ap = tp; first = false; }
         else { ar = ar + tr; ap = ap + tp; }
       }
-      r2 = ar / (1 - wl[sl]) + rho0;
-      p2 = ap / (1 - wl[sl]) + P0;
+      r2 = ar / (1 - wsl) + rho0;
+      p2 = ap / (1 - wsl) + P0;
     }
     double su = 0, sv = 0, sw = 0;
     bool first = true;
@@ -374,7 +421,7 @@ __global__ void k_ghost(GhostArgs a, int count) {
       if (first) { su = wl[m] * Uu[m]; sv = wl[m] * Vv[m]; sw = wl[m] * Ww[m]; first = false; }
       else { su = su + wl[m] * Uu[m]; sv = sv + wl[m] * Vv[m]; sw = sw + wl[m] * Ww[m]; }
     }
-    double U2 = su / (2 - wl[sl]), V2 = sv / (2 - wl[sl]), W2 = sw / (2 - wl[sl]);
+    double U2 = su / (2 - wsl), V2 = sv / (2 - wsl), W2 = sw / (2 - wsl);
     double VV2 = U2 * U2 + V2 * V2 + W2 * W2;
     o[0] = r2;
     o[1] = r2 * U2;
