@@ -349,6 +349,12 @@ class CaseContext:
         t = _lib.Tuning(int(flux_tile), int(lusgs_threads))
         check(lib().bcmg_case_set_tuning(self.h, C.byref(t)))
 
+    def set_face_copies(self, in_flux=True):
+        """Split-precision RK stages: make the same-level face copies inside
+        the flux kernel (True, default) or in the interface call after it
+        (False).  Both give the same bits."""
+        check(lib().bcmg_case_set_face_copies(self.h, 1 if in_flux else 0))
+
     def autotune(self, reps=3):
         """Times the launch-shape candidates on this context's state, applies the
         fastest and returns the choice with the measured milliseconds."""

@@ -208,6 +208,16 @@ struct bcmg_case {
   int *task_cube_p = nullptr;
   FaceTask *tasks_p = nullptr;
   int ntasks_p = 0;
+  // Split-precision RK stages copy same-level faces inside the flux kernel
+  // (push table, see FluxSplitArgs::push); their closing interface call then
+  // runs only the level-jump tasks (and the edge fill).  push == nullptr:
+  // the table could not be formed (a face with two same-level sources).
+  int *push = nullptr;
+  bool push_on = true;  // bcmg_case_set_face_copies
+  const int *push_table() const { return push_on ? push : nullptr; }
+  int *task_cube_q = nullptr;
+  FaceTask *tasks_q = nullptr;
+  int ntasks_q = 0;
   int *bc_cubes = nullptr, *bc_masks = nullptr;
   int nbc = 0;
   Ibm ibm;  // minus entries then plus entries, one combined schedule
@@ -300,7 +310,7 @@ struct bcmg_case {
     dfree(U1_); dfree(U1); dfree(U1q); dfree(U1p1); dfree(U1p2); dfree(Rku1); dfree(Residual1);
     dfree(M); dfree(D2); dfree(inv_dx);
     dfree(FWS); dfree(cube_size); dfree(task_cube); dfree(tasks); dfree(task_cube_p);
-    dfree(tasks_p); dfree(bc_cubes);
+    dfree(tasks_p); dfree(push); dfree(task_cube_q); dfree(tasks_q); dfree(bc_cubes);
     dfree(bc_masks); dfree(partials); dfree(er); dfree(emax);
     dfree(cases); dfree(cube_case); dfree(rk_blk); dfree(case_blk_rk); dfree(case_blk_flux);
     dfree(case_blk_cube);
@@ -378,6 +388,7 @@ int case_flux(bcmg_case *c, int RK) {
     sa.partials = c->partials;
     sa.Residual1 = c->Residual1;
     sa.bt = c->bt();
+    sa.push = RK >= 1 ? c->push_table() : nullptr;
     CK(launch_flux_split(sa, c->ncube - 1, c->stream));
   } else {
     CK(launch_flux_fp64(a, c->ncube - 1, c->stream));
@@ -387,12 +398,24 @@ int case_flux(bcmg_case *c, int RK) {
   return BCMG_OK;
 }
 
-int case_interface(bcmg_case *c, bool full = true) {
+// Which face tasks an interface call runs.
+enum IfaceList { kIfaceFull, kIfacePrologue, kIfaceClosing };
+
+int case_interface(bcmg_case *c, IfaceList list = kIfaceFull) {
   InterfaceArgs ia;
   ia.n = c->ph.n;
-  ia.ntasks = full ? c->ntasks : c->ntasks_p;
-  ia.task_cube = full ? c->task_cube : c->task_cube_p;
-  ia.tasks = full ? c->tasks : c->tasks_p;
+  ia.ntasks = c->ntasks;
+  ia.task_cube = c->task_cube;
+  ia.tasks = c->tasks;
+  if (list == kIfacePrologue) {
+    ia.ntasks = c->ntasks_p;
+    ia.task_cube = c->task_cube_p;
+    ia.tasks = c->tasks_p;
+  } else if (list == kIfaceClosing) {
+    ia.ntasks = c->ntasks_q;
+    ia.task_cube = c->task_cube_q;
+    ia.tasks = c->tasks_q;
+  }
   ia.U1_ = c->U1_;
   ia.bt = c->bt();
   CK(launch_interface(ia, c->ncube, c->stream));
@@ -420,7 +443,7 @@ int case_prologue(bcmg_case *c, bool full = true) {
   if ((r = ibm_run(c->ibm, c->ph.n, c->ph.rho0, c->ph.P0, c->U1_, c->stream, &c->launches,
                    c->bt())))
     return r;
-  return case_interface(c, full);
+  return case_interface(c, full ? kIfaceFull : kIfacePrologue);
 }
 
 // One LU-SGS sub-iteration: prologue, residual, sweeps with the update and
@@ -497,7 +520,8 @@ int case_stage(bcmg_case *c, int RK, bool full = true) {
         CK(launch_norms(c->ph, c->partials, nb, c->er, c->stream, c->bt().active));
       ++c->launches;
     }
-    return case_interface(c);
+    // the flux kernel made the same-level copies of the updated cells
+    return case_interface(c, c->push_table() ? kIfaceClosing : kIfaceFull);
   }
   RkArgs k;
   k.ph = c->ph;
@@ -941,6 +965,41 @@ int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out)
                         cudaMemcpyHostToDevice), "copy")))
       return fail(BCMG_ERR_CUDA);
   }
+  // Push table of the split-precision flux kernel and the closing list that
+  // goes with it (level-jump tasks only).
+  if (d->precision == BCMG_PRECISION_SPLIT) {
+    std::vector<int> push(6 * (size_t)d->ncube, 0);
+    bool ok_push = true;
+    std::vector<FaceTask> tq;
+    std::vector<int> cq;
+    for (size_t t = 0; t < tasks.size(); ++t) {
+      const FaceTask &f = tasks[t];
+      if (f.kind != 0) {
+        tq.push_back(f);
+        cq.push_back(task_cube[t]);
+        continue;
+      }
+      // side 1 (high ghosts) copies the source's layers 2, 3: slot 0
+      int &slot = push[6 * (size_t)f.src + 2 * f.axis + (f.side == 1 ? 0 : 1)];
+      if (slot != 0 && slot != task_cube[t]) ok_push = false;
+      slot = task_cube[t];
+    }
+    if (ok_push) {
+      c->ntasks_q = (int)tq.size();
+      if (!(ck(dalloc(&c->push, push.size()), "alloc") &&
+            ck(cudaMemcpy(c->push, push.data(), sizeof(int) * push.size(),
+                          cudaMemcpyHostToDevice), "copy")))
+        return fail(BCMG_ERR_CUDA);
+      if (!tq.empty() &&
+          !(ck(dalloc(&c->tasks_q, tq.size()), "alloc") &&
+            ck(dalloc(&c->task_cube_q, cq.size()), "alloc") &&
+            ck(cudaMemcpy(c->tasks_q, tq.data(), sizeof(FaceTask) * tq.size(),
+                          cudaMemcpyHostToDevice), "copy") &&
+            ck(cudaMemcpy(c->task_cube_q, cq.data(), sizeof(int) * cq.size(),
+                          cudaMemcpyHostToDevice), "copy")))
+        return fail(BCMG_ERR_CUDA);
+    }
+  }
   *out = c;
   return BCMG_OK;
 }
@@ -1037,8 +1096,13 @@ int bcmg_case_advance(bcmg_case *c, int steps, int subiters, int use_graph, doub
       // bc, IBM levels, interface (faces + edges), [mirror], flux, [rk],
       // interface (faces + edges)
       const long long ifl = c->ntasks > 0 ? 2 : 1, ifp = c->ntasks_p > 0 ? 2 : 1;
+      // split RK stages close with the level-jump list when the flux kernel
+      // made the same-level copies
+      const long long ifc =
+          c->push_table() && c->precision == BCMG_PRECISION_SPLIT ? (c->ntasks_q > 0 ? 2 : 1)
+                                                                   : ifl;
       // stages after the first of a step run the reduced prologue copies
-      const long long stage = (c->nbc > 0) + L + ifp + 1 + 1 + ifl;
+      const long long stage = (c->nbc > 0) + L + ifp + 1 + 1 + ifc;
       // LU-SGS: prologue, residual, sweeps, norms, interface
       const long long lu = (c->nbc > 0) + L + ifp + 1 + 1 + 1 + ifl;
       const long long sub = c->method == BCMG_METHOD_LUSGS ? lu : 3 * stage + 1;
@@ -1380,8 +1444,11 @@ int bcmg_case_advance_converged(bcmg_case *c, int steps, int max_subiters, doubl
     // bcmg_case_advance, plus reset, check and shift
     const int L = (int)(c->ibm.level_off.size() > 0 ? c->ibm.level_off.size() - 1 : 0);
     const long long ifl = c->ntasks > 0 ? 2 : 1, ifp = c->ntasks_p > 0 ? 2 : 1;
+    const long long ifc =
+        c->push_table() && c->precision == BCMG_PRECISION_SPLIT ? (c->ntasks_q > 0 ? 2 : 1)
+                                                                   : ifl;
     // RK: the second and third stages run the reduced prologue copies
-    const long long stage = (c->nbc > 0) + L + 1 + 1 + ifl;
+    const long long stage = (c->nbc > 0) + L + 1 + 1 + ifc;
     const long long lu = (c->nbc > 0) + L + ifl + 1 + 1 + 1 + ifl;
     const long long sub =
         (c->method == BCMG_METHOD_LUSGS ? lu : 3 * stage + ifl + 2 * ifp) + 1 + 1;
@@ -1587,6 +1654,18 @@ int bcmg_case_set_tuning(bcmg_case *c, const bcmg_tuning *t) {
     CK(cudaMemcpy(c->case_blk_flux, cbf.data(), sizeof(int) * cbf.size(), cudaMemcpyHostToDevice));
   }
   if (c->graph) cudaGraphExecDestroy(c->graph);  // captured steps hold the old shapes
+  c->graph = nullptr;
+  c->graph_subiters = -1;
+  if (c->cgraph) cudaGraphExecDestroy(c->cgraph);
+  c->cgraph = nullptr;
+  return BCMG_OK;
+}
+
+int bcmg_case_set_face_copies(bcmg_case *c, int in_flux) {
+  clear_err();
+  if (!c) { set_err("null context"); return BCMG_ERR_ARG; }
+  c->push_on = in_flux != 0;
+  if (c->graph) cudaGraphExecDestroy(c->graph);  // captured steps hold the old lists
   c->graph = nullptr;
   c->graph_subiters = -1;
   if (c->cgraph) cudaGraphExecDestroy(c->cgraph);

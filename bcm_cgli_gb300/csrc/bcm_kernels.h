@@ -79,6 +79,12 @@ struct FluxSplitArgs {
   double *partials;    // [blocks][7] norm/force partial sums (stage 3)
   double *Residual1;
   Batch bt;
+  // [ncube][6] (stages 1..3, optional): push[6c + 2 axis + 0] is the cube
+  // whose high ghost layers copy cube c's low interior layers (2, 3) along
+  // axis at the same level, push[6c + 2 axis + 1] the cube whose low ghost
+  // layers copy its high layers (n, n+1); 0 where none.  Updated fluid
+  // cells in those layers write their new value there too.
+  const int *push = nullptr;
 };
 // Tile edge a flux launch uses (tile: 0 default, else 8 or 4 when it divides n).
 int flux_tile(int n, int tile);

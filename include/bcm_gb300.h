@@ -274,6 +274,14 @@ typedef struct bcmg_tuning {
 int bcmg_case_set_tuning(bcmg_case *c, const bcmg_tuning *t);
 int bcmg_case_autotune(bcmg_case *c, int reps, bcmg_tuning *out);
 
+/* Where split-precision RK stages make the interface's same-level face
+ * copies of the updated cells: in_flux = 1 (default) inside the flux kernel,
+ * each updated cell next to a same-level face writing its new value into
+ * the neighbour's ghost layer, so the interface call after the stage runs
+ * only the level-jump tasks and the edge fill; 0: in that interface call.
+ * Both give the same bits.  No effect on the FP64 path or LU-SGS. */
+int bcmg_case_set_face_copies(bcmg_case *c, int in_flux);
+
 /* Waits for all work of the context. */
 int bcmg_case_sync(bcmg_case *c);
 
