@@ -919,42 +919,18 @@ int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out)
     int r = ibm_upload(c->ibm, nm + np, w.data(), gc.data(), ip.data(), d->n, d->ncube, s);
     if (r) return fail(r);
   }
-  // Reduced face-task list of the prologue interface calls.  Per cube, bits
-  // 0..5: its ghost face (axis, side) is written by the boundary fill or
-  // holds an IBM ghost cell; bits 6..11: the two interior layers that face
-  // (axis, side) of a neighbour copies from hold an IBM ghost cell.
+  // Reduced face-task list of the prologue interface calls.
   {
-    const int n = d->n;
-    std::vector<uint16_t> hot((size_t)d->ncube, 0);
-    for (size_t q = 0; q < bcc.size(); ++q) hot[bcc[q]] |= (uint16_t)(bcm[q] & 63);
-    auto mark = [&](const int *G, int cnt) {
-      for (int e = 0; e < cnt; ++e) {
-        const int g = G[1 + 4 * e];
-        const int x[3] = {G[2 + 4 * e], G[3 + 4 * e], G[4 + 4 * e]};
-        if (g <= 0 || g >= d->ncube) continue;
-        for (int ax = 0; ax < 3; ++ax) {
-          const int a = x[(ax + 1) % 3], b = x[(ax + 2) % 3];
-          if (a < 2 || a > n + 1 || b < 2 || b > n + 1) continue;
-          const int l = x[ax];
-          if (l == 0 || l == 1) hot[g] |= (uint16_t)(1 << (2 * ax));
-          if (l == n + 2 || l == n + 3) hot[g] |= (uint16_t)(1 << (2 * ax + 1));
-          if (l == n || l == n + 1) hot[g] |= (uint16_t)(1 << (6 + 2 * ax));
-          if (l == 2 || l == 3) hot[g] |= (uint16_t)(1 << (6 + 2 * ax + 1));
-        }
-      }
-    };
-    if (nm) mark(d->gc_minus, nm);
-    if (np) mark(d->gc_plus, np);
+    std::vector<char> keep;
+    prologue_task_mask(d->n, d->ncube, tasks, task_cube, bcc, bcm, d->gc_minus, nm, d->gc_plus,
+                       np, keep);
     std::vector<FaceTask> tp;
     std::vector<int> cp;
-    for (size_t t = 0; t < tasks.size(); ++t) {
-      const FaceTask &f = tasks[t];
-      const int face = 2 * f.axis + f.side;
-      if (f.kind != 0 || (hot[task_cube[t]] >> face & 1) || (hot[f.src] >> (6 + face) & 1)) {
-        tp.push_back(f);
+    for (size_t t = 0; t < tasks.size(); ++t)
+      if (keep[t]) {
+        tp.push_back(tasks[t]);
         cp.push_back(task_cube[t]);
       }
-    }
     c->ntasks_p = (int)tp.size();
     if (!tp.empty() &&
         !(ck(dalloc(&c->tasks_p, tp.size()), "alloc") &&
@@ -968,22 +944,15 @@ int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out)
   // Push table of the split-precision flux kernel and the closing list that
   // goes with it (level-jump tasks only).
   if (d->precision == BCMG_PRECISION_SPLIT) {
-    std::vector<int> push(6 * (size_t)d->ncube, 0);
-    bool ok_push = true;
+    std::vector<int> push;
+    const bool ok_push = build_push_table(d->ncube, tasks, task_cube, push);
     std::vector<FaceTask> tq;
     std::vector<int> cq;
-    for (size_t t = 0; t < tasks.size(); ++t) {
-      const FaceTask &f = tasks[t];
-      if (f.kind != 0) {
-        tq.push_back(f);
+    for (size_t t = 0; t < tasks.size(); ++t)
+      if (tasks[t].kind != 0) {
+        tq.push_back(tasks[t]);
         cq.push_back(task_cube[t]);
-        continue;
       }
-      // side 1 (high ghosts) copies the source's layers 2, 3: slot 0
-      int &slot = push[6 * (size_t)f.src + 2 * f.axis + (f.side == 1 ? 0 : 1)];
-      if (slot != 0 && slot != task_cube[t]) ok_push = false;
-      slot = task_cube[t];
-    }
     if (ok_push) {
       c->ntasks_q = (int)tq.size();
       if (!(ck(dalloc(&c->push, push.size()), "alloc") &&

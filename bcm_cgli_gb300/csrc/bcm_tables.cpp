@@ -5,6 +5,7 @@
 #include "bcm_tables.h"
 
 #include <algorithm>
+#include <cstdint>
 #include <cstdio>
 #include <unordered_map>
 
@@ -272,6 +273,54 @@ bool build_ibm_levels(int nbc, const int *GC, const int *IP, int n, int ncube,
   return true;
 }
 
+void prologue_task_mask(int n, int ncube, const std::vector<FaceTask> &tasks,
+                        const std::vector<int> &task_cube, const std::vector<int> &bc_cubes,
+                        const std::vector<int> &bc_masks, const int *gc_minus, int nminus,
+                        const int *gc_plus, int nplus, std::vector<char> &keep) {
+  // Per cube, bits 0..5: ghost face (axis, side) written by the boundary
+  // fill or holding an IBM ghost cell; bits 6..11: the interior layers a
+  // neighbour's face (axis, side) copies from hold an IBM ghost cell.
+  std::vector<uint16_t> hot((size_t)std::max(ncube, 0), 0);
+  for (size_t q = 0; q < bc_cubes.size(); ++q) hot[bc_cubes[q]] |= (uint16_t)(bc_masks[q] & 63);
+  auto mark = [&](const int *G, int cnt) {
+    for (int e = 0; e < cnt; ++e) {
+      const int g = G[1 + 4 * e];
+      const int x[3] = {G[2 + 4 * e], G[3 + 4 * e], G[4 + 4 * e]};
+      if (g <= 0 || g >= ncube) continue;
+      for (int ax = 0; ax < 3; ++ax) {
+        const int a = x[(ax + 1) % 3], b = x[(ax + 2) % 3];
+        if (a < 2 || a > n + 1 || b < 2 || b > n + 1) continue;
+        const int l = x[ax];
+        if (l == 0 || l == 1) hot[g] |= (uint16_t)(1 << (2 * ax));
+        if (l == n + 2 || l == n + 3) hot[g] |= (uint16_t)(1 << (2 * ax + 1));
+        if (l == n || l == n + 1) hot[g] |= (uint16_t)(1 << (6 + 2 * ax));
+        if (l == 2 || l == 3) hot[g] |= (uint16_t)(1 << (6 + 2 * ax + 1));
+      }
+    }
+  };
+  if (gc_minus && nminus > 0) mark(gc_minus, nminus);
+  if (gc_plus && nplus > 0) mark(gc_plus, nplus);
+  keep.assign(tasks.size(), 0);
+  for (size_t t = 0; t < tasks.size(); ++t) {
+    const FaceTask &f = tasks[t];
+    const int face = 2 * f.axis + f.side;
+    keep[t] = f.kind != 0 || (hot[task_cube[t]] >> face & 1) || (hot[f.src] >> (6 + face) & 1);
+  }
+}
+
+bool build_push_table(int ncube, const std::vector<FaceTask> &tasks,
+                      const std::vector<int> &task_cube, std::vector<int> &push) {
+  push.assign(6 * (size_t)std::max(ncube, 0), 0);
+  for (size_t t = 0; t < tasks.size(); ++t) {
+    const FaceTask &f = tasks[t];
+    if (f.kind != 0) continue;
+    int &slot = push[6 * (size_t)f.src + 2 * f.axis + (f.side == 1 ? 0 : 1)];
+    if (slot != 0 && slot != task_cube[t]) return false;
+    slot = task_cube[t];
+  }
+  return true;
+}
+
 }  // namespace bcmg
 
 // ---------------------------------------------------------------------------
@@ -309,4 +358,30 @@ extern "C" int bcmg_interface_tasks(int ncube, const int *adj_number, const int 
       task_words[5 * t + 4] = tasks[t].slot;
     }
   return (int)tasks.size();
+}
+
+extern "C" int bcmg_interface_plan(int n, int ncube, const int *adj_number, const int *csl,
+                                   const int *const bc_lists[6], const int bc_counts[6],
+                                   const int *gc_minus, int nminus, const int *gc_plus, int nplus,
+                                   int *keep_prologue, int *push, int max_tasks) {
+  std::vector<int> off;
+  std::vector<bcmg::FaceTask> tasks;
+  std::string err;
+  if (ncube < 2 || n < 1 || !adj_number || !csl || !bc_lists || !bc_counts) return -1;
+  if (!bcmg::build_interface_tasks(ncube, adj_number, csl, off, tasks, err)) return -1;
+  std::vector<int> bcc, bcm;
+  if (!bcmg::build_bc_entries(ncube, bc_lists, bc_counts, bcc, bcm, err)) return -1;
+  if ((int)tasks.size() > max_tasks) return -2;
+  std::vector<int> task_cube(tasks.size());
+  for (int c = 1; c < ncube; ++c)
+    for (int t = off[c]; t < off[c + 1]; ++t) task_cube[t] = c;
+  std::vector<char> keep;
+  bcmg::prologue_task_mask(n, ncube, tasks, task_cube, bcc, bcm, gc_minus, nminus, gc_plus, nplus,
+                           keep);
+  if (keep_prologue)
+    for (size_t t = 0; t < keep.size(); ++t) keep_prologue[t] = keep[t];
+  std::vector<int> tbl;
+  const bool ok = bcmg::build_push_table(ncube, tasks, task_cube, tbl);
+  if (push) std::copy(tbl.begin(), tbl.end(), push);
+  return ok ? (int)tasks.size() : -3;
 }

@@ -20,5 +20,22 @@ bool build_bc_entries(int ncube, const int *const lists[6], const int counts[6],
                       std::vector<int> &cubes, std::vector<int> &masks, std::string &err);
 bool build_ibm_levels(int nbc, const int *GC, const int *IP, int n, int ncube,
                       std::vector<int> &order, std::vector<int> &level_off, std::string &err);
+// Which face tasks the interface call ahead of a stage must repeat right
+// after the previous stage's closing call: keep[t] = 1 for level-jump tasks,
+// for faces the boundary fill writes (bc cubes/masks as build_bc_entries
+// makes them) and for faces whose destination ghost layers or source
+// interior layers hold an IBM ghost cell (GC tables 1-based, 4 ints per
+// entry: cube, i, j, k).
+void prologue_task_mask(int n, int ncube, const std::vector<FaceTask> &tasks,
+                        const std::vector<int> &task_cube, const std::vector<int> &bc_cubes,
+                        const std::vector<int> &bc_masks, const int *gc_minus, int nminus,
+                        const int *gc_plus, int nplus, std::vector<char> &keep);
+// Same-level push table of the split flux kernel (FluxSplitArgs::push):
+// push[6 src + 2 axis + 0] = destination of the task copying src's layers
+// 2, 3 (its side 1), push[6 src + 2 axis + 1] = destination of the task
+// copying layers n, n+1 (side 0).  False when one slot would need two
+// destinations.
+bool build_push_table(int ncube, const std::vector<FaceTask> &tasks,
+                      const std::vector<int> &task_cube, std::vector<int> &push);
 
 }  // namespace bcmg

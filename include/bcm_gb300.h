@@ -401,6 +401,23 @@ int bcmg_ibm_schedule(int nbc, const int *GCindex, const int *IPsur, int n, int 
 int bcmg_interface_tasks(int ncube, const int *adj_number, const int *csl, int *task_off,
                          int *task_words, int max_tasks);
 
+/* The interface plan of a resident context, for the tasks of
+ * bcmg_interface_tasks (same order).  keep_prologue[t] = 1 when the
+ * interface call ahead of a stage must repeat task t right after the
+ * previous stage's closing call (level jumps; faces the boundary fill
+ * writes, from the 0-based boundary lists as in bcmg_case_desc; faces whose
+ * ghost or source layers hold an IBM ghost cell, from the 1-based GC
+ * tables).  push[6 ncube]: the split flux kernel's same-level push table
+ * (push[6 c + 2 axis + 0]: cube whose high ghost layers copy cube c's
+ * layers 2, 3; + 1: cube whose low ghost layers copy layers n, n+1; 0 where
+ * none).  Returns the task count, -1 for invalid input, -2 if max_tasks is
+ * too small, -3 if a push slot would need two destinations (the context
+ * then keeps the copies in the interface call). */
+int bcmg_interface_plan(int n, int ncube, const int *adj_number, const int *csl,
+                        const int *const bc_lists[6], const int bc_counts[6],
+                        const int *gc_minus, int nminus, const int *gc_plus, int nplus,
+                        int *keep_prologue, int *push, int max_tasks);
+
 #ifdef __cplusplus
 }
 #endif

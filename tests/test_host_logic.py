@@ -156,6 +156,97 @@ def test_level_jump_beyond_2_to_1_is_rejected():
     assert nt == -1
 
 
+def _plan(case):
+    """bcmg_interface_plan of a case: (tasks [t, 5], destination cube per
+    task, keep_prologue, push table [ncube, 6], return code)."""
+    adj = np.ascontiguousarray(case.adj, np.int32)
+    csl = np.ascontiguousarray(case.csl, np.int32)
+    cap = 24 * case.ncube
+    off = np.zeros(case.ncube + 1, np.int32)
+    words = np.zeros(5 * cap, np.int32)
+    nt = lib().bcmg_interface_tasks(case.ncube, adj, csl, off, words, cap)
+    assert nt >= 0
+    lists = [np.ascontiguousarray(a, np.int32) for a in case.bc_lists()]
+    ptrs = (C.c_void_p * 6)(*[a.ctypes.data if len(a) else None for a in lists])
+    counts = (C.c_int * 6)(*[len(a) for a in lists])
+    gcs = []
+    for t in (case.ibm_minus, case.ibm_plus):
+        g = None if t is None else np.ascontiguousarray(t[1], np.int32)
+        gcs.append((g, 0 if g is None else (len(g) - 1) // 4))
+    keep = np.zeros(max(nt, 1), np.int32)
+    push = np.zeros(6 * case.ncube, np.int32)
+    r = lib().bcmg_interface_plan(case.n, case.ncube, adj, csl, C.cast(ptrs, C.c_void_p),
+                                  C.cast(counts, C.c_void_p),
+                                  None if gcs[0][0] is None else gcs[0][0].ctypes.data, gcs[0][1],
+                                  None if gcs[1][0] is None else gcs[1][0].ctypes.data, gcs[1][1],
+                                  keep, push, cap)
+    dst = np.repeat(np.arange(case.ncube), np.diff(off))
+    return words[:5 * nt].reshape(-1, 5), dst, keep[:nt], push.reshape(case.ncube, 6), r
+
+
+def _prologue_rule(case, tasks, dst):
+    """Restatement of the opening-call rule: a level jump, a face the
+    boundary fill writes, or a face whose ghost layers (destination) or
+    copied interior layers (source) hold an IBM ghost cell."""
+    n = case.n
+    mask = np.zeros(case.ncube, np.int64)
+    for bit, lst in enumerate(case.bc_lists()):
+        for c in lst:
+            mask[c] |= 1 << bit
+    gc = set()
+    for t in (case.ibm_minus, case.ibm_plus):
+        if t is not None:
+            g = np.asarray(t[1][1:]).reshape(-1, 4)
+            gc |= {tuple(int(v) for v in row) for row in g}
+
+    def holds(cube, ax, layers):
+        for (g, *x) in gc:
+            if g == cube and x[ax] in layers and all(
+                    2 <= x[a] <= n + 1 for a in range(3) if a != ax):
+                return True
+        return False
+
+    out = []
+    for (src, ax, side, kind, slot), c in zip(tasks, dst):
+        dl = (0, 1) if side == 0 else (n + 2, n + 3)
+        sl = (n, n + 1) if side == 0 else (2, 3)
+        out.append(int(kind != 0 or (mask[c] >> (2 * ax + side)) & 1 or holds(c, ax, dl)
+                       or holds(src, ax, sl)))
+    return np.array(out, np.int32)
+
+
+def test_prologue_plan_periodic_box_keeps_box_faces():
+    """Periodic 4x4x4 box (the boundary fill runs on box faces before the
+    periodic copy overwrites it): the opening call keeps exactly the tasks
+    whose destination face lies on the box boundary, 96 of 384."""
+    case = cases.taylor_green(ncx=4, n=4)
+    tasks, dst, keep, push, r = _plan(case)
+    assert r == len(tasks) == 384
+    assert keep.sum() == 96
+    assert np.array_equal(keep, _prologue_rule(case, tasks, dst))
+
+
+@pytest.mark.parametrize("make", [
+    lambda: cases.random_two_level_case(seed=6, n=8, periodic=False),
+    lambda: cases.random_two_level_case(seed=1, n=4),
+    lambda: cases.random_case(seed=3, n=8, periodic=True),
+    lambda: cases.sphere_ibm(n=8, coarse=2.0, box=((-2, 4), (-2, 2), (-2, 2)),
+                             refine_box=((-2, 2), (-2, 2), (-2, 2)))])
+def test_prologue_plan_matches_rule(make):
+    """Level jumps, boundary faces and faces touching IBM ghost cells are
+    kept, nothing else; the push table has one slot per same-level task,
+    pointing at its destination, and none for level jumps."""
+    case = make()
+    tasks, dst, keep, push, r = _plan(case)
+    assert r == len(tasks)
+    assert np.array_equal(keep, _prologue_rule(case, tasks, dst))
+    assert keep.sum() < len(tasks)
+    same = tasks[:, 3] == 0
+    assert np.count_nonzero(push) == np.count_nonzero(same)
+    for (src, ax, side, kind, slot), c in zip(tasks[same], dst[same]):
+        assert push[src, 2 * ax + (0 if side == 1 else 1)] == c
+
+
 @pytest.mark.skipif(not O.reference_available(), reason="reference sources not on this host")
 def test_reference_shim_compiles_against_main_h(tmp_path):
     """The C++ shim provides exactly the signatures the reference's main.h
