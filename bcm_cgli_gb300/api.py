@@ -350,9 +350,9 @@ class CaseContext:
         check(lib().bcmg_case_set_tuning(self.h, C.byref(t)))
 
     def set_face_copies(self, in_flux=True):
-        """Split-precision RK stages: make the same-level face copies inside
-        the flux kernel (True, default) or in the interface call after it
-        (False).  Both give the same bits."""
+        """Split-precision RK stages and LU-SGS sweeps: make the same-level
+        face copies inside the updating kernel (True, default) or in the
+        interface call after it (False).  Both give the same bits."""
         check(lib().bcmg_case_set_face_copies(self.h, 1 if in_flux else 0))
 
     def autotune(self, reps=3):

@@ -468,6 +468,7 @@ LusgsSplitArgs lusgs_split_args(bcmg_case *c) {
   l.partials = c->partials;
   l.bt = c->bt();
   l.threads = c->lu_threads;
+  l.push = c->push_table();
   return l;
 }
 
@@ -501,7 +502,10 @@ int case_lusgs(bcmg_case *c, bool full = true) {
   else
     CK(launch_norms(c->ph, c->partials, c->ncube - 1, c->er, c->stream, c->bt().active));
   ++c->launches;
-  return case_interface(c);
+  // the split sweep made the same-level copies of the updated cells
+  return case_interface(c, c->precision == BCMG_PRECISION_SPLIT && c->push_table()
+                               ? kIfaceClosing
+                               : kIfaceFull);
 }
 
 int case_stage(bcmg_case *c, int RK, bool full = true) {
@@ -1073,7 +1077,7 @@ int bcmg_case_advance(bcmg_case *c, int steps, int subiters, int use_graph, doub
       // stages after the first of a step run the reduced prologue copies
       const long long stage = (c->nbc > 0) + L + ifp + 1 + 1 + ifc;
       // LU-SGS: prologue, residual, sweeps, norms, interface
-      const long long lu = (c->nbc > 0) + L + ifp + 1 + 1 + 1 + ifl;
+      const long long lu = (c->nbc > 0) + L + ifp + 1 + 1 + 1 + ifc;
       const long long sub = c->method == BCMG_METHOD_LUSGS ? lu : 3 * stage + 1;
       per = subiters * (sub + 1) + (ifl - ifp) + 1 +
             (c->precision == BCMG_PRECISION_SPLIT ? 1 : 0);
@@ -1418,7 +1422,7 @@ int bcmg_case_advance_converged(bcmg_case *c, int steps, int max_subiters, doubl
                                                                    : ifl;
     // RK: the second and third stages run the reduced prologue copies
     const long long stage = (c->nbc > 0) + L + 1 + 1 + ifc;
-    const long long lu = (c->nbc > 0) + L + ifl + 1 + 1 + 1 + ifl;
+    const long long lu = (c->nbc > 0) + L + ifl + 1 + 1 + 1 + ifc;
     const long long sub =
         (c->method == BCMG_METHOD_LUSGS ? lu : 3 * stage + ifl + 2 * ifp) + 1 + 1;
     long long tot = 0;

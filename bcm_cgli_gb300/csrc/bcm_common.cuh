@@ -36,6 +36,35 @@ __host__ __device__ inline size_t cell_index(int S, int c, int i, int j, int k) 
   return ((((size_t)c * S + i) * S + j) * S + k);
 }
 
+// Same-level interface copy of one updated interior cell (ci, cj, ck) of
+// `cube`, made by the kernel that updates it (BCM_Interface.cpp:1745-1783
+// copies exactly this after the update): a cell in layers 2, 3 (slot 0) or
+// n, n+1 (slot 1) along an axis writes its new value un[5] into ghost
+// layers n+2, n+3 or 0, 1 of the cube push[6 cube + 2 axis + slot] (0:
+// none).  Safe only while no other thread reads the FP64 state's ghost
+// layers.
+__device__ __forceinline__ void push_same_level(double *U, const int *push, int n, int cube,
+                                                int ci, int cj, int ck, const double *un) {
+  const int cg[3] = {ci, cj, ck};
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) {
+    const int x = cg[ax];
+    const int slot = x <= 3 ? 0 : (x >= n ? 1 : -1);
+    if (slot < 0) continue;
+#ifdef __CUDA_ARCH__
+    const int d = __ldg(push + 6 * cube + 2 * ax + slot);
+#else
+    const int d = push[6 * cube + 2 * ax + slot];
+#endif
+    if (d <= 0) continue;
+    int dc[3] = {ci, cj, ck};
+    dc[ax] = slot == 0 ? x + n : x - n;
+    double *g = U + 5 * cell_index(n + 4, d, dc[0], dc[1], dc[2]);
+#pragma unroll
+    for (int r = 0; r < 5; ++r) g[r] = un[r];
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Preconditioned Roe-type face flux (BCM_Flux_XYZ_Viscous_Runge_kutta.cpp
 // :606-693 z, :1057-1146 x, :1503-1594 y).  AX is the face normal.

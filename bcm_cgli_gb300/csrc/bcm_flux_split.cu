@@ -705,30 +705,10 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
       un[r] = xq[r] + to_double_exact(dq[r]);
       u[r] = un[r];
     }
-    // Same-level interface copy of this cell, done here: a cell in the two
-    // interior layers next to a face with a same-level neighbour writes its
-    // new value into that neighbour's ghost layer (BCM_Interface.cpp
-    // :1745-1783 copies exactly this after the update).  No CTA reads the
+    // Same-level interface copy of this cell, done here.  No CTA reads the
     // FP64 state of another cell during the stage, so the write races with
     // nothing.
-    if (a.push) {
-      const int cg[3] = {bi + mi, bj + mj, bk + mk};
-#pragma unroll
-      for (int ax = 0; ax < 3; ++ax) {
-        const int x = cg[ax];
-        const int slot = x <= 3 ? 0 : (x >= n ? 1 : -1);
-        if (slot >= 0) {
-          const int dcube = __ldg(a.push + 6 * cube + 2 * ax + slot);
-          if (dcube > 0) {
-            int dc[3] = {cg[0], cg[1], cg[2]};
-            dc[ax] = slot == 0 ? x + n : x - n;
-            double *g = a.U1_ + 5 * cell_index(S, dcube, dc[0], dc[1], dc[2]);
-#pragma unroll
-            for (int r = 0; r < 5; ++r) g[r] = un[r];
-          }
-        }
-      }
-    }
+    if (a.push) push_same_level(a.U1_, a.push, n, cube, bi + mi, bj + mj, bk + mk, un);
     if (a.RK == 3) {
       // Change norms of p, u, v, w, T from the increment, in FP32; summed
       // in FP64 (BCM_Flux...cpp:2530-2566).

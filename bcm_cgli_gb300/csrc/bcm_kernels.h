@@ -162,6 +162,7 @@ struct LusgsSplitArgs {
   const double *Residual1;
   double *partials;        // [ncube-1][7]
   Batch bt;
+  const int *push = nullptr;  // same-level push table (FluxSplitArgs::push)
 };
 cudaError_t launch_lusgs_split(const LusgsSplitArgs &a, int ncubes, cudaStream_t s);
 // Floats of that scratch per cube.

@@ -310,8 +310,15 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 448 ? 2 : 1) k_lusgs_split(Lusgs
       float dq[5];
 #pragma unroll
       for (int v = 0; v < 5; ++v) dq[v] = stage[v * nn + jk];
+      double un[5];
 #pragma unroll
-      for (int v = 0; v < 5; ++v) a.U1_[5 * o + v] = a.U1_[5 * o + v] + (double)dq[v];
+      for (int v = 0; v < 5; ++v) {
+        un[v] = a.U1_[5 * o + v] + (double)dq[v];
+        a.U1_[5 * o + v] = un[v];
+      }
+      // Same-level interface copy of this cell, done here: no block reads
+      // the FP64 state of another cube during the sweep.
+      if (a.push) push_same_level(a.U1_, a.push, n, cube, i + 2, j + 2, k + 2, un);
       const float *mm_ = a.M + 5 * o;
       const float rf = rho0 + mm_[0];
       const float m1 = mm_[1], m2 = mm_[2], m3 = mm_[3];

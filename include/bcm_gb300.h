@@ -274,12 +274,13 @@ typedef struct bcmg_tuning {
 int bcmg_case_set_tuning(bcmg_case *c, const bcmg_tuning *t);
 int bcmg_case_autotune(bcmg_case *c, int reps, bcmg_tuning *out);
 
-/* Where split-precision RK stages make the interface's same-level face
- * copies of the updated cells: in_flux = 1 (default) inside the flux kernel,
- * each updated cell next to a same-level face writing its new value into
- * the neighbour's ghost layer, so the interface call after the stage runs
- * only the level-jump tasks and the edge fill; 0: in that interface call.
- * Both give the same bits.  No effect on the FP64 path or LU-SGS. */
+/* Where split-precision RK stages and LU-SGS sweeps make the interface's
+ * same-level face copies of the updated cells: in_flux = 1 (default) inside
+ * the updating kernel, each updated cell next to a same-level face writing
+ * its new value into the neighbour's ghost layer, so the interface call
+ * after the update runs only the level-jump tasks and the edge fill; 0: in
+ * that interface call.  Both give the same bits.  No effect on the FP64
+ * path. */
 int bcmg_case_set_face_copies(bcmg_case *c, int in_flux);
 
 /* Waits for all work of the context. */

@@ -102,6 +102,25 @@ def test_face_copies_in_flux_kernel_change_no_cell(name, graph):
         assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
 
 
+@pytest.mark.parametrize("name", ["sphere_two_level", "tgv_n8"])
+def test_face_copies_in_lusgs_sweep_change_no_cell(name):
+    """The split LU-SGS sweep makes the same-level copies of the cells it
+    updates as well; with the copies left to the interface call the state is
+    the same, bit for bit."""
+    case = _prologue_cases()[name]
+    states = []
+    for in_flux in (True, False):
+        ctx = api.CaseContext(case, precision=api.PRECISION_SPLIT)
+        ctx.set_method(api.METHOD_LUSGS)
+        ctx.set_face_copies(in_flux)
+        ctx.set_state(case.U, case.U, case.U)
+        ctx.advance(1, 3)
+        states.append(ctx.get_state())
+        ctx.close()
+    for a, b in zip(*states):
+        assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
 def test_face_copies_in_flux_kernel_batch():
     """The same for a batch (periodic TGV, a random two-level case with IBM
     tables, the two-level sphere), through fixed and convergence-driven
