@@ -208,10 +208,11 @@ struct bcmg_case {
   int *task_cube_p = nullptr;
   FaceTask *tasks_p = nullptr;
   int ntasks_p = 0;
-  // Split-precision RK stages copy same-level faces inside the flux kernel
-  // (push table, see FluxSplitArgs::push); their closing interface call then
-  // runs only the level-jump tasks (and the edge fill).  push == nullptr:
-  // the table could not be formed (a face with two same-level sources).
+  // Split-precision RK stages and LU-SGS sweeps make the same-level face
+  // copies of the cells they update inside the updating kernel (push table,
+  // see FluxSplitArgs::push); their closing interface call then runs only
+  // the level-jump tasks (and the edge fill).  push == nullptr: the table
+  // could not be formed (one source layer pair feeding two faces).
   int *push = nullptr;
   bool push_on = true;  // bcmg_case_set_face_copies
   const int *push_table() const { return push_on ? push : nullptr; }
@@ -272,6 +273,9 @@ struct bcmg_case {
   }
   cudaGraphExec_t graph = nullptr;
   int graph_subiters = -1;
+  // Kernel nodes of the captured step graph, counted while capturing; of
+  // the convergence-driven graph, per pass of the while body and outside it.
+  long long graph_launches = 0, cgraph_body = 0, cgraph_outer = 0;
   long long launches = 0;
   bool profile = false;
   std::vector<cudaEvent_t> ev;
@@ -632,18 +636,22 @@ int build_conv_graph(bcmg_case *c, int max_subiters, double tol) {
   CK(cudaGraphAddNode(&wnode, g, &reset, nullptr, 1, &p));
   cudaGraph_t body = p.conditional.phGraph_out[0];
   CK(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, mode));
+  const long long l0 = c->launches;
   int r = case_subiter(c);
   if (!r) {
     k_conv_check<<<1, 32, 0, c->stream>>>(c->er, c->active, c->iters, c->ncase, tol,
                                           max_subiters, c->cont, h, 1);
     le = cudaGetLastError();
   }
+  c->cgraph_body = c->launches - l0 + 1;  // + the check
   cudaError_t ce = cudaStreamEndCapture(c->stream, &body);
   if (r) return r;
   CK(le);
   CK(ce);
   CK(cudaStreamBeginCaptureToGraph(c->stream, g, &wnode, nullptr, 1, mode));
+  const long long l1 = c->launches;
   r = case_shift(c);
+  c->cgraph_outer = c->launches - l1 + 1;  // + the reset
   ce = cudaStreamEndCapture(c->stream, &g);
   if (r) return r;
   CK(ce);
@@ -1053,6 +1061,7 @@ int bcmg_case_advance(bcmg_case *c, int steps, int subiters, int use_graph, doub
       CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
       long long saved = c->launches;
       int r = case_step(c, subiters);
+      c->graph_launches = c->launches - saved;
       cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
       if (r) return r;
       if (ce != cudaSuccess) { set_err(cudaGetErrorString(ce)); return BCMG_ERR_CUDA; }
@@ -1062,26 +1071,7 @@ int bcmg_case_advance(bcmg_case *c, int steps, int subiters, int use_graph, doub
       c->graph_subiters = subiters;
       c->launches = saved;
     }
-    long long per = 0;
-    {
-      // kernel nodes per step, counted like case_step
-      int L = (int)(c->ibm.level_off.size() > 0 ? c->ibm.level_off.size() - 1 : 0);
-      // bc, IBM levels, interface (faces + edges), [mirror], flux, [rk],
-      // interface (faces + edges)
-      const long long ifl = c->ntasks > 0 ? 2 : 1, ifp = c->ntasks_p > 0 ? 2 : 1;
-      // split RK stages close with the level-jump list when the flux kernel
-      // made the same-level copies
-      const long long ifc =
-          c->push_table() && c->precision == BCMG_PRECISION_SPLIT ? (c->ntasks_q > 0 ? 2 : 1)
-                                                                   : ifl;
-      // stages after the first of a step run the reduced prologue copies
-      const long long stage = (c->nbc > 0) + L + ifp + 1 + 1 + ifc;
-      // LU-SGS: prologue, residual, sweeps, norms, interface
-      const long long lu = (c->nbc > 0) + L + ifp + 1 + 1 + 1 + ifc;
-      const long long sub = c->method == BCMG_METHOD_LUSGS ? lu : 3 * stage + 1;
-      per = subiters * (sub + 1) + (ifl - ifp) + 1 +
-            (c->precision == BCMG_PRECISION_SPLIT ? 1 : 0);
-    }
+    const long long per = c->graph_launches;  // kernel nodes of one step
     for (int s = 0; s < steps; ++s) CK(cudaGraphLaunch(c->graph, c->stream));
     c->launches = per * steps;
   } else {
@@ -1413,23 +1403,13 @@ int bcmg_case_advance_converged(bcmg_case *c, int steps, int max_subiters, doubl
   CK(cudaStreamSynchronize(c->stream));
   if (subiters_out) std::copy(h.begin(), h.begin() + (size_t)steps * c->ncase, subiters_out);
   if (use_graph && !c->profile) {
-    // kernel launches of the replayed graphs: per sub-iteration as in
-    // bcmg_case_advance, plus reset, check and shift
-    const int L = (int)(c->ibm.level_off.size() > 0 ? c->ibm.level_off.size() - 1 : 0);
-    const long long ifl = c->ntasks > 0 ? 2 : 1, ifp = c->ntasks_p > 0 ? 2 : 1;
-    const long long ifc =
-        c->push_table() && c->precision == BCMG_PRECISION_SPLIT ? (c->ntasks_q > 0 ? 2 : 1)
-                                                                   : ifl;
-    // RK: the second and third stages run the reduced prologue copies
-    const long long stage = (c->nbc > 0) + L + 1 + 1 + ifc;
-    const long long lu = (c->nbc > 0) + L + ifl + 1 + 1 + 1 + ifc;
-    const long long sub =
-        (c->method == BCMG_METHOD_LUSGS ? lu : 3 * stage + ifl + 2 * ifp) + 1 + 1;
+    // kernel launches of the replayed graphs: the while body once per
+    // sub-iteration of the slowest case, plus reset and shift
     long long tot = 0;
     for (int st = 0; st < steps; ++st) {
       int mx = 0;
       for (int q = 0; q < c->ncase; ++q) mx = std::max(mx, h[(size_t)st * c->ncase + q]);
-      tot += mx * sub + 2 + (c->precision == BCMG_PRECISION_SPLIT ? 1 : 0);
+      tot += mx * c->cgraph_body + c->cgraph_outer;
     }
     c->launches = tot;
   }

@@ -228,6 +228,27 @@ def _small_sphere():
                             refine_box=((-2, 2), (-2, 2), (-2, 2)))
 
 
+@pytest.mark.parametrize("precision", [api.PRECISION_FP64, api.PRECISION_SPLIT])
+@pytest.mark.parametrize("method", [api.METHOD_RK3, api.METHOD_LUSGS])
+@pytest.mark.parametrize("make", [lambda: _cases()["tgv_n8"], _small_sphere],
+                         ids=["tgv_n8", "sphere"])
+def test_graph_launch_count_equals_eager(precision, method, make):
+    """The kernel count a replayed step graph reports (computed from the
+    case's tables) equals the count of the same steps launched one by one."""
+    case = make()
+    counts = []
+    for graph in (False, True):
+        ctx = api.CaseContext(case, precision=precision)
+        ctx.set_method(method)
+        ctx.set_state(case.U, case.U, case.U)
+        ctx.advance(1, 3, use_graph=graph)
+        if graph:  # the first graph call captures; count a replay
+            ctx.advance(1, 3, use_graph=True)
+        counts.append(ctx.launch_count())
+        ctx.close()
+    assert counts[0] == counts[1] > 0, counts
+
+
 @pytest.mark.parametrize("graph", [False, True])
 def test_sphere_ibm_two_level_bitwise(port, graph):
     """Sphere with IBM ghost cells on a two-level grid with open-domain
