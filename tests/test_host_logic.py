@@ -247,6 +247,47 @@ def test_prologue_plan_matches_rule(make):
         assert push[src, 2 * ax + (0 if side == 1 else 1)] == c
 
 
+def _create_error(case_list, precision=0):
+    """bcmg_case_create / bcmg_batch_create of invalid descriptors: they fail
+    in the host validation, before any device work (so on a CPU too)."""
+    from bcm_cgli_gb300 import api
+    try:
+        if len(case_list) == 1:
+            api.CaseContext(case_list[0], precision=precision)
+        else:
+            api.BatchContext(case_list, precision=precision)
+    except api.BcmgError as e:
+        return str(e)
+    return None
+
+
+def test_invalid_descriptors_rejected_on_the_host():
+    good = cases.random_case(seed=3, n=4)
+
+    def variant(**kw):
+        c = cases.random_case(seed=3, n=4)
+        for k, v in kw.items():
+            setattr(c, k, v)
+        return c
+
+    adj = good.adj.copy()
+    adj[1, 1, 2] = good.ncube + 5  # neighbour outside the cube list
+    assert _create_error([variant(adj=adj)]) is not None
+    cs = good.cube_size.copy()
+    cs[2] = 0.0
+    assert "cube_size" in _create_error([variant(cube_size=cs)])
+    assert "n must be a multiple of 4" in _create_error([variant(n=6)])
+    assert "precision" in _create_error([good], precision=7)
+    two = cases.random_two_level_case(seed=1, n=4)
+    csl = two.csl.copy()
+    csl[csl == 1] = 3  # an 8:1 jump between neighbours
+    two.csl = csl
+    assert "2:1" in _create_error([two])
+    # a batch needs one n and one precision across its cases
+    other = cases.random_case(seed=4, n=8)
+    assert "same n" in _create_error([good, other])
+
+
 @pytest.mark.skipif(not O.reference_available(), reason="reference sources not on this host")
 def test_reference_shim_compiles_against_main_h(tmp_path):
     """The C++ shim provides exactly the signatures the reference's main.h
