@@ -122,8 +122,8 @@ def test_face_copies_in_lusgs_sweep_change_no_cell(name):
 
 
 def test_face_copies_in_flux_kernel_batch():
-    """The same for a batch (periodic TGV, a random two-level case with IBM
-    tables, the two-level sphere), through fixed and convergence-driven
+    """The same for a batch (periodic TGV, a random two-level case, the
+    two-level sphere with IBM tables), through fixed and convergence-driven
     stepping."""
     cs = [cases.taylor_green(ncx=2, n=8), cases.random_two_level_case(seed=6, n=8, periodic=False),
           _prologue_cases()["sphere_two_level"]]
