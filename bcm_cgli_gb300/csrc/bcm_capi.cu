@@ -14,6 +14,7 @@
 #include "../../include/bcm_gb300.h"
 #include "bcm_kernels.h"
 #include "bcm_tables.h"
+#include "bcm_trace.h"
 
 using namespace bcmg;
 
@@ -716,6 +717,7 @@ int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out)
 }  // namespace
 
 extern "C" int bcmg_case_create(const bcmg_case_desc *d, bcmg_case **out) {
+  TraceRange trace("bcmg_case_create");
   return create_common(d, nullptr, out);
 }
 
@@ -997,6 +999,7 @@ void bcmg_case_destroy(bcmg_case *c) {
 }
 
 int bcmg_case_set_state(bcmg_case *c, const double *U1_, const double *U1, const double *U1q) {
+  TraceRange trace("bcmg_case_set_state");
   clear_err();
   if (!c) { set_err("null context"); return BCMG_ERR_ARG; }
   const size_t b = c->ncell * 5 * sizeof(double);
@@ -1010,6 +1013,7 @@ int bcmg_case_set_state(bcmg_case *c, const double *U1_, const double *U1, const
 }
 
 int bcmg_case_get_state(bcmg_case *c, double *U1_, double *U1, double *U1q) {
+  TraceRange trace("bcmg_case_get_state");
   clear_err();
   if (!c) { set_err("null context"); return BCMG_ERR_ARG; }
   const size_t b = c->ncell * 5 * sizeof(double);
@@ -1035,6 +1039,7 @@ int bcmg_case_get_scratch(bcmg_case *c, double *U1p1, double *U1p2, double *Rku1
 }
 
 int bcmg_case_stage(bcmg_case *c, int RK) {
+  TraceRange trace("bcmg_case_stage");
   clear_err();
   if (!c || RK < 1 || RK > 3) { set_err("bad context or RK"); return BCMG_ERR_ARG; }
   c->launches = 0;
@@ -1046,6 +1051,7 @@ int bcmg_case_stage(bcmg_case *c, int RK) {
 
 int bcmg_case_advance(bcmg_case *c, int steps, int subiters, int use_graph, double *er,
                       double *emax) {
+  TraceRange trace("bcmg_case_advance");
   clear_err();
   if (!c || steps < 0 || subiters < 1) { set_err("bad arguments"); return BCMG_ERR_ARG; }
   if (emax)
@@ -1176,6 +1182,7 @@ int bcmg_case_profile(const bcmg_case *c, double *flux_ms_total, long long *flux
 // table indexed through a cube -> case map.
 // ---------------------------------------------------------------------------
 int bcmg_batch_create(int ncase, const bcmg_case_desc *descs, bcmg_case **out) {
+  TraceRange trace("bcmg_batch_create");
   clear_err();
   if (!out || !descs || ncase < 1) {
     set_err("null argument or ncase < 1");
@@ -1334,6 +1341,7 @@ int bcmg_case_set_method(bcmg_case *c, int method, double cfl, double omega) {
 
 int bcmg_case_advance_converged(bcmg_case *c, int steps, int max_subiters, double tol,
                                 int use_graph, int *subiters_out, double *er, double *emax) {
+  TraceRange trace("bcmg_case_advance_converged");
   clear_err();
   if (!c || steps < 0 || max_subiters < 1 || !(tol > 0)) {
     set_err("bad arguments");
@@ -1518,6 +1526,7 @@ int out_launch(bcmg_case *c, const char *path, int ncube_out, int ng, size_t ndo
 }  // namespace
 
 int bcmg_case_output_q(bcmg_case *c, int q, int ncube_out, const char *path) {
+  TraceRange trace("bcmg_case_output_q");
   clear_err();
   if (!c || !path) { set_err("null argument"); return BCMG_ERR_ARG; }
   int g0 = 0, ng = 0, r;
@@ -1532,6 +1541,7 @@ int bcmg_case_output_q(bcmg_case *c, int q, int ncube_out, const char *path) {
 
 int bcmg_case_output_x(bcmg_case *c, int q, int ncube_out, const char *path,
                        const double *origin) {
+  TraceRange trace("bcmg_case_output_x");
   clear_err();
   if (!c || !path || !origin) { set_err("null argument"); return BCMG_ERR_ARG; }
   int g0 = 0, ng = 0, r;
@@ -1943,6 +1953,7 @@ void BCM_Flux_XYZ_Viscous_Runge_kutta(int myid, int ncube, int RK, double deltaT
                                       double *cube_size, double *U1_, double *U1, double *U1q,
                                       double *U1p1, double *U1p2, double *Rku1,
                                       double *Residual1, double *er) {
+  TraceRange trace("BCM_Flux_XYZ_Viscous_Runge_kutta");
   (void)myid;
   (void)csl;
   clear_err();
@@ -2066,6 +2077,7 @@ void BCM_Interface(int myid, int ncube, int mPI_Nadj, int ncpu_bs, int ncpu_eq, 
                    int *adjY_sb_plus, int *adjY_bs_minus, int *adjY_sb_minus,
                    int *adjZ_bs_plus, int *adjZ_sb_plus, int *adjZ_bs_minus,
                    int *adjZ_sb_minus, double *U1_) {
+  TraceRange trace("BCM_Interface");
   (void)myid; (void)mPI_Nadj; (void)max_nei_bs; (void)max_nei_eq; (void)max_nei_sb;
   (void)rank_map; (void)MPI_cpu; (void)MPI_cube; (void)MPI_cpu_adj; (void)MPI_cube_adj;
   (void)MPI_direction; (void)MPI_interface; (void)neighbor_cpu_eq; (void)Ncube_Ncpu_eq;

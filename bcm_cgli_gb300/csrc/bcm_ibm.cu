@@ -35,6 +35,7 @@
 #include "../../include/bcm_gb300.h"
 #include "bcm_common.cuh"
 #include "bcm_kernels.h"
+#include "bcm_trace.h"
 
 namespace bcmg {
 namespace {
@@ -643,6 +644,7 @@ extern "C" int bcmg_ibm_preprocess(int n, int ncube, const double *cube_size, co
                                    int *FWS, int ntri, const double *tri, int cap, int *nminus,
                                    int *gc_minus, int *ip_minus, double *w_minus, int *nplus,
                                    int *gc_plus, int *ip_plus, double *w_plus) {
+  bcmg::TraceRange trace("bcmg_ibm_preprocess");
   bcmg_internal_set_error(nullptr);
   if (!nminus || !nplus) return fail("bad arguments", BCMG_ERR_ARG);
   *nminus = 0;
@@ -679,6 +681,7 @@ extern "C" void BCM_Immersed_boundary(int myid, int ncube, int n_wallcube, int *
                                       double Zmax, double *cube_size, int *csl, double *Xcube,
                                       double *Ycube, double *Zcube, double *Xcnt, double *Ycnt,
                                       double *Zcnt, int *FWS, int *wallcube) {
+  bcmg::TraceRange trace("BCM_Immersed_boundary");
   (void)n_wallcube; (void)NBC; (void)Xmin; (void)Xmax; (void)Ymin; (void)Ymax; (void)Zmin;
   (void)Zmax; (void)wallcube;
   bcmg_internal_set_error(nullptr);
