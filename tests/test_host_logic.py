@@ -247,6 +247,29 @@ def test_prologue_plan_matches_rule(make):
         assert push[src, 2 * ax + (0 if side == 1 else 1)] == c
 
 
+def test_interface_plan_error_codes():
+    """-2 when the task buffer is too small, -1 for invalid input."""
+    case = cases.taylor_green(ncx=2, n=4)
+    adj = np.ascontiguousarray(case.adj, np.int32)
+    csl = np.ascontiguousarray(case.csl, np.int32)
+    lists = [np.ascontiguousarray(a, np.int32) for a in case.bc_lists()]
+    ptrs = (C.c_void_p * 6)(*[a.ctypes.data if len(a) else None for a in lists])
+    counts = (C.c_int * 6)(*[len(a) for a in lists])
+    keep = np.zeros(64, np.int32)
+    push = np.zeros(6 * case.ncube, np.int32)
+
+    def plan(ncube, adj_, cap):
+        return lib().bcmg_interface_plan(case.n, ncube, adj_, csl, C.cast(ptrs, C.c_void_p),
+                                         C.cast(counts, C.c_void_p), None, 0, None, 0, keep,
+                                         push, cap)
+    assert plan(case.ncube, adj, 64) == 6 * (case.ncube - 1)
+    assert plan(case.ncube, adj, 10) == -2
+    bad = adj.copy()
+    bad[1, 1, 2] = case.ncube + 3
+    assert plan(case.ncube, bad, 64) == -1
+    assert plan(1, adj, 64) == -1
+
+
 def _create_error(case_list, precision=0):
     """bcmg_case_create / bcmg_batch_create of invalid descriptors: they fail
     in the host validation, before any device work (so on a CPU too)."""
