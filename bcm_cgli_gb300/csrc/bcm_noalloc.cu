@@ -76,6 +76,9 @@ extern "C" int bcmg_flux_rk_stage_noalloc(int ncube, int RK, double deltaT, doub
     return fail("bcmg_flux_rk_stage_noalloc: bad arguments");
   bcmg_reference_config cfg;
   bcmg_get_reference_config(&cfg);
+  if (cfg.ncube_x <= 0 || cfg.ncube_x % 4 != 0 || cfg.ncube_x > 256)
+    return fail("bcmg_flux_rk_stage_noalloc: the reference configuration's ncube_x must be a "
+                "positive multiple of 4 up to 256");
   const long long n3 = (long long)cfg.ncube_x * cfg.ncube_x * cfg.ncube_x;
   const long long total = (long long)(ncube - 1) * n3;
   if (total > kMaxCells)

@@ -347,9 +347,12 @@ int bcmg_case_get_case_state(bcmg_case *c, int q, double *U1_, double *U1, doubl
  * reference.  It serves callers that cannot let a library call cudaMalloc:
  * solvers that hand out every device buffer from their own pre-sized arena,
  * and latency-sensitive hosts that cannot accept the implicit device
- * synchronisation an allocation may cause.  Same arithmetic and results as
+ * synchronisation an allocation may cause.  Same arithmetic as
  * BCM_Flux_XYZ_Viscous_Runge_kutta (with the bcmg_set_reference_config
- * values), but every array argument is a DEVICE pointer owned by the caller
+ * values): U1_, U1p1, U1p2, Rku1 and Residual1 are bit-identical to it; the
+ * norms er[1..7] are summed over fixed 4096-cell blocks, a different order,
+ * so they agree within rounding (about 1e-12 relative).  Unlike it, every
+ * array argument is a DEVICE pointer owned by the caller
  * (cube_size and er included; er[0] is set to 0), the work is queued on
  * `stream` (a cudaStream_t, NULL for the legacy default stream) and the call
  * returns without waiting.  Its only scratch, the per-block norm partial

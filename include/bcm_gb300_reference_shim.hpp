@@ -10,7 +10,7 @@
 // link, gives main.cpp the same
 // C++ symbols, now running on the GPU through the C ABI of bcm_gb300.h.
 // Call bcmg_set_reference_config() once at start-up with the values of
-// Resolution.h / prm.h.
+// Resolution.h / prm.h (NcubeX, MPI_Ncube, mu_L, rho0, U0, Uin, P0).
 #pragma once
 
 #include "bcm_gb300.h"

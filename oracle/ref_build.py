@@ -1,7 +1,8 @@
 """Build recipe for ``oracle/_ref``: the reference's own CPU code as a library.
 
 TEST INFRASTRUCTURE ONLY.  This compiles the reference's C++ sources where they
-lie (``/root/reference``, read-only; nothing is copied) into
+lie (the directory named by ``BCM_REFERENCE_DIR``, by default ``reference``
+beside this repository's root; read-only, nothing is copied) into
 ``oracle/_ref/libbcmref_<config>.so`` together with ``oracle/ref_driver.cpp``
 (which only forwards arrays and replays the reference's per-stage call order).
 
@@ -20,7 +21,7 @@ Build flags: ``-O2 -fopenmp -ffp-contract=off``.  ``-ffp-contract=off`` matters
 on aarch64, where GCC otherwise fuses multiply-adds and the results stop being
 the IEEE sequence the reference's source spells out.
 
-When ``/root/reference`` is absent (the GPU host), nothing is built and the
+When the reference directory is absent (the GPU host), nothing is built and the
 tests that need the compiled reference skip; the committed golden fixtures in
 ``tests/golden`` carry its outputs instead.
 """
@@ -32,7 +33,8 @@ import sys
 from dataclasses import dataclass, field
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_DIR = os.environ.get("BCM_REFERENCE_DIR", "/root/reference")
+REF_DIR = os.environ.get("BCM_REFERENCE_DIR",
+                         os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 OUT_DIR = os.path.join(HERE, "_ref")
 
 # The reference translation units on the hot path.

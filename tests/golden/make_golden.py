@@ -1,7 +1,7 @@
 """Generate tests/golden/golden.json from the REFERENCE's own compiled code.
 
 Runs each case of golden_cases.py through oracle/_ref (the reference's
-BCM_*.cpp compiled from /root/reference by oracle/ref_build.py, one OpenMP
+BCM_*.cpp compiled where they lie (BCM_REFERENCE_DIR) by oracle/ref_build.py, one OpenMP
 thread so its norm sums are serial) and records SHA-256 digests of every
 output array plus the norms.  Run here, where the reference sources exist:
 
