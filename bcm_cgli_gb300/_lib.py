@@ -94,8 +94,10 @@ def _declare(L):
     L.bcmg_batch_create.argtypes = [C.c_int, C.POINTER(CaseDesc), C.POINTER(P)]
     L.bcmg_case_set_method.argtypes = [P, C.c_int, C.c_double, C.c_double]
     L.bcmg_case_mirror.argtypes = [P, P]
+    L.bcmg_case_mirror_current.argtypes = [P, P]
     L.bcmg_case_set_tuning.argtypes = [P, C.POINTER(Tuning)]
     L.bcmg_case_set_face_copies.argtypes = [P, C.c_int]
+    L.bcmg_case_set_mirror_each_stage.argtypes = [P, C.c_int]
     L.bcmg_case_autotune.argtypes = [P, C.c_int, C.POINTER(Tuning)]
     L.bcmg_case_output_q.argtypes = [P, C.c_int, C.c_int, C.c_char_p]
     L.bcmg_case_output_x.argtypes = [P, C.c_int, C.c_int, C.c_char_p, P]

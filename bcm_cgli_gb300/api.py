@@ -355,6 +355,13 @@ class CaseContext:
         interface call after it (False).  Both give the same bits."""
         check(lib().bcmg_case_set_face_copies(self.h, 1 if in_flux else 0))
 
+    def set_mirror_each_stage(self, on=True):
+        """Split precision: form the whole FP32 mirror of the state before
+        every flux launch (True) instead of once per dual-time step with the
+        state-writing kernels keeping it current (False, default).  Both
+        give the same bits."""
+        check(lib().bcmg_case_set_mirror_each_stage(self.h, 1 if on else 0))
+
     def autotune(self, reps=3):
         """Times the launch-shape candidates on this context's state, applies the
         fastest and returns the choice with the measured milliseconds."""
@@ -368,6 +375,13 @@ class CaseContext:
         """FP32 mirror of the current state (split-precision path)."""
         out = np.empty(self.shape, np.float32)
         check(lib().bcmg_case_mirror(self.h, out.ctypes.data))
+        return out
+
+    def mirror_current(self):
+        """The FP32 mirror as the kernels keep it during stepping (not
+        re-formed; split-precision path)."""
+        out = np.empty(self.shape, np.float32)
+        check(lib().bcmg_case_mirror_current(self.h, out.ctypes.data))
         return out
 
     def sync(self):

@@ -157,7 +157,7 @@ int ibm_upload(Ibm &t, int nbc, const double *w, const int *gc, const int *ip, i
 }
 
 int ibm_run(const Ibm &t, int n, double rho0, double P0, double *U, cudaStream_t s,
-            long long *launches, const Batch &bt = Batch()) {
+            long long *launches, const Batch &bt = Batch(), const Mirror &mir = Mirror()) {
   for (size_t l = 1; l < t.level_off.size(); ++l) {
     GhostArgs g;
     g.n = n;
@@ -169,6 +169,7 @@ int ibm_run(const Ibm &t, int n, double rho0, double P0, double *U, cudaStream_t
     g.IPsur = t.ip;
     g.U1_ = U;
     g.bt = bt;
+    g.mir = mir;
     CK(launch_ghost(g, t.level_off[l] - t.level_off[l - 1], s));
     if (launches) ++*launches;
   }
@@ -191,7 +192,25 @@ struct bcmg_case {
   cudaStream_t stream = nullptr;
   double *U1_ = nullptr, *U1 = nullptr, *U1q = nullptr, *U1p1 = nullptr, *U1p2 = nullptr,
          *Rku1 = nullptr, *Residual1 = nullptr;
-  float *M = nullptr;                    // split precision: FP32 deltas of U1_
+  // Split precision: the FP32 mirror of U1_ (deltas from each case's
+  // reference state) in two buffers, the device flag naming the current one
+  // (bcm_mirror.cuh), and whether the whole mirror is re-formed before every
+  // flux launch (the old per-stage pass; kept to check the incremental
+  // mirror against it) instead of once per dual-time step.
+  float *M = nullptr, *M2 = nullptr;
+  int *mpar = nullptr;
+  bool mirror_each_stage = false;
+  Mirror mir() const {
+    Mirror m;
+    if (M) {
+      m.buf[0] = M;
+      m.buf[1] = M2;
+      m.parity = mpar;
+      m.rho0 = ph.rho0;
+      m.E0 = ph.P0 / (BCMG_K - 1);
+    }
+    return m;
+  }
   float *D2 = nullptr;                   // split precision: FP32 of U1 - U1q
   float *inv_dx = nullptr;               // split precision: n / cube_size per cube
   int *FWS = nullptr;
@@ -313,7 +332,7 @@ struct bcmg_case {
     for (auto x : ev) cudaEventDestroy(x);
     ev.clear();
     dfree(U1_); dfree(U1); dfree(U1q); dfree(U1p1); dfree(U1p2); dfree(Rku1); dfree(Residual1);
-    dfree(M); dfree(D2); dfree(inv_dx);
+    dfree(M); dfree(M2); dfree(mpar); dfree(D2); dfree(inv_dx);
     dfree(FWS); dfree(cube_size); dfree(task_cube); dfree(tasks); dfree(task_cube_p);
     dfree(tasks_p); dfree(push); dfree(task_cube_q); dfree(tasks_q); dfree(bc_cubes);
     dfree(bc_masks); dfree(partials); dfree(er); dfree(emax);
@@ -355,12 +374,12 @@ int case_flux(bcmg_case *c, int RK) {
     e1 = c->ev[c->ev_used + 1];
     c->ev_used += 2;
   }
-  if (c->precision == BCMG_PRECISION_SPLIT) {
-    CK(launch_mirror(c->U1_, c->M, c->ph.n, c->ncube, c->ph.rho0, c->ph.P0, c->bt(),
+  if (c->precision == BCMG_PRECISION_SPLIT && c->mirror_each_stage) {
+    CK(launch_mirror(c->U1_, c->M, c->M2, c->ph.n, c->ncube, c->ph.rho0, c->ph.P0, c->bt(),
                      c->stream));
     ++c->launches;
   }
-  // the timed span is the flux kernel alone (the mirror pass precedes it)
+  // the timed span is the flux kernel alone
   if (c->profile) CK(cudaEventRecord(e0, c->stream));
   if (c->precision == BCMG_PRECISION_SPLIT) {
     FluxSplitArgs sa;
@@ -380,7 +399,7 @@ int case_flux(bcmg_case *c, int RK) {
     sa.inv_dx = c->inv_dx;
     sa.FWS = c->FWS;
     sa.cube_size = c->cube_size;
-    sa.M = c->M;
+    sa.mir = c->mir();
     sa.U1_ = c->U1_;
     sa.U1 = c->U1;
     sa.U1q = c->U1q;
@@ -400,6 +419,11 @@ int case_flux(bcmg_case *c, int RK) {
   }
   if (c->profile) CK(cudaEventRecord(e1, c->stream));
   ++c->launches;
+  if (c->precision == BCMG_PRECISION_SPLIT && RK >= 1) {
+    // the flux kernel wrote the stage's mirror into the other buffer
+    CK(launch_mirror_flip(c->mpar, c->stream));
+    ++c->launches;
+  }
   return BCMG_OK;
 }
 
@@ -423,6 +447,7 @@ int case_interface(bcmg_case *c, IfaceList list = kIfaceFull) {
   }
   ia.U1_ = c->U1_;
   ia.bt = c->bt();
+  ia.mir = c->mir();
   CK(launch_interface(ia, c->ncube, c->stream));
   c->launches += ia.ntasks > 0 ? 2 : 1;
   return BCMG_OK;
@@ -442,11 +467,12 @@ int case_prologue(bcmg_case *c, bool full = true) {
     b.axes = 7;
     b.U1_ = c->U1_;
     b.bt = c->bt();
+    b.mir = c->mir();
     CK(launch_bc(b, c->nbc, c->stream));
     ++c->launches;
   }
   if ((r = ibm_run(c->ibm, c->ph.n, c->ph.rho0, c->ph.P0, c->U1_, c->stream, &c->launches,
-                   c->bt())))
+                   c->bt(), c->mir())))
     return r;
   return case_interface(c, full ? kIfaceFull : kIfacePrologue);
 }
@@ -465,7 +491,7 @@ LusgsSplitArgs lusgs_split_args(bcmg_case *c) {
   l.mu_Lf = (float)c->ph.mu_L;
   l.FWS = c->FWS;
   l.inv_dx = c->inv_dx;
-  l.M = c->M;
+  l.mir = c->mir();
   l.U1_ = c->U1_;
   l.R32 = reinterpret_cast<const float *>(c->Rku1);
   l.scr = c->lu_scr;
@@ -598,8 +624,22 @@ int case_shift(bcmg_case *c) {
   return BCMG_OK;
 }
 
+// The whole mirror of the current state, into both buffers: at the start of
+// every dual-time step (and of a single-stage call), so that a state set or
+// changed from outside, or a case that sat out sub-iterations after it
+// converged, is mirrored exactly; within the step the kernels that write the
+// state keep it current.
+int case_mirror_all(bcmg_case *c) {
+  if (c->precision != BCMG_PRECISION_SPLIT) return BCMG_OK;
+  CK(launch_mirror(c->U1_, c->M, c->M2, c->ph.n, c->ncube, c->ph.rho0, c->ph.P0, c->bt(),
+                   c->stream));
+  ++c->launches;
+  return BCMG_OK;
+}
+
 int case_step(bcmg_case *c, int subiters) {
   int r;
+  if ((r = case_mirror_all(c))) return r;
   for (int it = 0; it < subiters; ++it)  // the step's first stage runs every face copy
     if ((r = case_subiter(c, it == 0))) return r;
   return case_shift(c);
@@ -623,11 +663,23 @@ int build_conv_graph(bcmg_case *c, int max_subiters, double tol) {
   CK(cudaStreamBeginCaptureToGraph(c->stream, g, nullptr, nullptr, 0, mode));
   k_conv_reset<<<1, 128, 0, c->stream>>>(c->active, c->iters, c->ncase);
   cudaError_t le = cudaGetLastError();
+  const long long l_pre = c->launches;
+  int rm = le == cudaSuccess ? case_mirror_all(c) : BCMG_OK;
+  const long long pre_nodes = 1 + (c->launches - l_pre);
   CK(cudaStreamEndCapture(c->stream, &g));
+  if (rm) return rm;
   CK(le);
-  cudaGraphNode_t reset;
-  size_t nn = 1;
-  CK(cudaGraphGetNodes(g, &reset, &nn));
+  // the node the while node follows: the last of the nodes captured above
+  // (reset, then the mirror on the split path), which form a chain
+  std::vector<cudaGraphNode_t> pre((size_t)pre_nodes);
+  size_t nn = pre.size();
+  CK(cudaGraphGetNodes(g, pre.data(), &nn));
+  cudaGraphNode_t reset = nullptr;
+  for (size_t i = 0; i < nn; ++i) {
+    size_t ndep = 0;
+    CK(cudaGraphNodeGetDependentNodes(pre[i], nullptr, nullptr, &ndep));
+    if (ndep == 0) reset = pre[i];
+  }
   cudaGraphNodeParams p = {};
   p.type = cudaGraphNodeTypeConditional;
   p.conditional.handle = h;
@@ -652,7 +704,7 @@ int build_conv_graph(bcmg_case *c, int max_subiters, double tol) {
   CK(cudaStreamBeginCaptureToGraph(c->stream, g, &wnode, nullptr, 1, mode));
   const long long l1 = c->launches;
   r = case_shift(c);
-  c->cgraph_outer = c->launches - l1 + 1;  // + the reset
+  c->cgraph_outer = c->launches - l1 + pre_nodes;  // + the reset and the step's mirror
   ce = cudaStreamEndCapture(c->stream, &g);
   if (r) return r;
   CK(ce);
@@ -696,6 +748,7 @@ CaseConst case_const(const bcmg_case_desc &d) {
   q.U0 = d.U0;
   q.Uin = d.Uin;
   q.P0 = d.P0;
+  q.E0 = d.P0 / (BCMG_K - 1);
   q.dT = d.deltaT;
   q.dTau = d.deltaTau;
   q.e = d.e;
@@ -817,10 +870,12 @@ int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out)
             ck(dalloc(&c->emax, 6 * (size_t)c->ncase), "alloc");
   if (!ok) return fail(BCMG_ERR_CUDA);
   if (d->precision == BCMG_PRECISION_SPLIT &&
-      !(ck(dalloc(&c->M, nd), "alloc") &&
+      !(ck(dalloc(&c->M, nd), "alloc") && ck(dalloc(&c->M2, nd), "alloc") &&
+        ck(dalloc(&c->mpar, 1), "alloc") && ck(cudaMemset(c->mpar, 0, sizeof(int)), "memset") &&
         ck(dalloc(&c->D2, nd), "alloc") && ck(cudaMemset(c->D2, 0, nd * sizeof(float)), "memset") &&
         ck(dalloc(&c->inv_dx, (size_t)d->ncube), "alloc") &&
         ck(cudaMemset(c->M, 0, nd * sizeof(float)), "memset") &&
+        ck(cudaMemset(c->M2, 0, nd * sizeof(float)), "memset") &&
         true))
     return fail(BCMG_ERR_CUDA);
   if (c->inv_dx) {
@@ -1043,7 +1098,8 @@ int bcmg_case_stage(bcmg_case *c, int RK) {
   clear_err();
   if (!c || RK < 1 || RK > 3) { set_err("bad context or RK"); return BCMG_ERR_ARG; }
   c->launches = 0;
-  int r = case_stage(c, RK);
+  int r = case_mirror_all(c);
+  if (!r) r = case_stage(c, RK);
   if (r) return r;
   CK(cudaStreamSynchronize(c->stream));
   return BCMG_OK;
@@ -1135,14 +1191,17 @@ int bcmg_case_time_flux(bcmg_case *c, int reps, double *ms) {
   // state in the (split-unused) U1p1 buffer and restore it afterwards.
   if (c->precision == BCMG_PRECISION_SPLIT)
     CK(cudaMemcpyAsync(c->U1p1, c->U1_, bytes, cudaMemcpyDeviceToDevice, c->stream));
-  int r = case_flux(c, 1);  // warm-up
+  int r = case_mirror_all(c);
+  if (!r) r = case_flux(c, 1);  // warm-up
   if (!r) {
     cudaEventRecord(a, c->stream);
     for (int i = 0; i < reps && !r; ++i) r = case_flux(c, 1);
     cudaEventRecord(b, c->stream);
   }
-  if (c->precision == BCMG_PRECISION_SPLIT)
+  if (c->precision == BCMG_PRECISION_SPLIT) {
     CK(cudaMemcpyAsync(c->U1_, c->U1p1, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    if (!r) r = case_mirror_all(c);
+  }
   c->profile = prof;
   if (r) { cudaEventDestroy(a); cudaEventDestroy(b); return r; }
   CK(cudaEventSynchronize(b));
@@ -1580,8 +1639,26 @@ int bcmg_case_mirror(bcmg_case *c, float *M) {
     set_err("the FP32 mirror exists on the split-precision path only");
     return BCMG_ERR_ARG;
   }
-  CK(launch_mirror(c->U1_, c->M, c->ph.n, c->ncube, c->ph.rho0, c->ph.P0, c->bt(), c->stream));
+  CK(launch_mirror(c->U1_, c->M, c->M2, c->ph.n, c->ncube, c->ph.rho0, c->ph.P0, c->bt(),
+                   c->stream));
   CK(cudaMemcpyAsync(M, c->M, c->ncell * 5 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return BCMG_OK;
+}
+
+// The current mirror buffer as the kernels keep it, not re-formed.
+int bcmg_case_mirror_current(bcmg_case *c, float *M) {
+  clear_err();
+  if (!c || !M) { set_err("null argument"); return BCMG_ERR_ARG; }
+  if (c->precision != BCMG_PRECISION_SPLIT) {
+    set_err("the FP32 mirror exists on the split-precision path only");
+    return BCMG_ERR_ARG;
+  }
+  int par = 0;
+  CK(cudaMemcpyAsync(&par, c->mpar, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  CK(cudaMemcpyAsync(M, par ? c->M2 : c->M, c->ncell * 5 * sizeof(float), cudaMemcpyDeviceToHost,
+                     c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return BCMG_OK;
 }
@@ -1621,6 +1698,19 @@ int bcmg_case_set_tuning(bcmg_case *c, const bcmg_tuning *t) {
   c->graph_subiters = -1;
   if (c->cgraph) cudaGraphExecDestroy(c->cgraph);
   c->cgraph = nullptr;
+  return BCMG_OK;
+}
+
+int bcmg_case_set_mirror_each_stage(bcmg_case *c, int on) {
+  clear_err();
+  if (!c) { set_err("null context"); return BCMG_ERR_ARG; }
+  c->mirror_each_stage = on != 0;
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  c->graph = nullptr;
+  c->graph_subiters = -1;
+  if (c->cgraph) cudaGraphExecDestroy(c->cgraph);
+  c->cgraph = nullptr;
+  c->cgraph_max = -1;
   return BCMG_OK;
 }
 
@@ -1669,7 +1759,8 @@ int bcmg_case_autotune(bcmg_case *c, int reps, bcmg_tuning *out) {
     const int cand[2] = {full, ((full / 2) + 31) / 32 * 32};
     const size_t bytes = c->ncell * 5 * sizeof(double);
     CK(cudaMemcpyAsync(c->U1p1, c->U1_, bytes, cudaMemcpyDeviceToDevice, c->stream));
-    int r = case_flux(c, 0);  // residual and mirror of the current state
+    int r = case_mirror_all(c);
+    if (!r) r = case_flux(c, 0);  // residual of the current state
     if (r) return r;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
@@ -1700,6 +1791,7 @@ int bcmg_case_autotune(bcmg_case *c, int reps, bcmg_tuning *out) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     CK(cudaMemcpyAsync(c->U1_, c->U1p1, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    if ((r = case_mirror_all(c))) return r;  // the sweeps updated the mirror in place
     CK(cudaStreamSynchronize(c->stream));
   }
   int r = bcmg_case_set_tuning(c, &best);

@@ -41,10 +41,11 @@ __host__ __device__ inline size_t cell_index(int S, int c, int i, int j, int k) 
 // copies exactly this after the update): a cell in layers 2, 3 (slot 0) or
 // n, n+1 (slot 1) along an axis writes its new value un[5] into ghost
 // layers n+2, n+3 or 0, 1 of the cube push[6 cube + 2 axis + slot] (0:
-// none).  Safe only while no other thread reads the FP64 state's ghost
-// layers.
-__device__ __forceinline__ void push_same_level(double *U, const int *push, int n, int cube,
-                                                int ci, int cj, int ck, const double *un) {
+// none).  Safe only while no other thread reads those ghost layers of U
+// (the FP64 state, or the FP32 mirror buffer being written).
+template <typename T>
+__device__ __forceinline__ void push_same_level(T *U, const int *push, int n, int cube, int ci,
+                                                int cj, int ck, const T *un) {
   const int cg[3] = {ci, cj, ck};
 #pragma unroll
   for (int ax = 0; ax < 3; ++ax) {
@@ -59,7 +60,7 @@ __device__ __forceinline__ void push_same_level(double *U, const int *push, int 
     if (d <= 0) continue;
     int dc[3] = {ci, cj, ck};
     dc[ax] = slot == 0 ? x + n : x - n;
-    double *g = U + 5 * cell_index(n + 4, d, dc[0], dc[1], dc[2]);
+    T *g = U + 5 * cell_index(n + 4, d, dc[0], dc[1], dc[2]);
 #pragma unroll
     for (int r = 0; r < 5; ++r) g[r] = un[r];
   }

@@ -25,92 +25,26 @@
 namespace bcmg {
 
 // ---------------------------------------------------------------------------
-// FP64 -> FP32 deltas of the state, all cells of all cubes (ghosts included).
-// 16-byte loads and 8-byte stores (a cube holds S^3 cells, S even, so cells
-// pair up within a cube); 32-bit indices within a cube.
+// FP64 -> FP32 deltas of the state, all cells of all cubes (ghosts included),
+// into one or both mirror buffers: once per dual-time step, and whenever the
+// state was set from outside.  16-byte loads and 8-byte stores (a cube holds
+// S^3 cells, S even, so cells pair up within a cube); 32-bit indices within a
+// cube.  The conversions (to_float_rn, delta_rn) are the integer-pipe IEEE
+// roundings of bcm_mirror.cuh, which every other mirror writer uses too.
 // ---------------------------------------------------------------------------
-// double -> float, round to nearest even (IEEE 754), on the integer pipes:
-// this part's FP64 pipe, where the hardware conversion runs, is its
-// narrowest (1/64 of FP32) and would otherwise bound this memory-bound pass.
-// Results outside the normal float range (|x| < 2^-126, overflow, zero,
-// inf/nan) take the hardware conversion.
-__device__ __forceinline__ float to_float_rn(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
-  if ((b << 1) == 0) return __uint_as_float(hi);  // signed zero (common: rest momenta)
-  const int e = (int)((hi >> 20) & 0x7FF) - 1023 + 127;  // float exponent field
-  if (e <= 0 || e >= 255) return (float)x;
-  const unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);  // top 23 fraction bits
-  const unsigned rem = lo & 0x1FFFFFFFu, half = 0x10000000u;
-  unsigned r = ((unsigned)e << 23) | m;
-  r += (rem > half || (rem == half && (m & 1u))) ? 1u : 0u;  // a carry may raise the exponent
-  return __uint_as_float((hi & 0x80000000u) | r);
-}
-
-// float -> double (exact) on the integer pipes, for the same reason; zero,
-// subnormal, inf and nan inputs take the hardware conversion.
-__device__ __forceinline__ double to_double_exact(float f) {
-  const unsigned b = __float_as_uint(f);
-  const unsigned e = (b >> 23) & 0xFFu;
-  if ((b & 0x7FFFFFFFu) == 0) return __hiloint2double((int)(b & 0x80000000u), 0);
-  if (e == 0 || e == 255) return (double)f;
-  const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7FFFFFu) >> 3);
-  return __hiloint2double((int)hi, (int)(b << 29));
-}
-
-// (float)(x - r) without FP64 arithmetic when x and r have the same sign and
-// binade: their difference is then exact in FP64 (Sterbenz), so the integer
-// difference of the 53-bit significands, rounded once to nearest even, is
-// bit for bit the FP64 subtraction followed by the conversion.  Other inputs
-// take that subtraction.
-__device__ __forceinline__ float delta_rn(double x, double r) {
-  const unsigned long long bx = (unsigned long long)__double_as_longlong(x),
-                           br = (unsigned long long)__double_as_longlong(r);
-  const int ex = (int)((bx >> 52) & 0x7FF);
-  if (ex != (int)((br >> 52) & 0x7FF) || ex == 0 || ex == 0x7FF || ((bx ^ br) >> 63))
-    return to_float_rn(x - r);
-  const long long mx = (long long)((bx & 0xFFFFFFFFFFFFFull) | (1ull << 52));
-  const long long mr = (long long)((br & 0xFFFFFFFFFFFFFull) | (1ull << 52));
-  long long d = mx - mr;  // value = d * 2^(ex - 1075)
-  if (bx >> 63) d = -d;
-  if (d == 0) return 0.0f;  // x - x is +0 when rounding to nearest
-  const unsigned sign = d < 0 ? 0x80000000u : 0u;
-  const unsigned long long a = d < 0 ? (unsigned long long)(-d) : (unsigned long long)d;
-  const int bl = 64 - __clzll((long long)a);  // bit length, at most 53
-  int fe = (bl - 1) + (ex - 1075) + 127;     // float exponent field
-  if (fe <= 0) return to_float_rn(x - r);    // subnormal float: hardware path
-  unsigned m;
-  if (bl <= 24) {
-    m = (unsigned)(a << (24 - bl));
-  } else {
-    const int sh = bl - 24;
-    const unsigned long long keep = a >> sh, rem = a & ((1ull << sh) - 1), half = 1ull << (sh - 1);
-    m = (unsigned)keep;
-    if (rem > half || (rem == half && (keep & 1))) {
-      m += 1;
-      if (m == (1u << 24)) {  // the carry raises the exponent
-        m >>= 1;
-        fe += 1;
-      }
-    }
-  }
-  if (fe >= 255) return to_float_rn(x - r);
-  return __uint_as_float(sign | ((unsigned)fe << 23) | (m & 0x7FFFFFu));
-}
-
 // One block row per cube (blockIdx.y); a thread converts two cells, i.e.
 // five 16-byte pairs whose components are known at compile time, so only
 // the density and energy components take an FP64 subtraction.
 __global__ void __launch_bounds__(256) k_mirror(const double2 *__restrict__ U,
-                                                float2 *__restrict__ M, double rho0_,
-                                                double E0_, Batch bt, int cube_cell_pairs,
-                                                int ncubes) {
+                                                float2 *__restrict__ M, float2 *__restrict__ M1,
+                                                double rho0_, double E0_, Batch bt,
+                                                int cube_cell_pairs, int ncubes) {
   for (int cube = 1 + blockIdx.y; cube <= ncubes; cube += gridDim.y) {
     double rho0 = rho0_, E0 = E0_;
     if (bt.cube_case) {  // the reference state of the cube's case
       const CaseConst *cq = bt.cases + bt.cube_case[cube];
       rho0 = cq->rho0;
-      E0 = cq->P0 / (BCMG_K - 1);
+      E0 = cq->E0;
     }
     const size_t base = (size_t)cube * cube_cell_pairs * 5;  // in 16-byte pairs
 #pragma unroll
@@ -118,28 +52,40 @@ __global__ void __launch_bounds__(256) k_mirror(const double2 *__restrict__ U,
       const int q = (blockIdx.x * 2 + r) * 256 + threadIdx.x;  // cell pair in the cube
       if (q < cube_cell_pairs) {
         const double2 *u = U + base + 5 * (size_t)q;
-        float2 *m = M + base + 5 * (size_t)q;
         const double2 a = u[0], b = u[1], c = u[2], d = u[3], e = u[4];
         // doubles: rho, mx, my, mz, E | rho, mx, my, mz, E
-        m[0] = make_float2(delta_rn(a.x, rho0), to_float_rn(a.y));
-        m[1] = make_float2(to_float_rn(b.x), to_float_rn(b.y));
-        m[2] = make_float2(delta_rn(c.x, E0), delta_rn(c.y, rho0));
-        m[3] = make_float2(to_float_rn(d.x), to_float_rn(d.y));
-        m[4] = make_float2(to_float_rn(e.x), delta_rn(e.y, E0));
+        const float2 m0 = make_float2(delta_rn(a.x, rho0), to_float_rn(a.y));
+        const float2 m1 = make_float2(to_float_rn(b.x), to_float_rn(b.y));
+        const float2 m2 = make_float2(delta_rn(c.x, E0), delta_rn(c.y, rho0));
+        const float2 m3 = make_float2(to_float_rn(d.x), to_float_rn(d.y));
+        const float2 m4 = make_float2(to_float_rn(e.x), delta_rn(e.y, E0));
+        float2 *m = M + base + 5 * (size_t)q;
+        m[0] = m0; m[1] = m1; m[2] = m2; m[3] = m3; m[4] = m4;
+        if (M1) {
+          float2 *o = M1 + base + 5 * (size_t)q;
+          o[0] = m0; o[1] = m1; o[2] = m2; o[3] = m3; o[4] = m4;
+        }
       }
     }
   }
 }
 
-cudaError_t launch_mirror(const double *U, float *M, int n, int ncube, double rho0, double P0,
-                          const Batch &bt, cudaStream_t s) {
+cudaError_t launch_mirror(const double *U, float *M0, float *M1, int n, int ncube, double rho0,
+                          double P0, const Batch &bt, cudaStream_t s) {
   if (ncube <= 1) return cudaSuccess;  // cube slot 0 is unused
   const int S = n + 4;
   const int cube_cell_pairs = S * S * S / 2;  // S is even
   const dim3 grid((cube_cell_pairs + 511) / 512, ncube - 1 < 65535 ? ncube - 1 : 65535);
   k_mirror<<<grid, 256, 0, s>>>(reinterpret_cast<const double2 *>(U),
-                               reinterpret_cast<float2 *>(M), rho0, P0 / (BCMG_K - 1), bt,
-                               cube_cell_pairs, ncube - 1);
+                               reinterpret_cast<float2 *>(M0), reinterpret_cast<float2 *>(M1),
+                               rho0, P0 / (BCMG_K - 1), bt, cube_cell_pairs, ncube - 1);
+  return cudaGetLastError();
+}
+
+__global__ void k_mirror_flip(int *parity) { *parity ^= 1; }
+
+cudaError_t launch_mirror_flip(int *parity, cudaStream_t s) {
+  k_mirror_flip<<<1, 1, 0, s>>>(parity);
   return cudaGetLastError();
 }
 
@@ -425,16 +371,22 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
   if (!case_active(a.bt, cube)) return;  // converged case (uniform per CTA)
   const int tl = blockIdx.x % tiles;
   const int bi = 2 + (tl / (nt * nt)) * T, bj = 2 + ((tl / nt) % nt) * T, bk = 2 + (tl % nt) * T;
-  const float *__restrict__ M = a.M;
+  // Mirror buffers: read the current one; stages 1..3 write the deltas of
+  // the tile's cells into the other one.
+  const int par = *a.mir.parity;
+  const float *__restrict__ M = a.mir.buf[par];
+  float *const Mw = a.RK >= 1 ? a.mir.buf[par ^ 1] : nullptr;
   const int *__restrict__ F = a.FWS;
   const size_t cb = cell_index(S, cube, 0, 0, 0);
   // Constants of the cube's case (kernel arguments for a single case).
   float rho0 = a.rho0f, P0 = a.P0f, RT0 = a.RT0f /* R * T0 */, ef = a.ef, T0c = a.T0f,
         mu_Lc = a.mu_Lf, i2dtc = a.i2dtf, dTc = a.dTf, dTauc = a.dTauf;
+  double rho0d = a.mir.rho0, E0d = a.mir.E0;  // mirror reference state (FP64)
   if (a.bt.cube_case) {
     const CaseConst *cq = a.bt.cases + __ldg(a.bt.cube_case + cube);
     rho0 = cq->rho0f; P0 = cq->P0f; RT0 = cq->RT0f; ef = cq->ef; T0c = cq->T0f;
     mu_Lc = cq->mu_Lf; i2dtc = cq->i2dtf; dTc = cq->dTf; dTauc = cq->dTauf;
+    rho0d = cq->rho0; E0d = cq->E0;
   }
   const float iR = 1.0f / 287.0f;
 
@@ -635,7 +587,7 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
   const int IF = FL(mi, mj, mk);
   const float i2dt = i2dtc;
   float Rk[5];
-  double xq[5];
+  double xq[5], un[5];
 #pragma unroll
   for (int v = 0; v < 5; ++v) {
     const double x = u[v], y = __ldg(uu + v);
@@ -697,7 +649,6 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
     // combinations with Q1 = Q2 = Q on fluid cells at stage entry.
     const float w = a.RK == 1 ? 1.0f : (a.RK == 2 ? 0.25f : 2.0f / 3.0f);
     float dq[5];
-    double un[5];
 #pragma unroll
     for (int r = 0; r < 5; ++r) {
       dq[r] = w * dTau * (d[r][0] * Rk[0] + d[r][1] * Rk[1] + d[r][2] * Rk[2] +
@@ -741,6 +692,25 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
     a.Residual1[5 * go + 1] = r1;
     s5[5] += r0;
     s5[6] += r1;
+  }
+  if (Mw) {
+    // The cell's mirror value after the stage into the next buffer (the
+    // staged value where the cell did not change), and into the same-level
+    // neighbour's ghost layers: every cell of those layers pushes, since the
+    // next buffer's ghost layers hold values two stages old.
+    float m5[5];
+    if (IF == kFluid) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) m5[v] = mirror_value(un[v], v, rho0d, E0d);
+    } else {
+      const float *qm = BX(mi, mj, mk);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) m5[v] = qm[v];
+    }
+    float *mw = Mw + 5 * go;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) mw[v] = m5[v];
+    if (a.push) push_same_level(Mw, a.push, n, cube, bi + mi, bj + mj, bk + mk, m5);
   }
   }  // cells of this thread
   if (a.RK != 3) return;

@@ -34,6 +34,8 @@ constexpr int kHaloThreads = 256;
 //  kind 2, fine -> coarse: the big cube's two ghost layers over the slot's
 //    quadrant take 0.125 * the sum of the small cube's 2x2x2 interior cells,
 //    summed in the reference's order (000,100,010,001,110,101,011,111 in i,j,k).
+// With a mirror (split precision) every written value's mirror value is
+// written too: injections copy the source's, averages are converted.
 __device__ __forceinline__ void level_face(const InterfaceArgs &a, int c, const FaceTask &ft) {
   const int n = a.n, S = n + 4, h = n / 2;
   const int ax = ft.axis;
@@ -41,6 +43,9 @@ __device__ __forceinline__ void level_face(const InterfaceArgs &a, int c, const 
   const int o0 = (ft.slot == 2 || ft.slot == 4) ? h : 0;
   const int o1 = (ft.slot == 3 || ft.slot == 4) ? h : 0;
   double *U = a.U1_;
+  float *M = mirror_current(a.mir);
+  double r0 = 0, e0 = 0;
+  if (M) mirror_base(a.mir, a.bt, c, r0, e0);
   if (ft.kind == 1) {
     const int gs = ft.side == 0 ? n + 1 : 2;
     for (int w = threadIdx.x; w < 2 * n * n * 5; w += blockDim.x) {
@@ -53,8 +58,10 @@ __device__ __forceinline__ void level_face(const InterfaceArgs &a, int c, const 
       sr[ax] = gs;
       sr[t0] = p / 2 + 1 + o0;
       sr[t1] = q / 2 + 1 + o1;
-      U[5 * cell_index(S, c, d[0], d[1], d[2]) + v] =
-          U[5 * cell_index(S, ft.src, sr[0], sr[1], sr[2]) + v];
+      const size_t od = 5 * cell_index(S, c, d[0], d[1], d[2]) + v;
+      const size_t os = 5 * cell_index(S, ft.src, sr[0], sr[1], sr[2]) + v;
+      U[od] = U[os];
+      if (M) M[od] = M[os];
     }
   } else {
     for (int w = threadIdx.x; w < 2 * h * h * 5; w += blockDim.x) {
@@ -77,7 +84,9 @@ __device__ __forceinline__ void level_face(const InterfaceArgs &a, int c, const 
       sum = sum + B[si + sk];
       sum = sum + B[sj + sk];
       sum = sum + B[si + sj + sk];
-      U[5 * cell_index(S, c, d[0], d[1], d[2]) + v] = 0.125 * sum;
+      const size_t od = 5 * cell_index(S, c, d[0], d[1], d[2]) + v;
+      U[od] = 0.125 * sum;
+      if (M) M[od] = mirror_value(0.125 * sum, v, r0, e0);
     }
   }
 }
@@ -101,10 +110,13 @@ __global__ void __launch_bounds__(kHaloThreads) k_iface_faces(InterfaceArgs a) {
     level_face(a, c, ft);
     return;
   }
-  // Copies move 16-byte pairs of doubles: S is even, so every row below
-  // starts at an even cell index (an even double index) and is 5n or 10
-  // doubles long (n is a multiple of 4).
+  // Copies move pairs of values (16-byte pairs of doubles, 8-byte pairs of
+  // mirror floats): S is even, so every row below starts at an even cell
+  // index (an even value index) and is 5n or 10 values long (n is a multiple
+  // of 4).  The mirror (split precision) is copied like the state: an exact
+  // copy of a value has the same rounding.
   double2 *U2 = reinterpret_cast<double2 *>(U);
+  float2 *M2 = reinterpret_cast<float2 *>(mirror_current(a.mir));
   // Source (the neighbour's interior) and destination (this cube's ghost
   // layers) never overlap: each thread issues its loads for kBatch items
   // before storing them, so the copies are not a chain of round trips.
@@ -112,6 +124,7 @@ __global__ void __launch_bounds__(kHaloThreads) k_iface_faces(InterfaceArgs a) {
   auto copy = [&](int total, auto index) {
     for (int w0 = threadIdx.x; w0 < total; w0 += kBatch * kHaloThreads) {
       double2 u[kBatch];
+      float2 m[kBatch];
       size_t od[kBatch];
 #pragma unroll
       for (int b = 0; b < kBatch; ++b) {
@@ -120,11 +133,15 @@ __global__ void __launch_bounds__(kHaloThreads) k_iface_faces(InterfaceArgs a) {
           size_t os;
           index(w, od[b], os);
           u[b] = U2[os];
+          if (M2) m[b] = M2[os];
         }
       }
 #pragma unroll
       for (int b = 0; b < kBatch; ++b)
-        if (w0 + b * kHaloThreads < total) U2[od[b]] = u[b];
+        if (w0 + b * kHaloThreads < total) {
+          U2[od[b]] = u[b];
+          if (M2) M2[od[b]] = m[b];
+        }
     }
   };
   if (ax < 2) {
@@ -159,7 +176,16 @@ __global__ void __launch_bounds__(1024) k_iface_edges(InterfaceArgs a) {
   const int c = blockIdx.x + 1;
   if (!case_active(a.bt, c)) return;
   double *U = a.U1_;
+  float *M = mirror_current(a.mir);
+  double r0 = 0, e0 = 0;
+  if (M) mirror_base(a.mir, a.bt, c, r0, e0);
   auto Q = [&](int i, int j, int k) { return U + 5 * cell_index(S, c, i, j, k); };
+  // average of two face ghosts into an edge ghost, and its mirror value
+  auto avg = [&](double *d, const double *x, const double *y, int v) {
+    const double r = 0.5 * (x[v] + y[v]);
+    d[v] = r;
+    if (M) M[(d - U) + v] = mirror_value(r, v, r0, e0);
+  };
   // Phase 1: i-edges, i = 2..nx.
   for (int w = threadIdx.x; w < 4 * n * 5; w += blockDim.x) {
     const int v = w % 5, e = (w / 5) % 4, i = 2 + (w / 20);
@@ -169,7 +195,7 @@ __global__ void __launch_bounds__(1024) k_iface_edges(InterfaceArgs a) {
     else if (e == 1) { d = Q(i, nyy, 1); x = Q(i, nyy, 2); y = Q(i, nx, 1); }
     else if (e == 2) { d = Q(i, 1, nyy); x = Q(i, 1, nx); y = Q(i, 2, nyy); }
     else { d = Q(i, nyy, nyy); x = Q(i, nyy, nx); y = Q(i, nx, nyy); }
-    d[v] = 0.5 * (x[v] + y[v]);
+    avg(d, x, y, v);
   }
   __syncthreads();
   // Phase 2: j-edges, j = 1..nyy.
@@ -181,7 +207,7 @@ __global__ void __launch_bounds__(1024) k_iface_edges(InterfaceArgs a) {
     else if (e == 1) { d = Q(1, j, nyy); x = Q(2, j, nyy); y = Q(1, j, nx); }
     else if (e == 2) { d = Q(nyy, j, 1); x = Q(nx, j, 1); y = Q(nyy, j, 2); }
     else { d = Q(nyy, j, nyy); x = Q(nx, j, nyy); y = Q(nyy, j, nx); }
-    d[v] = 0.5 * (x[v] + y[v]);
+    avg(d, x, y, v);
   }
   __syncthreads();
   // Phase 3: k-edges, k = 1..nyy.
@@ -193,7 +219,7 @@ __global__ void __launch_bounds__(1024) k_iface_edges(InterfaceArgs a) {
     else if (e == 1) { d = Q(1, nyy, k); x = Q(2, nyy, k); y = Q(1, nx, k); }
     else if (e == 2) { d = Q(nyy, 1, k); x = Q(nx, 1, k); y = Q(nyy, 2, k); }
     else { d = Q(nyy, nyy, k); x = Q(nx, nyy, k); y = Q(nyy, nx, k); }
-    d[v] = 0.5 * (x[v] + y[v]);
+    avg(d, x, y, v);
   }
 }
 
@@ -226,6 +252,9 @@ __global__ void __launch_bounds__(kBcThreads) k_bc(BcArgs a) {
   const int m = a.masks[blockIdx.x];
   const int T = (S + gridDim.y - 1) / gridDim.y, i0 = blockIdx.y * T, i1 = min(S, i0 + T);
   double *U = a.U1_;
+  float *M = mirror_current(a.mir);  // split precision: mirror values of every write
+  double r0 = 0, e0 = 0;
+  if (M) mirror_base(a.mir, a.bt, c, r0, e0);
   auto Q = [&](int i, int j, int k) { return U + 5 * cell_index(S, c, i, j, k); };
   auto at = [&](int i, int j, int k) { return (size_t)5 * cell_index(S, c, i, j, k); };
   // Zero-gradient and slip faces: both ghost layers take one interior value.
@@ -253,6 +282,11 @@ __global__ void __launch_bounds__(kBcThreads) k_bc(BcArgs a) {
         if (w0 + b * kBcThreads < total) {
           U[d1[b]] = x[b];
           U[d0[b]] = x[b];
+          if (M) {
+            const float m = mirror_value(x[b], (int)(d1[b] % 5), r0, e0);
+            M[d1[b]] = m;
+            M[d0[b]] = m;
+          }
         }
     }
   };
@@ -271,6 +305,14 @@ __global__ void __launch_bounds__(kBcThreads) k_bc(BcArgs a) {
         double *d1 = Q(1, j, k), *d0 = Q(0, j, k);
 #pragma unroll
         for (int v = 0; v < 5; ++v) { d1[v] = o[v]; d0[v] = o[v]; }
+        if (M) {
+#pragma unroll
+          for (int v = 0; v < 5; ++v) {
+            const float m = mirror_value(o[v], v, r0, e0);
+            M[(d1 - U) + v] = m;
+            M[(d0 - U) + v] = m;
+          }
+        }
       }
     }
     if ((m & 2) && i1 == S)  // x upper: zero gradient (:85-118)
@@ -429,9 +471,16 @@ __global__ void k_ghost(GhostArgs a, int count) {
     o[3] = r2 * W2;
     o[4] = p2 / (BCMG_K - 1) + 0.5 * r2 * VV2;
   }
-  double *g = a.U1_ + 5 * cell_index(S, gc, gi, gj, gk);
+  const size_t go = 5 * cell_index(S, gc, gi, gj, gk);
+  double *g = a.U1_ + go;
 #pragma unroll
   for (int v = 0; v < 5; ++v) g[v] = o[v];
+  if (float *M = mirror_current(a.mir)) {
+    double r0, e0;
+    mirror_base(a.mir, a.bt, gc, r0, e0);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) M[go + v] = mirror_value(o[v], v, r0, e0);
+  }
 }
 
 cudaError_t launch_ghost(const GhostArgs &a, int count, cudaStream_t s) {

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include "bcm_common.cuh"
+#include "bcm_mirror.cuh"
 
 extern "C" void bcmg_internal_set_error(const char *msg);
 
@@ -17,6 +18,7 @@ namespace bcmg {
 // copies for the split path are formed once on the host.
 struct CaseConst {
   double mu_L, rho0, U0, Uin, P0;
+  double E0;  // P0 / (K - 1), the energy of the mirror's reference state
   double dT, dTau, e;
   int mpi_ncube;
   float ef, rho0f, P0f, RT0f, T0f, mu_Lf, i2dtf, dTf, dTauf;
@@ -37,6 +39,20 @@ __device__ __forceinline__ int case_of(const Batch &bt, int cube) {
 __device__ __forceinline__ bool case_active(const Batch &bt, int cube) {
   return !bt.active || bt.active[case_of(bt, cube)] != 0;
 }
+#ifdef __CUDACC__
+// Reference state (rho0, E0 = P0/(K-1)) of the mirror deltas of a cube.
+__device__ __forceinline__ void mirror_base(const Mirror &m, const Batch &bt, int cube,
+                                            double &rho0, double &E0) {
+  if (bt.cube_case) {
+    const CaseConst &q = bt.cases[bt.cube_case[cube]];
+    rho0 = q.rho0;
+    E0 = q.E0;
+  } else {
+    rho0 = m.rho0;
+    E0 = m.E0;
+  }
+}
+#endif
 
 struct FluxArgs {
   Phys ph;
@@ -68,7 +84,11 @@ struct FluxSplitArgs {
   const float *inv_dx;  // [ncube] n / cube_size
   const int *FWS;
   const double *cube_size;
-  const float *M;  // FP32 deltas of U1_ (k_mirror)
+  // FP32 deltas of U1_: the kernel reads the current buffer; at stages 1..3
+  // it writes the deltas of every interior cell of its tile (updated or
+  // not) and of the same-level ghost layers it pushes into the other buffer
+  // (launch_mirror_flip then makes that one current).
+  Mirror mir;
   double *U1_;     // updated in place for the CTA's own cells
   const double *U1, *U1q;
   const float *D2;  // FP32 of the FP64 difference U1 - U1q (k_level_diff)
@@ -90,8 +110,11 @@ struct FluxSplitArgs {
 int flux_tile(int n, int tile);
 // Blocks of one split flux launch over ncubes cubes (one per tile).
 int flux_split_blocks(int n, int ncubes, int tile = 0);
-cudaError_t launch_mirror(const double *U, float *M, int n, int ncube, double rho0, double P0,
-                          const Batch &bt, cudaStream_t s);
+// Full mirror of U into M0 and, when not null, M1 (all cells of all cubes).
+cudaError_t launch_mirror(const double *U, float *M0, float *M1, int n, int ncube, double rho0,
+                          double P0, const Batch &bt, cudaStream_t s);
+// Makes the other mirror buffer current (after an RK-stage flux launch).
+cudaError_t launch_mirror_flip(int *parity, cudaStream_t s);
 cudaError_t launch_flux_split(const FluxSplitArgs &a, int ncubes, cudaStream_t s);
 cudaError_t launch_level_diff(const double *U1, const double *U1q, float *D2, int n, int ncube,
                               cudaStream_t s);
@@ -154,7 +177,7 @@ struct LusgsSplitArgs {
   float rho0f, P0f, T0f, mu_Lf;
   const int *FWS;
   const float *inv_dx;     // [ncube] n / cube_size
-  const float *M;          // FP32 deltas of the state
+  Mirror mir;              // FP32 deltas of the state: read and updated in place
   double *U1_;             // updated in place on fluid cells
   const float *R32;        // residual (FP32) of every cell
   float *scr;              // [ncube-1][11][n^3] sweep scratch (lusgs_split_scratch)
@@ -194,6 +217,7 @@ struct InterfaceArgs {
   const FaceTask *tasks;  // [ntasks]
   double *U1_;
   Batch bt;
+  Mirror mir;  // split precision: every written cell's mirror value too
 };
 cudaError_t launch_interface(const InterfaceArgs &a, int ndst, cudaStream_t s);
 
@@ -208,6 +232,7 @@ struct BcArgs {
   int axes;
   double *U1_;
   Batch bt;  // batches: Uin of the cube's case
+  Mirror mir;  // split precision: every written cell's mirror value too
 };
 cudaError_t launch_bc(const BcArgs &a, int ncubes, cudaStream_t s);
 
@@ -221,6 +246,7 @@ struct GhostArgs {
   const int *IPsur;        // 1-based packed [4*nbc+1]
   double *U1_;
   Batch bt;  // batches: rho0, P0 of the ghost cell's case
+  Mirror mir;  // split precision: the ghost cell's mirror value too
 };
 cudaError_t launch_ghost(const GhostArgs &a, int count, cudaStream_t s);
 

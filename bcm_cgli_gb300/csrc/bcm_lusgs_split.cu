@@ -90,10 +90,17 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 448 ? 2 : 1) k_lusgs_split(Lusgs
   const int cube = 1 + blockIdx.x;
   if (!case_active(a.bt, cube)) return;  // converged case
   float dT = a.dTf, mu_L = a.mu_Lf, rho0 = a.rho0f, P0 = a.P0f, T0 = a.T0f;
+  double rho0d = a.mir.rho0, E0d = a.mir.E0;  // mirror reference state (FP64)
   if (a.bt.cube_case) {
     const CaseConst *q = a.bt.cases + a.bt.cube_case[cube];
     dT = q->dTf; mu_L = q->mu_Lf; rho0 = q->rho0f; P0 = q->P0f; T0 = q->T0f;
+    rho0d = q->rho0; E0d = q->E0;
   }
+  // The mirror of the state, read by the pack and updated in place with the
+  // state: this block reads only its own cube's interior cells of it, and
+  // writes those and (same-level pushes) other cubes' ghost cells, which no
+  // block of this launch reads.
+  float *const Mc = mirror_current(a.mir);
   const float omega = a.omegaf, cfl = a.cflf;
   const float idx = a.inv_dx[cube];
   const size_t cb = cell_index(S, cube, 0, 0, 0);
@@ -153,7 +160,7 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 448 ? 2 : 1) k_lusgs_split(Lusgs
       const size_t o = cb + ((size_t)(i + 2) * S + (j + 2)) * S + (k + 2);
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
-        stage[v * nn + jk] = a.M[5 * o + v];
+        stage[v * nn + jk] = Mc[5 * o + v];
         stage[(5 + v) * nn + jk] = a.R32[5 * o + v];
       }
       stage[10 * nn + jk] = a.FWS[o] == kFluid ? 1.f : 0.f;
@@ -310,20 +317,26 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 448 ? 2 : 1) k_lusgs_split(Lusgs
       float dq[5];
 #pragma unroll
       for (int v = 0; v < 5; ++v) dq[v] = stage[v * nn + jk];
-      double un[5];
-#pragma unroll
-      for (int v = 0; v < 5; ++v) {
-        un[v] = a.U1_[5 * o + v] + (double)dq[v];
-        a.U1_[5 * o + v] = un[v];
-      }
-      // Same-level interface copy of this cell, done here: no block reads
-      // the FP64 state of another cube during the sweep.
-      if (a.push) push_same_level(a.U1_, a.push, n, cube, i + 2, j + 2, k + 2, un);
-      const float *mm_ = a.M + 5 * o;
+      float *mm_ = Mc + 5 * o;
       const float rf = rho0 + mm_[0];
       const float m1 = mm_[1], m2 = mm_[2], m3 = mm_[3];
       const float mm = m1 * m1 + m2 * m2 + m3 * m3;
       const float Pc = P0 + (mm_[4] - 0.5f * mm / rf) * 0.4f;
+      double un[5];
+      float mn[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        un[v] = a.U1_[5 * o + v] + (double)dq[v];
+        a.U1_[5 * o + v] = un[v];
+        mn[v] = mirror_value(un[v], v, rho0d, E0d);
+        mm_[v] = mn[v];
+      }
+      // Same-level interface copy of this cell (state and mirror), done
+      // here: no block reads another cube's cells during the sweep.
+      if (a.push) {
+        push_same_level(a.U1_, a.push, n, cube, i + 2, j + 2, k + 2, un);
+        push_same_level(Mc, a.push, n, cube, i + 2, j + 2, k + 2, mn);
+      }
       const float dr = dq[0], e1 = dq[1], e2 = dq[2], e3 = dq[3], dE = dq[4];
       const float den = 1.0f / (rf * (rf + dr));
       const float dU = (e1 * rf - m1 * dr) * den;

@@ -638,11 +638,11 @@ def run_gpu_arm(args, dist):
 
 def run_flux_only(args):
     """Profiling target: the flux kernel alone on a Taylor-Green case of
-    ncx^3 cubes of 24^3 cells (ncx=6: 216 cubes, 3.0 M cells, 190 MB per
+    ncx^3 cubes of n^3 cells (ncx=6, n=24: 216 cubes, 3.0 M cells, 190 MB per
     state array, above the 129 MB L2), one warm-up launch and `steps` timed
     launches.  Used by the ncu commands recorded under profiles/."""
     from bcm_cgli_gb300 import api, cases
-    case = cases.taylor_green(ncx=args.ncx, n=24)
+    case = cases.taylor_green(ncx=args.ncx, n=args.n)
     prec = api.PRECISION_SPLIT if args.precision == "split" else api.PRECISION_FP64
     ctx = api.CaseContext(case, precision=prec)
     ctx.set_state(case.U, case.U, case.U)
@@ -654,10 +654,10 @@ def run_flux_only(args):
 
 def run_lusgs_only(args):
     """Profiling target: LU-SGS sub-iterations (residual + sweeps) on a
-    Taylor-Green case of ncx^3 cubes of 24^3 cells, `steps` sub-iterations
+    Taylor-Green case of ncx^3 cubes of n^3 cells, `steps` sub-iterations
     after one warm-up step."""
     from bcm_cgli_gb300 import api, cases
-    case = cases.taylor_green(ncx=args.ncx, n=24)
+    case = cases.taylor_green(ncx=args.ncx, n=args.n)
     prec = api.PRECISION_SPLIT if args.precision == "split" else api.PRECISION_FP64
     ctx = api.CaseContext(case, precision=prec)
     ctx.set_method(api.METHOD_LUSGS)
@@ -694,6 +694,8 @@ def main():
                     help="LU-SGS sub-iterations alone on a smaller case (profiling target)")
     ap.add_argument("--ncx", type=int, default=6,
                     help="cubes per edge for --flux-only / --lusgs-only")
+    ap.add_argument("--n", type=int, default=24,
+                    help="cells per cube edge for --flux-only / --lusgs-only")
     ap.add_argument("--method", default="rk3", choices=["rk3", "lusgs"],
                     help="sub-iteration method (rk3: the reference's RK; lusgs: LU-SGS sweeps)")
     ap.add_argument("--workload", default="batch", choices=sorted(WORKLOADS),

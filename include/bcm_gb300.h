@@ -253,6 +253,10 @@ int bcmg_case_output_wait(bcmg_case *c);
  * deltas from each case's reference state (rho0, 0, 0, 0, P0/(K-1)) that the
  * flux kernel reads) and copies it to M[ncell][5] on the host, for checks. */
 int bcmg_case_mirror(bcmg_case *c, float *M);
+/* The mirror as the kernels keep it during stepping (the current buffer,
+ * not re-formed), for checks: it equals the rounding of the current state
+ * in every cell. */
+int bcmg_case_mirror_current(bcmg_case *c, float *M);
 
 /* Launch shapes.  flux_tile: edge of the cube tile one flux CTA works on,
  * 8 or 4 (0: 8 when it divides n, else 4); lusgs_threads: threads per cube
@@ -282,6 +286,16 @@ int bcmg_case_autotune(bcmg_case *c, int reps, bcmg_tuning *out);
  * that interface call.  Both give the same bits.  No effect on the FP64
  * path. */
 int bcmg_case_set_face_copies(bcmg_case *c, int in_flux);
+
+/* Split-precision path: how the FP32 mirror of the state (the deltas the
+ * flux and LU-SGS kernels read) is kept.  on = 0 (default): formed whole
+ * once per dual-time step (and per bcmg_case_stage call); within the step
+ * every kernel that writes the state writes the mirror values of the cells
+ * it writes (the flux kernel into a second buffer, since other blocks read
+ * its cells' old values during the launch).  on = 1: formed whole before
+ * every flux launch instead (a pass over every cell; for checks).  Both
+ * give the same bits.  No effect on the FP64 path. */
+int bcmg_case_set_mirror_each_stage(bcmg_case *c, int on);
 
 /* Waits for all work of the context. */
 int bcmg_case_sync(bcmg_case *c);

@@ -38,6 +38,14 @@ RUN_STEPS = 2
 RUN_SUBITERS = 2
 
 
+def horizon_cases():
+    """(case, steps, sub-iterations) of the long-run records: the inviscid
+    isentropic vortex of 4x4x4 cubes of 16^3 cells (262,144 cells, Mach 0.5,
+    strength 5, dT = 1e-3) over its whole run of 100 dual-time steps x 10
+    RK sub-iterations."""
+    return {"vortex_full": (cases.isentropic_vortex(ncx=4, n=16, dT=1e-3), 100, 10)}
+
+
 def ibm_cases():
     """(case, triangles) pairs for the IBM preprocessing fixtures: a sphere of
     diameter 1 on a two-level grid of n=8 cubes (fine cubes of edge 1, cells

@@ -7,6 +7,7 @@ output array plus the norms.  Run here, where the reference sources exist:
 
     python tests/golden/make_golden.py            # everything
     python tests/golden/make_golden.py --ibm-only # the IBM preprocessing records
+    python tests/golden/make_golden.py --horizon  # the long-run records only
 """
 import hashlib
 import json
@@ -21,7 +22,8 @@ sys.path[:0] = [ROOT, os.path.join(ROOT, "oracle"), HERE]
 import numpy as np  # noqa: E402
 
 import oracle as O  # noqa: E402
-from golden_cases import RUN_STEPS, RUN_SUBITERS, canonical, golden_cases, ibm_cases  # noqa: E402
+from golden_cases import (RUN_STEPS, RUN_SUBITERS, canonical, golden_cases,  # noqa: E402
+                          horizon_cases, ibm_cases)
 from bcm_cgli_gb300 import cases as _cases  # noqa: E402
 
 
@@ -49,8 +51,33 @@ def ibm_records():
     return out
 
 
+def horizon_records():
+    """Digests of the state after the long runs of horizon_cases(): the
+    reference's own loop (one OpenMP thread) over every dual-time step and
+    sub-iteration of the configuration."""
+    out = {}
+    for name, (case, steps, subiters) in horizon_cases().items():
+        ref = O.Ref(case)
+        ref.set_threads(1)
+        st = O.State(case)
+        ref.run(case, st, steps, subiters)
+        out[name] = {"steps": steps, "subiters": subiters,
+                     "state": {k: digest(getattr(st, k)) for k in ("U1_", "U1", "U1q")},
+                     "er": [repr(float(x)) for x in st.er],
+                     "sum": [repr(float(x)) for x in st.U1_.reshape(-1, 5).sum(axis=0)]}
+        print(name, "done", file=sys.stderr)
+    return out
+
+
 def main():
     path = os.path.join(HERE, "golden.json")
+    if "--horizon" in sys.argv:
+        with open(path) as f:
+            doc = json.load(f)
+        doc["horizon"] = horizon_records()
+        with open(path, "w") as f:
+            json.dump(doc, f, indent=1)
+        return
     if "--ibm-only" in sys.argv:
         with open(path) as f:
             doc = json.load(f)
@@ -98,7 +125,7 @@ def main():
         json.dump({"generator": "tests/golden/make_golden.py (reference compiled by "
                                 "oracle/ref_build.py, OMP_NUM_THREADS=1)",
                    "steps": RUN_STEPS, "subiters": RUN_SUBITERS, "cases": out,
-                   "ibm": ibm_records()}, f, indent=1)
+                   "ibm": ibm_records(), "horizon": horizon_records()}, f, indent=1)
 
 
 if __name__ == "__main__":

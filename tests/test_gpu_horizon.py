@@ -1,0 +1,88 @@
+"""Parity and accuracy over whole runs, not just a few sub-iterations.
+
+* FP64: the inviscid isentropic vortex of 4x4x4 cubes of 16^3 cells over its
+  full run (100 dual-time steps x 10 RK sub-iterations, 262,144 cells) must
+  leave U1_, U1 and U1q bit for bit equal to the reference's own compiled
+  loop (SHA-256 digests in tests/golden/golden.json, made by
+  tests/golden/make_golden.py --horizon with one OpenMP thread).  Signed
+  zeros are folded to +0 before hashing (equal values).
+* Split precision against FP64 over 20 dual-time steps at benchmark size
+  (viscous Taylor-Green 8^3 cubes of 24^3 cells; sphere with IBM ghost
+  cells on two levels, 1,584 cubes of 16^3): relative L2 <= 1e-5 per
+  variable at every fifth step, drag within 0.1%, lift error within 0.1%
+  of the drag (a sphere's lift is ~0 here, so its own scale is noise).
+"""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from bcm_cgli_gb300 import api, cases
+from golden import golden_cases as G
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SPLIT_BOUND = 1e-5
+DRAG_BOUND = 1e-3
+ER_RTOL = 1e-10  # norms of the last sub-iteration: sum order differs from the reference's
+
+
+def _golden():
+    with open(os.path.join(HERE, "golden", "golden.json")) as f:
+        return json.load(f)
+
+
+def _digest(a):
+    return hashlib.sha256(G.canonical(a)).hexdigest()
+
+
+def test_vortex_full_run_equals_reference_bit_for_bit():
+    gold = _golden()["horizon"]["vortex_full"]
+    case, steps, subiters = G.horizon_cases()["vortex_full"]
+    assert (steps, subiters) == (gold["steps"], gold["subiters"])
+    ctx = api.CaseContext(case, precision=api.PRECISION_FP64)
+    ctx.set_state(case.U, case.U, case.U)
+    er = ctx.advance(steps, subiters, use_graph=True)
+    U1_, U1, U1q = ctx.get_state()
+    ctx.close()
+    for k, a in (("U1_", U1_), ("U1", U1), ("U1q", U1q)):
+        assert _digest(a) == gold["state"][k], k
+    ref_er = [float(x) for x in gold["er"]]
+    for m in range(1, 6):
+        assert abs(er[m] - ref_er[m]) <= ER_RTOL * max(abs(ref_er[m]), 1e-300), (m, er, ref_er)
+
+
+def _rel_l2(a, b, n):
+    ai = a[1:, 2:n + 2, 2:n + 2, 2:n + 2].reshape(-1, 5)
+    bi = b[1:, 2:n + 2, 2:n + 2, 2:n + 2].reshape(-1, 5)
+    d = ai - bi
+    mom = np.linalg.norm(bi[:, 1:4])
+    return [np.linalg.norm(d[:, 0]) / np.linalg.norm(bi[:, 0])] + \
+           [np.linalg.norm(d[:, v]) / mom for v in (1, 2, 3)] + \
+           [np.linalg.norm(d[:, 4]) / np.linalg.norm(bi[:, 4])]
+
+
+@pytest.mark.parametrize("workload", ["tgv", "sphere"])
+def test_split_within_bound_over_twenty_steps(workload):
+    case = (cases.taylor_green(ncx=8, n=24) if workload == "tgv"
+            else cases.sphere_ibm(preprocess=api.ibm_preprocess))
+    ctxs = {p: api.CaseContext(case, precision=p)
+            for p in (api.PRECISION_FP64, api.PRECISION_SPLIT)}
+    for c in ctxs.values():
+        c.set_state(case.U, case.U, case.U)
+    for block in range(4):  # 4 x 5 steps
+        ers, states = {}, {}
+        for p, c in ctxs.items():
+            ers[p] = c.advance(5, 10, use_graph=True)
+            states[p] = c.get_result()
+        err = _rel_l2(states[api.PRECISION_SPLIT], states[api.PRECISION_FP64], case.n)
+        assert max(err) <= SPLIT_BOUND, (5 * (block + 1), err)
+        if workload == "sphere":
+            a, b = ers[api.PRECISION_FP64], ers[api.PRECISION_SPLIT]
+            assert abs(b[6] - a[6]) <= DRAG_BOUND * abs(a[6]), (5 * (block + 1), a[6], b[6])
+            assert abs(b[7] - a[7]) <= DRAG_BOUND * abs(a[6]), (5 * (block + 1), a[7], b[7])
+    for c in ctxs.values():
+        c.close()

@@ -232,3 +232,72 @@ def test_mirror_is_the_ieee_rounding_of_the_deltas():
         assert np.array_equal(M[g:g + c.ncube - 1].view(np.uint32), ref.view(np.uint32))
         g += c.ncube - 1
     bt.close()
+
+
+def _state_mirror(U, members):
+    """numpy's IEEE rounding of the state's deltas, per case of a batch."""
+    out = np.empty(U.shape, np.float32)
+    g = 1
+    for c in members:
+        m = c.ncube - 1
+        out[g:g + m] = _mirror_ref(U[g:g + m], c.phys.rho0, c.phys.P0)
+        g += m
+    return out
+
+
+@pytest.mark.parametrize("name", sorted(_prologue_cases()))
+@pytest.mark.parametrize("method", ["rk3", "lusgs"])
+def test_kept_mirror_is_the_rounding_of_the_state(name, method):
+    """The mirror the kernels keep during stepping (one full pass per
+    dual-time step; the flux kernel, interface, boundary and IBM kernels and
+    the LU-SGS sweep write the values of the cells they change) equals the
+    IEEE rounding of the state in every cell after single stages, eager and
+    graph steps, and the state equals the one obtained with a full mirror
+    pass before every flux launch, bit for bit."""
+    case = _prologue_cases()[name]
+    states = []
+    for each_stage in (False, True):
+        ctx = api.CaseContext(case, precision=api.PRECISION_SPLIT)
+        if method == "lusgs":
+            ctx.set_method(api.METHOD_LUSGS)
+        ctx.set_mirror_each_stage(each_stage)
+        ctx.set_state(case.U, case.U, case.U)
+        if method == "rk3":
+            ctx.stage(1)
+            ctx.stage(2)
+        ctx.advance(1, 2, use_graph=False)
+        ctx.advance(2, 2, use_graph=True)
+        U = ctx.get_state()
+        if not each_stage:
+            M = ctx.mirror_current()
+            ref = _state_mirror(U[0], [case])
+            assert np.array_equal(M[1:].view(np.uint32), ref[1:].view(np.uint32))
+        states.append(U)
+        ctx.close()
+    for a, b in zip(*states):
+        assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
+def test_kept_mirror_batch_with_converged_cases():
+    """A batch whose cases converge at different sub-iterations (converged
+    cases sit out the rest of the step, then rejoin at the next): the kept
+    mirror still equals the rounding of the state, and the states equal
+    those of a full mirror pass before every flux launch."""
+    cs = [cases.taylor_green(ncx=2, n=8), cases.random_two_level_case(seed=6, n=8, periodic=False),
+          _prologue_cases()["sphere_two_level"]]
+    out = []
+    for each_stage in (False, True):
+        bt = api.BatchContext(cs, precision=api.PRECISION_SPLIT)
+        bt.set_mirror_each_stage(each_stage)
+        for q, c in enumerate(cs):
+            bt.set_case_state(q, c.U, c.U, c.U)
+        bt.advance(1, 2)
+        _, its = bt.advance_converged(2, 7, tol=0.5)
+        bt.advance(1, 1)
+        U = bt.get_state()[0]
+        if not each_stage:
+            M = bt.mirror_current()
+            assert np.array_equal(M[1:].view(np.uint32), _state_mirror(U, cs)[1:].view(np.uint32))
+        out.append(U)
+        bt.close()
+    assert np.array_equal(out[0][1:].view(np.uint64), out[1][1:].view(np.uint64))
