@@ -44,8 +44,8 @@ class CaseDesc(C.Structure):
 
 
 class Tuning(C.Structure):
-    _fields_ = [("flux_tile", C.c_int), ("lusgs_threads", C.c_int),
-                ("flux_ms", C.c_double * 2), ("lusgs_ms", C.c_double * 2)]
+    _fields_ = [("flux_tile", C.c_int), ("lusgs_threads", C.c_int), ("flux_form", C.c_int),
+                ("flux_ms", C.c_double * 3), ("lusgs_ms", C.c_double * 2)]
 
 
 class RefConfig(C.Structure):

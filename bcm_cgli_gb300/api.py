@@ -343,10 +343,11 @@ class CaseContext:
         check(lib().bcmg_case_output_x(self.h, int(q), int(ncube_out), os.fsencode(path),
                                        o.ctypes.data))
 
-    def set_tuning(self, flux_tile=0, lusgs_threads=0):
-        """Launch shapes: flux tile edge (0, 4 or 8) and threads per cube of the
-        split LU-SGS sweep (0: the widest plane)."""
-        t = _lib.Tuning(int(flux_tile), int(lusgs_threads))
+    def set_tuning(self, flux_tile=0, lusgs_threads=0, flux_form=0):
+        """Launch shapes: flux tile edge (0, 4 or 8), threads per cube of the
+        split LU-SGS sweep (0: the widest plane) and the split flux form on
+        8^3 tiles (1 packed face pairs, 2 one face at a time, 0 default)."""
+        t = _lib.Tuning(int(flux_tile), int(lusgs_threads), int(flux_form))
         check(lib().bcmg_case_set_tuning(self.h, C.byref(t)))
 
     def set_face_copies(self, in_flux=True):
@@ -368,7 +369,9 @@ class CaseContext:
         t = _lib.Tuning()
         check(lib().bcmg_case_autotune(self.h, int(reps), C.byref(t)))
         return {"flux_tile": t.flux_tile, "lusgs_threads": t.lusgs_threads,
-                "flux_ms": {"8": t.flux_ms[0], "4": t.flux_ms[1]},
+                "flux_form": t.flux_form,
+                "flux_ms": {"8_packed": t.flux_ms[0], "8_single": t.flux_ms[1],
+                            "4": t.flux_ms[2]},
                 "lusgs_ms": {"widest": t.lusgs_ms[0], "half": t.lusgs_ms[1]}}
 
     def mirror(self):

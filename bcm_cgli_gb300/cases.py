@@ -173,6 +173,24 @@ def _grid(case_geom, n):
     return X, Y, Z
 
 
+def exp_portable(x):
+    """exp(x) from IEEE additions, multiplications and exact scalings only,
+    so the same inputs give the same bits on every machine (numpy's exp and
+    pow differ in the last bit between x86 and Arm builds).  x = k ln2 + r
+    with |r| <= ln2/2 (ln2 split in a 32-bit head and its tail, so k ln2 is
+    exact), exp(r) by its Taylor series to r^16 in Horner form (truncation
+    below 1e-17 relative), times 2^k."""
+    x = np.asarray(x, dtype=np.float64)
+    ln2_hi = 0.693145751953125          # 22 significant bits: k * ln2_hi is exact
+    ln2_lo = 1.4286068203094172321e-06  # ln2 - ln2_hi
+    k = np.floor(x / 0.6931471805599453 + 0.5)
+    r = (x - k * ln2_hi) - k * ln2_lo
+    p = np.ones_like(r)
+    for m in range(16, 0, -1):
+        p = 1.0 + r * p / m
+    return np.ldexp(p, k.astype(np.int64))
+
+
 def isentropic_vortex(ncx=4, n=16, length=1.0, mach=0.5, strength=5.0, radius=0.1,
                       dT=1e-3, sub_ratio=200.0, name="vortex") -> Case:
     """Inviscid isentropic vortex in a periodic box (ncx^3 cubes of n^3 cells).
@@ -182,6 +200,9 @@ def isentropic_vortex(ncx=4, n=16, length=1.0, mach=0.5, strength=5.0, radius=0.
     of U0) and core radius `radius` centred in the box:
     u_theta = A r~ exp((1-r~^2)/2), A = beta U0 / (2 pi), r~ = r/radius;
     isentropic radial equilibrium gives T = T0 - A^2 exp(1-r~^2) / (2 cp).
+    The field is formed with IEEE arithmetic only (exp_portable; the density
+    power 1/(K-1) = 2.5 as t*t*sqrt(t)), so every machine builds the same
+    bits and results can be compared with records made elsewhere.
     """
     ph = Phys(mu_L=0.0, rho0=1.1842, P0=101300.0, mpi_ncube=ncx ** 3)
     c0 = np.sqrt(GAMMA * ph.P0 / ph.rho0)
@@ -193,14 +214,15 @@ def isentropic_vortex(ncx=4, n=16, length=1.0, mach=0.5, strength=5.0, radius=0.
     dyr = (Y - yc) / radius
     r2 = dxr * dxr + dyr * dyr
     A = strength * ph.U0 / (2 * np.pi)
-    g = np.exp(0.5 * (1 - r2))
+    g = exp_portable(0.5 * (1 - r2))
     u = ph.U0 - A * dyr * g
     v = A * dxr * g
     w = np.zeros_like(u)
     cp = CV * GAMMA
     T0 = ph.P0 / (ph.rho0 * R_GAS)
-    T = T0 - A * A * np.exp(1 - r2) / (2 * cp)
-    rho = ph.rho0 * (T / T0) ** (1.0 / (GAMMA - 1))
+    T = T0 - A * A * exp_portable(1 - r2) / (2 * cp)
+    t = T / T0
+    rho = ph.rho0 * (t * t * np.sqrt(t))  # (T/T0)^(1/(K-1)), K = 1.4
     p = rho * R_GAS * T
     U = conservative(rho, u, v, w, p)
     ncube, cube_size, csl, origin, adj = geom

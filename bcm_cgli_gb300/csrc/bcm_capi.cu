@@ -263,6 +263,7 @@ struct bcmg_case {
   // Launch shapes (bcmg_case_set_tuning / bcmg_case_autotune): flux tile
   // edge (0: default) and threads per cube of the split LU-SGS sweep.
   int tile = 0, lu_threads = 0;
+  int form = 0;  // split flux on 8^3 tiles: 0 default (packed pairs), 1 packed, 2 one face at a time
   double lu_cfl = 0.0, lu_omega = 1.5;
   // Convergence-driven stepping (bcmg_case_advance_converged)
   bool conv = false;                 // kernels see the active masks
@@ -409,6 +410,7 @@ int case_flux(bcmg_case *c, int RK) {
     // path does not otherwise use
     sa.R32 = reinterpret_cast<float *>(c->Rku1);
     sa.tile = c->tile;
+    sa.form = c->form == 2 ? 0 : 1;
     sa.partials = c->partials;
     sa.Residual1 = c->Residual1;
     sa.bt = c->bt();
@@ -1684,9 +1686,14 @@ int bcmg_case_set_tuning(bcmg_case *c, const bcmg_tuning *t) {
     set_err("lusgs_threads must be 0 or a multiple of 32 up to the widest plane of a cube");
     return BCMG_ERR_ARG;
   }
+  if (t->flux_form < 0 || t->flux_form > 2) {
+    set_err("flux_form must be 0, 1 or 2");
+    return BCMG_ERR_ARG;
+  }
   const int old_tiles = flux_split_blocks(n, 1, c->tile);
   c->tile = t->flux_tile;
   c->lu_threads = t->lusgs_threads;
+  c->form = t->flux_form;
   const int tiles = flux_split_blocks(n, 1, c->tile);
   if (c->batched && tiles != old_tiles) {
     std::vector<int> cbf(c->ncase + 1);
@@ -1733,14 +1740,18 @@ int bcmg_case_autotune(bcmg_case *c, int reps, bcmg_tuning *out) {
   bcmg_tuning best{};
   best.flux_tile = c->tile;
   best.lusgs_threads = c->lu_threads;
-  // Flux: tile edges 8 and 4 (8 only when it divides n), timed on the
+  best.flux_form = c->form;
+  // Flux: tile 8 with packed face pairs, tile 8 one face at a time (the two
+  // forms differ on the split path only), tile 4; each timed on the
   // context's own state (bcmg_case_time_flux restores it).
-  const int tiles[2] = {8, 4};
+  const int tiles[3] = {8, 8, 4}, forms[3] = {1, 2, 0};
   double best_ms = 1e300;
-  for (int v = 0; v < 2; ++v) {
+  for (int v = 0; v < 3; ++v) {
     if (n % tiles[v] != 0) continue;
+    if (v == 1 && c->precision != BCMG_PRECISION_SPLIT) continue;
     bcmg_tuning t = best;
     t.flux_tile = tiles[v];
+    t.flux_form = forms[v];
     int r = bcmg_case_set_tuning(c, &t);
     if (r) return r;
     double ms = 0;
@@ -1749,7 +1760,12 @@ int bcmg_case_autotune(bcmg_case *c, int reps, bcmg_tuning *out) {
     if (ms < best_ms) {
       best_ms = ms;
       best.flux_tile = tiles[v];
+      best.flux_form = forms[v];
     }
+  }
+  {
+    int r = bcmg_case_set_tuning(c, &best);  // the LU-SGS candidates run on the chosen flux
+    if (r) return r;
   }
   // Split LU-SGS sweep: the widest plane's threads or half of them (wide
   // planes then take two passes), timed on the residual of the current

@@ -245,6 +245,96 @@ __device__ __forceinline__ void face_flux_delta(const float *ML, const float *MR
   dPp = 0.5f * (_pp + pp_);
 }
 
+// Packed FP32 pairs: Blackwell's FFMA2 / FADD2 / FMUL2 do the arithmetic of
+// two independent evaluations (lane .x and lane .y) in one instruction, so
+// a thread evaluating two faces at once issues about half the FP32
+// instructions.  Subtraction is a - b = fma(b, -1, a) (exact: b * -1 is
+// exact); reciprocals and square roots stay per lane (no packed form).
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+  return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 rcp2(float2 a) { return make_float2(1.0f / a.x, 1.0f / a.y); }
+__device__ __forceinline__ float2 sqrt2(float2 a) { return make_float2(sqrtf(a.x), sqrtf(a.y)); }
+
+// face_flux_delta for two faces of one axis at once (same formulas; lane .x
+// and .y are the two faces).
+template <int AX>
+__device__ __forceinline__ void face_flux_delta2(const float2 *ML, const float2 *MR, float e,
+                                                 float rho0, float P0, float2 *F, float2 &dPp) {
+  const float2 K = f2(1.4f), Km1 = f2(0.4f), half = f2(0.5f);
+  const float2 dU1 = sub2(MR[0], ML[0]), dU2 = sub2(MR[1], ML[1]), dU3 = sub2(MR[2], ML[2]),
+               dU4 = sub2(MR[3], ML[3]), dU5 = sub2(MR[4], ML[4]);
+  const float2 r0 = f2(rho0), p0 = f2(P0);
+  const float2 _rho = add2(r0, ML[0]);
+  const float2 _ir = rcp2(_rho);
+  const float2 _U = mul2(ML[1], _ir), _V = mul2(ML[2], _ir), _W = mul2(ML[3], _ir);
+  const float2 _VV = fma2(_W, _W, fma2(_V, _V, mul2(_U, _U)));
+  const float2 _pp = mul2(fma2(mul2(f2(-0.5f), _rho), _VV, ML[4]), Km1);
+  const float2 _P = add2(p0, _pp);
+  const float2 _C = mul2(mul2(K, _P), _ir);
+  const float2 _H = fma2(_C, f2(2.5f), mul2(half, _VV));
+  const float2 rho_ = add2(r0, MR[0]);
+  const float2 ir_ = rcp2(rho_);
+  const float2 U_ = mul2(MR[1], ir_), V_ = mul2(MR[2], ir_), W_ = mul2(MR[3], ir_);
+  const float2 VV_ = fma2(W_, W_, fma2(V_, V_, mul2(U_, U_)));
+  const float2 pp_ = mul2(fma2(mul2(f2(-0.5f), rho_), VV_, MR[4]), Km1);
+  const float2 P_ = add2(p0, pp_);
+  const float2 C_ = mul2(mul2(K, P_), ir_);
+  const float2 H_ = fma2(C_, f2(2.5f), mul2(half, VV_));
+  const float2 temp5 = sqrt2(_rho), temp6 = sqrt2(rho_);
+  const float2 it4 = rcp2(add2(temp5, temp6));
+  const float2 rho = mul2(temp5, temp6);
+  const float2 U = mul2(fma2(temp6, U_, mul2(temp5, _U)), it4);
+  const float2 V = mul2(fma2(temp6, V_, mul2(temp5, _V)), it4);
+  const float2 W = mul2(fma2(temp6, W_, mul2(temp5, _W)), it4);
+  const float2 VV = fma2(W, W, fma2(V, V, mul2(U, U)));
+  const float2 H = mul2(fma2(temp6, H_, mul2(temp5, _H)), it4);
+  const float2 C = mul2(fma2(f2(-0.5f), VV, H), Km1);
+  const float2 q = mul2(VV, rcp2(C));
+  const float2 beta = make_float2(fmaxf(q.x, e), fmaxf(q.y, e));
+  const float2 un = AX == 0 ? U : (AX == 1 ? V : W);
+  const float2 _un = AX == 0 ? _U : (AX == 1 ? _V : _W);
+  const float2 un_ = AX == 0 ? U_ : (AX == 1 ? V_ : W_);
+  const float2 omb = sub2(f2(1.0f), beta);
+  const float2 temp = mul2(mul2(half, add2(f2(1.0f), beta)), un);
+  const float2 Sp = mul2(half, sqrt2(fma2(mul2(f2(4.0f), beta), C, mul2(mul2(un, un), mul2(omb, omb)))));
+  const float2 iS = rcp2(Sp);
+  const float2 dp = sub2(pp_, _pp);
+  const float2 temp1 = mul2(dp, rcp2(mul2(mul2(rho, beta), C)));
+  const float2 tS = mul2(temp, iS);
+  const float2 dun = sub2(un_, _un);
+  const float2 temp2 = mul2(tS, dun);
+  const float2 temp3 = mul2(mul2(mul2(mul2(half, omb), un), temp), iS);
+  const float2 an = make_float2(fabsf(un.x), fabsf(un.y));
+  const float2 deltaU = fma2(sub2(sub2(Sp, temp3), mul2(beta, an)), temp1, temp2);
+  const float2 deltaP = fma2(mul2(add2(sub2(Sp, an), temp3), rho), dun, mul2(tS, dp));
+  const float2 dr = mul2(deltaU, rho);
+  float2 Fav1 = fma2(an, dU1, dr);
+  float2 Fav2 = fma2(an, dU2, mul2(dr, U));
+  float2 Fav3 = fma2(an, dU3, mul2(dr, V));
+  float2 Fav4 = fma2(an, dU4, mul2(dr, W));
+  if (AX == 0) Fav2 = add2(Fav2, deltaP);
+  if (AX == 1) Fav3 = add2(Fav3, deltaP);
+  if (AX == 2) Fav4 = add2(Fav4, deltaP);
+  const float2 Fav5 = fma2(deltaP, un, fma2(an, dU5, mul2(dr, H)));
+  const float2 _rhoun = mul2(_rho, _un), rhoun_ = mul2(rho_, un_);
+  F[0] = mul2(half, sub2(add2(_rhoun, rhoun_), Fav1));
+  F[1] = AX == 0 ? mul2(half, sub2(add2(fma2(_rhoun, _U, _pp), fma2(rhoun_, U_, pp_)), Fav2))
+                 : mul2(half, sub2(fma2(rhoun_, U_, mul2(_rhoun, _U)), Fav2));
+  F[2] = AX == 1 ? mul2(half, sub2(add2(fma2(_rhoun, _V, _pp), fma2(rhoun_, V_, pp_)), Fav3))
+                 : mul2(half, sub2(fma2(rhoun_, V_, mul2(_rhoun, _V)), Fav3));
+  F[3] = AX == 2 ? mul2(half, sub2(add2(fma2(_rhoun, _W, _pp), fma2(rhoun_, W_, pp_)), Fav4))
+                 : mul2(half, sub2(fma2(rhoun_, W_, mul2(_rhoun, _W)), Fav4));
+  const float2 EL = fma2(mul2(half, _rho), _VV, mul2(f2(3.5f), _P));
+  const float2 ER = fma2(mul2(half, rho_), VV_, mul2(f2(3.5f), P_));
+  F[4] = mul2(half, sub2(fma2(un_, ER, mul2(_un, EL)), Fav5));
+  dPp = mul2(half, add2(_pp, pp_));
+}
+
 template <int AX, bool FWD>
 __device__ __forceinline__ void visc_face_f(float mu_L, float T0, const PrimF &c, const PrimF &o,
                                             float inv, const PrimF &a0, const PrimF &a1,
@@ -342,9 +432,13 @@ __device__ __forceinline__ void recon_split(int ord, Ld ld, float *ML, float *MR
   }
 }
 
-template <int T, bool VISCOUS>
+// PACK (8^3 tiles only): each thread evaluates its two faces of an axis
+// together in packed FP32 pairs; otherwise one after the other.
+template <int T, bool VISCOUS, bool PACK>
 __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
     k_flux_split(FluxSplitArgs a) {
+  static_assert(!PACK || (T == 8 && 2 * split_threads<T>() == (T + 1) * T * T),
+                "packed face pairs: two faces of an axis per thread");
   using SM = SplitSmem<T>;
   constexpr int B = SM::B;
   constexpr int X = SM::X;
@@ -467,40 +561,76 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
   // The three axes are unrolled: every axis-dependent index, stride and
   // flux variant is then a compile-time choice (6% of the launch on the
   // 7 M-cell TGV case, measured).
+  // One face f of axis ax: reconstruction order of the stored view, the
+  // left/right states, the second-view bit; returns the face's slot.
+  auto face_prep = [&](int ax, int f, float *ML, float *MR) -> int {
+    const int fa = f / (T * T), p = (f / T) % T, q = f % T;
+    int li, lj, lk;  // a warp covers 4 x 8 faces of a plane (8 x 4 for z-faces)
+    if (ax == 0) { li = fa; lj = p; lk = q; }
+    else if (ax == 1) { li = p; lj = fa; lk = q; }
+    else { li = q; lj = p; lk = fa; }
+    const int g = (ax == 0 ? bi + li : (ax == 1 ? bj + lj : bk + lk));
+    const int di = ax == 0, dj = ax == 1, dk = ax == 2;
+    const int fm2 = FL(li - 2 * di, lj - 2 * dj, lk - 2 * dk),
+              fm1 = FL(li - di, lj - dj, lk - dk), f0 = FL(li, lj, lk),
+              fp1 = FL(li + di, lj + dj, lk + dk);
+    const bool needB = fa < T, needF = fa > 0;
+    const int ob = order_backward(g, fm2, fm1, fp1);
+    const int of = order_forward(g, nx, fm2, f0, fp1);
+    const float *base = BX(li, lj, lk);
+    const int sstride = ax == 0 ? SM::PP : (ax == 1 ? SM::RP : 5);
+    auto ld = [&](int d, int v) -> float { return base[sstride * d + v]; };
+    // The stored view is the plus-side cell's (the minus-side cell's for
+    // the last face, which has no plus cell in the tile); where the
+    // minus-side cell's order differs it recomputes its own view.
+    recon_split(needB ? ob : of, ld, ML, MR);
+    const int fi = face_idx<T>(ax, fa, p, q);
+    if (needB && needF && ob != of) {
+      const int bit = ax * NF + fi;
+      atomicOr(dbits + (bit >> 5), 1u << (bit & 31));
+    }
+    return fi;
+  };
+
+  // The three axes are unrolled: every axis-dependent index, stride and
+  // flux variant is then a compile-time choice (6% of the launch on the
+  // 7 M-cell TGV case, measured).
 #pragma unroll
   for (int ax = 0; ax < 3; ++ax) {
-    for (int f = tid; f < (T + 1) * T * T; f += NT) {
-      const int fa = f / (T * T), p = (f / T) % T, q = f % T;
-      int li, lj, lk;  // a warp covers 4 x 8 faces of a plane (8 x 4 for z-faces)
-      if (ax == 0) { li = fa; lj = p; lk = q; }
-      else if (ax == 1) { li = p; lj = fa; lk = q; }
-      else { li = q; lj = p; lk = fa; }
-      const int g = (ax == 0 ? bi + li : (ax == 1 ? bj + lj : bk + lk));
-      const int di = ax == 0, dj = ax == 1, dk = ax == 2;
-      const int fm2 = FL(li - 2 * di, lj - 2 * dj, lk - 2 * dk),
-                fm1 = FL(li - di, lj - dj, lk - dk), f0 = FL(li, lj, lk),
-                fp1 = FL(li + di, lj + dj, lk + dk);
-      const bool needB = fa < T, needF = fa > 0;
-      const int ob = order_backward(g, fm2, fm1, fp1);
-      const int of = order_forward(g, nx, fm2, f0, fp1);
-      const float *base = BX(li, lj, lk);
-      const int sstride = ax == 0 ? SM::PP : (ax == 1 ? SM::RP : 5);
-      auto ld = [&](int d, int v) -> float { return base[sstride * d + v]; };
-      // The stored view is the plus-side cell's (the minus-side cell's for
-      // the last face, which has no plus cell in the tile); where the
-      // minus-side cell's order differs it recomputes its own view.
-      float ML[5], MR[5], Fx[5], dP;
-      recon_split(needB ? ob : of, ld, ML, MR);
-      if (ax == 0) face_flux_delta<0>(ML, MR, ef, rho0, P0, Fx, dP);
-      else if (ax == 1) face_flux_delta<1>(ML, MR, ef, rho0, P0, Fx, dP);
-      else face_flux_delta<2>(ML, MR, ef, rho0, P0, Fx, dP);
-      const int fi = face_idx<T>(ax, fa, p, q);
+    if (PACK) {
+      // 8^3 tiles: the axis's 576 faces are two per thread (f and f + 288),
+      // evaluated together in packed pairs.
+      float MLa[5], MRa[5], MLb[5], MRb[5];
+      const int fa_ = face_prep(ax, tid, MLa, MRa);
+      const int fb_ = face_prep(ax, tid + NT, MLb, MRb);
+      float2 ML2[5], MR2[5], F2v[5], dP2;
 #pragma unroll
-      for (int v = 0; v < 5; ++v) FF[(5 * ax + v) * NF + fi] = Fx[v];
-      if (ax != 1) FdP[(ax == 2) * NF + fi] = dP;
-      if (needB && needF && ob != of) {
-        const int bit = ax * NF + fi;
-        atomicOr(dbits + (bit >> 5), 1u << (bit & 31));
+      for (int v = 0; v < 5; ++v) {
+        ML2[v] = make_float2(MLa[v], MLb[v]);
+        MR2[v] = make_float2(MRa[v], MRb[v]);
+      }
+      if (ax == 0) face_flux_delta2<0>(ML2, MR2, ef, rho0, P0, F2v, dP2);
+      else if (ax == 1) face_flux_delta2<1>(ML2, MR2, ef, rho0, P0, F2v, dP2);
+      else face_flux_delta2<2>(ML2, MR2, ef, rho0, P0, F2v, dP2);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        FF[(5 * ax + v) * NF + fa_] = F2v[v].x;
+        FF[(5 * ax + v) * NF + fb_] = F2v[v].y;
+      }
+      if (ax != 1) {
+        FdP[(ax == 2) * NF + fa_] = dP2.x;
+        FdP[(ax == 2) * NF + fb_] = dP2.y;
+      }
+    } else {
+      for (int f = tid; f < (T + 1) * T * T; f += NT) {
+        float ML[5], MR[5], Fx[5], dP;
+        const int fi = face_prep(ax, f, ML, MR);
+        if (ax == 0) face_flux_delta<0>(ML, MR, ef, rho0, P0, Fx, dP);
+        else if (ax == 1) face_flux_delta<1>(ML, MR, ef, rho0, P0, Fx, dP);
+        else face_flux_delta<2>(ML, MR, ef, rho0, P0, Fx, dP);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) FF[(5 * ax + v) * NF + fi] = Fx[v];
+        if (ax != 1) FdP[(ax == 2) * NF + fi] = dP;
       }
     }
   }
@@ -698,10 +828,15 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
     // staged value where the cell did not change), and into the same-level
     // neighbour's ghost layers: every cell of those layers pushes, since the
     // next buffer's ghost layers hold values two stages old.
+    // The conversion is the hardware's (IEEE round to nearest, the same bits
+    // as the integer-pipe routine of the other writers): this kernel's FP64
+    // pipe has room, its integer pipes do not (measured: the integer routine
+    // made the launch 17% longer, this form 9%).
     float m5[5];
     if (IF == kFluid) {
 #pragma unroll
-      for (int v = 0; v < 5; ++v) m5[v] = mirror_value(un[v], v, rho0d, E0d);
+      for (int v = 0; v < 5; ++v)
+        m5[v] = __double2float_rn(v == 0 ? un[v] - rho0d : (v == 4 ? un[v] - E0d : un[v]));
     } else {
       const float *qm = BX(mi, mj, mk);
 #pragma unroll
@@ -732,25 +867,26 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
   }
 }
 
+template <int T, bool VISCOUS, bool PACK>
+static cudaError_t launch_split_k(const FluxSplitArgs &a, unsigned grid, cudaStream_t s) {
+  const size_t smem = SplitSmem<T>::bytes;
+  cudaError_t e = cudaFuncSetAttribute(k_flux_split<T, VISCOUS, PACK>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_flux_split<T, VISCOUS, PACK><<<grid, split_threads<T>(), smem, s>>>(a);
+  return cudaGetLastError();
+}
+
 template <int T>
 static cudaError_t launch_split_t(const FluxSplitArgs &a, int ncubes, cudaStream_t s) {
   const int nt = a.ph.n / T;
-  const size_t smem = SplitSmem<T>::bytes;
   const unsigned grid = (unsigned)(ncubes * nt * nt * nt);
   if (grid == 0) return cudaSuccess;
-  cudaError_t e;
-  if (a.ph.mu_L != 0.0) {
-    e = cudaFuncSetAttribute(k_flux_split<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-    if (e != cudaSuccess) return e;
-    k_flux_split<T, true><<<grid, split_threads<T>(), smem, s>>>(a);
-  } else {
-    e = cudaFuncSetAttribute(k_flux_split<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-    if (e != cudaSuccess) return e;
-    k_flux_split<T, false><<<grid, split_threads<T>(), smem, s>>>(a);
-  }
-  return cudaGetLastError();
+  const bool visc = a.ph.mu_L != 0.0;
+  if (T == 8 && a.form == 1)
+    return visc ? launch_split_k<T, true, T == 8>(a, grid, s)
+                : launch_split_k<T, false, T == 8>(a, grid, s);
+  return visc ? launch_split_k<T, true, false>(a, grid, s) : launch_split_k<T, false, false>(a, grid, s);
 }
 
 int flux_tile(int n, int tile) {

@@ -96,6 +96,7 @@ struct FluxSplitArgs {
                        // 0: it writes the FP32 residual to R32 instead
   float *R32 = nullptr;  // [ncell][5] (RK == 0)
   int tile = 0;          // tile edge 8 or 4 (0: 8 when n is a multiple of 8, else 4)
+  int form = 0;          // 8^3 tiles: 0 faces one at a time, 1 in packed FP32 pairs
   double *partials;    // [blocks][7] norm/force partial sums (stage 3)
   double *Residual1;
   Batch bt;

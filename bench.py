@@ -382,8 +382,11 @@ def measure(api, case, precision_name, args, dist, clocks_on=True, method=None, 
     # launch shapes from the committed autotuner table (bcm_cgli_gb300/autotune.py)
     from bcm_cgli_gb300 import autotune
     shape = autotune.lookup(case.n, precision_name, meth)
+    if getattr(args, "flux_form", None) is not None:
+        shape = dict(shape or {"flux_tile": 0, "lusgs_threads": 0})
+        shape["flux_form"] = args.flux_form
     if shape:
-        ctx.set_tuning(shape["flux_tile"], shape["lusgs_threads"])
+        ctx.set_tuning(shape["flux_tile"], shape["lusgs_threads"], shape.get("flux_form", 0))
     ctx.set_state(case.U, case.U, case.U)
     for _ in range(max(1, warmup)):  # the last warm-up step captures the step graph
         ctx.advance(1, SUBITERS, use_graph=True)
@@ -415,6 +418,7 @@ def measure(api, case, precision_name, args, dist, clocks_on=True, method=None, 
     flux_ms, flux_n = ctx.profile()
     ctx.set_profiling(False)
     out = {"tuning": ({"flux_tile": shape["flux_tile"], "lusgs_threads": shape["lusgs_threads"],
+                       "flux_form": shape.get("flux_form", 0),
                        "from": "bcm_cgli_gb300/tuning_gb300.json"} if shape else None),
            "value": dist.throughput(case.n_cells * SUBITERS * steps, ms),
            "ms_per_step": ms / steps, "steps": steps, "warmup": max(1, warmup),
@@ -645,6 +649,8 @@ def run_flux_only(args):
     case = cases.taylor_green(ncx=args.ncx, n=args.n)
     prec = api.PRECISION_SPLIT if args.precision == "split" else api.PRECISION_FP64
     ctx = api.CaseContext(case, precision=prec)
+    if args.flux_form is not None:
+        ctx.set_tuning(0, 0, args.flux_form)
     ctx.set_state(case.U, case.U, case.U)
     ms = ctx.time_flux(reps=max(1, args.steps))
     ctx.close()
@@ -702,6 +708,9 @@ def main():
                     help="batch (default: 16 batched sphere cases, the configuration the "
                          "metric's split-precision target is quoted on), tgv, vortex, sphere, "
                          "tgv32")
+    ap.add_argument("--flux-form", type=int, default=None, choices=[0, 1, 2],
+                    help="override the split flux form of the tuning table (1 packed face "
+                         "pairs, 2 one face at a time)")
     ap.add_argument("--acc-steps", type=int, default=ACC_STEPS,
                     help="dual-time steps of the split-vs-FP64 accuracy comparison")
     args = ap.parse_args()

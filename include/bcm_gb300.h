@@ -259,20 +259,26 @@ int bcmg_case_mirror(bcmg_case *c, float *M);
 int bcmg_case_mirror_current(bcmg_case *c, float *M);
 
 /* Launch shapes.  flux_tile: edge of the cube tile one flux CTA works on,
- * 8 or 4 (0: 8 when it divides n, else 4); lusgs_threads: threads per cube
- * of the split-precision LU-SGS sweep, a multiple of 32 up to the widest
- * plane of a cube (0: the widest plane; fewer threads take wide planes in
- * several passes).  The shapes change how work is spread over the GPU, not
- * any cell's arithmetic (the FP64 path stays bit-identical to the
- * reference).  bcmg_case_autotune times the candidates on the context's own
- * state with CUDA events (`reps` launches each, state restored), applies the
- * fastest and reports every time in `out` (flux_ms: tiles 8 and 4;
- * lusgs_ms: widest plane, half of it; 0 where not measured).  The LU-SGS
- * candidates are timed only on the split path with LU-SGS selected. */
+ * 8 or 4 (0: 8 when it divides n, else 4); flux_form (split precision, 8^3
+ * tiles): 1 each thread evaluates its two faces of an axis together in
+ * packed FP32 pairs (Blackwell FFMA2/FADD2/FMUL2), 2 one after the other, 0
+ * the default (1); lusgs_threads: threads per cube of the split-precision
+ * LU-SGS sweep, a multiple of 32 up to the widest plane of a cube (0: the
+ * widest plane; fewer threads take wide planes in several passes).  The
+ * shapes change how work is spread over the GPU, not the FP64 path's
+ * arithmetic (it stays bit-identical to the reference); the two split flux
+ * forms round differently (both within the split path's error bound).
+ * bcmg_case_autotune times the candidates on the context's own state with
+ * CUDA events (`reps` launches each, state restored), applies the fastest
+ * and reports every time in `out` (flux_ms: tile 8 packed, tile 8 one face
+ * at a time, tile 4; lusgs_ms: widest plane, half of it; 0 where not
+ * measured).  The LU-SGS candidates are timed only on the split path with
+ * LU-SGS selected. */
 typedef struct bcmg_tuning {
   int flux_tile;
   int lusgs_threads;
-  double flux_ms[2];
+  int flux_form;
+  double flux_ms[3];
   double lusgs_ms[2];
 } bcmg_tuning;
 int bcmg_case_set_tuning(bcmg_case *c, const bcmg_tuning *t);

@@ -61,7 +61,7 @@ def horizon_records():
         ref.set_threads(1)
         st = O.State(case)
         ref.run(case, st, steps, subiters)
-        out[name] = {"steps": steps, "subiters": subiters,
+        out[name] = {"steps": steps, "subiters": subiters, "initial": digest(case.U),
                      "state": {k: digest(getattr(st, k)) for k in ("U1_", "U1", "U1q")},
                      "er": [repr(float(x)) for x in st.er],
                      "sum": [repr(float(x)) for x in st.U1_.reshape(-1, 5).sum(axis=0)]}

@@ -43,6 +43,9 @@ def test_vortex_full_run_equals_reference_bit_for_bit():
     gold = _golden()["horizon"]["vortex_full"]
     case, steps, subiters = G.horizon_cases()["vortex_full"]
     assert (steps, subiters) == (gold["steps"], gold["subiters"])
+    # the record's run started from the same bits (the field is built with
+    # IEEE arithmetic only, so every machine forms it alike)
+    assert _digest(case.U) == gold["initial"]
     ctx = api.CaseContext(case, precision=api.PRECISION_FP64)
     ctx.set_state(case.U, case.U, case.U)
     er = ctx.advance(steps, subiters, use_graph=True)
