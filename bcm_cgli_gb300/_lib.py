@@ -58,6 +58,13 @@ def _declare(L):
     L.bcmg_last_error.restype = C.c_char_p
     L.bcmg_version.restype = C.c_char_p
     L.bcmg_set_reference_config.argtypes = [C.POINTER(RefConfig)]
+    L.bcmg_set_reference_precision.argtypes = [C.c_int]
+    L.bcmg_release_host_arrays.argtypes = []
+    L.bcmg_release_host_arrays.restype = None
+    L.bcmg_set_host_pinning.argtypes = [C.c_int]
+    L.bcmg_set_host_pinning.restype = None
+    L.bcmg_set_twin_scratch_kept.argtypes = [C.c_int]
+    L.bcmg_set_twin_scratch_kept.restype = None
     L.bcmg_get_reference_config.argtypes = [C.POINTER(RefConfig)]
     L.BCM_Flux_XYZ_Viscous_Runge_kutta.argtypes = [
         C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, ip, ip, dp, dp, dp, dp,

@@ -61,6 +61,32 @@ def reference_config_for(case):
     set_reference_config(case.n, ph.mpi_ncube, ph.mu_L, ph.rho0, ph.U0, ph.Uin, ph.P0)
 
 
+def set_reference_precision(precision):
+    """Arithmetic of the BCM_Flux_XYZ_Viscous_Runge_kutta twin:
+    PRECISION_FP64 (default, bit-identical to the reference) or
+    PRECISION_SPLIT (the stage update inside the flux kernel; Rku1 is not
+    written)."""
+    check(lib().bcmg_set_reference_precision(int(precision)))
+
+
+def release_host_arrays():
+    """Unregisters every host array the twins page-locked and forgets them
+    (before freeing an array the twins have seen)."""
+    lib().bcmg_release_host_arrays()
+
+
+def set_host_pinning(on=True):
+    """Whether the twins page-lock the caller's arrays (default on)."""
+    lib().bcmg_set_host_pinning(1 if on else 0)
+
+
+def set_twin_scratch_kept(on=True):
+    """The flux twin uploads its write-only scratch arrays (U1p1 at RK 1,
+    U1p2 at RK 2, Rku1, Residual1 at RK 1 and 2) once per host array instead
+    of every call: for callers that change them only through the twins."""
+    lib().bcmg_set_twin_scratch_kept(1 if on else 0)
+
+
 # ---------------------------------------------------------------------------
 # Reference-named entry points (in place on host arrays)
 # ---------------------------------------------------------------------------

@@ -9,6 +9,7 @@
 #include <new>
 #include <string>
 #include <thread>
+#include <map>
 #include <vector>
 
 #include "../../include/bcm_gb300.h"
@@ -65,6 +66,23 @@ __global__ void k_time_shift(int n, int ncubes, const double2 *__restrict__ U1_,
       U1q[o] = a;
       U1[o] = b;
     }
+}
+
+// Split-precision flux twin: the stage's new state of the fluid interior
+// cells into U1p1 (RK 1) or U1p2 (RK 2), as the reference's stage
+// combination leaves them (BCM_Flux_XYZ_Viscous_Runge_kutta.cpp:2417-2599).
+__global__ void k_copy_fluid(int n, int ncubes, const double *__restrict__ U1_,
+                             const int *__restrict__ FWS, double *__restrict__ dst) {
+  const int S = n + 4;
+  const long long n3 = (long long)n * n * n, total = n3 * ncubes;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int c = 1 + (int)(t / n3), r = (int)(t % n3);
+    const size_t o = cell_index(S, c, 2 + r / (n * n), 2 + (r / n) % n, 2 + r % n);
+    if (FWS[o] != kFluid) continue;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) dst[5 * o + v] = U1_[5 * o + v];
+  }
 }
 
 __global__ void k_emax(double *er, double *emax, const int *active) {
@@ -1892,6 +1910,11 @@ struct Compat {
   FaceTask *tasks = nullptr;
   size_t tasks_cap = 0;
   Ibm ibm;
+  // split-precision flux twin (bcmg_set_reference_precision): mirror
+  // buffers and flag, FP32 level difference, n / cube_size
+  int precision = BCMG_PRECISION_FP64;
+  float *M = nullptr, *M2 = nullptr, *D2 = nullptr, *inv_dx = nullptr;
+  int *mpar = nullptr;
 
   Phys phys() const {
     Phys p;
@@ -1915,6 +1938,7 @@ struct Compat {
     if (nc == ncube && Sx == S && U1_) return BCMG_OK;
     dfree(U1_); dfree(U1); dfree(U1q); dfree(U1p1); dfree(U1p2); dfree(Rku1);
     dfree(Residual1); dfree(cube_size); dfree(partials); dfree(er); dfree(FWS);
+    dfree(M); dfree(M2); dfree(D2); dfree(inv_dx); dfree(mpar);
     ncube = nc;
     S = Sx;
     ncell = (size_t)nc * S * S * S;
@@ -1925,8 +1949,16 @@ struct Compat {
     RkArgs probe{};
     probe.ph = phys();
     probe.ncube = nc;
-    nparts = rk_partial_blocks(probe);
+    nparts = std::max(rk_partial_blocks(probe), flux_split_blocks(cfg.ncube_x, nc - 1));
     CK(dalloc(&partials, (size_t)nparts * 7));
+    return BCMG_OK;
+  }
+  int ensure_split() {
+    if (M) return BCMG_OK;
+    const size_t nd = ncell * 5;
+    CK(dalloc(&M, nd)); CK(dalloc(&M2, nd)); CK(dalloc(&D2, nd));
+    CK(dalloc(&inv_dx, (size_t)ncube)); CK(dalloc(&mpar, 1));
+    CK(cudaMemsetAsync(mpar, 0, sizeof(int), s));
     return BCMG_OK;
   }
   template <typename T>
@@ -1941,12 +1973,62 @@ struct Compat {
 
 Compat g_compat;
 
+// Caller arrays of the twins, page-locked once (cudaHostRegister) so that
+// every later copy of them runs at the host link's full rate instead of
+// through pageable staging.  A region that cannot be registered (already
+// registered elsewhere, or refused) is copied pageable.  The registration
+// lasts until bcmg_release_host_arrays() (call it before freeing an array
+// the twins have seen) or the process ends.
+struct HostPins {
+  std::map<const void *, size_t> reg;  // registered base -> bytes
+  std::map<const void *, size_t> refused;
+  bool enabled = true;
+  void pin(const void *p, size_t bytes) {
+    if (!enabled || !p || bytes == 0) return;
+    auto it = reg.find(p);
+    if (it != reg.end() && it->second >= bytes) return;
+    auto rf = refused.find(p);
+    if (rf != refused.end() && rf->second >= bytes) return;
+    if (it != reg.end()) {  // grown: register the larger region afresh
+      cudaHostUnregister(const_cast<void *>(p));
+      reg.erase(it);
+    }
+    if (cudaHostRegister(const_cast<void *>(p), bytes, cudaHostRegisterDefault) == cudaSuccess) {
+      reg[p] = bytes;
+    } else {
+      cudaGetLastError();  // not sticky: the copies run pageable
+      refused[p] = bytes;
+    }
+  }
+  void release() {
+    for (auto &kv : reg) cudaHostUnregister(const_cast<void *>(kv.first));
+    reg.clear();
+    refused.clear();
+  }
+};
+HostPins g_pins;
+
+// Host arrays of the flux twin whose device copies already hold the cells
+// the routine never writes (uploaded once per host pointer): U1p1, U1p2,
+// Rku1, Residual1 when a stage only writes them.  Only with
+// bcmg_set_twin_scratch_kept(1): by default every array a stage returns is
+// uploaded too, since a freed array's address may come back for another.
+struct TwinSeen {
+  const void *p[4] = {nullptr, nullptr, nullptr, nullptr};
+  size_t ncell = 0;
+};
+TwinSeen g_twin_seen;
+bool g_scratch_kept = false;
+
 // Gather the listed cubes of a host array into the compact device buffer
 // (slot 0 unused, slot m = cubes[m-1]); returns cube count.
 int gather_cubes(Compat &C, const std::vector<int> &cubes, const double *hostU) {
   const size_t per = (size_t)C.S * C.S * C.S * 5;
   int r;
   if ((r = C.grow(&C.cubes, C.cubes_cap, per * (cubes.size() + 1)))) return r;
+  int top = 0;
+  for (int c : cubes) top = std::max(top, c);
+  g_pins.pin(hostU, per * (top + 1) * sizeof(double));  // the array up to the last cube used
   for (size_t m = 0; m < cubes.size(); ++m)
     CK(cudaMemcpyAsync(C.cubes + per * (m + 1), hostU + per * cubes[m], per * sizeof(double),
                        cudaMemcpyHostToDevice, C.s));
@@ -2052,6 +2134,32 @@ int bcmg_set_reference_config(const bcmg_reference_config *cfg) {
   return BCMG_OK;
 }
 
+void bcmg_release_host_arrays(void) {
+  clear_err();
+  g_pins.release();
+  g_twin_seen = TwinSeen{};
+}
+
+int bcmg_set_reference_precision(int precision) {
+  clear_err();
+  if (precision != BCMG_PRECISION_FP64 && precision != BCMG_PRECISION_SPLIT) {
+    set_err("precision must be BCMG_PRECISION_FP64 or BCMG_PRECISION_SPLIT");
+    return BCMG_ERR_ARG;
+  }
+  g_compat.precision = precision;
+  return BCMG_OK;
+}
+
+void bcmg_set_twin_scratch_kept(int on) {
+  g_scratch_kept = on != 0;
+  g_twin_seen = TwinSeen{};
+}
+
+void bcmg_set_host_pinning(int on) {
+  g_pins.enabled = on != 0;
+  if (!on) g_pins.release();
+}
+
 void bcmg_get_reference_config(bcmg_reference_config *cfg) {
   if (cfg) *cfg = g_compat.cfg;
 }
@@ -2081,15 +2189,98 @@ void BCM_Flux_XYZ_Viscous_Runge_kutta(int myid, int ncube, int RK, double deltaT
     if ((r = C.ensure_full(ncube))) return r;
     const size_t b = C.ncell * 5 * sizeof(double);
     cudaStream_t s = C.s;
+    TwinSeen &seen = g_twin_seen;
+    if (seen.ncell != C.ncell) seen = TwinSeen{nullptr, nullptr, nullptr, nullptr, C.ncell};
+    // Per stage, the arrays it reads go up (RK 1: U1_, U1, U1q; RK 2: also
+    // U1p1; RK 3: also U1p2 and Residual1, whose fluid cells the norms sum);
+    // the ones it only writes go up once per host array, since the routine
+    // never writes their other cells.  Results come back whole.
+    auto up = [&](double *dev, const double *host) -> int {
+      g_pins.pin(host, b);
+      CK(cudaMemcpyAsync(dev, host, b, cudaMemcpyHostToDevice, s));
+      return BCMG_OK;
+    };
+    auto up_once = [&](double *dev, const double *host, int slot) -> int {
+      if (g_scratch_kept && seen.p[slot] == host) return BCMG_OK;
+      int rr = up(dev, host);
+      if (!rr) seen.p[slot] = host;
+      return rr;
+    };
+    g_pins.pin(FWS, C.ncell * sizeof(int));
     CK(cudaMemcpyAsync(C.FWS, FWS, C.ncell * sizeof(int), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(C.cube_size, cube_size, sizeof(double) * ncube, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(C.U1_, U1_, b, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(C.U1, U1, b, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(C.U1q, U1q, b, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(C.U1p1, U1p1, b, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(C.U1p2, U1p2, b, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(C.Rku1, Rku1, b, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(C.Residual1, Residual1, b, cudaMemcpyHostToDevice, s));
+    if ((r = up(C.U1_, U1_)) || (r = up(C.U1, U1)) || (r = up(C.U1q, U1q))) return r;
+    if (RK == 1 && (r = up_once(C.U1p1, U1p1, 0))) return r;
+    if (RK == 2 && ((r = up(C.U1p1, U1p1)) || (r = up_once(C.U1p2, U1p2, 1)))) return r;
+    if (RK == 3 && (r = up(C.U1p2, U1p2))) return r;
+    if ((r = up_once(C.Rku1, Rku1, 2))) return r;
+    if (RK == 3 ? (r = up(C.Residual1, Residual1)) : (r = up_once(C.Residual1, Residual1, 3)))
+      return r;
+    if (RK == 3) seen.p[3] = Residual1;
+    for (double *h : {U1_, Rku1, Residual1}) g_pins.pin(h, b);
+    if (RK == 1) g_pins.pin(U1p1, b);
+    if (RK == 2) g_pins.pin(U1p2, b);
+    int nb = 0;
+    if (C.precision == BCMG_PRECISION_SPLIT) {
+      // Split precision: FP32 mirror and level difference of this call's
+      // state, then the split flux kernel applies the stage update in place
+      // (Q += w dQ; Rku1 is not formed); U1p1 / U1p2 take the new state of
+      // the fluid cells as the reference's combination leaves them.
+      if ((r = C.ensure_split())) return r;
+      const Phys ph = C.phys();
+      std::vector<float> inv((size_t)ncube, 0.f);
+      for (int i = 1; i < ncube; ++i) inv[i] = (float)(ph.n / cube_size[i]);
+      CK(cudaMemcpyAsync(C.inv_dx, inv.data(), sizeof(float) * ncube, cudaMemcpyHostToDevice, s));
+      CK(launch_mirror(C.U1_, C.M, C.M2, ph.n, ncube, ph.rho0, ph.P0, Batch(), s));
+      CK(launch_level_diff(C.U1, C.U1q, C.D2, ph.n, ncube, s));
+      FluxSplitArgs sa;
+      sa.ph = ph;
+      sa.cube0 = 1;
+      sa.dT = deltaT;
+      sa.dTau = deltaTau;
+      sa.ef = (float)e;
+      sa.rho0f = (float)ph.rho0;
+      sa.P0f = (float)ph.P0;
+      sa.RT0f = (float)(ph.P0 / ph.rho0);
+      sa.T0f = (float)(ph.P0 / ph.rho0 / BCMG_R);
+      sa.mu_Lf = (float)ph.mu_L;
+      sa.i2dtf = (float)(1.0 / (2.0 * deltaT));
+      sa.dTf = (float)deltaT;
+      sa.dTauf = (float)deltaTau;
+      sa.inv_dx = C.inv_dx;
+      sa.FWS = C.FWS;
+      sa.cube_size = C.cube_size;
+      sa.mir.buf[0] = C.M;
+      sa.mir.buf[1] = C.M2;
+      sa.mir.parity = C.mpar;
+      sa.mir.rho0 = ph.rho0;
+      sa.mir.E0 = ph.P0 / (BCMG_K - 1);
+      sa.U1_ = C.U1_;
+      sa.U1 = C.U1;
+      sa.U1q = C.U1q;
+      sa.D2 = C.D2;
+      sa.RK = RK;
+      sa.form = 1;
+      sa.partials = C.partials;
+      sa.Residual1 = C.Residual1;
+      CK(launch_flux_split(sa, ncube - 1, s));
+      const long long total = (long long)(ncube - 1) * ph.n * ph.n * ph.n;
+      const int blocks = (int)std::min<long long>(152 * 8, (total + 255) / 256);
+      if (RK == 1 || RK == 2) {
+        k_copy_fluid<<<blocks, 256, 0, s>>>(ph.n, ncube - 1, C.U1_, C.FWS,
+                                            RK == 1 ? C.U1p1 : C.U1p2);
+        CK(cudaGetLastError());
+      }
+      nb = flux_split_blocks(ph.n, ncube - 1);
+      if (RK == 3) CK(launch_norms(ph, C.partials, nb, C.er, s));
+      CK(cudaMemcpyAsync(U1_, C.U1_, b, cudaMemcpyDeviceToHost, s));
+      CK(cudaMemcpyAsync(Residual1, C.Residual1, b, cudaMemcpyDeviceToHost, s));
+      if (RK == 1) CK(cudaMemcpyAsync(U1p1, C.U1p1, b, cudaMemcpyDeviceToHost, s));
+      if (RK == 2) CK(cudaMemcpyAsync(U1p2, C.U1p2, b, cudaMemcpyDeviceToHost, s));
+      if (RK == 3) CK(cudaMemcpyAsync(er + 1, C.er + 1, 7 * sizeof(double), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      return BCMG_OK;
+    }
     FluxArgs a;
     a.ph = C.phys();
     a.cube0 = 1;
@@ -2115,7 +2306,6 @@ void BCM_Flux_XYZ_Viscous_Runge_kutta(int myid, int ncube, int RK, double deltaT
     k.Rku1 = C.Rku1;
     k.Residual1 = C.Residual1;
     k.partials = C.partials;
-    int nb = 0;
     CK(launch_rk(k, &nb, s));
     if (RK == 3) CK(launch_norms(C.phys(), C.partials, nb, C.er, s));
     CK(cudaMemcpyAsync(U1_, C.U1_, b, cudaMemcpyDeviceToHost, s));
@@ -2239,6 +2429,7 @@ void BCM_Interface(int myid, int ncube, int mPI_Nadj, int ncpu_bs, int ncpu_eq, 
     if (!tasks.empty())
       CK(cudaMemcpyAsync(C.tasks, tasks.data(), sizeof(FaceTask) * tasks.size(),
                          cudaMemcpyHostToDevice, C.s));
+    g_pins.pin(U1_, b);
     CK(cudaMemcpyAsync(C.U1_, U1_, b, cudaMemcpyHostToDevice, C.s));
     InterfaceArgs ia;
     ia.n = C.cfg.ncube_x;

@@ -451,6 +451,58 @@ def measure_e2e(ctx, case, args, dist, cell_subiters):
     return cell_subiters / (ms_e2e * 1e-3)
 
 
+def measure_twins(api, case, precision_name, subiters=2):
+    """The drop-in twins end to end: sub-iterations in main.cpp's call order
+    (main.cpp:1161-1241: X/Y/Z boundary conditions, IBM ghost cells,
+    interface, flux/RK stage, interface; three stages) on host arrays, each
+    call copying its arrays to the GPU and back as the reference's routines
+    are replaced one for one.  The reference runs one case per process, so
+    this times one case: the workload's largest.  Wall clock, after one
+    untimed sub-iteration (which page-locks the arrays and sizes the device
+    buffers)."""
+    c = max(case.cases, key=lambda x: x.n_cells) if is_batch(case) else case
+    api.reference_config_for(c)
+    api.set_reference_precision(api.PRECISION_SPLIT if precision_name == "split"
+                                else api.PRECISION_FP64)
+    api.set_twin_scratch_kept(True)  # main.cpp keeps its scratch arrays
+    U1_, U1, U1q = c.U.copy(), c.U.copy(), c.U.copy()
+    U1p1, U1p2, Rku1, Res = (np.zeros_like(c.U) for _ in range(4))
+    er = np.zeros(8)
+    lists = [api._one_based(x) for x in c.bc_lists()]
+    tables = [(f, t) for f, t in ((api.BCM_Ghostcell_minus, c.ibm_minus),
+                                  (api.BCM_Ghostcell_plus, c.ibm_plus)) if t is not None]
+
+    def subiteration():
+        xl, xu, yl, yu, zl, zu = lists
+        for RK in (1, 2, 3):
+            api.BCM_X_boundary_condition(0, len(xl) - 1, len(xu) - 1, xl, xu, U1_)
+            api.BCM_Y_boundary_condition(len(yl) - 1, len(yu) - 1, yl, yu, U1_)
+            api.BCM_Z_boundary_condition(len(zl) - 1, len(zu) - 1, zl, zu, U1_)
+            for f, (W, Gi, I) in tables:
+                f(0, (len(Gi) - 1) // 4, W, Gi, I, c.fws, U1_)
+            api.BCM_Interface_for_case(c, U1_)
+            api.BCM_Flux_XYZ_Viscous_Runge_kutta(0, c.ncube, RK, c.dT, c.dTau, c.e, c.fws, c.csl,
+                                                 c.cube_size, U1_, U1, U1q, U1p1, U1p2, Rku1,
+                                                 Res, er)
+            api.BCM_Interface_for_case(c, U1_)
+
+    try:
+        subiteration()
+        t0 = time.perf_counter()
+        for _ in range(subiters):
+            subiteration()
+        dt = time.perf_counter() - t0
+    finally:
+        api.set_reference_precision(api.PRECISION_FP64)
+        api.set_twin_scratch_kept(False)
+        api.release_host_arrays()
+    return {"value": c.n_cells * subiters / dt, "unit": UNIT, "precision": precision_name,
+            "case": f"{c.name}: {c.ncube - 1} cubes, {c.n_cells} cells",
+            "subiters": subiters, "seconds": dt,
+            "note": "drop-in twins in main.cpp's call order on host arrays (page-locked once, "
+                    "scratch arrays kept), wall clock"}
+
+
 def measure_converged(api, case, precision_name, method, args, dist, steps=2, max_subiters=50,
                       tol=0.02):
     """Physical steps with the reference's convergence test (main.cpp:1249-
@@ -621,6 +673,8 @@ def run_gpu_arm(args, dist):
                          "note": "LU-SGS sub-iterations (hyperplane sweeps) instead of the "
                                  "reference's 3-stage RK, same residual and workload"}
         m_lu["ctx"].close()
+    if not args.no_e2e and not args.quick:
+        line["e2e_twins"] = {p: measure_twins(api, case, p) for p in ("split", "fp64")}
     if not args.no_converged and not args.quick:
         conv = {m: measure_converged(api, case, head, m, args, dist) for m in ("rk3", "lusgs")}
         conv["tol"] = 0.02

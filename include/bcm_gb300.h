@@ -61,6 +61,36 @@ typedef struct bcmg_reference_config {
 int bcmg_set_reference_config(const bcmg_reference_config *cfg);
 void bcmg_get_reference_config(bcmg_reference_config *cfg);
 
+/* Host arrays of the twins.  The twins page-lock each caller array the
+ * first time they see it (cudaHostRegister), so later copies run at the
+ * host link's full rate; an array that cannot be registered is copied
+ * pageable.  bcmg_release_host_arrays() unregisters every array and
+ * forgets it: call it before freeing an array the twins have seen.
+ * bcmg_set_host_pinning(0) stops the page-locking (and releases).
+ *
+ * BCM_Flux_XYZ_Viscous_Runge_kutta uploads the arrays a stage reads (RK 1:
+ * U1_, U1, U1q; RK 2: also U1p1; RK 3: also U1p2 and Residual1, whose fluid
+ * cells the norms sum) and, by default, also the ones it only writes, since
+ * it returns them whole and writes only some of their cells.  With
+ * bcmg_set_twin_scratch_kept(1) the write-only arrays (U1p1 at RK 1, U1p2 at
+ * RK 2, Rku1, Residual1 at RK 1 and 2) are uploaded once per host array
+ * instead: correct for a caller that, like the reference's main.cpp, keeps
+ * those scratch arrays and changes them only through this routine (call
+ * bcmg_release_host_arrays() when that stops being true). */
+void bcmg_release_host_arrays(void);
+
+/* Arithmetic of the BCM_Flux_XYZ_Viscous_Runge_kutta twin:
+ * BCMG_PRECISION_FP64 (default, bit-identical to the reference) or
+ * BCMG_PRECISION_SPLIT (FP32 reconstruction, fluxes, viscous terms and
+ * preconditioner on deltas from the reference state, FP64 state update and
+ * norms; within 1e-5 relative L2 of FP64, see the resident path).  With split
+ * precision the stage update is applied inside the flux kernel, so Rku1 is
+ * not written; U1_, U1p1 (RK 1), U1p2 (RK 2), Residual1 and er are.  Returns
+ * BCMG_ERR_ARG for any other value. */
+int bcmg_set_reference_precision(int precision);
+void bcmg_set_host_pinning(int on);
+void bcmg_set_twin_scratch_kept(int on);
+
 /* ----------------------------------------------------------------------- */
 /* 1. Drop-in twins of the reference routines                              */
 /* ----------------------------------------------------------------------- */
