@@ -76,7 +76,9 @@ def release_host_arrays():
 
 
 def set_host_pinning(on=True):
-    """Whether the twins page-lock the caller's arrays (default on)."""
+    """Whether the twins page-lock the caller's arrays (default off).  With it
+    on, call release_host_arrays() before any array the twins have seen is
+    freed."""
     lib().bcmg_set_host_pinning(1 if on else 0)
 
 

@@ -1973,16 +1973,19 @@ struct Compat {
 
 Compat g_compat;
 
-// Caller arrays of the twins, page-locked once (cudaHostRegister) so that
-// every later copy of them runs at the host link's full rate instead of
-// through pageable staging.  A region that cannot be registered (already
-// registered elsewhere, or refused) is copied pageable.  The registration
-// lasts until bcmg_release_host_arrays() (call it before freeing an array
-// the twins have seen) or the process ends.
+// Caller arrays of the twins, page-locked once (cudaHostRegister) when the
+// caller opts in (bcmg_set_host_pinning(1)), so that every later copy of
+// them runs at the host link's full rate instead of through pageable
+// staging.  Opt-in because a registration must end before its memory is
+// freed: a caller that frees arrays the twins have seen (a scripting
+// front end, say) would leave registrations behind that a later array at
+// the same address trips over.  A region that cannot be registered is
+// copied pageable.  The registration lasts until bcmg_release_host_arrays()
+// or the process ends.
 struct HostPins {
   std::map<const void *, size_t> reg;  // registered base -> bytes
   std::map<const void *, size_t> refused;
-  bool enabled = true;
+  bool enabled = false;
   void pin(const void *p, size_t bytes) {
     if (!enabled || !p || bytes == 0) return;
     auto it = reg.find(p);

@@ -709,7 +709,11 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
       vF[v] = ((Lf[v - 1] - Lb[v - 1]) + (Mf[v - 1] - Mb[v - 1]) + (Nf[v - 1] - Nb[v - 1])) * inv;
   }
 
-  // BDF2 source from FP64 time-level differences, then FP32.
+  // BDF2 source from FP64 time-level differences, then FP32.  The FP64 <->
+  // FP32 conversions of this tail are the hardware's (IEEE round to
+  // nearest): here the FP64 pipe has room and the integer pipes do not
+  // (measured: the integer-pipe routines of k_mirror made the launch 7-8%
+  // longer).
   const size_t go = cb + ((size_t)(bi + mi) * S + (bj + mj)) * S + (bk + mk);
   double *u = a.U1_ + 5 * go;  // only this thread reads or writes these cells
   const double *uu = a.U1 + 5 * go;
@@ -722,7 +726,7 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
   for (int v = 0; v < 5; ++v) {
     const double x = u[v], y = __ldg(uu + v);
     xq[v] = x;
-    const float d1 = to_float_rn(x - y), d2 = __ldg(d2p + v);
+    const float d1 = __double2float_rn(x - y), d2 = __ldg(d2p + v);
     const float Rp = -(3.0f * d1 - d2) * i2dt;
     Rk[v] = Rp - acc[v] + vF[v];
   }
@@ -783,7 +787,7 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
     for (int r = 0; r < 5; ++r) {
       dq[r] = w * dTau * (d[r][0] * Rk[0] + d[r][1] * Rk[1] + d[r][2] * Rk[2] +
                           d[r][3] * Rk[3] + d[r][4] * Rk[4]);
-      un[r] = xq[r] + to_double_exact(dq[r]);
+      un[r] = xq[r] + (double)dq[r];
       u[r] = un[r];
     }
     // Same-level interface copy of this cell, done here.  No CTA reads the
@@ -793,8 +797,8 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
     if (a.RK == 3) {
       // Change norms of p, u, v, w, T from the increment, in FP32; summed
       // in FP64 (BCM_Flux...cpp:2530-2566).
-      const float rf = rho, m1 = to_float_rn(xq[1]), m2 = to_float_rn(xq[2]),
-                  m3 = to_float_rn(xq[3]);
+      const float rf = rho, m1 = __double2float_rn(xq[1]), m2 = __double2float_rn(xq[2]),
+                  m3 = __double2float_rn(xq[3]);
       const float dr = dq[0], e1 = dq[1], e2 = dq[2], e3 = dq[3], dE = dq[4];
       const float den = 1.0f / (rf * (rf + dr));
       const float dU = (e1 * rf - m1 * dr) * den;
@@ -805,11 +809,11 @@ __global__ void __launch_bounds__(split_threads<T>(), split_ctas_per_sm<T>())
           0.5f * ((2.f * (m1 * e1 + m2 * e2 + m3 * e3) + e1 * e1 + e2 * e2 + e3 * e3) * rf - mm * dr) * den;
       const float dP = Km1 * (dE - dKE);
       const float dTt = (dP * rf - Pc * dr) * den;
-      s5[0] += to_double_exact(dP * dP);
-      s5[1] += to_double_exact(dU * dU);
-      s5[2] += to_double_exact(dVv * dVv);
-      s5[3] += to_double_exact(dW * dW);
-      s5[4] += to_double_exact(dTt * dTt);
+      s5[0] += (double)(dP * dP);
+      s5[1] += (double)(dU * dU);
+      s5[2] += (double)(dVv * dVv);
+      s5[3] += (double)(dW * dW);
+      s5[4] += (double)(dTt * dTt);
     }
   } else {
     // Force integrands on non-fluid cells (:2395-2398); their sum over the

@@ -365,55 +365,74 @@ cudaError_t launch_bc(const BcArgs &a, int ncubes, cudaStream_t s) {
 
 // ---------------------------------------------------------------------------
 // IBM ghost cells (BCM_Ghostcell_minus.cpp:72-489; _plus is identical).  One
-// thread per entry of one dependency level: within a level no entry reads a
-// cell another entry of the level writes, and the host orders the levels so
-// every read sees exactly the value the reference's serial loop sees.
+// dependency level per launch: within a level no entry reads a cell another
+// entry of the level writes, and the host orders the levels so every read
+// sees exactly the value the reference's serial loop sees.
+//
+// Eight lanes per entry, one stencil cell each: a cell's primitives take
+// three FP64 divisions, which on this part's narrow FP64 pipe dominate an
+// entry's latency, so the eight cells run side by side; their weighted terms
+// go through shared memory to the group's first lane, which sums them in
+// the reference's order (000,100,010,001,110,101,011,111) and writes the
+// ghost cell.  The levels are short, so the launch is latency-bound and
+// this parallelism is what shortens it.
 // ---------------------------------------------------------------------------
-__global__ void k_ghost(GhostArgs a, int count) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= count) return;
-  const int e = a.entries[t];
+constexpr int kGhostThreads = 128, kGhostPer = kGhostThreads / 8;  // entries per CTA
+
+__global__ void __launch_bounds__(kGhostThreads) k_ghost(GhostArgs a, int count) {
+  // per entry and stencil cell: rho, p, u, v, w and the weighted density and
+  // pressure deltas
+  __shared__ double sh[kGhostPer][8][7];
+  const int g = threadIdx.x >> 3, m = threadIdx.x & 7;
+  const int t = blockIdx.x * kGhostPer + g;
+  const bool live = t < count;
+  const int e = live ? a.entries[t] : 0;
   const int S = a.n + 4;
   const int b = (e - 1) * 4;
-  const int c = a.IPsur[b + 1], i = a.IPsur[b + 2], j = a.IPsur[b + 3], k = a.IPsur[b + 4];
-  if (!case_active(a.bt, c)) return;
+  int c = 0, i = 0, j = 0, k = 0;
+  bool act = false;
+  if (live) {
+    c = a.IPsur[b + 1]; i = a.IPsur[b + 2]; j = a.IPsur[b + 3]; k = a.IPsur[b + 4];
+    act = case_active(a.bt, c);
+  }
   double rho0 = a.rho0, P0 = a.P0;
-  if (a.bt.cube_case) {  // the case of the stencil's cube
+  if (act && a.bt.cube_case) {  // the case of the stencil's cube
     const CaseConst &cq = a.bt.cases[a.bt.cube_case[c]];
     rho0 = cq.rho0;
     P0 = cq.P0;
   }
-  double rh[8], Uu[8], Vv[8], Ww[8], Pp[8];
-#pragma unroll
-  for (int m = 0; m < 8; ++m) {
-    // Order 000,100,010,001,110,101,011,111 (:81-145).
+  if (act) {
+    // cell m of the stencil, order 000,100,010,001,110,101,011,111 (:81-145)
     const int oi = (m == 1 || m == 4 || m == 5 || m == 7);
     const int oj = (m == 2 || m == 4 || m == 6 || m == 7);
     const int ok = (m == 3 || m == 5 || m == 6 || m == 7);
     const double *q = a.U1_ + 5 * cell_index(S, c, i + oi, j + oj, k + ok);
-    rh[m] = q[0];
-    Uu[m] = q[1] / rh[m];
-    Vv[m] = q[2] / rh[m];
-    Ww[m] = q[3] / rh[m];
-    double VV = Uu[m] * Uu[m] + Vv[m] * Vv[m] + Ww[m] * Ww[m];
-    Pp[m] = (q[4] - 0.5 * rh[m] * VV) * (BCMG_K - 1);
+    const double rh = q[0];
+    const double Uu = q[1] / rh, Vv = q[2] / rh, Ww = q[3] / rh;
+    const double VV = Uu * Uu + Vv * Vv + Ww * Ww;
+    const double Pp = (q[4] - 0.5 * rh * VV) * (BCMG_K - 1);
+    double *o = sh[g][m];
+    o[0] = rh; o[1] = Pp; o[2] = Uu; o[3] = Vv; o[4] = Ww;
   }
+  __syncwarp();
+  if (!act || m != 0) return;
+  const double(*X)[7] = sh[g];
   const double *w = a.weight + (size_t)(e - 1) * 8 + 1;
   double wl[8];
 #pragma unroll
-  for (int m = 0; m < 8; ++m) wl[m] = w[m];
+  for (int l = 0; l < 8; ++l) wl[l] = w[l];
   const int gc = a.GCindex[b + 1], gi = a.GCindex[b + 2], gj = a.GCindex[b + 3],
             gk = a.GCindex[b + 4];
-  double rho = wl[0] * (rh[0] - rho0);
-  double P = wl[0] * (Pp[0] - P0);
-  double U = wl[0] * Uu[0], V = wl[0] * Vv[0], W = wl[0] * Ww[0];
+  double rho = wl[0] * (X[0][0] - rho0);
+  double P = wl[0] * (X[0][1] - P0);
+  double U = wl[0] * X[0][2], V = wl[0] * X[0][3], W = wl[0] * X[0][4];
 #pragma unroll
-  for (int m = 1; m < 8; ++m) {
-    rho = rho + wl[m] * (rh[m] - rho0);
-    P = P + wl[m] * (Pp[m] - P0);
-    U = U + wl[m] * Uu[m];
-    V = V + wl[m] * Vv[m];
-    W = W + wl[m] * Ww[m];
+  for (int l = 1; l < 8; ++l) {
+    rho = rho + wl[l] * (X[l][0] - rho0);
+    P = P + wl[l] * (X[l][1] - P0);
+    U = U + wl[l] * X[l][2];
+    V = V + wl[l] * X[l][3];
+    W = W + wl[l] * X[l][4];
   }
   rho = rho + rho0;
   P = P + P0;
@@ -427,17 +446,9 @@ __global__ void k_ghost(GhostArgs a, int count) {
                     (gk - k == 0 || gk - k == 1);
   if (self) {
     // bit pattern (di,dj,dk) -> stencil slot in the 000,100,010,001,...
-    // order (patterns 3 and 4 swap); the slot's values picked by selects so
-    // the arrays stay in registers
+    // order (patterns 3 and 4 swap)
     const int sl = s == 3 ? 4 : (s == 4 ? 3 : s);
-    double wsl = 0, rsl = 0, psl = 0;
-#pragma unroll
-    for (int m = 0; m < 8; ++m)
-      if (m == sl) {
-        wsl = wl[m];
-        rsl = rh[m];
-        psl = Pp[m];
-      }
+    const double wsl = wl[sl], rsl = X[sl][0], psl = X[sl][1];
     double r2, p2;
     if (wsl > 0.9999) {
       r2 = rsl;
@@ -445,10 +456,9 @@ __global__ void k_ghost(GhostArgs a, int count) {
     } else {
       double ar = 0, ap = 0;
       bool first = true;
-#pragma unroll
-      for (int m = 0; m < 8; ++m) {
-        if (m == sl) continue;
-        double tr = wl[m] * (rh[m] - rho0), tp = wl[m] * (Pp[m] - P0);
+      for (int l = 0; l < 8; ++l) {
+        if (l == sl) continue;
+        double tr = wl[l] * (X[l][0] - rho0), tp = wl[l] * (X[l][1] - P0);
         if (first) { ar = tr; ap = tp; first = false; }
         else { ar = ar + tr; ap = ap + tp; }
       }
@@ -457,11 +467,10 @@ __global__ void k_ghost(GhostArgs a, int count) {
     }
     double su = 0, sv = 0, sw = 0;
     bool first = true;
-#pragma unroll
-    for (int m = 0; m < 8; ++m) {
-      if (m == sl) continue;
-      if (first) { su = wl[m] * Uu[m]; sv = wl[m] * Vv[m]; sw = wl[m] * Ww[m]; first = false; }
-      else { su = su + wl[m] * Uu[m]; sv = sv + wl[m] * Vv[m]; sw = sw + wl[m] * Ww[m]; }
+    for (int l = 0; l < 8; ++l) {
+      if (l == sl) continue;
+      if (first) { su = wl[l] * X[l][2]; sv = wl[l] * X[l][3]; sw = wl[l] * X[l][4]; first = false; }
+      else { su = su + wl[l] * X[l][2]; sv = sv + wl[l] * X[l][3]; sw = sw + wl[l] * X[l][4]; }
     }
     double U2 = su / (2 - wsl), V2 = sv / (2 - wsl), W2 = sw / (2 - wsl);
     double VV2 = U2 * U2 + V2 * V2 + W2 * W2;
@@ -472,9 +481,9 @@ __global__ void k_ghost(GhostArgs a, int count) {
     o[4] = p2 / (BCMG_K - 1) + 0.5 * r2 * VV2;
   }
   const size_t go = 5 * cell_index(S, gc, gi, gj, gk);
-  double *g = a.U1_ + go;
+  double *gp = a.U1_ + go;
 #pragma unroll
-  for (int v = 0; v < 5; ++v) g[v] = o[v];
+  for (int v = 0; v < 5; ++v) gp[v] = o[v];
   if (float *M = mirror_current(a.mir)) {
     double r0, e0;
     mirror_base(a.mir, a.bt, gc, r0, e0);
@@ -485,7 +494,7 @@ __global__ void k_ghost(GhostArgs a, int count) {
 
 cudaError_t launch_ghost(const GhostArgs &a, int count, cudaStream_t s) {
   if (count <= 0) return cudaSuccess;
-  k_ghost<<<(count + 127) / 128, 128, 0, s>>>(a, count);
+  k_ghost<<<(count + kGhostPer - 1) / kGhostPer, kGhostThreads, 0, s>>>(a, count);
   return cudaGetLastError();
 }
 

@@ -465,6 +465,7 @@ def measure_twins(api, case, precision_name, subiters=2):
     api.set_reference_precision(api.PRECISION_SPLIT if precision_name == "split"
                                 else api.PRECISION_FP64)
     api.set_twin_scratch_kept(True)  # main.cpp keeps its scratch arrays
+    api.set_host_pinning(True)       # and its arrays for the whole run
     U1_, U1, U1q = c.U.copy(), c.U.copy(), c.U.copy()
     U1p1, U1p2, Rku1, Res = (np.zeros_like(c.U) for _ in range(4))
     er = np.zeros(8)
@@ -493,9 +494,10 @@ def measure_twins(api, case, precision_name, subiters=2):
             subiteration()
         dt = time.perf_counter() - t0
     finally:
+        api.release_host_arrays()  # before the arrays go
+        api.set_host_pinning(False)
         api.set_reference_precision(api.PRECISION_FP64)
         api.set_twin_scratch_kept(False)
-        api.release_host_arrays()
     return {"value": c.n_cells * subiters / dt, "unit": UNIT, "precision": precision_name,
             "case": f"{c.name}: {c.ncube - 1} cubes, {c.n_cells} cells",
             "subiters": subiters, "seconds": dt,

@@ -61,12 +61,15 @@ typedef struct bcmg_reference_config {
 int bcmg_set_reference_config(const bcmg_reference_config *cfg);
 void bcmg_get_reference_config(bcmg_reference_config *cfg);
 
-/* Host arrays of the twins.  The twins page-lock each caller array the
- * first time they see it (cudaHostRegister), so later copies run at the
- * host link's full rate; an array that cannot be registered is copied
- * pageable.  bcmg_release_host_arrays() unregisters every array and
- * forgets it: call it before freeing an array the twins have seen.
- * bcmg_set_host_pinning(0) stops the page-locking (and releases).
+/* Host arrays of the twins.  After bcmg_set_host_pinning(1) the twins
+ * page-lock each caller array the first time they see it
+ * (cudaHostRegister), so later copies run at the host link's full rate; an
+ * array that cannot be registered is copied pageable.  Off by default: a
+ * registration must end before its memory is freed, so only a caller whose
+ * arrays outlive the calls (like the reference's main.cpp) should turn it
+ * on, and it must call bcmg_release_host_arrays() (unregisters every array
+ * and forgets it) before freeing any of them.  bcmg_set_host_pinning(0)
+ * stops the page-locking and releases.
  *
  * BCM_Flux_XYZ_Viscous_Runge_kutta uploads the arrays a stage reads (RK 1:
  * U1_, U1, U1q; RK 2: also U1p1; RK 3: also U1p2 and Residual1, whose fluid

@@ -27,8 +27,7 @@ def twin_defaults():
     yield
     api.set_reference_precision(api.PRECISION_FP64)
     api.set_twin_scratch_kept(False)
-    api.set_host_pinning(True)
-    api.release_host_arrays()
+    api.set_host_pinning(False)
     api.set_reference_config()
 
 
@@ -75,6 +74,7 @@ def test_twin_subiterations_bitwise_in_every_copy_mode(name, mode, twin_defaults
     for _ in range(2):
         _oracle_subiteration(port, case, a)
         _subiteration_twins(case, b)
+    api.release_host_arrays()  # while the arrays are alive
     for k in ARRAYS:
         assert np.array_equal(getattr(a, k), getattr(b, k)), (name, mode, k)
 
