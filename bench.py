@@ -696,6 +696,48 @@ def run_gpu_arm(args, dist):
         print(json.dumps(line), flush=True)
 
 
+def run_accuracy(args):
+    """Accuracy over a configuration's own horizon: the FP64 and the split
+    path advance the workload from the same initial state for
+    args.accuracy dual-time steps (args.method sub-iterations, SUBITERS
+    each, one graph launch per step); at every checkpoint (a quarter of the
+    run) the split state and forces are compared with the FP64 path's
+    (relative L2 per variable, per-case drag and lift).  Prints one JSON
+    line; not the benchmark line."""
+    from bcm_cgli_gb300 import api
+    case = workload_case(TimedPreprocess(api.ibm_preprocess, "GPU, bcmg_ibm_preprocess"))
+    steps = args.accuracy
+    ctxs = {}
+    for p in ("fp64", "split"):
+        ctx = make_context(api, case, api.PRECISION_SPLIT if p == "split" else api.PRECISION_FP64)
+        if args.method == "lusgs":
+            ctx.set_method(api.METHOD_LUSGS, cfl=0.0, omega=1.5)
+        ctx.set_state(case.U, case.U, case.U)
+        ctxs[p] = ctx
+    marks = sorted({max(1, (steps * q) // 4) for q in (1, 2, 3, 4)})
+    out, done, secs = [], 0, {"fp64": 0.0, "split": 0.0}
+    for m in marks:
+        res = {}
+        for p, ctx in ctxs.items():
+            t0 = time.perf_counter()
+            er = None
+            for _ in range(m - done):
+                er = ctx.advance(1, SUBITERS, use_graph=True)
+            secs[p] += time.perf_counter() - t0
+            res[p] = (ctx.get_state()[0], er)
+        done = m
+        acc = accuracy(case, res["split"], res["fp64"], m)
+        out.append(acc)
+        print(json.dumps({"checkpoint": m, "max_rel_l2": acc["max_rel_l2"],
+                          "cd_rel_err_max": acc.get("cd_rel_err_max")}), file=sys.stderr,
+              flush=True)
+    for ctx in ctxs.values():
+        ctx.close()
+    print(json.dumps({"accuracy_horizon": WORKLOAD, "workload": WORKLOADS[WORKLOAD],
+                      "method": args.method, "subiters_per_step": SUBITERS, "steps": steps,
+                      "checkpoints": out, "seconds": secs}), flush=True)
+
+
 def run_flux_only(args):
     """Profiling target: the flux kernel alone on a Taylor-Green case of
     ncx^3 cubes of n^3 cells (ncx=6, n=24: 216 cubes, 3.0 M cells, 190 MB per
@@ -767,6 +809,9 @@ def main():
     ap.add_argument("--flux-form", type=int, default=None, choices=[0, 1, 2],
                     help="override the split flux form of the tuning table (1 packed face "
                          "pairs, 2 one face at a time)")
+    ap.add_argument("--accuracy", type=int, default=0, metavar="STEPS",
+                    help="accuracy over STEPS dual-time steps (split vs FP64 from the same "
+                         "state, checkpoints at each quarter) instead of the benchmark")
     ap.add_argument("--acc-steps", type=int, default=ACC_STEPS,
                     help="dual-time steps of the split-vs-FP64 accuracy comparison")
     args = ap.parse_args()
@@ -774,6 +819,9 @@ def main():
     WORKLOAD = args.workload
     if args.flux_only:
         run_flux_only(args)
+        return
+    if args.accuracy > 0:
+        run_accuracy(args)
         return
     if args.lusgs_only:
         run_lusgs_only(args)
