@@ -48,6 +48,10 @@ class Tuning(C.Structure):
                 ("flux_ms", C.c_double * 3), ("lusgs_ms", C.c_double * 2)]
 
 
+# int (*)(void *user, int phase, void *stream): the exchange hook of sharded runs
+EXCHANGE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_void_p)
+
+
 class RefConfig(C.Structure):
     _fields_ = [("ncube_x", C.c_int), ("mpi_ncube", C.c_int), ("mu_L", C.c_double),
                 ("rho0", C.c_double), ("U0", C.c_double), ("Uin", C.c_double),
@@ -82,6 +86,19 @@ def _declare(L):
     L.BCM_Interface.restype = None
     P = C.c_void_p
     L.bcmg_case_create.argtypes = [C.POINTER(CaseDesc), C.POINTER(P)]
+    L.bcmg_case_create_shard.argtypes = [C.POINTER(CaseDesc), C.c_int, C.POINTER(P)]
+    L.bcmg_shard_plan.argtypes = [C.c_int, P, P, P, C.c_int, C.c_int, C.POINTER(C.c_int), P,
+                                  C.POINTER(C.c_int), P]
+    L.bcmg_shard_bands.argtypes = [C.c_int, P, P, P, C.c_int, C.c_int, C.c_int,
+                                   C.POINTER(C.c_int), P]
+    L.bcmg_case_set_exchange.argtypes = [P, EXCHANGE_FN, P]
+    L.bcmg_case_set_halo.argtypes = [P, C.c_int, P, P, P, P]
+    L.bcmg_case_halo_bytes.argtypes = [P, C.c_int, C.POINTER(C.c_size_t),
+                                       C.POINTER(C.c_size_t)]
+    L.bcmg_case_halo_pack.argtypes = [P, C.c_int, P]
+    L.bcmg_case_halo_unpack.argtypes = [P, C.c_int, P]
+    L.bcmg_case_norm_sums.argtypes = [P, C.POINTER(P)]
+    L.bcmg_case_norm_sums_host.argtypes = [P, P, C.c_int]
     L.bcmg_case_destroy.argtypes = [P]
     L.bcmg_case_destroy.restype = None
     L.bcmg_case_set_state.argtypes = [P, P, P, P]

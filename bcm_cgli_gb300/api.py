@@ -20,7 +20,7 @@ import os
 
 import numpy as np
 
-from . import _lib
+from . import _lib, cases
 from ._lib import BcmgError, check, lib
 
 PRECISION_FP64 = 0
@@ -272,12 +272,17 @@ def _case_desc(case, precision, keep):
 class CaseContext:
     """A case resident in HBM (``bcmg_case_*``)."""
 
-    def __init__(self, case, precision=PRECISION_FP64):
+    def __init__(self, case, precision=PRECISION_FP64, nproxy=0):
+        """nproxy > 0: a rank's share of a cube-sharded run whose last nproxy
+        cube slots are proxies of remote cubes (bcmg_case_create_shard)."""
         self.case = case
         keep = []
         d = _case_desc(case, precision, keep)
         h = C.c_void_p()
-        check(lib().bcmg_case_create(C.byref(d), C.byref(h)))
+        if nproxy:
+            check(lib().bcmg_case_create_shard(C.byref(d), int(nproxy), C.byref(h)))
+        else:
+            check(lib().bcmg_case_create(C.byref(d), C.byref(h)))
         del keep
         self.h = h
         self.shape = case.U.shape
@@ -487,3 +492,150 @@ def probe_fp64_gflops():
     g = C.c_double()
     check(lib().bcmg_probe_fp64_rate(C.byref(g)))
     return g.value
+
+
+# ---------------------------------------------------------------------------
+# Cube-sharded runs
+# ---------------------------------------------------------------------------
+XCHG_HALO = 0
+XCHG_NORMS = 1
+
+
+class ShardedRun:
+    """One case split over ranks by cube (the reference's rank_map,
+    main.cpp:576-596), run in this process on the current GPU: a context per
+    rank (its own cubes, then proxies of the remote cubes its face tasks
+    read), each stepped by its own host thread.  The exchange hook of each
+    context packs its face bands for every peer into a device buffer, meets
+    the other ranks at a host barrier, unpacks the peers' bands into its
+    proxies, and for the norms adds the ranks' raw sums in rank order (the
+    reference's MPI_Allreduce, BCM_Flux_XYZ_Viscous_Runge_kutta.cpp:2641-2652).
+    Ranks meet only at host barriers, so no kernel of one rank ever waits on
+    another rank's.  The cells evolve bit for bit as in one context; ranks on
+    separate GPUs would move the same buffers with their own transport."""
+
+    def __init__(self, case, rank_of_cube, precision=PRECISION_FP64):
+        import threading
+
+        import torch
+        self.case = case
+        rk = np.asarray(rank_of_cube, np.int32)
+        self.nrank = int(rk[1:].max()) + 1
+        self.parts = [cases.shard_case(case, rk, r) for r in range(self.nrank)]
+        self.ctx = [CaseContext(sub, precision, nproxy=len(prox)) for sub, _, prox in self.parts]
+        self._keep = []
+        for r, (sub, own, prox) in enumerate(self.parts):
+            g2l = np.zeros(case.ncube, np.int32)
+            g2l[own] = np.arange(1, len(own) + 1)
+            g2l[prox] = np.arange(len(own) + 1, len(own) + len(prox) + 1)
+            send, recv = [], []
+            for p in range(self.nrank):
+                sb = cases.shard_bands(case, rk, r, p) if p != r else np.zeros((0, 4), np.int32)
+                rb = cases.shard_bands(case, rk, p, r) if p != r else np.zeros((0, 4), np.int32)
+                sb, rb = sb.copy(), rb.copy()
+                sb[:, 0] = g2l[sb[:, 0]]
+                rb[:, 0] = g2l[rb[:, 0]]
+                send.append(np.ascontiguousarray(sb, np.int32))
+                recv.append(np.ascontiguousarray(rb, np.int32))
+            self._keep += send + recv
+            ns = (C.c_int * self.nrank)(*[len(x) for x in send])
+            nr = (C.c_int * self.nrank)(*[len(x) for x in recv])
+            ps = (C.c_void_p * self.nrank)(*[x.ctypes.data for x in send])
+            pr = (C.c_void_p * self.nrank)(*[x.ctypes.data for x in recv])
+            check(lib().bcmg_case_set_halo(self.ctx[r].h, self.nrank, ns, ps, nr, pr))
+        self.buf = [[None] * self.nrank for _ in range(self.nrank)]
+        for r in range(self.nrank):
+            for p in range(self.nrank):
+                sb, _ = self.halo_bytes(r, p)
+                self.buf[r][p] = torch.empty(max(sb, 16), dtype=torch.uint8, device="cuda")
+        self.barrier = threading.Barrier(self.nrank)
+        self.sums = np.zeros((self.nrank, 7))
+        self.error = None
+        self._hooks = [_lib.EXCHANGE_FN(self._make_hook(r)) for r in range(self.nrank)]
+        for r in range(self.nrank):
+            check(lib().bcmg_case_set_exchange(self.ctx[r].h, self._hooks[r], None))
+
+    def halo_bytes(self, r, p):
+        a, b = C.c_size_t(), C.c_size_t()
+        check(lib().bcmg_case_halo_bytes(self.ctx[r].h, int(p), C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def _make_hook(self, r):
+        L = lib()
+
+        def hook(user, phase, stream):
+            try:
+                h = self.ctx[r].h
+                if phase == XCHG_HALO:
+                    for p in range(self.nrank):
+                        if p != r:
+                            check(L.bcmg_case_halo_pack(h, p, self.buf[r][p].data_ptr()))
+                    check(L.bcmg_case_sync(h))
+                    self.barrier.wait()  # every rank's bands are packed
+                    for p in range(self.nrank):
+                        if p != r:
+                            check(L.bcmg_case_halo_unpack(h, p, self.buf[p][r].data_ptr()))
+                    check(L.bcmg_case_sync(h))
+                    self.barrier.wait()  # the buffers may be packed again
+                else:
+                    s = np.zeros(7)
+                    check(L.bcmg_case_norm_sums_host(h, s.ctypes.data, 0))
+                    self.sums[r] = s
+                    self.barrier.wait()
+                    tot = self.sums[0].copy()
+                    for p in range(1, self.nrank):  # rank order: the same bits on every rank
+                        tot = tot + self.sums[p]
+                    check(L.bcmg_case_norm_sums_host(h, tot.ctypes.data, 1))
+                    self.barrier.wait()
+                return 0
+            except Exception as exc:  # reported by the stepping call
+                self.error = exc
+                self.barrier.abort()
+                return 1
+        return hook
+
+    def _run(self, fn):
+        import threading
+        out = [None] * self.nrank
+        errs = []
+
+        def work(r):
+            try:
+                out[r] = fn(self.ctx[r])
+            except Exception as exc:
+                errs.append(exc)
+                self.barrier.abort()
+
+        ts = [threading.Thread(target=work, args=(r,)) for r in range(self.nrank)]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+        if errs or self.error:
+            raise BcmgError(f"sharded step failed: {self.error or errs[0]}")
+        return out
+
+    def set_state(self, U1_, U1, U1q):
+        for (sub, own, prox), ctx in zip(self.parts, self.ctx):
+            sl = np.concatenate([[0], own, prox])
+            ctx.set_state(U1_[sl], U1[sl], U1q[sl])
+
+    def advance(self, steps, subiters):
+        """Dual-time steps on every rank together; returns er (the same on
+        every rank)."""
+        ers = self._run(lambda c: c.advance(steps, subiters, use_graph=False))
+        return ers[0]
+
+    def get_state(self):
+        """(U1_, U1, U1q) in the global layout, each cube from its owner."""
+        out = [np.array(self.case.U) for _ in range(3)]
+        for (sub, own, prox), ctx in zip(self.parts, self.ctx):
+            st = ctx.get_state()
+            for g, a in zip(out, st):
+                g[own] = a[1:1 + len(own)]
+        return out
+
+    def close(self):
+        for c in self.ctx:
+            lib().bcmg_case_set_exchange(c.h, _lib.EXCHANGE_FN(), None)
+            c.close()

@@ -71,6 +71,9 @@ class Case:
     ibm_minus: tuple | None = None  # (weight[8n+1], GCindex[4n+1], IPsur[4n+1])
     ibm_plus: tuple | None = None
     meta: dict = field(default_factory=dict)
+    # Boundary-cube lists given explicitly (a rank's share of a sharded case,
+    # whose own bounding box is not the domain's); None: from the geometry.
+    bc: tuple | None = None
 
     @property
     def S(self) -> int:
@@ -87,6 +90,8 @@ class Case:
         Returns six int32 arrays (x lower, x upper, y lower, y upper, z lower,
         z upper) of cube numbers in increasing order.
         """
+        if self.bc is not None:
+            return [np.asarray(x, np.int32) for x in self.bc]
         c = np.arange(1, self.ncube)
         o = self.origin[1:]
         s = self.cube_size[1:]
@@ -704,3 +709,88 @@ class CaseBatch:
                 g += c.ncube - 1
             self._U = U
         return self._U
+
+
+def shard_plan(case, rank_of_cube, rank):
+    """(own cubes, proxy cubes) of `rank` in a cube-sharded run, global
+    numbers, from the library's planner (bcmg_shard_plan): the proxies are
+    the remote cubes whose faces the rank's face tasks read."""
+    import ctypes as C
+    from . import _lib
+    L = _lib.lib()
+    adj = np.ascontiguousarray(case.adj, np.int32)
+    csl = np.ascontiguousarray(case.csl, np.int32)
+    rk = np.ascontiguousarray(rank_of_cube, np.int32)
+    cap = case.ncube
+    loc, prox = np.zeros(cap, np.int32), np.zeros(cap, np.int32)
+    nl, npx = C.c_int(), C.c_int()
+    r = L.bcmg_shard_plan(case.ncube, adj.ctypes.data, csl.ctypes.data, rk.ctypes.data,
+                          int(rank), cap, C.byref(nl), loc.ctypes.data, C.byref(npx),
+                          prox.ctypes.data)
+    if r != 0:
+        raise ValueError(f"bcmg_shard_plan failed ({r})")
+    return loc[:nl.value].copy(), prox[:npx.value].copy()
+
+
+def shard_bands(case, rank_of_cube, src, dst):
+    """Face bands rank dst reads from rank src: [m, 4] (global source cube,
+    axis, side of the source's face, layers), in the library's fixed order."""
+    import ctypes as C
+    from . import _lib
+    L = _lib.lib()
+    adj = np.ascontiguousarray(case.adj, np.int32)
+    csl = np.ascontiguousarray(case.csl, np.int32)
+    rk = np.ascontiguousarray(rank_of_cube, np.int32)
+    nb = C.c_int()
+    r = L.bcmg_shard_bands(case.ncube, adj.ctypes.data, csl.ctypes.data, rk.ctypes.data,
+                           int(src), int(dst), 0, C.byref(nb), None)
+    if r not in (0, -2):
+        raise ValueError(f"bcmg_shard_bands failed ({r})")
+    out = np.zeros(4 * max(nb.value, 1), np.int32)
+    r = L.bcmg_shard_bands(case.ncube, adj.ctypes.data, csl.ctypes.data, rk.ctypes.data,
+                           int(src), int(dst), nb.value, C.byref(nb), out.ctypes.data)
+    if r != 0:
+        raise ValueError(f"bcmg_shard_bands failed ({r})")
+    return out[:4 * nb.value].reshape(-1, 4)
+
+
+def shard_case(case, rank_of_cube, rank):
+    """The case of one rank of a cube-sharded run (the reference's rank_map,
+    main.cpp:576-596): its own cubes in slots 1..nlocal (ascending global
+    numbers), then one proxy slot per remote cube its face tasks read;
+    adjacency, sizes, levels, flags and state taken from the global case,
+    adjacency entries mapped to local slots (0 for cubes of neither list),
+    boundary lists and IBM tables of the own cubes only.  Returns (case,
+    own cubes, proxy cubes)."""
+    own, prox = shard_plan(case, rank_of_cube, rank)
+    slots = np.concatenate([[0], own, prox]).astype(np.int64)
+    g2l = np.zeros(case.ncube, np.int32)
+    g2l[own] = np.arange(1, len(own) + 1)
+    g2l[prox] = np.arange(len(own) + 1, len(own) + len(prox) + 1)
+    adj = g2l[case.adj[slots]]
+    adj[0] = 0
+    cube_size = case.cube_size[slots].copy()
+    cube_size[0] = case.cube_size[0]
+    mine = np.zeros(case.ncube, bool)
+    mine[own] = True
+    bc = tuple(g2l[x[mine[x]]] for x in case.bc_lists())
+
+    def ibm(t):
+        if t is None:
+            return None
+        W, G, I = t
+        m = (len(G) - 1) // 4
+        gc, ip, w = G[1:].reshape(m, 4).copy(), I[1:].reshape(m, 4).copy(), W[1:].reshape(m, 8)
+        keep = mine[gc[:, 0]] if m else np.zeros(0, bool)
+        gc, ip, w = gc[keep], ip[keep], w[keep]
+        gc[:, 0] = g2l[gc[:, 0]]
+        ip[:, 0] = g2l[ip[:, 0]]
+        return _pack_tables(gc, ip, w)
+
+    sub = Case(n=case.n, ncube=len(slots), phys=case.phys, cube_size=cube_size,
+               csl=case.csl[slots].astype(np.int32), origin=case.origin[slots].copy(),
+               adj=np.ascontiguousarray(adj, np.int32),
+               fws=np.ascontiguousarray(case.fws[slots]), U=np.ascontiguousarray(case.U[slots]),
+               dT=case.dT, dTau=case.dTau, e=case.e, name=f"{case.name}.rank{rank}",
+               ibm_minus=ibm(case.ibm_minus), ibm_plus=ibm(case.ibm_plus), bc=bc)
+    return sub, own, prox

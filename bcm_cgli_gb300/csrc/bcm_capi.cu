@@ -204,6 +204,20 @@ bool valid_n(int n) { return n >= 4 && n % 4 == 0 && n <= 256; }
 struct bcmg_case {
   Phys ph{};
   int ncube = 0, S = 0;
+  // Cube-sharded runs (bcmg_case_create_shard): cube slots 1..nreal are this
+  // rank's cubes, the rest proxies of remote cubes (read by face tasks,
+  // filled by the halo exchange, never advanced).  nreal = ncube - 1 else.
+  int nreal = 0;
+  bcmg_exchange_fn xchg = nullptr;
+  void *xchg_user = nullptr;
+  double *nsum = nullptr;  // device [7]: raw norm sums handed to the exchange hook
+  struct Halo {
+    int *send = nullptr, *recv = nullptr;            // device band tables (4 ints each)
+    long long *soff = nullptr, *roff = nullptr;      // device first cell of each band
+    int nsend = 0, nrecv = 0;
+    long long send_cells = 0, recv_cells = 0;
+  };
+  std::vector<Halo> halo;
   double dT = 0, dTau = 0, e = 0;
   int precision = 0;
   size_t ncell = 0;
@@ -357,6 +371,11 @@ struct bcmg_case {
     dfree(bc_masks); dfree(partials); dfree(er); dfree(emax);
     dfree(cases); dfree(cube_case); dfree(rk_blk); dfree(case_blk_rk); dfree(case_blk_flux);
     dfree(case_blk_cube);
+    dfree(nsum);
+    for (auto &h : halo) {
+      dfree(h.send); dfree(h.recv); dfree(h.soff); dfree(h.roff);
+    }
+    halo.clear();
     ibm.release();
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
@@ -433,9 +452,9 @@ int case_flux(bcmg_case *c, int RK) {
     sa.Residual1 = c->Residual1;
     sa.bt = c->bt();
     sa.push = RK >= 1 ? c->push_table() : nullptr;
-    CK(launch_flux_split(sa, c->ncube - 1, c->stream));
+    CK(launch_flux_split(sa, c->nreal, c->stream));
   } else {
-    CK(launch_flux_fp64(a, c->ncube - 1, c->stream));
+    CK(launch_flux_fp64(a, c->nreal, c->stream));
   }
   if (c->profile) CK(cudaEventRecord(e1, c->stream));
   ++c->launches;
@@ -451,6 +470,12 @@ int case_flux(bcmg_case *c, int RK) {
 enum IfaceList { kIfaceFull, kIfacePrologue, kIfaceClosing };
 
 int case_interface(bcmg_case *c, IfaceList list = kIfaceFull) {
+  if (c->xchg) {  // sharded: the proxies' face bands first
+    if (c->xchg(c->xchg_user, BCMG_XCHG_HALO, c->stream) != 0) {
+      set_err("exchange hook failed (halo)");
+      return BCMG_ERR_CUDA;
+    }
+  }
   InterfaceArgs ia;
   ia.n = c->ph.n;
   ia.ntasks = c->ntasks;
@@ -523,12 +548,30 @@ LusgsSplitArgs lusgs_split_args(bcmg_case *c) {
   return l;
 }
 
+// Norms of one case over nb partial blocks; sharded contexts hand the raw
+// sums to the exchange hook, which adds them over the ranks.
+int case_norms(bcmg_case *c, int nb) {
+  if (!c->xchg) {
+    CK(launch_norms(c->ph, c->partials, nb, c->er, c->stream, c->bt().active));
+    ++c->launches;
+    return BCMG_OK;
+  }
+  CK(launch_norm_sums(c->partials, nb, c->nsum, c->stream, c->bt().active));
+  if (c->xchg(c->xchg_user, BCMG_XCHG_NORMS, c->stream) != 0) {
+    set_err("exchange hook failed (norms)");
+    return BCMG_ERR_CUDA;
+  }
+  CK(launch_norm_final(c->ph, c->nsum, c->er, c->stream, c->bt().active));
+  c->launches += 2;
+  return BCMG_OK;
+}
+
 int case_lusgs(bcmg_case *c, bool full = true) {
   int r;
   if ((r = case_prologue(c, full))) return r;
   if ((r = case_flux(c, 0))) return r;
   if (c->precision == BCMG_PRECISION_SPLIT) {
-    CK(launch_lusgs_split(lusgs_split_args(c), c->ncube - 1, c->stream));
+    CK(launch_lusgs_split(lusgs_split_args(c), c->nreal, c->stream));
   } else {
     LusgsArgs l;
     l.ph = c->ph;
@@ -544,15 +587,15 @@ int case_lusgs(bcmg_case *c, bool full = true) {
     l.Residual1 = c->Residual1;
     l.partials = c->partials;
     l.bt = c->bt();
-    CK(launch_lusgs(l, c->ncube - 1, c->stream));
+    CK(launch_lusgs(l, c->nreal, c->stream));
   }
   ++c->launches;
   if (c->batched)
     CK(launch_norms_batch(c->ph.n, c->cases, c->case_blk_cube, c->ncase, c->partials, c->er,
                           c->stream, c->bt().active));
-  else
-    CK(launch_norms(c->ph, c->partials, c->ncube - 1, c->er, c->stream, c->bt().active));
-  ++c->launches;
+  else if ((r = case_norms(c, c->nreal)))
+    return r;
+  if (c->batched) ++c->launches;
   // the split sweep made the same-level copies of the updated cells
   return case_interface(c, c->precision == BCMG_PRECISION_SPLIT && c->push_table()
                                ? kIfaceClosing
@@ -566,21 +609,22 @@ int case_stage(bcmg_case *c, int RK, bool full = true) {
   int nb = 0;
   if (c->precision == BCMG_PRECISION_SPLIT) {
     // the split flux kernel applied the stage update and wrote the partials
-    nb = flux_split_blocks(c->ph.n, c->ncube - 1, c->tile);
+    nb = flux_split_blocks(c->ph.n, c->nreal, c->tile);
     if (RK == 3) {
-      if (c->batched)
+      if (c->batched) {
         CK(launch_norms_batch(c->ph.n, c->cases, c->case_blk_flux, c->ncase, c->partials, c->er,
                               c->stream, c->bt().active));
-      else
-        CK(launch_norms(c->ph, c->partials, nb, c->er, c->stream, c->bt().active));
-      ++c->launches;
+        ++c->launches;
+      } else if ((r = case_norms(c, nb))) {
+        return r;
+      }
     }
     // the flux kernel made the same-level copies of the updated cells
     return case_interface(c, c->push_table() ? kIfaceClosing : kIfaceFull);
   }
   RkArgs k;
   k.ph = c->ph;
-  k.ncube = c->ncube;
+  k.ncube = c->nreal + 1;
   k.RK = RK;
   k.FWS = c->FWS;
   k.U1_ = c->U1_;
@@ -598,12 +642,14 @@ int case_stage(bcmg_case *c, int RK, bool full = true) {
   }
   ++c->launches;
   if (RK == 3) {
-    if (c->batched)
+    if (c->batched) {
       CK(launch_norms_batch(c->ph.n, c->cases, c->case_blk_rk, c->ncase, c->partials, c->er,
                             c->stream, c->bt().active));
-    else
-      CK(launch_norms(c->ph, c->partials, nb, c->er, c->stream, c->bt().active));
-    ++c->launches;
+      ++c->launches;
+    } else {
+      int r = case_norms(c, nb);
+      if (r) return r;
+    }
   }
   return case_interface(c);
 }
@@ -785,7 +831,8 @@ CaseConst case_const(const bcmg_case_desc &d) {
   return q;
 }
 
-int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out);
+int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out,
+                  int nproxy = 0);
 
 }  // namespace
 
@@ -794,12 +841,141 @@ extern "C" int bcmg_case_create(const bcmg_case_desc *d, bcmg_case **out) {
   return create_common(d, nullptr, out);
 }
 
+extern "C" int bcmg_case_create_shard(const bcmg_case_desc *d, int nproxy, bcmg_case **out) {
+  TraceRange trace("bcmg_case_create_shard");
+  return create_common(d, nullptr, out, nproxy);
+}
+
+extern "C" int bcmg_case_set_exchange(bcmg_case *c, bcmg_exchange_fn fn, void *user) {
+  clear_err();
+  if (!c) { set_err("null context"); return BCMG_ERR_ARG; }
+  if (c->batched && fn) { set_err("batches are not sharded"); return BCMG_ERR_UNSUPPORTED; }
+  c->xchg = fn;
+  c->xchg_user = user;
+  if (c->graph) cudaGraphExecDestroy(c->graph);  // captured steps lack the hook
+  c->graph = nullptr;
+  c->graph_subiters = -1;
+  if (c->cgraph) cudaGraphExecDestroy(c->cgraph);
+  c->cgraph = nullptr;
+  return BCMG_OK;
+}
+
+extern "C" int bcmg_case_set_halo(bcmg_case *c, int npeer, const int *nsend,
+                                  const int *const *send, const int *nrecv,
+                                  const int *const *recv) {
+  clear_err();
+  if (!c || npeer < 0 || (npeer > 0 && (!nsend || !send || !nrecv || !recv))) {
+    set_err("bad arguments");
+    return BCMG_ERR_ARG;
+  }
+  const int n = c->ph.n;
+  // Every band names an own cube (send) or a proxy (recv), an axis, a side
+  // and 1..n layers: the kernels then stay inside the case's arrays.
+  auto valid = [&](int cnt, const int *b, bool own) {
+    if (cnt < 0 || (cnt > 0 && !b)) return false;
+    for (int i = 0; i < cnt; ++i) {
+      const int cube = b[4 * i], ax = b[4 * i + 1], side = b[4 * i + 2], L = b[4 * i + 3];
+      const bool cube_ok = own ? (cube >= 1 && cube <= c->nreal)
+                               : (cube > c->nreal && cube < c->ncube);
+      if (!cube_ok || ax < 0 || ax > 2 || side < 0 || side > 1 || L < 1 || L > n) return false;
+    }
+    return true;
+  };
+  for (int p = 0; p < npeer; ++p)
+    if (!valid(nsend[p], send[p], true) || !valid(nrecv[p], recv[p], false)) {
+      set_err("halo band outside the context (send: own cubes, recv: proxy slots)");
+      return BCMG_ERR_ARG;
+    }
+  for (auto &h : c->halo) {
+    dfree(h.send); dfree(h.recv); dfree(h.soff); dfree(h.roff);
+  }
+  c->halo.assign((size_t)npeer, bcmg_case::Halo());
+  auto upload = [&](int cnt, const int *b, int **tab, long long **off, long long &cells) {
+    std::vector<long long> o((size_t)cnt);
+    cells = 0;
+    for (int i = 0; i < cnt; ++i) {
+      o[i] = cells;
+      cells += (long long)b[4 * i + 3] * n * n;
+    }
+    if (cnt == 0) return BCMG_OK;
+    CK(dalloc(tab, 4 * (size_t)cnt));
+    CK(dalloc(off, (size_t)cnt));
+    CK(cudaMemcpy(*tab, b, sizeof(int) * 4 * cnt, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(*off, o.data(), sizeof(long long) * cnt, cudaMemcpyHostToDevice));
+    return BCMG_OK;
+  };
+  for (int p = 0; p < npeer; ++p) {
+    bcmg_case::Halo &h = c->halo[p];
+    h.nsend = nsend[p];
+    h.nrecv = nrecv[p];
+    int r = upload(h.nsend, send[p], &h.send, &h.soff, h.send_cells);
+    if (!r) r = upload(h.nrecv, recv[p], &h.recv, &h.roff, h.recv_cells);
+    if (r) return r;
+  }
+  return BCMG_OK;
+}
+
+extern "C" int bcmg_case_halo_bytes(const bcmg_case *c, int peer, size_t *send_bytes,
+                                    size_t *recv_bytes) {
+  if (!c || peer < 0 || peer >= (int)c->halo.size()) return BCMG_ERR_ARG;
+  const size_t per = 5 * sizeof(double) + (c->M ? 5 * sizeof(float) : 0);
+  if (send_bytes) *send_bytes = per * (size_t)c->halo[peer].send_cells;
+  if (recv_bytes) *recv_bytes = per * (size_t)c->halo[peer].recv_cells;
+  return BCMG_OK;
+}
+
+static int halo_move(bcmg_case *c, int peer, void *buf, int unpack) {
+  clear_err();
+  if (!c || peer < 0 || peer >= (int)c->halo.size() || !buf) {
+    set_err("bad context, peer or buffer");
+    return BCMG_ERR_ARG;
+  }
+  const bcmg_case::Halo &h = c->halo[peer];
+  if (unpack)
+    CK(launch_halo(c->U1_, c->mir(), h.recv, h.roff, h.nrecv, h.recv_cells, c->ph.n, buf, 1,
+                   c->stream));
+  else
+    CK(launch_halo(c->U1_, c->mir(), h.send, h.soff, h.nsend, h.send_cells, c->ph.n, buf, 0,
+                   c->stream));
+  return BCMG_OK;
+}
+
+extern "C" int bcmg_case_halo_pack(bcmg_case *c, int peer, void *dev_buf) {
+  return halo_move(c, peer, dev_buf, 0);
+}
+
+extern "C" int bcmg_case_halo_unpack(bcmg_case *c, int peer, const void *dev_buf) {
+  return halo_move(c, peer, const_cast<void *>(dev_buf), 1);
+}
+
+extern "C" int bcmg_case_norm_sums(bcmg_case *c, double **dev_sums) {
+  if (!c || !dev_sums) return BCMG_ERR_ARG;
+  *dev_sums = c->nsum;
+  return BCMG_OK;
+}
+
+extern "C" int bcmg_case_norm_sums_host(bcmg_case *c, double *sums, int write) {
+  clear_err();
+  if (!c || !sums) { set_err("null argument"); return BCMG_ERR_ARG; }
+  if (write)
+    CK(cudaMemcpyAsync(c->nsum, sums, 7 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  else
+    CK(cudaMemcpyAsync(sums, c->nsum, 7 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return BCMG_OK;
+}
+
 namespace {
 
-int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out) {
+int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out,
+                  int nproxy) {
   clear_err();
   if (!d || !out) {
     set_err("null argument");
+    return BCMG_ERR_ARG;
+  }
+  if (nproxy < 0 || nproxy > d->ncube - 2 || (nproxy > 0 && bi)) {
+    set_err("nproxy must leave at least one own cube (and batches are not sharded)");
     return BCMG_ERR_ARG;
   }
   *out = nullptr;
@@ -834,6 +1010,7 @@ int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out)
   c->ph.Uin = d->Uin;
   c->ph.P0 = d->P0;
   c->ncube = d->ncube;
+  c->nreal = d->ncube - 1 - nproxy;
   c->S = d->n + 4;
   c->dT = d->deltaT;
   c->dTau = d->deltaTau;
@@ -857,6 +1034,17 @@ int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out)
   std::vector<int> task_cube(tasks.size());
   for (int cc = 1; cc < d->ncube; ++cc)
     for (int t = off[cc]; t < off[cc + 1]; ++t) task_cube[t] = cc;
+  if (nproxy > 0) {  // proxies are read, never written
+    std::vector<FaceTask> kt;
+    std::vector<int> kc;
+    for (size_t t = 0; t < tasks.size(); ++t)
+      if (task_cube[t] <= c->nreal) {
+        kt.push_back(tasks[t]);
+        kc.push_back(task_cube[t]);
+      }
+    tasks.swap(kt);
+    task_cube.swap(kc);
+  }
   c->ntasks = (int)tasks.size();
   const int *lists[6] = {d->xl, d->xu, d->yl, d->yu, d->zl, d->zu};
   const int counts[6] = {d->nxl, d->nxu, d->nyl, d->nyu, d->nzl, d->nzu};
@@ -887,6 +1075,7 @@ int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out)
             ck(dalloc(&c->bc_cubes, bcc.size()), "alloc") &&
             ck(dalloc(&c->bc_masks, bcm.size()), "alloc") &&
             ck(dalloc(&c->er, 8 * (size_t)c->ncase), "alloc") &&
+            ck(dalloc(&c->nsum, 7), "alloc") &&
             ck(dalloc(&c->emax, 6 * (size_t)c->ncase), "alloc");
   if (!ok) return fail(BCMG_ERR_CUDA);
   if (d->precision == BCMG_PRECISION_SPLIT &&
@@ -1013,6 +1202,9 @@ int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out)
     std::vector<char> keep;
     prologue_task_mask(d->n, d->ncube, tasks, task_cube, bcc, bcm, d->gc_minus, nm, d->gc_plus,
                        np, keep);
+    // a proxy's bands are refilled by the exchange before every call
+    for (size_t t = 0; t < tasks.size(); ++t)
+      if (tasks[t].src > c->nreal) keep[t] = 1;
     std::vector<FaceTask> tp;
     std::vector<int> cp;
     for (size_t t = 0; t < tasks.size(); ++t)
@@ -1038,7 +1230,7 @@ int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out)
     std::vector<FaceTask> tq;
     std::vector<int> cq;
     for (size_t t = 0; t < tasks.size(); ++t)
-      if (tasks[t].kind != 0) {
+      if (tasks[t].kind != 0 || tasks[t].src > c->nreal) {  // proxies push nothing
         tq.push_back(tasks[t]);
         cq.push_back(task_cube[t]);
       }
@@ -1130,6 +1322,10 @@ int bcmg_case_advance(bcmg_case *c, int steps, int subiters, int use_graph, doub
   TraceRange trace("bcmg_case_advance");
   clear_err();
   if (!c || steps < 0 || subiters < 1) { set_err("bad arguments"); return BCMG_ERR_ARG; }
+  if (use_graph && c->xchg) {
+    set_err("a context with an exchange hook steps without CUDA graphs (use_graph = 0)");
+    return BCMG_ERR_UNSUPPORTED;
+  }
   if (emax)
     CK(cudaMemcpyAsync(c->emax, emax, 6 * sizeof(double) * c->ncase, cudaMemcpyHostToDevice,
                        c->stream));
@@ -1425,6 +1621,10 @@ int bcmg_case_advance_converged(bcmg_case *c, int steps, int max_subiters, doubl
   if (!c || steps < 0 || max_subiters < 1 || !(tol > 0)) {
     set_err("bad arguments");
     return BCMG_ERR_ARG;
+  }
+  if (use_graph && c->xchg) {
+    set_err("a context with an exchange hook steps without CUDA graphs (use_graph = 0)");
+    return BCMG_ERR_UNSUPPORTED;
   }
   if (!c->active) {
     CK(dalloc(&c->active, (size_t)c->ncase));

@@ -223,6 +223,55 @@ __global__ void __launch_bounds__(1024) k_iface_edges(InterfaceArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Halo exchange of cube-sharded runs: the face bands a remote rank's face
+// tasks read, gathered from this rank's cubes into a buffer, or scattered
+// from a buffer into the proxy slots that stand for the remote cubes.  One
+// CTA per band; a band's cells go in (layer, first in-face index, second)
+// order, the in-face axes in x<y<z order.  Pure copies, so the proxies hold
+// the remote cells bit for bit.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kHaloThreads)
+    k_halo(double *U, Mirror mir, const int *bands, const long long *offs, long long total_cells,
+           int n, double *bufU, int unpack) {
+  float *M = mirror_current(mir);  // split precision: the current mirror too
+  const int b = blockIdx.x;
+  const int c = bands[4 * b], ax = bands[4 * b + 1], side = bands[4 * b + 2],
+            L = bands[4 * b + 3];
+  const int S = n + 4;
+  const int t0 = ax == 0 ? 1 : 0, t1 = ax == 2 ? 1 : 2;
+  const int l0 = side == 1 ? n + 2 - L : 2;  // first layer along the axis
+  const long long o0 = offs[b];
+  float *bufM = M ? reinterpret_cast<float *>(bufU + 5 * total_cells) : nullptr;
+  const int cells = L * n * n;
+  for (int w = threadIdx.x; w < cells * 5; w += blockDim.x) {
+    const int v = w % 5, cell = w / 5;
+    const int l = cell / (n * n), p = (cell / n) % n, q = cell % n;
+    int x[3];
+    x[ax] = l0 + l;
+    x[t0] = 2 + p;
+    x[t1] = 2 + q;
+    const size_t g = 5 * cell_index(S, c, x[0], x[1], x[2]) + v;
+    const size_t h = 5 * (size_t)(o0 + cell) + v;
+    if (unpack) {
+      U[g] = bufU[h];
+      if (M) M[g] = bufM[h];
+    } else {
+      bufU[h] = U[g];
+      if (M) bufM[h] = M[g];
+    }
+  }
+}
+
+cudaError_t launch_halo(double *U, const Mirror &mir, const int *bands, const long long *offs,
+                        int nband, long long total_cells, int n, void *buf, int unpack,
+                        cudaStream_t s) {
+  if (nband <= 0) return cudaSuccess;
+  k_halo<<<nband, kHaloThreads, 0, s>>>(U, mir, bands, offs, total_cells, n,
+                                        static_cast<double *>(buf), unpack);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_interface(const InterfaceArgs &a, int ncubes_total, cudaStream_t s) {
   if (ncubes_total <= 1) return cudaSuccess;
   if (a.ntasks > 0) {

@@ -145,6 +145,12 @@ cudaError_t launch_rk_chunked(const RkArgs &a, long long chunk, int nblocks, cud
 // Deterministic final reduction of partials -> er[1..7] (device, 8 doubles).
 cudaError_t launch_norms(const Phys &ph, const double *partials, int nblocks, double *er,
                          cudaStream_t s, const int *active = nullptr);
+// Cube-sharded runs: raw sums of the partial blocks (sums[7]), and the norms
+// er[1..7] from sums added over the ranks.
+cudaError_t launch_norm_sums(const double *partials, int nblocks, double *sums, cudaStream_t s,
+                             const int *active = nullptr);
+cudaError_t launch_norm_final(const Phys &ph, const double *sums, double *er, cudaStream_t s,
+                              const int *active = nullptr);
 // Batches: case q reduces partial blocks [case_blk[q], case_blk[q+1]) into
 // er[8q .. 8q+7] with its own normalisers.
 cudaError_t launch_norms_batch(int n, const CaseConst *cases, const int *case_blk, int ncase,
@@ -221,6 +227,17 @@ struct InterfaceArgs {
   Mirror mir;  // split precision: every written cell's mirror value too
 };
 cudaError_t launch_interface(const InterfaceArgs &a, int ndst, cudaStream_t s);
+
+// Halo exchange of cube-sharded runs: band b = bands[4b..4b+3] = (cube slot,
+// axis, side 1 high / 0 low face, layers); its cells are the `layers`
+// interior layers next to that face over the whole n x n face, starting at
+// cell offs[b] of the buffer; the buffer holds every cell's five doubles,
+// then (split precision) its five mirror floats.  unpack = 0 gathers U (and
+// the current mirror buffer) into the buffer, 1 scatters the buffer into
+// them.
+cudaError_t launch_halo(double *U, const Mirror &mir, const int *bands, const long long *offs,
+                        int nband, long long total_cells, int n, void *buf, int unpack,
+                        cudaStream_t s);
 
 // X/Y/Z boundary conditions for a list of (cube, mask) pairs; mask bits
 // 0..5 = x lower, x upper, y lower, y upper, z lower, z upper.  axes selects

@@ -156,6 +156,22 @@ __global__ void k_norms(Phys ph, const double *partials, int nblocks, double *er
   if (threadIdx.x == 0) write_norms(ph.n, ph.mpi_ncube, ph.rho0, ph.U0, tot, er);
 }
 
+// Cube-sharded runs: the raw sums of this rank's blocks (the ranks' sums are
+// then added, as the reference's MPI_Allreduce does, BCM_Flux...cpp
+// :2641-2652), and the norms from the summed values.
+__global__ void k_norm_sums(const double *partials, int nblocks, double *sums,
+                            const int *active) {
+  if (active && !active[0]) return;
+  __shared__ double tot[7];
+  sum_partials(partials, 0, nblocks, tot);
+  if (threadIdx.x < 7) sums[threadIdx.x] = tot[threadIdx.x];
+}
+
+__global__ void k_norm_final(Phys ph, const double *sums, double *er, const int *active) {
+  if (active && !active[0]) return;
+  write_norms(ph.n, ph.mpi_ncube, ph.rho0, ph.U0, sums, er);
+}
+
 // One CTA per case of a batch.
 __global__ void k_norms_batch(int n, const CaseConst *cases, const int *case_blk,
                               const double *partials, double *er, const int *active) {
@@ -198,6 +214,18 @@ cudaError_t launch_rk(const RkArgs &a, int *nblocks_out, cudaStream_t s) {
 cudaError_t launch_norms(const Phys &ph, const double *partials, int nblocks, double *er,
                          cudaStream_t s, const int *active) {
   k_norms<<<1, 7 * 32 * kNormWarps, 0, s>>>(ph, partials, nblocks, er, active);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_norm_sums(const double *partials, int nblocks, double *sums, cudaStream_t s,
+                             const int *active) {
+  k_norm_sums<<<1, 7 * 32 * kNormWarps, 0, s>>>(partials, nblocks, sums, active);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_norm_final(const Phys &ph, const double *sums, double *er, cudaStream_t s,
+                              const int *active) {
+  k_norm_final<<<1, 1, 0, s>>>(ph, sums, er, active);
   return cudaGetLastError();
 }
 

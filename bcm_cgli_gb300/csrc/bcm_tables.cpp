@@ -5,8 +5,10 @@
 #include "bcm_tables.h"
 
 #include <algorithm>
+#include <array>
 #include <cstdint>
 #include <cstdio>
+#include <map>
 #include <unordered_map>
 
 namespace bcmg {
@@ -384,4 +386,97 @@ extern "C" int bcmg_interface_plan(int n, int ncube, const int *adj_number, cons
   const bool ok = bcmg::build_push_table(ncube, tasks, task_cube, tbl);
   if (push) std::copy(tbl.begin(), tbl.end(), push);
   return ok ? (int)tasks.size() : -3;
+}
+
+// ---------------------------------------------------------------------------
+// Cube-sharded runs.  The reference spreads cubes over MPI ranks by
+// rank_map.dat (main.cpp:576-596) and exchanges the face layers of cubes on
+// other ranks every interface call (BCM_Interface.cpp:213-1738,
+// :4367-5634).  Here a rank holds its own cubes, then one "proxy" slot per
+// remote cube that a face task of one of its cubes reads; before each
+// interface call the face bands those tasks read are copied into the proxy
+// slots, and the interface kernels run unchanged.
+// ---------------------------------------------------------------------------
+namespace {
+
+// Face tasks of the global case whose destination is on rank `dst` and whose
+// source is on rank `src`, as bands of the source cube: (source cube, axis,
+// side of the source's face: 1 = its high face, layers it reads).  A
+// same-level copy reads the source's two layers next to the face, an
+// injection one (two are sent), a fine -> coarse average four.
+bool shard_bands(int ncube, const int *adj, const int *csl, const int *rank_of_cube, int src,
+                 int dst, std::vector<std::array<int, 4>> &out, std::string &err) {
+  std::vector<int> off;
+  std::vector<bcmg::FaceTask> tasks;
+  if (!bcmg::build_interface_tasks(ncube, adj, csl, off, tasks, err)) return false;
+  std::map<std::array<int, 3>, int> need;  // (cube, axis, side) -> layers
+  for (int c = 1; c < ncube; ++c) {
+    if (rank_of_cube[c] != dst) continue;
+    for (int t = off[c]; t < off[c + 1]; ++t) {
+      const bcmg::FaceTask &f = tasks[t];
+      if (rank_of_cube[f.src] != src || f.src == c) continue;
+      // the task fills the destination's ghost layers on side f.side, so it
+      // reads the source's face on the other side
+      const std::array<int, 3> key = {f.src, (int)f.axis, 1 - (int)f.side};
+      int &l = need[key];
+      l = std::max(l, f.kind == 2 ? 4 : 2);
+    }
+  }
+  out.clear();
+  for (auto &kv : need) out.push_back({kv.first[0], kv.first[1], kv.first[2], kv.second});
+  return true;
+}
+
+bool check_ranks(int ncube, const int *rank_of_cube, int rank) {
+  if (!rank_of_cube || rank < 0) return false;
+  for (int c = 1; c < ncube; ++c)
+    if (rank_of_cube[c] < 0) return false;
+  return true;
+}
+
+}  // namespace
+
+extern "C" int bcmg_shard_plan(int ncube, const int *adj_number, const int *csl,
+                               const int *rank_of_cube, int rank, int cap, int *nlocal,
+                               int *local_cubes, int *nproxy, int *proxy_cubes) {
+  std::string err;
+  if (ncube < 2 || !adj_number || !csl || !nlocal || !nproxy ||
+      !check_ranks(ncube, rank_of_cube, rank))
+    return -1;
+  std::vector<int> off;
+  std::vector<bcmg::FaceTask> tasks;
+  if (!bcmg::build_interface_tasks(ncube, adj_number, csl, off, tasks, err)) return -1;
+  std::vector<int> loc, prox;
+  std::vector<char> isprox((size_t)ncube, 0);
+  for (int c = 1; c < ncube; ++c) {
+    if (rank_of_cube[c] != rank) continue;
+    loc.push_back(c);
+    for (int t = off[c]; t < off[c + 1]; ++t)
+      if (rank_of_cube[tasks[t].src] != rank) isprox[tasks[t].src] = 1;
+  }
+  for (int c = 1; c < ncube; ++c)
+    if (isprox[c]) prox.push_back(c);
+  *nlocal = (int)loc.size();
+  *nproxy = (int)prox.size();
+  if ((int)loc.size() > cap || (int)prox.size() > cap) return -2;
+  if (local_cubes) std::copy(loc.begin(), loc.end(), local_cubes);
+  if (proxy_cubes) std::copy(prox.begin(), prox.end(), proxy_cubes);
+  return 0;
+}
+
+extern "C" int bcmg_shard_bands(int ncube, const int *adj_number, const int *csl,
+                                const int *rank_of_cube, int src_rank, int dst_rank, int cap,
+                                int *nband, int *bands) {
+  std::string err;
+  if (ncube < 2 || !adj_number || !csl || !nband ||
+      !check_ranks(ncube, rank_of_cube, std::min(src_rank, dst_rank)))
+    return -1;
+  std::vector<std::array<int, 4>> b;
+  if (!shard_bands(ncube, adj_number, csl, rank_of_cube, src_rank, dst_rank, b, err)) return -1;
+  *nband = (int)b.size();
+  if ((int)b.size() > cap) return -2;
+  if (bands)
+    for (size_t i = 0; i < b.size(); ++i)
+      for (int w = 0; w < 4; ++w) bands[4 * i + w] = b[i][w];
+  return 0;
 }

@@ -25,6 +25,8 @@
 #ifndef BCM_GB300_H
 #define BCM_GB300_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -423,6 +425,73 @@ int bcmg_flux_rk_stage_noalloc(int ncube, int RK, double deltaT, double deltaTau
                                const double *U1, const double *U1q, double *U1p1,
                                double *U1p2, double *Rku1, double *Residual1, double *er,
                                void *stream);
+
+/* Cube-sharded runs (one rank per GPU).  The reference spreads cubes over
+ * MPI ranks by rank_map.dat (main.cpp:576-596), exchanges the face layers
+ * of cubes on other ranks in every interface call (BCM_Interface.cpp
+ * :213-1738, :4367-5634) and sums the norms with MPI_Allreduce
+ * (BCM_Flux_XYZ_Viscous_Runge_kutta.cpp:2641-2652).  Here a rank's context
+ * holds its own cubes in slots 1..nlocal and, after them, nproxy "proxy"
+ * slots: remote cubes whose faces its cubes' face tasks read.  Proxies are
+ * never advanced; before every interface call the exchange hook must fill
+ * the proxies' face bands (bcmg_case_halo_pack on the owning rank, the
+ * transport of the caller's choice, bcmg_case_halo_unpack here), and after
+ * the norm sums of a sub-iteration it must replace the 7 raw sums
+ * (bcmg_case_norm_sums) by their sum over the ranks.  The cells then evolve
+ * bit for bit as in one context holding every cube.
+ *
+ * bcmg_shard_plan: the cubes of rank `rank` (local_cubes, ascending) and the
+ * remote cubes its face tasks read (proxy_cubes, ascending), global numbers;
+ * rank_of_cube[ncube] (slot 0 unused).  bcmg_shard_bands: the face bands
+ * rank dst_rank reads from rank src_rank, 4 ints each (global source cube,
+ * axis 0..2, side 1 high / 0 low face of the source, interior layers next to
+ * it: 2, or 4 for fine -> coarse averages), in one fixed order, so the
+ * sender and the receiver compute the same list.  Both return 0, -1 for
+ * invalid input, -2 when a list exceeds cap (the counts are still set). */
+int bcmg_shard_plan(int ncube, const int *adj_number, const int *csl, const int *rank_of_cube,
+                    int rank, int cap, int *nlocal, int *local_cubes, int *nproxy,
+                    int *proxy_cubes);
+int bcmg_shard_bands(int ncube, const int *adj_number, const int *csl, const int *rank_of_cube,
+                     int src_rank, int dst_rank, int cap, int *nband, int *bands);
+
+/* A rank's context: desc describes its nlocal + nproxy cubes in local
+ * numbering (cube slot 1 + i: local_cubes[i], then proxy_cubes) with the
+ * adjacency mapped to local slots (entries naming a cube of neither list:
+ * 0), boundary lists and IBM tables of its own cubes only.  Face tasks into
+ * proxies are dropped; tasks out of proxies run in every interface call.
+ * Batches are not sharded. */
+int bcmg_case_create_shard(const bcmg_case_desc *desc, int nproxy, bcmg_case **out);
+
+/* Exchange hook, called in the context's stream order (stream = the
+ * context's cudaStream_t) with phase BCMG_XCHG_HALO before every interface
+ * call and BCMG_XCHG_NORMS after the norm sums of a sub-iteration; returns
+ * 0, or non-zero to fail the stepping call.  A context with a hook steps
+ * without CUDA graphs (use_graph must be 0). */
+#define BCMG_XCHG_HALO 0
+#define BCMG_XCHG_NORMS 1
+typedef int (*bcmg_exchange_fn)(void *user, int phase, void *stream);
+int bcmg_case_set_exchange(bcmg_case *c, bcmg_exchange_fn fn, void *user);
+
+/* Halo bands per peer, in local cube slots: send[p] (4 ints per band: a
+ * local cube 1..nlocal, axis, side, layers) are packed for peer p, recv[p]
+ * (a proxy slot) unpacked from it, each in the order bcmg_shard_bands gives.
+ * bcmg_case_halo_bytes: buffer bytes of one peer's send / recv (every
+ * cell's five doubles, plus five floats on the split path).  pack / unpack
+ * enqueue on the context's stream; dev_buf is device memory of at least
+ * those bytes. */
+int bcmg_case_set_halo(bcmg_case *c, int npeer, const int *nsend, const int *const *send,
+                       const int *nrecv, const int *const *recv);
+int bcmg_case_halo_bytes(const bcmg_case *c, int peer, size_t *send_bytes, size_t *recv_bytes);
+int bcmg_case_halo_pack(bcmg_case *c, int peer, void *dev_buf);
+int bcmg_case_halo_unpack(bcmg_case *c, int peer, const void *dev_buf);
+/* Device address of the 7 raw norm sums (squared changes of p, u, v, w, T
+ * and the two force sums) that the BCMG_XCHG_NORMS hook adds over the ranks
+ * in place. */
+int bcmg_case_norm_sums(bcmg_case *c, double **dev_sums);
+/* The same 7 sums through host memory (for a host-side transport): write =
+ * 0 copies them to sums[7], write = 1 copies sums[7] back; both wait for the
+ * copy. */
+int bcmg_case_norm_sums_host(bcmg_case *c, double *sums, int write);
 
 /* Device-time marks on the context's stream: bcmg_case_timer_mark records
  * event `slot` (0..15); bcmg_case_timer_elapsed waits for mark b and returns

@@ -1,0 +1,86 @@
+"""Cube-sharded runs on one GPU against one context holding every cube.
+
+api.ShardedRun gives every rank its own context (its cubes, then proxies
+of the remote cubes its face tasks read) and host thread; the exchange hook
+moves the face bands through device buffers and adds the ranks' norm sums.
+After whole dual-time steps every cube's cells (ghost layers included) must
+equal the single context's bit for bit, FP64 and split precision, RK and
+LU-SGS sub-iterations, two and three ranks, contiguous and scattered
+partitions; the norms agree to 1e-12 (the ranks' sums are added in another
+order than one context's blocks).
+"""
+import numpy as np
+import pytest
+
+from bcm_cgli_gb300 import api, cases
+from golden import golden_cases as G
+
+pytestmark = pytest.mark.gpu
+
+NORM_RTOL = 1e-12
+
+
+def _case(name):
+    if name == "sphere_two_level":
+        return cases.sphere_ibm(n=8, coarse=2.0, box=((-2, 4), (-2, 2), (-2, 2)),
+                                refine_box=((-2, 2), (-2, 2), (-2, 2)))
+    return G.golden_cases()[name]
+
+
+def _ranks(case, nrank, scattered):
+    rk = np.zeros(case.ncube, np.int32)
+    m = case.ncube - 1
+    rk[1:] = np.arange(m) % nrank if scattered else (np.arange(m) * nrank) // m
+    return rk
+
+
+@pytest.mark.parametrize("name", ["tgv_n8", "two_level_open_n8", "random_open_n4",
+                                  "sphere_two_level"])
+@pytest.mark.parametrize("precision", [api.PRECISION_FP64, api.PRECISION_SPLIT])
+@pytest.mark.parametrize("nrank,scattered", [(2, False), (3, True)])
+def test_sharded_run_equals_one_context(name, precision, nrank, scattered):
+    case = _case(name)
+    one = api.CaseContext(case, precision=precision)
+    one.set_state(case.U, case.U, case.U)
+    er1 = one.advance(2, 2, use_graph=False)
+    ref = one.get_state()
+    one.close()
+    sh = api.ShardedRun(case, _ranks(case, nrank, scattered), precision=precision)
+    sh.set_state(case.U, case.U, case.U)
+    er2 = sh.advance(2, 2)
+    got = sh.get_state()
+    sh.close()
+    for k, a, b in zip(("U1_", "U1", "U1q"), ref, got):
+        bad = np.argwhere(a[1:] != b[1:])
+        assert bad.size == 0, f"{name} {k}: {len(bad)} mismatches, first {bad[:3]}"
+    for m in range(1, 8):
+        assert abs(er1[m] - er2[m]) <= NORM_RTOL * max(abs(er1[m]), 1e-300) + 1e-300, (m, er1,
+                                                                                      er2)
+
+
+@pytest.mark.parametrize("precision", [api.PRECISION_FP64, api.PRECISION_SPLIT])
+def test_sharded_lusgs_equals_one_context(precision):
+    case = _case("two_level_open_n8")
+    one = api.CaseContext(case, precision=precision)
+    one.set_method(api.METHOD_LUSGS)
+    one.set_state(case.U, case.U, case.U)
+    one.advance(1, 3, use_graph=False)
+    ref = one.get_state()
+    one.close()
+    sh = api.ShardedRun(case, _ranks(case, 2, True), precision=precision)
+    for c in sh.ctx:
+        c.set_method(api.METHOD_LUSGS)
+    sh.set_state(case.U, case.U, case.U)
+    sh.advance(1, 3)
+    got = sh.get_state()
+    sh.close()
+    for a, b in zip(ref, got):
+        assert np.array_equal(a[1:], b[1:])
+
+
+def test_sharded_context_refuses_graphs():
+    case = _case("tgv_n8")
+    sh = api.ShardedRun(case, _ranks(case, 2, False))
+    with pytest.raises(api.BcmgError):
+        sh.ctx[0].advance(1, 1, use_graph=True)
+    sh.close()
