@@ -23,7 +23,8 @@ def _header_functions():
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
         for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b([A-Za-z_]\w*)\s*\(", src,
                              flags=re.M):
-            if m.group(1) not in ("if", "defined"):
+            if m.group(1) not in ("if", "defined") and \
+                    not m.group(0).lstrip().startswith("typedef"):
                 names.add(m.group(1))
     return names
 
