@@ -639,3 +639,118 @@ class ShardedRun:
         for c in self.ctx:
             lib().bcmg_case_set_exchange(c.h, _lib.EXCHANGE_FN(), None)
             c.close()
+
+
+class DistShard:
+    """This process's rank of a cube-sharded run over torch.distributed (one
+    process per GPU; RANK/WORLD_SIZE as torchrun sets them): its share of the
+    case in one context, the face bands and the norm sums exchanged through
+    the process group.  Bands are packed on the GPU, staged through pinned
+    host memory and sent with point-to-point messages; the norm sums of all
+    ranks are gathered and added in rank order, so every rank finalises the
+    same norms.  The exchange runs on the host between kernels, so ranks
+    never have kernels waiting on each other (several ranks may share a GPU).
+    Works with any backend that moves CPU tensors (gloo)."""
+
+    def __init__(self, case, rank_of_cube, precision=PRECISION_FP64, group=None):
+        import torch
+        import torch.distributed as dist
+        self.dist, self.torch, self.group = dist, torch, group
+        self.rank = dist.get_rank(group)
+        self.world = dist.get_world_size(group)
+        rk = np.asarray(rank_of_cube, np.int32)
+        if int(rk[1:].max()) + 1 != self.world:
+            raise ValueError("rank_of_cube must name every rank of the group")
+        self.case = case
+        sub, own, prox = cases.shard_case(case, rk, self.rank)
+        self.sub, self.own, self.prox = sub, own, prox
+        self.ctx = CaseContext(sub, precision, nproxy=len(prox))
+        g2l = np.zeros(case.ncube, np.int32)
+        g2l[own] = np.arange(1, len(own) + 1)
+        g2l[prox] = np.arange(len(own) + 1, len(own) + len(prox) + 1)
+        send, recv = [], []
+        for p in range(self.world):
+            sb = cases.shard_bands(case, rk, self.rank, p) if p != self.rank else np.zeros((0, 4))
+            rb = cases.shard_bands(case, rk, p, self.rank) if p != self.rank else np.zeros((0, 4))
+            sb, rb = np.array(sb, np.int32), np.array(rb, np.int32)
+            sb[:, 0] = g2l[sb[:, 0]]
+            rb[:, 0] = g2l[rb[:, 0]]
+            send.append(np.ascontiguousarray(sb))
+            recv.append(np.ascontiguousarray(rb))
+        self._keep = send + recv
+        W = self.world
+        check(lib().bcmg_case_set_halo(
+            self.ctx.h, W, (C.c_int * W)(*[len(x) for x in send]),
+            (C.c_void_p * W)(*[x.ctypes.data for x in send]),
+            (C.c_int * W)(*[len(x) for x in recv]),
+            (C.c_void_p * W)(*[x.ctypes.data for x in recv])))
+        self.peers = [p for p in range(W) if p != self.rank]
+        self.dbuf, self.hsend, self.hrecv = {}, {}, {}
+        for p in self.peers:
+            a, b = C.c_size_t(), C.c_size_t()
+            check(lib().bcmg_case_halo_bytes(self.ctx.h, p, C.byref(a), C.byref(b)))
+            self.dbuf[p] = (torch.empty(max(a.value, 16), dtype=torch.uint8, device="cuda"),
+                            torch.empty(max(b.value, 16), dtype=torch.uint8, device="cuda"))
+            self.hsend[p] = torch.empty(a.value, dtype=torch.uint8).pin_memory()
+            self.hrecv[p] = torch.empty(b.value, dtype=torch.uint8).pin_memory()
+        self.error = None
+        self._hook = _lib.EXCHANGE_FN(self._exchange)
+        check(lib().bcmg_case_set_exchange(self.ctx.h, self._hook, None))
+
+    def _exchange(self, user, phase, stream):
+        try:
+            L, h, torch, dist = lib(), self.ctx.h, self.torch, self.dist
+            if phase == XCHG_HALO:
+                for p in self.peers:
+                    check(L.bcmg_case_halo_pack(h, p, self.dbuf[p][0].data_ptr()))
+                check(L.bcmg_case_sync(h))
+                for p in self.peers:
+                    self.hsend[p].copy_(self.dbuf[p][0][:self.hsend[p].numel()])
+                # a peer's send list is the other's receive list, so both
+                # skip the same empty messages
+                ops = [dist.P2POp(dist.isend, self.hsend[p], p, self.group)
+                       for p in self.peers if self.hsend[p].numel()]
+                ops += [dist.P2POp(dist.irecv, self.hrecv[p], p, self.group)
+                        for p in self.peers if self.hrecv[p].numel()]
+                for w in (dist.batch_isend_irecv(ops) if ops else []):
+                    w.wait()
+                for p in self.peers:
+                    self.dbuf[p][1][:self.hrecv[p].numel()].copy_(self.hrecv[p])
+                torch.cuda.synchronize()
+                for p in self.peers:
+                    check(L.bcmg_case_halo_unpack(h, p, self.dbuf[p][1].data_ptr()))
+            else:
+                s = np.zeros(7)
+                check(L.bcmg_case_norm_sums_host(h, s.ctypes.data, 0))
+                got = [torch.zeros(7, dtype=torch.float64) for _ in range(self.world)]
+                dist.all_gather(got, torch.from_numpy(s), group=self.group)
+                tot = got[0].numpy().copy()
+                for p in range(1, self.world):  # rank order: the same bits everywhere
+                    tot = tot + got[p].numpy()
+                check(L.bcmg_case_norm_sums_host(h, tot.ctypes.data, 1))
+            return 0
+        except Exception as exc:
+            self.error = exc
+            return 1
+
+    def set_state(self, U1_, U1, U1q):
+        sl = np.concatenate([[0], self.own, self.prox])
+        self.ctx.set_state(U1_[sl], U1[sl], U1q[sl])
+
+    def advance(self, steps, subiters):
+        try:
+            return self.ctx.advance(steps, subiters, use_graph=False)
+        except BcmgError:
+            if self.error:
+                raise BcmgError(f"sharded step failed: {self.error}")
+            raise
+
+    def own_state(self):
+        """(own cubes, U1_, U1, U1q of those cubes)."""
+        st = self.ctx.get_state()
+        k = len(self.own)
+        return self.own, st[0][1:1 + k], st[1][1:1 + k], st[2][1:1 + k]
+
+    def close(self):
+        lib().bcmg_case_set_exchange(self.ctx.h, _lib.EXCHANGE_FN(), None)
+        self.ctx.close()

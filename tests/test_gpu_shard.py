@@ -84,3 +84,55 @@ def test_sharded_context_refuses_graphs():
     with pytest.raises(api.BcmgError):
         sh.ctx[0].advance(1, 1, use_graph=True)
     sh.close()
+
+
+def _dist_rank(rank, world, port, name, precision, q):
+    import os
+    import sys
+    os.environ.update(RANK=str(rank), WORLD_SIZE=str(world), MASTER_ADDR="127.0.0.1",
+                      MASTER_PORT=str(port))
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path[:0] = [root, os.path.join(root, "tests"), os.path.join(root, "oracle")]
+    import torch.distributed as dist
+    from bcm_cgli_gb300 import api as A
+    dist.init_process_group("gloo")
+    case = _case(name)
+    sh = A.DistShard(case, _ranks(case, world, True), precision=precision)
+    sh.set_state(case.U, case.U, case.U)
+    er = sh.advance(2, 2)
+    own, u, u1, uq = sh.own_state()
+    sh.close()
+    dist.destroy_process_group()
+    q.put((rank, own, u, u1, uq, er))
+
+
+@pytest.mark.parametrize("precision", [api.PRECISION_FP64, api.PRECISION_SPLIT])
+def test_two_processes_over_gloo_equal_one_context(precision):
+    """Two processes, each a rank of the sharded run on this GPU, exchanging
+    through torch.distributed (gloo, host-staged): the same bits as one
+    context."""
+    import os
+
+    import torch.multiprocessing as mp
+    name = "two_level_open_n8"
+    case = _case(name)
+    one = api.CaseContext(case, precision=precision)
+    one.set_state(case.U, case.U, case.U)
+    er1 = one.advance(2, 2, use_graph=False)
+    ref = one.get_state()
+    one.close()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = 29900 + os.getpid() % 90
+    ps = [ctx.Process(target=_dist_rank, args=(r, 2, port, name, precision, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    res = [q.get(timeout=600) for _ in range(2)]
+    for p in ps:
+        p.join(120)
+        assert p.exitcode == 0
+    for rank, own, u, u1, uq, er in res:
+        for a, b in zip(ref, (u, u1, uq)):
+            assert np.array_equal(a[own], b)
+        for m in range(1, 8):
+            assert abs(er[m] - er1[m]) <= NORM_RTOL * max(abs(er1[m]), 1e-300) + 1e-300
