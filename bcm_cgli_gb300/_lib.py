@@ -99,6 +99,9 @@ def _declare(L):
     L.bcmg_case_halo_unpack.argtypes = [P, C.c_int, P]
     L.bcmg_case_norm_sums.argtypes = [P, C.POINTER(P)]
     L.bcmg_case_norm_sums_host.argtypes = [P, P, C.c_int]
+    L.bcmg_case_advance_async.argtypes = [P, C.c_int, C.c_int]
+    L.bcmg_case_copy_state_async.argtypes = [P, C.c_int, P, P, P]
+    L.bcmg_case_get_norms.argtypes = [P, P, P]
     L.bcmg_case_destroy.argtypes = [P]
     L.bcmg_case_destroy.restype = None
     L.bcmg_case_set_state.argtypes = [P, P, P, P]

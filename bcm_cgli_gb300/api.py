@@ -349,6 +349,24 @@ class CaseContext:
                                       er.ctypes.data, self.emax.ctypes.data))
         return er.reshape(self.ncase, 8) if isinstance(self, BatchContext) else er
 
+    def advance_async(self, steps, subiters):
+        """Enqueues `steps` graph-replayed dual-time steps and returns at once
+        (bcmg_case_advance_async); norms stay on the device (get_norms)."""
+        check(lib().bcmg_case_advance_async(self.h, int(steps), int(subiters)))
+
+    def copy_state_async(self, to_device, U1_=None, U1=None, U1q=None):
+        """Enqueues host <-> device copies of the given full arrays (page-
+        locked host arrays, left untouched until sync(), make it asynchronous)."""
+        ptr = lambda a: None if a is None else _dp(a).ctypes.data
+        check(lib().bcmg_case_copy_state_async(self.h, 1 if to_device else 0, ptr(U1_), ptr(U1),
+                                               ptr(U1q)))
+
+    def get_norms(self):
+        """er of the last step (after waiting for the stream)."""
+        er = np.zeros(8 * self.ncase)
+        check(lib().bcmg_case_get_norms(self.h, er.ctypes.data, self.emax.ctypes.data))
+        return er.reshape(self.ncase, 8) if isinstance(self, BatchContext) else er
+
     def advance_converged(self, steps, max_subiters, tol=0.02, use_graph=True):
         """Steps with the reference's convergence test (main.cpp:1249-1271);
         returns (er, sub-iterations per step [steps] or [steps, ncase])."""

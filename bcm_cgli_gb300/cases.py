@@ -781,6 +781,10 @@ def shard_case(case, rank_of_cube, rank):
         W, G, I = t
         m = (len(G) - 1) // 4
         gc, ip, w = G[1:].reshape(m, 4).copy(), I[1:].reshape(m, 4).copy(), W[1:].reshape(m, 8)
+        if m and (gc[:, 0] != ip[:, 0]).any():
+            # a rank fills the ghosts of its own cubes from their own cells
+            raise ValueError("sharded runs need every IBM image-point stencil inside its ghost "
+                             "cell's cube (as BCM_Immersed_boundary's tables are)")
         keep = mine[gc[:, 0]] if m else np.zeros(0, bool)
         gc, ip, w = gc[keep], ip[keep], w[keep]
         gc[:, 0] = g2l[gc[:, 0]]

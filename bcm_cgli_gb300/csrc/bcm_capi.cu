@@ -1376,6 +1376,55 @@ int bcmg_case_advance(bcmg_case *c, int steps, int subiters, int use_graph, doub
   return BCMG_OK;
 }
 
+int bcmg_case_advance_async(bcmg_case *c, int steps, int subiters) {
+  TraceRange trace("bcmg_case_advance_async");
+  clear_err();
+  if (!c || steps < 0 || subiters < 1) { set_err("bad arguments"); return BCMG_ERR_ARG; }
+  if (c->profile || c->xchg) {
+    set_err("asynchronous steps need graphs: profiling and exchange hooks are synchronous");
+    return BCMG_ERR_UNSUPPORTED;
+  }
+  if (!c->graph || c->graph_subiters != subiters) {
+    // capture the step graph as bcmg_case_advance does (no step launched;
+    // this first call waits for the capture)
+    int r = bcmg_case_advance(c, 0, subiters, 1, nullptr, nullptr);
+    if (r) return r;
+  }
+  for (int s = 0; s < steps; ++s) CK(cudaGraphLaunch(c->graph, c->stream));
+  c->launches = c->graph_launches * steps;
+  return BCMG_OK;
+}
+
+int bcmg_case_copy_state_async(bcmg_case *c, int to_device, double *U1_, double *U1,
+                               double *U1q) {
+  clear_err();
+  if (!c) { set_err("null context"); return BCMG_ERR_ARG; }
+  const size_t b = c->ncell * 5 * sizeof(double);
+  const cudaMemcpyKind k = to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+  double *dev[3] = {c->U1_, c->U1, c->U1q};
+  double *host[3] = {U1_, U1, U1q};
+  for (int i = 0; i < 3; ++i)
+    if (host[i])
+      CK(cudaMemcpyAsync(to_device ? dev[i] : host[i], to_device ? host[i] : dev[i], b, k,
+                         c->stream));
+  if (to_device && c->precision == BCMG_PRECISION_SPLIT && (U1 || U1q))
+    CK(launch_level_diff(c->U1, c->U1q, c->D2, c->ph.n, c->ncube, c->stream));
+  return BCMG_OK;
+}
+
+int bcmg_case_get_norms(bcmg_case *c, double *er, double *emax) {
+  clear_err();
+  if (!c) { set_err("null context"); return BCMG_ERR_ARG; }
+  if (er)
+    CK(cudaMemcpyAsync(er, c->er, 8 * sizeof(double) * c->ncase, cudaMemcpyDeviceToHost,
+                       c->stream));
+  if (emax)
+    CK(cudaMemcpyAsync(emax, c->emax, 6 * sizeof(double) * c->ncase, cudaMemcpyDeviceToHost,
+                       c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return BCMG_OK;
+}
+
 int bcmg_case_sync(bcmg_case *c) {
   clear_err();
   if (!c) { set_err("null context"); return BCMG_ERR_ARG; }

@@ -86,7 +86,7 @@ __device__ __forceinline__ void level_face(const InterfaceArgs &a, int c, const 
       sum = sum + B[si + sj + sk];
       const size_t od = 5 * cell_index(S, c, d[0], d[1], d[2]) + v;
       U[od] = 0.125 * sum;
-      if (M) M[od] = mirror_value(0.125 * sum, v, r0, e0);
+      if (M) M[od] = mirror_value_hw(0.125 * sum, v, r0, e0);
     }
   }
 }
@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(1024) k_iface_edges(InterfaceArgs a) {
   auto avg = [&](double *d, const double *x, const double *y, int v) {
     const double r = 0.5 * (x[v] + y[v]);
     d[v] = r;
-    if (M) M[(d - U) + v] = mirror_value(r, v, r0, e0);
+    if (M) M[(d - U) + v] = mirror_value_hw(r, v, r0, e0);
   };
   // Phase 1: i-edges, i = 2..nx.
   for (int w = threadIdx.x; w < 4 * n * 5; w += blockDim.x) {
@@ -332,7 +332,7 @@ __global__ void __launch_bounds__(kBcThreads) k_bc(BcArgs a) {
           U[d1[b]] = x[b];
           U[d0[b]] = x[b];
           if (M) {
-            const float m = mirror_value(x[b], (int)(d1[b] % 5), r0, e0);
+            const float m = mirror_value_hw(x[b], (int)(d1[b] % 5), r0, e0);
             M[d1[b]] = m;
             M[d0[b]] = m;
           }
@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(kBcThreads) k_bc(BcArgs a) {
         if (M) {
 #pragma unroll
           for (int v = 0; v < 5; ++v) {
-            const float m = mirror_value(o[v], v, r0, e0);
+            const float m = mirror_value_hw(o[v], v, r0, e0);
             M[(d1 - U) + v] = m;
             M[(d0 - U) + v] = m;
           }
@@ -537,7 +537,7 @@ __global__ void __launch_bounds__(kGhostThreads) k_ghost(GhostArgs a, int count)
     double r0, e0;
     mirror_base(a.mir, a.bt, gc, r0, e0);
 #pragma unroll
-    for (int v = 0; v < 5; ++v) M[go + v] = mirror_value(o[v], v, r0, e0);
+    for (int v = 0; v < 5; ++v) M[go + v] = mirror_value_hw(o[v], v, r0, e0);
   }
 }
 

@@ -328,7 +328,7 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 448 ? 2 : 1) k_lusgs_split(Lusgs
       for (int v = 0; v < 5; ++v) {
         un[v] = a.U1_[5 * o + v] + (double)dq[v];
         a.U1_[5 * o + v] = un[v];
-        mn[v] = mirror_value(un[v], v, rho0d, E0d);
+        mn[v] = mirror_value_hw(un[v], v, rho0d, E0d);
         mm_[v] = mn[v];
       }
       // Same-level interface copy of this cell (state and mirror), done

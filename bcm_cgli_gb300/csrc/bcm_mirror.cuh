@@ -88,9 +88,17 @@ __device__ __forceinline__ float delta_rn(double x, double r) {
 }
 
 // Mirror value of component v (0..4) of a state cell: density and energy as
-// deltas from rho0 and E0 = P0/(K-1), momenta as they are.
+// deltas from rho0 and E0 = P0/(K-1), momenta as they are.  Two routes to
+// the same bits: on the integer pipes (for the whole-state pass k_mirror,
+// where the FP64 pipe is the bottleneck) and through the hardware
+// conversion (one FP64 subtraction and one conversion: for the kernels
+// that write a few cells each, where the integer routine's instructions
+// and branches cost more).
 __device__ __forceinline__ float mirror_value(double x, int v, double rho0, double E0) {
   return v == 0 ? delta_rn(x, rho0) : (v == 4 ? delta_rn(x, E0) : to_float_rn(x));
+}
+__device__ __forceinline__ float mirror_value_hw(double x, int v, double rho0, double E0) {
+  return __double2float_rn(v == 0 ? x - rho0 : (v == 4 ? x - E0 : x));
 }
 #endif  // __CUDACC__
 

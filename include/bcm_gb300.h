@@ -338,6 +338,21 @@ int bcmg_case_set_face_copies(bcmg_case *c, int in_flux);
  * give the same bits.  No effect on the FP64 path. */
 int bcmg_case_set_mirror_each_stage(bcmg_case *c, int on);
 
+/* Asynchronous stepping, for pipelines that overlap host transfers of one
+ * context with the steps of another: bcmg_case_advance_async enqueues
+ * `steps` graph launches of a step of `subiters` sub-iterations on the
+ * context's stream and returns (the first call for a sub-iteration count
+ * captures the graph and waits for that; not with profiling or an exchange
+ * hook); bcmg_case_copy_state_async enqueues the copies of the non-NULL
+ * arrays between the host and the device (to_device != 0: host -> device;
+ * page-locked host memory makes them asynchronous; the host arrays must stay
+ * untouched until bcmg_case_sync); bcmg_case_get_norms waits for the stream
+ * and copies er / emax (as bcmg_case_advance would return them). */
+int bcmg_case_advance_async(bcmg_case *c, int steps, int subiters);
+int bcmg_case_copy_state_async(bcmg_case *c, int to_device, double *U1_, double *U1,
+                               double *U1q);
+int bcmg_case_get_norms(bcmg_case *c, double *er, double *emax);
+
 /* Waits for all work of the context. */
 int bcmg_case_sync(bcmg_case *c);
 

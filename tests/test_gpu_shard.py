@@ -20,11 +20,27 @@ pytestmark = pytest.mark.gpu
 NORM_RTOL = 1e-12
 
 
+def _same_cube(t):
+    """The IBM entries whose image-point stencil lies in the ghost's own cube
+    (the random test tables also cross cubes, which real tables never do and
+    sharded runs refuse)."""
+    if t is None:
+        return None
+    W, Gi, I = t
+    m = (len(Gi) - 1) // 4
+    keep = Gi[1:].reshape(m, 4)[:, 0] == I[1:].reshape(m, 4)[:, 0]
+    return (np.concatenate([W[:1], W[1:].reshape(m, 8)[keep].reshape(-1)]),
+            np.concatenate([Gi[:1], Gi[1:].reshape(m, 4)[keep].reshape(-1)]).astype(np.int32),
+            np.concatenate([I[:1], I[1:].reshape(m, 4)[keep].reshape(-1)]).astype(np.int32))
+
+
 def _case(name):
     if name == "sphere_two_level":
         return cases.sphere_ibm(n=8, coarse=2.0, box=((-2, 4), (-2, 2), (-2, 2)),
                                 refine_box=((-2, 2), (-2, 2), (-2, 2)))
-    return G.golden_cases()[name]
+    case = G.golden_cases()[name]
+    case.ibm_minus, case.ibm_plus = _same_cube(case.ibm_minus), _same_cube(case.ibm_plus)
+    return case
 
 
 def _ranks(case, nrank, scattered):

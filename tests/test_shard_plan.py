@@ -46,7 +46,7 @@ def _rank(rank, world, port, q):
     for name in CASES:
         case = G.golden_cases()[name]
         for rk in _partitions(case, world):
-            _, own, prox = cases.shard_case(case, rk, rank)
+            own, prox = cases.shard_plan(case, rk, rank)
             send = {p: cases.shard_bands(case, rk, rank, p).tolist()
                     for p in range(world) if p != rank}
             recv = {p: cases.shard_bands(case, rk, p, rank).tolist()
@@ -66,7 +66,7 @@ def test_two_ranks_plan_the_same_exchange():
     ps = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
     for p in ps:
         p.start()
-    res = dict(q.get(timeout=300) for _ in range(2))
+    res = dict(q.get(timeout=120) for _ in range(2))
     for p in ps:
         p.join(120)
         assert p.exitcode == 0
@@ -106,3 +106,16 @@ def test_two_ranks_plan_the_same_exchange():
                 need = 4 if kind == 2 else 2
                 hit = [b for b in bands if b[0] == src and b[1] == ax and b[2] == 1 - side]
                 assert hit and hit[0][3] >= need, (name, c, t)
+
+
+def test_shard_case_refuses_cross_cube_ibm_stencils():
+    """A rank fills the IBM ghosts of its own cubes from their own cells; the
+    random test tables also reach into other cubes and are refused."""
+    sys.path[:0] = [ROOT, os.path.join(ROOT, "tests")]
+    from bcm_cgli_gb300 import cases
+    from golden import golden_cases as G
+    case = G.golden_cases()["random_open_n4"]
+    rk = np.zeros(case.ncube, np.int32)
+    rk[1:] = np.arange(case.ncube - 1) % 2
+    with pytest.raises(ValueError):
+        cases.shard_case(case, rk, 0)
