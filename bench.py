@@ -691,18 +691,24 @@ def run_gpu_arm(args, dist):
     def roofline(m, prec):
         alg_bytes = BYTES_PER_CELL_STAGE * case.n_cells
         achieved = alg_bytes / (m["flux_ms_avg"] * 1e-3) / 1e9
-        traffic = None
-        prof = os.path.join(ROOT, "profiles", f"flux_{prec}_traffic.json")
-        if os.path.isfile(prof):
-            try:
-                t = json.load(open(prof))
-                traffic = t["dram_bytes_per_cell_stage"] * case.n_cells
-            except Exception:
-                traffic = None
+        traffic, traffic_src = None, None
+        # DRAM bytes per cell-stage from an ncu capture of the same kernel on a
+        # smaller case of the same cube resolution (scaled by cells: a launch's
+        # traffic grows with its cells), else of another resolution
+        for fn in (f"flux_{prec}_traffic_n{case.n}.json", f"flux_{prec}_traffic.json"):
+            prof = os.path.join(ROOT, "profiles", fn)
+            if os.path.isfile(prof):
+                try:
+                    t = json.load(open(prof))
+                    traffic = t["dram_bytes_per_cell_stage"] * case.n_cells
+                    traffic_src = f"profiles/{fn}"
+                    break
+                except Exception:
+                    traffic = None
         return {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak, "traffic": traffic, "kernel": f"k_flux_{prec}",
                 "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": m["flux_ms_avg"],
-                "launches": m["flux_launches"],
+                "launches": m["flux_launches"], "traffic_from": traffic_src,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
 
     line = {"metric": METRIC, "value": m_head["value"], "unit": UNIT, "n_gpus": dist.world,
