@@ -266,6 +266,16 @@ def _port(threads=None):
     return O, runner, threads
 
 
+# The CPU arms time the C restatement of the reference loop: the reference's
+# own sources are not on the GPU host.  On an x86 host where both build, the
+# restatement runs at 0.72-0.82 of the reference's compiled code (1 and 8
+# threads, vortex and Taylor-Green cubes; oracle/time_port_vs_reference.py),
+# so this baseline understates the reference's CPU rate by about a quarter.
+PORT_NOTE = ("C restatement of the reference loop (the reference's sources are not on this "
+             "host); on an x86 host it ran at 0.72-0.82 of the reference's own compiled code "
+             "(oracle/time_port_vs_reference.py)")
+
+
 def host_cpu():
     """CPU model and logical core count of this host."""
     import platform
@@ -294,7 +304,7 @@ def cpu_sample(case, subiters=1, threads=None):
         dt += time.perf_counter() - t0
         del st
     return {"value": case.n_cells * subiters / dt, "unit": UNIT, "cores": threads, "ranks": 1,
-            "kind": "port", "host": host_cpu(),
+            "kind": "port", "host": host_cpu(), "note": PORT_NOTE,
             "sample": f"1 dual-time step x {subiters} sub-iteration(s) of the full workload "
                       f"({case.n_cells} cells) through the C restatement of the reference "
                       f"loop, {threads} OpenMP threads over cubes in 1 process (1 rank), "
@@ -331,7 +341,7 @@ def run_reference_arm(args, dist):
     steps = max(1, args.steps)
     v = timed_cells / timed_s
     cpu = {"value": v, "unit": UNIT, "cores": threads, "ranks": 1, "kind": "port",
-           "host": host_cpu(),
+           "host": host_cpu(), "note": PORT_NOTE,
            "sample": (f"per step: 1 sub-iteration of one case (cases {sampled[0]}.. in turn"
                       f", {timed_cells} cell-subiters over {steps} steps)" if is_batch(case)
                       else f"per step: 1 sub-iteration of the case ({case.n_cells} cells)") +
