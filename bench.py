@@ -836,6 +836,28 @@ def run_flux_only(args):
                       "cell_stages_per_s": case.n_cells / (ms * 1e-3)}), flush=True)
 
 
+def run_step_only(args):
+    """Profiling target of the kernels around the flux: one eager dual-time
+    step of one sub-iteration (split precision) on a Taylor-Green case of
+    ncx^3 cubes of n^3 cells, or with --workload sphere on the two-level
+    sphere with IBM ghost cells (1,584 cubes of 16^3, 260 MB per state
+    array), after one untimed step."""
+    from bcm_cgli_gb300 import api, cases
+    case = (cases.sphere_ibm() if args.workload == "sphere"
+            else cases.taylor_green(ncx=args.ncx, n=args.n))
+    ctx = api.CaseContext(case, precision=api.PRECISION_SPLIT)
+    ctx.set_state(case.U, case.U, case.U)
+    ctx.advance(1, 1, use_graph=False)
+    ctx.sync()
+    ctx.timer_mark(0)
+    ctx.advance(1, 1, use_graph=False)
+    ctx.timer_mark(1)
+    ms = ctx.timer_elapsed(0, 1)
+    ctx.close()
+    print(json.dumps({"step_only": case.name, "cells": case.n_cells, "ms_per_step": ms}),
+          flush=True)
+
+
 def run_lusgs_only(args):
     """Profiling target: LU-SGS sub-iterations (residual + sweeps) on a
     Taylor-Green case of ncx^3 cubes of n^3 cells, `steps` sub-iterations
@@ -874,6 +896,9 @@ def main():
                     help="headline path only (no second precision, no accuracy check)")
     ap.add_argument("--flux-only", action="store_true",
                     help="time the flux kernel alone on a smaller case (profiling target)")
+    ap.add_argument("--step-only", action="store_true",
+                    help="one eager step of one sub-iteration (profiling target of the "
+                         "interface, boundary and IBM kernels)")
     ap.add_argument("--lusgs-only", action="store_true",
                     help="LU-SGS sub-iterations alone on a smaller case (profiling target)")
     ap.add_argument("--ncx", type=int, default=6,
@@ -905,6 +930,9 @@ def main():
         return
     if args.lusgs_only:
         run_lusgs_only(args)
+        return
+    if args.step_only:
+        run_step_only(args)
         return
     if args.impl == "reference":
         # Rank 0 alone times the CPU implementation; other ranks exit at once.
