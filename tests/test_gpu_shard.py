@@ -7,7 +7,9 @@ After whole dual-time steps every cube's cells (ghost layers included) must
 equal the single context's bit for bit, FP64 and split precision, RK and
 LU-SGS sub-iterations, two and three ranks, contiguous and scattered
 partitions; the norms agree to 1e-12 (the ranks' sums are added in another
-order than one context's blocks).
+order than one context's blocks).  The two force sums (drag, lift) are sums
+of surface terms of both signs, so a near-zero lift is held to 1e-12 of the
+larger force magnitude rather than of itself.
 """
 import numpy as np
 import pytest
@@ -18,6 +20,15 @@ from golden import golden_cases as G
 pytestmark = pytest.mark.gpu
 
 NORM_RTOL = 1e-12
+
+
+def _norms_close(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    for m in range(1, 6):
+        assert abs(a[m] - b[m]) <= NORM_RTOL * max(abs(a[m]), 1e-300), (m, a, b)
+    force = max(abs(a[6]), abs(a[7]), 1e-300)
+    for m in (6, 7):
+        assert abs(a[m] - b[m]) <= NORM_RTOL * force, (m, a, b)
 
 
 def _same_cube(t):
@@ -69,9 +80,7 @@ def test_sharded_run_equals_one_context(name, precision, nrank, scattered):
     for k, a, b in zip(("U1_", "U1", "U1q"), ref, got):
         bad = np.argwhere(a[1:] != b[1:])
         assert bad.size == 0, f"{name} {k}: {len(bad)} mismatches, first {bad[:3]}"
-    for m in range(1, 8):
-        assert abs(er1[m] - er2[m]) <= NORM_RTOL * max(abs(er1[m]), 1e-300) + 1e-300, (m, er1,
-                                                                                      er2)
+    _norms_close(er1, er2)
 
 
 @pytest.mark.parametrize("precision", [api.PRECISION_FP64, api.PRECISION_SPLIT])
@@ -150,5 +159,4 @@ def test_two_processes_over_gloo_equal_one_context(precision):
     for rank, own, u, u1, uq, er in res:
         for a, b in zip(ref, (u, u1, uq)):
             assert np.array_equal(a[own], b)
-        for m in range(1, 8):
-            assert abs(er[m] - er1[m]) <= NORM_RTOL * max(abs(er1[m]), 1e-300) + 1e-300
+        _norms_close(er1, er)
