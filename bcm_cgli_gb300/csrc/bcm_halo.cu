@@ -301,9 +301,20 @@ __global__ void __launch_bounds__(kBcThreads) k_bc(BcArgs a) {
   const int m = a.masks[blockIdx.x];
   const int T = (S + gridDim.y - 1) / gridDim.y, i0 = blockIdx.y * T, i1 = min(S, i0 + T);
   double *U = a.U1_;
-  float *M = mirror_current(a.mir);  // split precision: mirror values of every write
+  // Split precision: the mirror values of every write, into both mirror
+  // buffers.  The flux kernel writes the next buffer's interior cells and
+  // same-level ghost layers, and the interface call after it the level-jump
+  // layers and edges; the boundary layers are written here only, so the
+  // next buffer takes them now and equals the state's rounding in every
+  // cell once it becomes current.
+  float *M = mirror_current(a.mir);
+  float *Mo = M ? a.mir.buf[*a.mir.parity ^ 1] : nullptr;
   double r0 = 0, e0 = 0;
   if (M) mirror_base(a.mir, a.bt, c, r0, e0);
+  auto put = [&](size_t at, float m) {
+    M[at] = m;
+    Mo[at] = m;
+  };
   auto Q = [&](int i, int j, int k) { return U + 5 * cell_index(S, c, i, j, k); };
   auto at = [&](int i, int j, int k) { return (size_t)5 * cell_index(S, c, i, j, k); };
   // Zero-gradient and slip faces: both ghost layers take one interior value.
@@ -333,8 +344,8 @@ __global__ void __launch_bounds__(kBcThreads) k_bc(BcArgs a) {
           U[d0[b]] = x[b];
           if (M) {
             const float m = mirror_value_hw(x[b], (int)(d1[b] % 5), r0, e0);
-            M[d1[b]] = m;
-            M[d0[b]] = m;
+            put(d1[b], m);
+            put(d0[b], m);
           }
         }
     }
@@ -358,8 +369,8 @@ __global__ void __launch_bounds__(kBcThreads) k_bc(BcArgs a) {
 #pragma unroll
           for (int v = 0; v < 5; ++v) {
             const float m = mirror_value_hw(o[v], v, r0, e0);
-            M[(d1 - U) + v] = m;
-            M[(d0 - U) + v] = m;
+            put((d1 - U) + v, m);
+            put((d0 - U) + v, m);
           }
         }
       }
