@@ -12,6 +12,8 @@
 #include <map>
 #include <vector>
 
+#include <unistd.h>
+
 #include "../../include/bcm_gb300.h"
 #include "bcm_kernels.h"
 #include "bcm_tables.h"
@@ -35,6 +37,7 @@ void clear_err() { g_has_err = false; }
     cudaError_t e__ = (expr);                                                        \
     if (e__ != cudaSuccess) {                                                        \
       set_err(std::string(#expr) + ": " + cudaGetErrorString(e__));                  \
+      cudaGetLastError(); /* a non-sticky error must not reach the next call */      \
       return BCMG_ERR_CUDA;                                                          \
     }                                                                                \
   } while (0)
@@ -2144,7 +2147,8 @@ namespace {
 struct Compat {
   bcmg_reference_config cfg = {16, 1150, 0.0000185, 1.1842, 38.889, 38.889, 101300.0};
   cudaStream_t s = nullptr;
-  int ncube = 0, S = 0;  // sized for the last whole-array call
+  int S = 0;                     // cube edge with ghosts of the current call
+  int ncube = 0, full_S = 0;     // the whole-array buffers' geometry
   size_t ncell = 0;
   double *U1_ = nullptr, *U1 = nullptr, *U1q = nullptr, *U1p1 = nullptr, *U1p2 = nullptr,
          *Rku1 = nullptr, *Residual1 = nullptr, *cube_size = nullptr, *partials = nullptr,
@@ -2183,13 +2187,15 @@ struct Compat {
   int ensure_full(int nc) {
     int r;
     if ((r = stream())) return r;
+    // The full arrays' own geometry: S alone is also set by the boundary
+    // and ghost-cell twins for the cube gathers, before any full call.
     const int Sx = cfg.ncube_x + 4;
-    if (nc == ncube && Sx == S && U1_) return BCMG_OK;
+    if (nc == ncube && Sx == full_S && U1_) return BCMG_OK;
     dfree(U1_); dfree(U1); dfree(U1q); dfree(U1p1); dfree(U1p2); dfree(Rku1);
     dfree(Residual1); dfree(cube_size); dfree(partials); dfree(er); dfree(FWS);
     dfree(M); dfree(M2); dfree(D2); dfree(inv_dx); dfree(mpar);
     ncube = nc;
-    S = Sx;
+    S = full_S = Sx;
     ncell = (size_t)nc * S * S * S;
     const size_t nd = ncell * 5;
     CK(dalloc(&U1_, nd)); CK(dalloc(&U1, nd)); CK(dalloc(&U1q, nd)); CK(dalloc(&U1p1, nd));
@@ -2228,37 +2234,105 @@ Compat g_compat;
 // staging.  Opt-in because a registration must end before its memory is
 // freed: a caller that frees arrays the twins have seen (a scripting
 // front end, say) would leave registrations behind that a later array at
-// the same address trips over.  A region that cannot be registered is
-// copied pageable.  The registration lasts until bcmg_release_host_arrays()
-// or the process ends.
+// the same address trips over.  The registration lasts until
+// bcmg_release_host_arrays() or the process ends.
+//
+// Only the whole pages inside an array are registered.  The pages at its
+// two ends may hold other objects (heap arrays of a few hundred KB sit side
+// by side, and this host's pages may be 64 KB): registering them would make
+// the runtime take a neighbour that starts there for page-locked memory
+// and refuse its copy ("invalid argument") where the neighbour runs past
+// the registration.  host_copy() therefore moves the registered middle of a
+// range as one page-locked copy and the ends through pageable staging.  A
+// region with no whole page, or that cannot be registered, is copied
+// pageable.
 struct HostPins {
-  std::map<const void *, size_t> reg;  // registered base -> bytes
+  struct Reg {
+    size_t bytes;
+    const char *lo;  // registered span [lo, hi): the array's whole pages
+  };
+  std::map<const void *, Reg> reg;              // array base -> registration
+  std::map<const char *, const char *> spans;   // lo -> hi, disjoint
   std::map<const void *, size_t> refused;
   bool enabled = false;
+  static size_t page() {
+    static const size_t p = [] {
+      const long v = sysconf(_SC_PAGESIZE);
+      return v > 0 ? (size_t)v : (size_t)4096;
+    }();
+    return p;
+  }
   void pin(const void *p, size_t bytes) {
     if (!enabled || !p || bytes == 0) return;
     auto it = reg.find(p);
-    if (it != reg.end() && it->second >= bytes) return;
+    if (it != reg.end() && it->second.bytes >= bytes) return;
     auto rf = refused.find(p);
     if (rf != refused.end() && rf->second >= bytes) return;
     if (it != reg.end()) {  // grown: register the larger region afresh
-      cudaHostUnregister(const_cast<void *>(p));
+      cudaHostUnregister(const_cast<char *>(it->second.lo));
+      spans.erase(it->second.lo);
       reg.erase(it);
     }
-    if (cudaHostRegister(const_cast<void *>(p), bytes, cudaHostRegisterDefault) == cudaSuccess) {
-      reg[p] = bytes;
+    const size_t P = page();
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p), e = a + bytes;
+    const uintptr_t lo = (a + P - 1) / P * P, hi = e / P * P;
+    if (hi > lo && cudaHostRegister(reinterpret_cast<void *>(lo), hi - lo,
+                                    cudaHostRegisterDefault) == cudaSuccess) {
+      reg[p] = Reg{bytes, reinterpret_cast<const char *>(lo)};
+      spans[reinterpret_cast<const char *>(lo)] = reinterpret_cast<const char *>(hi);
     } else {
       cudaGetLastError();  // not sticky: the copies run pageable
       refused[p] = bytes;
     }
   }
   void release() {
-    for (auto &kv : reg) cudaHostUnregister(const_cast<void *>(kv.first));
+    for (auto &kv : spans) cudaHostUnregister(const_cast<char *>(kv.first));
+    spans.clear();
     reg.clear();
     refused.clear();
   }
+  // Length of the piece of [h, h + bytes) that starts at h and lies either
+  // wholly inside one registered span or wholly outside all of them.
+  size_t piece(const char *h, size_t bytes, bool *locked) const {
+    auto it = spans.upper_bound(h);  // first span starting after h
+    if (it != spans.begin()) {
+      auto pv = std::prev(it);
+      if (pv->second > h) {
+        *locked = true;
+        return std::min(bytes, (size_t)(pv->second - h));
+      }
+    }
+    *locked = false;
+    return it == spans.end() ? bytes : std::min(bytes, (size_t)(it->first - h));
+  }
 };
 HostPins g_pins;
+
+// Copy between a caller's host array and the device, piece by piece so that
+// no single copy mixes registered and unregistered pages.
+cudaError_t host_copy(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind,
+                      cudaStream_t s) {
+  const bool up = kind == cudaMemcpyHostToDevice;
+  const char *h = static_cast<const char *>(up ? src : dst);
+  size_t off = 0;
+  while (off < bytes) {
+    bool locked = false;
+    const size_t len = g_pins.piece(h + off, bytes - off, &locked);
+    cudaError_t e = cudaMemcpyAsync(static_cast<char *>(dst) + off,
+                                    static_cast<const char *>(src) + off, len, kind, s);
+    if (e != cudaSuccess) return e;
+    off += len;
+  }
+  return cudaSuccess;
+}
+
+// A twin that stops on an error may leave copies of the caller's arrays in
+// flight on its stream; they finish before the twin returns, so the caller
+// may free or reuse its arrays (and end their registration) at once.
+void twin_drain(int status) {
+  if (status != BCMG_OK && g_compat.s) cudaStreamSynchronize(g_compat.s);
+  cudaGetLastError();
+}
 
 // Host arrays of the flux twin whose device copies already hold the cells
 // the routine never writes (uploaded once per host pointer): U1p1, U1p2,
@@ -2282,15 +2356,15 @@ int gather_cubes(Compat &C, const std::vector<int> &cubes, const double *hostU) 
   for (int c : cubes) top = std::max(top, c);
   g_pins.pin(hostU, per * (top + 1) * sizeof(double));  // the array up to the last cube used
   for (size_t m = 0; m < cubes.size(); ++m)
-    CK(cudaMemcpyAsync(C.cubes + per * (m + 1), hostU + per * cubes[m], per * sizeof(double),
-                       cudaMemcpyHostToDevice, C.s));
+    CK(host_copy(C.cubes + per * (m + 1), hostU + per * cubes[m], per * sizeof(double),
+                 cudaMemcpyHostToDevice, C.s));
   return BCMG_OK;
 }
 int scatter_cubes(Compat &C, const std::vector<int> &cubes, double *hostU) {
   const size_t per = (size_t)C.S * C.S * C.S * 5;
   for (size_t m = 0; m < cubes.size(); ++m)
-    CK(cudaMemcpyAsync(hostU + per * cubes[m], C.cubes + per * (m + 1), per * sizeof(double),
-                       cudaMemcpyDeviceToHost, C.s));
+    CK(host_copy(hostU + per * cubes[m], C.cubes + per * (m + 1), per * sizeof(double),
+                 cudaMemcpyDeviceToHost, C.s));
   CK(cudaStreamSynchronize(C.s));
   return BCMG_OK;
 }
@@ -2449,7 +2523,7 @@ void BCM_Flux_XYZ_Viscous_Runge_kutta(int myid, int ncube, int RK, double deltaT
     // never writes their other cells.  Results come back whole.
     auto up = [&](double *dev, const double *host) -> int {
       g_pins.pin(host, b);
-      CK(cudaMemcpyAsync(dev, host, b, cudaMemcpyHostToDevice, s));
+      CK(host_copy(dev, host, b, cudaMemcpyHostToDevice, s));
       return BCMG_OK;
     };
     auto up_once = [&](double *dev, const double *host, int slot) -> int {
@@ -2459,7 +2533,7 @@ void BCM_Flux_XYZ_Viscous_Runge_kutta(int myid, int ncube, int RK, double deltaT
       return rr;
     };
     g_pins.pin(FWS, C.ncell * sizeof(int));
-    CK(cudaMemcpyAsync(C.FWS, FWS, C.ncell * sizeof(int), cudaMemcpyHostToDevice, s));
+    CK(host_copy(C.FWS, FWS, C.ncell * sizeof(int), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(C.cube_size, cube_size, sizeof(double) * ncube, cudaMemcpyHostToDevice, s));
     if ((r = up(C.U1_, U1_)) || (r = up(C.U1, U1)) || (r = up(C.U1q, U1q))) return r;
     if (RK == 1 && (r = up_once(C.U1p1, U1p1, 0))) return r;
@@ -2525,10 +2599,10 @@ void BCM_Flux_XYZ_Viscous_Runge_kutta(int myid, int ncube, int RK, double deltaT
       }
       nb = flux_split_blocks(ph.n, ncube - 1);
       if (RK == 3) CK(launch_norms(ph, C.partials, nb, C.er, s));
-      CK(cudaMemcpyAsync(U1_, C.U1_, b, cudaMemcpyDeviceToHost, s));
-      CK(cudaMemcpyAsync(Residual1, C.Residual1, b, cudaMemcpyDeviceToHost, s));
-      if (RK == 1) CK(cudaMemcpyAsync(U1p1, C.U1p1, b, cudaMemcpyDeviceToHost, s));
-      if (RK == 2) CK(cudaMemcpyAsync(U1p2, C.U1p2, b, cudaMemcpyDeviceToHost, s));
+      CK(host_copy(U1_, C.U1_, b, cudaMemcpyDeviceToHost, s));
+      CK(host_copy(Residual1, C.Residual1, b, cudaMemcpyDeviceToHost, s));
+      if (RK == 1) CK(host_copy(U1p1, C.U1p1, b, cudaMemcpyDeviceToHost, s));
+      if (RK == 2) CK(host_copy(U1p2, C.U1p2, b, cudaMemcpyDeviceToHost, s));
       if (RK == 3) CK(cudaMemcpyAsync(er + 1, C.er + 1, 7 * sizeof(double), cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
       return BCMG_OK;
@@ -2560,31 +2634,31 @@ void BCM_Flux_XYZ_Viscous_Runge_kutta(int myid, int ncube, int RK, double deltaT
     k.partials = C.partials;
     CK(launch_rk(k, &nb, s));
     if (RK == 3) CK(launch_norms(C.phys(), C.partials, nb, C.er, s));
-    CK(cudaMemcpyAsync(U1_, C.U1_, b, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(Rku1, C.Rku1, b, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(Residual1, C.Residual1, b, cudaMemcpyDeviceToHost, s));
-    if (RK == 1) CK(cudaMemcpyAsync(U1p1, C.U1p1, b, cudaMemcpyDeviceToHost, s));
-    if (RK == 2) CK(cudaMemcpyAsync(U1p2, C.U1p2, b, cudaMemcpyDeviceToHost, s));
+    CK(host_copy(U1_, C.U1_, b, cudaMemcpyDeviceToHost, s));
+    CK(host_copy(Rku1, C.Rku1, b, cudaMemcpyDeviceToHost, s));
+    CK(host_copy(Residual1, C.Residual1, b, cudaMemcpyDeviceToHost, s));
+    if (RK == 1) CK(host_copy(U1p1, C.U1p1, b, cudaMemcpyDeviceToHost, s));
+    if (RK == 2) CK(host_copy(U1p2, C.U1p2, b, cudaMemcpyDeviceToHost, s));
     if (RK == 3) CK(cudaMemcpyAsync(er + 1, C.er + 1, 7 * sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     return BCMG_OK;
   };
-  run();
+  twin_drain(run());
 }
 
 void BCM_X_boundary_condition(int myid, int nXbc_l, int nXbc_u, int *Xbc_l, int *Xbc_u,
                               double *U1_) {
   (void)myid;
   clear_err();
-  compat_bc(0, nXbc_l, nXbc_u, Xbc_l, Xbc_u, U1_);
+  twin_drain(compat_bc(0, nXbc_l, nXbc_u, Xbc_l, Xbc_u, U1_));
 }
 void BCM_Y_boundary_condition(int nYbc_l, int nYbc_u, int *Ybc_l, int *Ybc_u, double *U1_) {
   clear_err();
-  compat_bc(1, nYbc_l, nYbc_u, Ybc_l, Ybc_u, U1_);
+  twin_drain(compat_bc(1, nYbc_l, nYbc_u, Ybc_l, Ybc_u, U1_));
 }
 void BCM_Z_boundary_condition(int nZbc_l, int nZbc_u, int *Zbc_l, int *Zbc_u, double *U1_) {
   clear_err();
-  compat_bc(2, nZbc_l, nZbc_u, Zbc_l, Zbc_u, U1_);
+  twin_drain(compat_bc(2, nZbc_l, nZbc_u, Zbc_l, Zbc_u, U1_));
 }
 
 void BCM_Ghostcell_minus(int myid, int *NNBC, double *weight, int *GCindex, int *IPsur,
@@ -2592,14 +2666,14 @@ void BCM_Ghostcell_minus(int myid, int *NNBC, double *weight, int *GCindex, int 
   (void)myid;
   (void)FWS;
   clear_err();
-  compat_ghost(NNBC, weight, GCindex, IPsur, U1_);
+  twin_drain(compat_ghost(NNBC, weight, GCindex, IPsur, U1_));
 }
 void BCM_Ghostcell_plus(int myid, int *NNBC, double *weight, int *GCindex, int *IPsur,
                         int *FWS, double *U1_) {
   (void)myid;
   (void)FWS;
   clear_err();
-  compat_ghost(NNBC, weight, GCindex, IPsur, U1_);
+  twin_drain(compat_ghost(NNBC, weight, GCindex, IPsur, U1_));
 }
 
 void BCM_Interface(int myid, int ncube, int mPI_Nadj, int ncpu_bs, int ncpu_eq, int ncpu_sb,
@@ -2682,7 +2756,7 @@ void BCM_Interface(int myid, int ncube, int mPI_Nadj, int ncpu_bs, int ncpu_eq, 
       CK(cudaMemcpyAsync(C.tasks, tasks.data(), sizeof(FaceTask) * tasks.size(),
                          cudaMemcpyHostToDevice, C.s));
     g_pins.pin(U1_, b);
-    CK(cudaMemcpyAsync(C.U1_, U1_, b, cudaMemcpyHostToDevice, C.s));
+    CK(host_copy(C.U1_, U1_, b, cudaMemcpyHostToDevice, C.s));
     InterfaceArgs ia;
     ia.n = C.cfg.ncube_x;
     ia.ntasks = (int)tasks.size();
@@ -2690,11 +2764,11 @@ void BCM_Interface(int myid, int ncube, int mPI_Nadj, int ncpu_bs, int ncpu_eq, 
     ia.tasks = C.tasks;
     ia.U1_ = C.U1_;
     CK(launch_interface(ia, ncube, C.s));
-    CK(cudaMemcpyAsync(U1_, C.U1_, b, cudaMemcpyDeviceToHost, C.s));
+    CK(host_copy(U1_, C.U1_, b, cudaMemcpyDeviceToHost, C.s));
     CK(cudaStreamSynchronize(C.s));
     return BCMG_OK;
   };
-  run();
+  twin_drain(run());
 }
 
 }  // extern "C"

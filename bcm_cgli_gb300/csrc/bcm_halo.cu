@@ -167,11 +167,22 @@ __global__ void __launch_bounds__(kHaloThreads) k_iface_faces(InterfaceArgs a) {
   }
 }
 
-// Edge fill after all face copies (BCM_Interface.cpp:5640-5732): three
-// ordered phases per cube with CTA barriers in between.  The block has one
-// thread per item of the largest phase (20 (n + 2) values, up to 1,024), so
-// each phase is one round of loads and stores.
-__global__ void __launch_bounds__(1024) k_iface_edges(InterfaceArgs a) {
+// Edge fill after all face copies (BCM_Interface.cpp:5640-5732).  The
+// reference fills the layer-1 edge ghosts in three ordered phases: i-edges
+// (i = 2..nx), then j-edges and k-edges over the whole ghost range, so the
+// last two end at the corners.  Every edge cell that is not a corner reads
+// two face ghosts (cells with one ghost coordinate), which no phase writes;
+// the j-edge phase's corner values are overwritten by the k-edge phase
+// before anything reads them; and the k-edge phase's corner value is the
+// average of the j-edge and i-edge cells next to the corner, themselves
+// averages of face ghosts.  So one pass computes each edge cell from two
+// face ghosts and each corner from the two edge values it averages (formed
+// from four face ghosts in registers): the reference's operations, the same
+// bits, one round trip to memory instead of three dependent ones.  A thread
+// issues the loads of kEdgeBatch items before their stores.
+constexpr int kEdgeThreads = 256, kEdgeBatch = 4;
+
+__global__ void __launch_bounds__(kEdgeThreads) k_iface_edges(InterfaceArgs a) {
   const int n = a.n, S = n + 4, nx = n + 1, nyy = n + 2;
   const int c = blockIdx.x + 1;
   if (!case_active(a.bt, c)) return;
@@ -179,47 +190,57 @@ __global__ void __launch_bounds__(1024) k_iface_edges(InterfaceArgs a) {
   float *M = mirror_current(a.mir);
   double r0 = 0, e0 = 0;
   if (M) mirror_base(a.mir, a.bt, c, r0, e0);
-  auto Q = [&](int i, int j, int k) { return U + 5 * cell_index(S, c, i, j, k); };
-  // average of two face ghosts into an edge ghost, and its mirror value
-  auto avg = [&](double *d, const double *x, const double *y, int v) {
-    const double r = 0.5 * (x[v] + y[v]);
-    d[v] = r;
-    if (M) M[(d - U) + v] = mirror_value_hw(r, v, r0, e0);
+  auto at = [&](int i, int j, int k, int v) { return 5 * cell_index(S, c, i, j, k) + v; };
+  auto ghost = [&](int x) { return x == 1 || x == nyy; };
+  auto in = [&](int x) { return x == 1 ? 2 : nx; };
+  // an edge cell (two ghost coordinates): the average of its two inward
+  // neighbours across its ghost axes, both face ghosts
+  auto edge = [&](int i, int j, int k, int v) -> double {
+    double p, q;
+    if (!ghost(i)) { p = U[at(i, in(j), k, v)]; q = U[at(i, j, in(k), v)]; }
+    else if (!ghost(j)) { p = U[at(in(i), j, k, v)]; q = U[at(i, j, in(k), v)]; }
+    else { p = U[at(in(i), j, k, v)]; q = U[at(i, in(j), k, v)]; }
+    return 0.5 * (p + q);
   };
-  // Phase 1: i-edges, i = 2..nx.
-  for (int w = threadIdx.x; w < 4 * n * 5; w += blockDim.x) {
-    const int v = w % 5, e = (w / 5) % 4, i = 2 + (w / 20);
-    double *d;
-    const double *x, *y;
-    if (e == 0) { d = Q(i, 1, 1); x = Q(i, 1, 2); y = Q(i, 2, 1); }
-    else if (e == 1) { d = Q(i, nyy, 1); x = Q(i, nyy, 2); y = Q(i, nx, 1); }
-    else if (e == 2) { d = Q(i, 1, nyy); x = Q(i, 1, nx); y = Q(i, 2, nyy); }
-    else { d = Q(i, nyy, nyy); x = Q(i, nyy, nx); y = Q(i, nx, nyy); }
-    avg(d, x, y, v);
-  }
-  __syncthreads();
-  // Phase 2: j-edges, j = 1..nyy.
-  for (int w = threadIdx.x; w < 4 * (n + 2) * 5; w += blockDim.x) {
-    const int v = w % 5, e = (w / 5) % 4, j = 1 + (w / 20);
-    double *d;
-    const double *x, *y;
-    if (e == 0) { d = Q(1, j, 1); x = Q(1, j, 2); y = Q(2, j, 1); }
-    else if (e == 1) { d = Q(1, j, nyy); x = Q(2, j, nyy); y = Q(1, j, nx); }
-    else if (e == 2) { d = Q(nyy, j, 1); x = Q(nx, j, 1); y = Q(nyy, j, 2); }
-    else { d = Q(nyy, j, nyy); x = Q(nx, j, nyy); y = Q(nyy, j, nx); }
-    avg(d, x, y, v);
-  }
-  __syncthreads();
-  // Phase 3: k-edges, k = 1..nyy.
-  for (int w = threadIdx.x; w < 4 * (n + 2) * 5; w += blockDim.x) {
-    const int v = w % 5, e = (w / 5) % 4, k = 1 + (w / 20);
-    double *d;
-    const double *x, *y;
-    if (e == 0) { d = Q(1, 1, k); x = Q(1, 2, k); y = Q(2, 1, k); }
-    else if (e == 1) { d = Q(1, nyy, k); x = Q(2, nyy, k); y = Q(1, nx, k); }
-    else if (e == 2) { d = Q(nyy, 1, k); x = Q(nx, 1, k); y = Q(nyy, 2, k); }
-    else { d = Q(nyy, nyy, k); x = Q(nx, nyy, k); y = Q(nyy, nx, k); }
-    avg(d, x, y, v);
+  const int nedge = 12 * n, items = 5 * (nedge + 8);
+  // the value and destination of item w
+  auto item = [&](int w, double &r, size_t &d, int &v) {
+    v = w % 5;
+    const int cell = w / 5;
+    int ci, cj, ck;
+    if (cell < nedge) {
+      // edge family f (free coordinate i, j or k = 2..nx) and its two ghost
+      // coordinates
+      const int f = cell / (4 * n), rem = cell - f * 4 * n;
+      const int pos = 2 + (rem >> 2), g1 = (rem & 1) ? nyy : 1, g2 = (rem & 2) ? nyy : 1;
+      if (f == 0) { ci = pos; cj = g1; ck = g2; }
+      else if (f == 1) { ci = g1; cj = pos; ck = g2; }
+      else { ci = g1; cj = g2; ck = pos; }
+      r = edge(ci, cj, ck, v);
+    } else {
+      // corner: the k-edge phase's average of the j-edge cell and the i-edge
+      // cell next to it
+      const int q = cell - nedge;
+      ci = (q & 1) ? nyy : 1; cj = (q & 2) ? nyy : 1; ck = (q & 4) ? nyy : 1;
+      const double xj = edge(ci, in(cj), ck, v), yi = edge(in(ci), cj, ck, v);
+      r = 0.5 * (xj + yi);
+    }
+    d = at(ci, cj, ck, v);
+  };
+  for (int w0 = threadIdx.x; w0 < items; w0 += kEdgeBatch * kEdgeThreads) {
+    double r0v = 0, r1v = 0, r2v = 0, r3v = 0;
+    size_t d0 = 0, d1 = 0, d2 = 0, d3 = 0;
+    int v0 = 0, v1 = 0, v2 = 0, v3 = 0;
+    const int w1 = w0 + kEdgeThreads, w2 = w0 + 2 * kEdgeThreads, w3 = w0 + 3 * kEdgeThreads;
+    item(w0, r0v, d0, v0);
+    if (w1 < items) item(w1, r1v, d1, v1);
+    if (w2 < items) item(w2, r2v, d2, v2);
+    if (w3 < items) item(w3, r3v, d3, v3);
+    U[d0] = r0v;
+    if (M) M[d0] = mirror_value_hw(r0v, v0, r0, e0);
+    if (w1 < items) { U[d1] = r1v; if (M) M[d1] = mirror_value_hw(r1v, v1, r0, e0); }
+    if (w2 < items) { U[d2] = r2v; if (M) M[d2] = mirror_value_hw(r2v, v2, r0, e0); }
+    if (w3 < items) { U[d3] = r3v; if (M) M[d3] = mirror_value_hw(r3v, v3, r0, e0); }
   }
 }
 
@@ -279,8 +300,7 @@ cudaError_t launch_interface(const InterfaceArgs &a, int ncubes_total, cudaStrea
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
-  const int et = std::min(1024, (20 * (a.n + 2) + 31) / 32 * 32);
-  k_iface_edges<<<ncubes_total - 1, et, 0, s>>>(a);
+  k_iface_edges<<<ncubes_total - 1, kEdgeThreads, 0, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -308,7 +328,7 @@ __global__ void __launch_bounds__(kBcThreads) k_bc(BcArgs a) {
   // next buffer takes them now and equals the state's rounding in every
   // cell once it becomes current.
   float *M = mirror_current(a.mir);
-  float *Mo = M ? a.mir.buf[*a.mir.parity ^ 1] : nullptr;
+  float *Mo = M ? (M == a.mir.buf[0] ? a.mir.buf[1] : a.mir.buf[0]) : nullptr;
   double r0 = 0, e0 = 0;
   if (M) mirror_base(a.mir, a.bt, c, r0, e0);
   auto put = [&](size_t at, float m) {

@@ -112,8 +112,10 @@ struct Mirror {
 };
 
 #ifdef __CUDACC__
+// (a select, not m.buf[*m.parity]: indexing a kernel argument's array with
+// a run-time value would copy the argument to local memory)
 __device__ __forceinline__ float *mirror_current(const Mirror &m) {
-  return m.buf[0] ? m.buf[*m.parity] : nullptr;
+  return m.buf[0] ? (*m.parity ? m.buf[1] : m.buf[0]) : nullptr;
 }
 #endif
 

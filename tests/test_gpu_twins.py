@@ -79,6 +79,70 @@ def test_twin_subiterations_bitwise_in_every_copy_mode(name, mode, twin_defaults
         assert np.array_equal(getattr(a, k), getattr(b, k)), (name, mode, k)
 
 
+def _packed_state(case):
+    """The run's seven arrays side by side in one buffer, each starting 16
+    bytes past the previous one's end (so neighbours share pages, as heap
+    arrays of a few hundred KB do)."""
+    st = O.State(case)
+    shape, cnt = st.U1_.shape, st.U1_.size
+    buf = np.zeros(len(ARRAYS) * (cnt + 2) + 1, np.float64)
+    for m, k in enumerate(ARRAYS):
+        v = buf[1 + m * (cnt + 2):1 + m * (cnt + 2) + cnt].reshape(shape)
+        v[...] = getattr(st, k)
+        setattr(st, k, v)
+    return st, buf
+
+
+@pytest.mark.parametrize("mode", ["pinned", "pinned_scratch_kept", "pageable"])
+def test_twin_arrays_sharing_pages(mode, twin_defaults):
+    """Caller arrays that share pages with each other: page-locking registers
+    only each array's whole pages, so a neighbour starting on a shared page
+    is never taken for page-locked memory, and every array still equals the
+    oracle's."""
+    case = G.golden_cases()["random_open_n4"]
+    api.reference_config_for(case)
+    api.set_host_pinning(mode != "pageable")
+    api.set_twin_scratch_kept(mode == "pinned_scratch_kept")
+    port = O.Port()
+    a = O.State(case)
+    b, buf = _packed_state(case)
+    for _ in range(2):
+        _oracle_subiteration(port, case, a)
+        _subiteration_twins(case, b)
+    api.release_host_arrays()  # while the arrays are alive
+    for k in ARRAYS:
+        assert np.array_equal(getattr(a, k), getattr(b, k)), (mode, k)
+    del buf
+
+
+def test_twins_follow_a_new_cube_size_with_the_same_cube_count(twin_defaults):
+    """A case of 8 cubes of 8^3 and then one of 8 cubes of 4^3: the twins
+    size their device arrays for the new configuration (the boundary twin,
+    called first, must not leave the flux twin the old cell count), copy
+    exactly the new arrays, and equal the oracle; the arrays sit in one
+    buffer between guard values that must stay untouched."""
+    port = O.Port()
+    for name in ("tgv_n8", "random_open_n4"):
+        case = G.golden_cases()[name]
+        api.reference_config_for(case)
+        api.set_host_pinning(True)
+        a = O.State(case)
+        b, buf = _packed_state(case)
+        # guards: before the first array, and the two values after each array
+        guards = [0] + [i for m in range(len(ARRAYS))
+                        for i in (1 + m * (case.U.size + 2) + case.U.size,
+                                  2 + m * (case.U.size + 2) + case.U.size)]
+        assert guards[-1] == len(buf) - 1
+        buf[guards] = -777.0
+        _oracle_subiteration(port, case, a)
+        _subiteration_twins(case, b)
+        api.release_host_arrays()  # while the arrays are alive
+        for k in ARRAYS:
+            assert np.array_equal(getattr(a, k), getattr(b, k)), (name, k)
+        assert np.all(buf[guards] == -777.0), name
+        del buf
+
+
 @pytest.mark.parametrize("name", ["random_periodic_n8", "tgv_n8", "vortex_n8"])
 def test_split_flux_twin_within_bound(name, twin_defaults):
     case = G.golden_cases()[name]
