@@ -125,6 +125,8 @@ def _declare(L):
     L.bcmg_case_set_tuning.argtypes = [P, C.POINTER(Tuning)]
     L.bcmg_case_set_face_copies.argtypes = [P, C.c_int]
     L.bcmg_case_set_mirror_each_stage.argtypes = [P, C.c_int]
+    L.bcmg_case_set_concurrent_ghosts.argtypes = [P, C.c_int]
+    L.bcmg_case_concurrent_ghosts.argtypes = [P]
     L.bcmg_case_autotune.argtypes = [P, C.c_int, C.POINTER(Tuning)]
     L.bcmg_case_output_q.argtypes = [P, C.c_int, C.c_int, C.c_char_p]
     L.bcmg_case_output_x.argtypes = [P, C.c_int, C.c_int, C.c_char_p, P]

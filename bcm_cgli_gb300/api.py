@@ -414,6 +414,16 @@ class CaseContext:
         give the same bits."""
         check(lib().bcmg_case_set_mirror_each_stage(self.h, 1 if on else 0))
 
+    def set_concurrent_ghosts(self, on=True):
+        """Run the IBM ghost fill beside the boundary fill (True, default;
+        only where no cube holds both) or after it (False).  Both give the
+        same bits."""
+        check(lib().bcmg_case_set_concurrent_ghosts(self.h, 1 if on else 0))
+
+    def concurrent_ghosts(self):
+        """Whether the ghost fill runs beside the boundary fill."""
+        return bool(lib().bcmg_case_concurrent_ghosts(self.h))
+
     def autotune(self, reps=3):
         """Times the launch-shape candidates on this context's state, applies the
         fastest and returns the choice with the measured milliseconds."""

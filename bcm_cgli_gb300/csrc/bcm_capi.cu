@@ -178,7 +178,8 @@ int ibm_upload(Ibm &t, int nbc, const double *w, const int *gc, const int *ip, i
 }
 
 int ibm_run(const Ibm &t, int n, double rho0, double P0, double *U, cudaStream_t s,
-            long long *launches, const Batch &bt = Batch(), const Mirror &mir = Mirror()) {
+            long long *launches, const Batch &bt = Batch(), const Mirror &mir = Mirror(),
+            int priority = 0) {
   for (size_t l = 1; l < t.level_off.size(); ++l) {
     GhostArgs g;
     g.n = n;
@@ -191,7 +192,7 @@ int ibm_run(const Ibm &t, int n, double rho0, double P0, double *U, cudaStream_t
     g.U1_ = U;
     g.bt = bt;
     g.mir = mir;
-    CK(launch_ghost(g, t.level_off[l] - t.level_off[l - 1], s));
+    CK(launch_ghost(g, t.level_off[l] - t.level_off[l - 1], s, priority));
     if (launches) ++*launches;
   }
   return BCMG_OK;
@@ -276,6 +277,16 @@ struct bcmg_case {
   int ntasks_q = 0;
   int *bc_cubes = nullptr, *bc_masks = nullptr;
   int nbc = 0;
+  // The IBM ghost fill on a side stream beside the boundary fill: allowed
+  // when no cube holds both an IBM entry's cells (ghost or stencil) and a
+  // boundary face, so neither reads or writes a cell of the other; the
+  // interface call after them waits for both.
+  bool ghost_beside_bc = false;  // a side table exists
+  Ibm ibm_side;                  // the entries filled beside the boundary fill
+  bool ghost_side_on = true;     // bcmg_case_set_concurrent_ghosts
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  int side_priority = 0;  // the device's highest scheduling priority
   Ibm ibm;  // minus entries then plus entries, one combined schedule
   double *partials = nullptr;
   int nparts = 0;
@@ -380,6 +391,12 @@ struct bcmg_case {
     }
     halo.clear();
     ibm.release();
+    ibm_side.release();
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    ev_fork = ev_join = nullptr;
+    if (side) cudaStreamDestroy(side);
+    side = nullptr;
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
   }
@@ -506,6 +523,15 @@ int case_interface(bcmg_case *c, IfaceList list = kIfaceFull) {
 // closing interface call, so only the face copies that can change run.
 int case_prologue(bcmg_case *c, bool full = true) {
   int r;
+  const bool beside = c->ghost_beside_bc && c->ghost_side_on;
+  if (beside) {  // fork: the side table's ghost levels on the side stream
+    CK(cudaEventRecord(c->ev_fork, c->stream));
+    CK(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+    if ((r = ibm_run(c->ibm_side, c->ph.n, c->ph.rho0, c->ph.P0, c->U1_, c->side, &c->launches,
+                     c->bt(), c->mir(), c->side_priority)))
+      return r;
+    CK(cudaEventRecord(c->ev_join, c->side));
+  }
   if (c->nbc > 0) {
     BcArgs b;
     b.n = c->ph.n;
@@ -518,6 +544,12 @@ int case_prologue(bcmg_case *c, bool full = true) {
     b.mir = c->mir();
     CK(launch_bc(b, c->nbc, c->stream));
     ++c->launches;
+  }
+  if (beside) {  // join; the other cases' entries after the boundary fill
+    CK(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
+  } else if ((r = ibm_run(c->ibm_side, c->ph.n, c->ph.rho0, c->ph.P0, c->U1_, c->stream,
+                          &c->launches, c->bt(), c->mir()))) {
+    return r;
   }
   if ((r = ibm_run(c->ibm, c->ph.n, c->ph.rho0, c->ph.P0, c->U1_, c->stream, &c->launches,
                    c->bt(), c->mir())))
@@ -777,7 +809,8 @@ int build_conv_graph(bcmg_case *c, int max_subiters, double tol) {
   ce = cudaStreamEndCapture(c->stream, &g);
   if (r) return r;
   CK(ce);
-  CK(cudaGraphInstantiate(&c->cgraph, g, 0));
+  // per-node priorities: the IBM ghost levels beside the boundary fill
+  CK(cudaGraphInstantiate(&c->cgraph, g, cudaGraphInstantiateFlagUseNodePriority));
   c->cgraph_max = max_subiters;
   c->cgraph_tol = tol;
   c->cgraph_method = c->method;
@@ -1197,8 +1230,72 @@ int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out,
       std::copy(d->gc_plus + 1, d->gc_plus + 1 + 4 * (size_t)np, gc.begin() + 1 + 4 * (size_t)nm);
       std::copy(d->ip_plus + 1, d->ip_plus + 1 + 4 * (size_t)np, ip.begin() + 1 + 4 * (size_t)nm);
     }
-    int r = ibm_upload(c->ibm, nm + np, w.data(), gc.data(), ip.data(), d->n, d->ncube, s);
+    // Cases whose cubes with boundary faces hold no IBM entry's cells (ghost
+    // or stencil): their entries form the side table, filled beside the
+    // boundary fill; the other cases' entries stay in the reference's order
+    // after it.  Cases never share cubes, so splitting the table by case
+    // keeps every dependency inside one table.
+    const int ne = nm + np;
+    auto case_of = [&](int cube) -> int {
+      if (!bi) return 0;
+      const auto &b0 = bi->case_cube0;
+      return (int)(std::upper_bound(b0.begin(), b0.end(), cube) - b0.begin()) - 1;
+    };
+    const int ncs = bi ? (int)bi->cases.size() : 1;
+    std::vector<char> ibm_cube((size_t)d->ncube, 0), shared((size_t)ncs, 0);
+    for (int e = 0; e < ne; ++e) {
+      const int g = gc[4 * (size_t)e + 1], q = ip[4 * (size_t)e + 1];
+      if (g > 0 && g < d->ncube) ibm_cube[g] = 1;
+      if (q > 0 && q < d->ncube) ibm_cube[q] = 1;
+    }
+    for (int cb : bcc)
+      if (cb > 0 && cb < d->ncube && ibm_cube[cb]) {
+        const int q = case_of(cb);
+        if (q >= 0 && q < ncs) shared[q] = 1;
+      }
+    for (int e = 0; e < ne; ++e) {  // an entry reaching into another case
+      const int q = case_of(gc[4 * (size_t)e + 1]);
+      if (q >= 0 && q < ncs && case_of(ip[4 * (size_t)e + 1]) != q) shared[q] = 1;
+    }
+    std::vector<char> to_side((size_t)ne, 0);
+    int nside = 0;
+    if (!bcc.empty())
+      for (int e = 0; e < ne; ++e) {
+        const int q = case_of(gc[4 * (size_t)e + 1]);
+        if (q >= 0 && q < ncs && !shared[q]) {
+          to_side[e] = 1;
+          ++nside;
+        }
+      }
+    auto upload = [&](Ibm &t, char which) -> int {
+      std::vector<double> ws(1, 0.0);
+      std::vector<int> gs(1, 0), is(1, 0);
+      int cnt = 0;
+      for (int e = 0; e < ne; ++e) {
+        if (to_side[e] != which) continue;
+        ws.insert(ws.end(), w.begin() + 1 + 8 * (size_t)e, w.begin() + 9 + 8 * (size_t)e);
+        gs.insert(gs.end(), gc.begin() + 1 + 4 * (size_t)e, gc.begin() + 5 + 4 * (size_t)e);
+        is.insert(is.end(), ip.begin() + 1 + 4 * (size_t)e, ip.begin() + 5 + 4 * (size_t)e);
+        ++cnt;
+      }
+      return cnt ? ibm_upload(t, cnt, ws.data(), gs.data(), is.data(), d->n, d->ncube, s)
+                 : BCMG_OK;
+    };
+    int r = nside == 0 ? ibm_upload(c->ibm, ne, w.data(), gc.data(), ip.data(), d->n, d->ncube, s)
+                       : upload(c->ibm, 0);
+    if (!r && nside > 0) r = upload(c->ibm_side, 1);
     if (r) return fail(r);
+    if (nside > 0) {
+      int least = 0, greatest = 0;
+      if (!ck(cudaDeviceGetStreamPriorityRange(&least, &greatest), "priority range"))
+        return fail(BCMG_ERR_CUDA);
+      c->side_priority = greatest;
+      if (!ck(cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, greatest), "stream") ||
+          !ck(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "event") ||
+          !ck(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming), "event"))
+        return fail(BCMG_ERR_CUDA);
+      c->ghost_beside_bc = true;
+    }
   }
   // Reduced face-task list of the prologue interface calls.
   {
@@ -1346,7 +1443,8 @@ int bcmg_case_advance(bcmg_case *c, int steps, int subiters, int use_graph, doub
       cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
       if (r) return r;
       if (ce != cudaSuccess) { set_err(cudaGetErrorString(ce)); return BCMG_ERR_CUDA; }
-      ce = cudaGraphInstantiate(&c->graph, g, 0);
+      // per-node priorities: the IBM ghost levels beside the boundary fill
+      ce = cudaGraphInstantiate(&c->graph, g, cudaGraphInstantiateFlagUseNodePriority);
       cudaGraphDestroy(g);
       if (ce != cudaSuccess) { set_err(cudaGetErrorString(ce)); return BCMG_ERR_CUDA; }
       c->graph_subiters = subiters;
@@ -2001,6 +2099,23 @@ int bcmg_case_set_face_copies(bcmg_case *c, int in_flux) {
   if (c->cgraph) cudaGraphExecDestroy(c->cgraph);
   c->cgraph = nullptr;
   return BCMG_OK;
+}
+
+int bcmg_case_set_concurrent_ghosts(bcmg_case *c, int on) {
+  clear_err();
+  if (!c) { set_err("null context"); return BCMG_ERR_ARG; }
+  c->ghost_side_on = on != 0;
+  if (c->graph) cudaGraphExecDestroy(c->graph);  // captured steps hold the old order
+  c->graph = nullptr;
+  c->graph_subiters = -1;
+  if (c->cgraph) cudaGraphExecDestroy(c->cgraph);
+  c->cgraph = nullptr;
+  return BCMG_OK;
+}
+
+int bcmg_case_concurrent_ghosts(bcmg_case *c) {
+  if (!c) return 0;
+  return c->ghost_beside_bc && c->ghost_side_on ? 1 : 0;
 }
 
 int bcmg_case_autotune(bcmg_case *c, int reps, bcmg_tuning *out) {

@@ -572,10 +572,24 @@ __global__ void __launch_bounds__(kGhostThreads) k_ghost(GhostArgs a, int count)
   }
 }
 
-cudaError_t launch_ghost(const GhostArgs &a, int count, cudaStream_t s) {
+cudaError_t launch_ghost(const GhostArgs &a, int count, cudaStream_t s, int priority) {
   if (count <= 0) return cudaSuccess;
-  k_ghost<<<(count + kGhostPer - 1) / kGhostPer, kGhostThreads, 0, s>>>(a, count);
-  return cudaGetLastError();
+  const unsigned grid = (count + kGhostPer - 1) / kGhostPer;
+  if (priority == 0) {
+    k_ghost<<<grid, kGhostThreads, 0, s>>>(a, count);
+    return cudaGetLastError();
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kGhostThreads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributePriority;
+  at[0].val.priority = priority;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_ghost, a, count);
 }
 
 }  // namespace bcmg

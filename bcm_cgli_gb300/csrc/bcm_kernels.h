@@ -266,6 +266,9 @@ struct GhostArgs {
   Batch bt;  // batches: rho0, P0 of the ghost cell's case
   Mirror mir;  // split precision: the ghost cell's mirror value too
 };
-cudaError_t launch_ghost(const GhostArgs &a, int count, cudaStream_t s);
+// priority != 0: launched with that scheduling priority (a launch
+// attribute, kept by stream capture), so its blocks go ahead of pending
+// blocks of lower-priority kernels running beside it
+cudaError_t launch_ghost(const GhostArgs &a, int count, cudaStream_t s, int priority = 0);
 
 }  // namespace bcmg

@@ -429,6 +429,7 @@ def measure(api, case, precision_name, args, dist, clocks_on=True, method=None, 
     ctx.set_profiling(False)
     out = {"tuning": ({"flux_tile": shape["flux_tile"], "lusgs_threads": shape["lusgs_threads"],
                        "flux_form": shape.get("flux_form", 0),
+                       "ghost_fill_beside_boundary_fill": ctx.concurrent_ghosts(),
                        "from": "bcm_cgli_gb300/tuning_gb300.json"} if shape else None),
            "value": dist.throughput(case.n_cells * SUBITERS * steps, ms),
            "ms_per_step": ms / steps, "steps": steps, "warmup": max(1, warmup),
