@@ -141,6 +141,8 @@ def _declare(L):
     L.bcmg_interface_tasks.argtypes = [C.c_int, ip, ip, ip, ip, C.c_int]
     L.bcmg_interface_plan.argtypes = [C.c_int, C.c_int, ip, ip, P, P, P, C.c_int, P, C.c_int,
                                       ip, ip, C.c_int]
+    L.bcmg_interface_closing_plan.argtypes = [C.c_int, C.c_int, ip, ip, P, P, P, C.c_int, P,
+                                              C.c_int, ip, ip, C.c_int]
     L.bcmg_ibm_preprocess.argtypes = [
         C.c_int, C.c_int, dp, ip, dp, dp, dp, ip, C.c_int, dp, C.c_int, C.POINTER(C.c_int), ip,
         ip, dp, C.POINTER(C.c_int), ip, ip, dp]

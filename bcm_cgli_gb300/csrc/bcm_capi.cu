@@ -275,6 +275,12 @@ struct bcmg_case {
   int *task_cube_q = nullptr;
   FaceTask *tasks_q = nullptr;
   int ntasks_q = 0;
+  // the closing call of split RK stages 1 and 2: the level jumps and edge
+  // fills read before the next stage's opening call rewrites them
+  int *task_cube_r = nullptr, *edge_r = nullptr;
+  FaceTask *tasks_r = nullptr;
+  int ntasks_r = 0, nedge_r = 0;
+  bool closing_reduced = false;
   int *bc_cubes = nullptr, *bc_masks = nullptr;
   int nbc = 0;
   // The IBM ghost fill on a side stream beside the boundary fill: allowed
@@ -382,6 +388,7 @@ struct bcmg_case {
     dfree(M); dfree(M2); dfree(mpar); dfree(D2); dfree(inv_dx);
     dfree(FWS); dfree(cube_size); dfree(task_cube); dfree(tasks); dfree(task_cube_p);
     dfree(tasks_p); dfree(push); dfree(task_cube_q); dfree(tasks_q); dfree(bc_cubes);
+    dfree(task_cube_r); dfree(tasks_r); dfree(edge_r);
     dfree(bc_masks); dfree(partials); dfree(er); dfree(emax);
     dfree(cases); dfree(cube_case); dfree(rk_blk); dfree(case_blk_rk); dfree(case_blk_flux);
     dfree(case_blk_cube);
@@ -487,7 +494,7 @@ int case_flux(bcmg_case *c, int RK) {
 }
 
 // Which face tasks an interface call runs.
-enum IfaceList { kIfaceFull, kIfacePrologue, kIfaceClosing };
+enum IfaceList { kIfaceFull, kIfacePrologue, kIfaceClosing, kIfaceClosingReduced };
 
 int case_interface(bcmg_case *c, IfaceList list = kIfaceFull) {
   if (c->xchg) {  // sharded: the proxies' face bands first
@@ -509,12 +516,19 @@ int case_interface(bcmg_case *c, IfaceList list = kIfaceFull) {
     ia.ntasks = c->ntasks_q;
     ia.task_cube = c->task_cube_q;
     ia.tasks = c->tasks_q;
+  } else if (list == kIfaceClosingReduced) {
+    ia.ntasks = c->ntasks_r;
+    ia.task_cube = c->task_cube_r;
+    ia.tasks = c->tasks_r;
+    ia.edge_list = true;
+    ia.edge_cubes = c->edge_r;
+    ia.nedge = c->nedge_r;
   }
   ia.U1_ = c->U1_;
   ia.bt = c->bt();
   ia.mir = c->mir();
   CK(launch_interface(ia, c->ncube, c->stream));
-  c->launches += ia.ntasks > 0 ? 2 : 1;
+  c->launches += (ia.ntasks > 0 ? 1 : 0) + (ia.edge_list && ia.nedge == 0 ? 0 : 1);
   return BCMG_OK;
 }
 
@@ -637,7 +651,10 @@ int case_lusgs(bcmg_case *c, bool full = true) {
                                : kIfaceFull);
 }
 
-int case_stage(bcmg_case *c, int RK, bool full = true) {
+// reduced: the stage is RK 1 or 2 of a sub-iteration that goes on (not a
+// single-stage call), so its closing interface call may leave out what the
+// next stage's opening call rewrites before anything reads it.
+int case_stage(bcmg_case *c, int RK, bool full = true, bool reduced = false) {
   int r;
   if ((r = case_prologue(c, full))) return r;
   if ((r = case_flux(c, RK))) return r;
@@ -655,7 +672,9 @@ int case_stage(bcmg_case *c, int RK, bool full = true) {
       }
     }
     // the flux kernel made the same-level copies of the updated cells
-    return case_interface(c, c->push_table() ? kIfaceClosing : kIfaceFull);
+    if (!c->push_table()) return case_interface(c, kIfaceFull);
+    return case_interface(c, reduced && c->closing_reduced && !c->xchg ? kIfaceClosingReduced
+                                                                      : kIfaceClosing);
   }
   RkArgs k;
   k.ph = c->ph;
@@ -697,7 +716,7 @@ int case_subiter(bcmg_case *c, bool full = true) {
     if ((r = case_lusgs(c, full))) return r;
   } else {
     for (int RK = 1; RK <= 3; ++RK)
-      if ((r = case_stage(c, RK, full && RK == 1))) return r;
+      if ((r = case_stage(c, RK, full && RK == 1, RK < 3))) return r;
   }
   k_emax<<<c->ncase, 32, 0, c->stream>>>(c->er, c->emax, c->bt().active);
   CK(cudaGetLastError());
@@ -1348,6 +1367,37 @@ int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out,
             ck(cudaMemcpy(c->task_cube_q, cq.data(), sizeof(int) * cq.size(),
                           cudaMemcpyHostToDevice), "copy")))
         return fail(BCMG_ERR_CUDA);
+      // the closing call of RK stages 1 and 2 (not for sharded contexts,
+      // whose proxies are refilled by each call's exchange)
+      if (c->nreal == d->ncube - 1) {
+        std::vector<char> keep_r, edge;
+        closing_plan(d->n, d->ncube, tasks, task_cube, bcc, bcm, d->ip_minus, nm, d->ip_plus,
+                     np, keep_r, edge);
+        std::vector<FaceTask> tr;
+        std::vector<int> cr, er_;
+        for (size_t t = 0; t < tasks.size(); ++t)
+          if (keep_r[t]) {
+            tr.push_back(tasks[t]);
+            cr.push_back(task_cube[t]);
+          }
+        for (int cb = 1; cb < d->ncube; ++cb)
+          if (edge[cb]) er_.push_back(cb);
+        c->ntasks_r = (int)tr.size();
+        c->nedge_r = (int)er_.size();
+        if ((!tr.empty() &&
+             !(ck(dalloc(&c->tasks_r, tr.size()), "alloc") &&
+               ck(dalloc(&c->task_cube_r, cr.size()), "alloc") &&
+               ck(cudaMemcpy(c->tasks_r, tr.data(), sizeof(FaceTask) * tr.size(),
+                             cudaMemcpyHostToDevice), "copy") &&
+               ck(cudaMemcpy(c->task_cube_r, cr.data(), sizeof(int) * cr.size(),
+                             cudaMemcpyHostToDevice), "copy"))) ||
+            (!er_.empty() &&
+             !(ck(dalloc(&c->edge_r, er_.size()), "alloc") &&
+               ck(cudaMemcpy(c->edge_r, er_.data(), sizeof(int) * er_.size(),
+                             cudaMemcpyHostToDevice), "copy"))))
+          return fail(BCMG_ERR_CUDA);
+        c->closing_reduced = true;
+      }
     }
   }
   *out = c;

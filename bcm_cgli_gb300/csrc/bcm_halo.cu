@@ -184,7 +184,7 @@ constexpr int kEdgeThreads = 256, kEdgeBatch = 4;
 
 __global__ void __launch_bounds__(kEdgeThreads) k_iface_edges(InterfaceArgs a) {
   const int n = a.n, S = n + 4, nx = n + 1, nyy = n + 2;
-  const int c = blockIdx.x + 1;
+  const int c = a.edge_list ? a.edge_cubes[blockIdx.x] : blockIdx.x + 1;
   if (!case_active(a.bt, c)) return;
   double *U = a.U1_;
   float *M = mirror_current(a.mir);
@@ -300,7 +300,8 @@ cudaError_t launch_interface(const InterfaceArgs &a, int ncubes_total, cudaStrea
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
-  k_iface_edges<<<ncubes_total - 1, kEdgeThreads, 0, s>>>(a);
+  const int ne = a.edge_list ? a.nedge : ncubes_total - 1;
+  if (ne > 0) k_iface_edges<<<ne, kEdgeThreads, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -225,6 +225,9 @@ struct InterfaceArgs {
   double *U1_;
   Batch bt;
   Mirror mir;  // split precision: every written cell's mirror value too
+  bool edge_list = false;           // the edge fill over edge_cubes only (else all)
+  const int *edge_cubes = nullptr;  // [nedge] cube numbers
+  int nedge = 0;
 };
 cudaError_t launch_interface(const InterfaceArgs &a, int ndst, cudaStream_t s);
 

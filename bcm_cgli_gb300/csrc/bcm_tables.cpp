@@ -310,6 +310,60 @@ void prologue_task_mask(int n, int ncube, const std::vector<FaceTask> &tasks,
   }
 }
 
+// The closing interface call of RK stages 1 and 2 on the split path (the
+// level jumps and the edge fill after the update).  The next stage's opening
+// call runs every level jump and the edge fill again, so of the closing
+// call's writes only those read before it matter: the boundary fill's y
+// faces read the x-ghost rows of their cube (all i, j = 2 or n + 1), its z
+// faces the x- and y-ghost rows and the edge cells (all i, j, k = 2 or
+// n + 1), and an IBM stencil may reach into its cube's ghost layers (face
+// ghosts, or edge cells where two coordinates are ghost).  keep[t] for the
+// tasks of the closing list (level jumps) writing such a face; edge[c] for
+// the cubes whose edge fill such a read sees.
+void closing_plan(int n, int ncube, const std::vector<FaceTask> &tasks,
+                  const std::vector<int> &task_cube, const std::vector<int> &bc_cubes,
+                  const std::vector<int> &bc_masks, const int *ip_minus, int nminus,
+                  const int *ip_plus, int nplus, std::vector<char> &keep,
+                  std::vector<char> &edge) {
+  std::vector<uint8_t> face((size_t)std::max(ncube, 0), 0);  // bit 2 axis + side
+  edge.assign((size_t)std::max(ncube, 0), 0);
+  for (size_t q = 0; q < bc_cubes.size(); ++q) {
+    const int c = bc_cubes[q], m = bc_masks[q];
+    if (c <= 0 || c >= ncube) continue;
+    if (m & 12) face[c] |= 3;  // y faces read the x ghost rows
+    if (m & 48) {              // z faces: x and y ghost rows, edge cells
+      face[c] |= 15;
+      edge[c] = 1;
+    }
+  }
+  auto ghost_side = [&](int x) { return x <= 1 ? 0 : (x >= n + 2 ? 1 : -1); };
+  auto mark = [&](const int *I, int cnt) {
+    for (int e = 0; e < cnt; ++e) {
+      const int c = I[1 + 4 * e];
+      if (c <= 0 || c >= ncube) continue;
+      for (int d = 0; d < 8; ++d) {
+        const int x[3] = {I[2 + 4 * e] + (d & 1), I[3 + 4 * e] + (d >> 1 & 1),
+                          I[4 + 4 * e] + (d >> 2 & 1)};
+        int ghosts = 0;
+        for (int ax = 0; ax < 3; ++ax) {
+          const int sd = ghost_side(x[ax]);
+          if (sd < 0) continue;
+          ++ghosts;
+          face[c] |= (uint8_t)(1 << (2 * ax + sd));
+        }
+        if (ghosts >= 2) edge[c] = 1;
+      }
+    }
+  };
+  if (ip_minus && nminus > 0) mark(ip_minus, nminus);
+  if (ip_plus && nplus > 0) mark(ip_plus, nplus);
+  keep.assign(tasks.size(), 0);
+  for (size_t t = 0; t < tasks.size(); ++t) {
+    const FaceTask &f = tasks[t];
+    keep[t] = f.kind != 0 && (face[task_cube[t]] >> (2 * f.axis + f.side) & 1);
+  }
+}
+
 bool build_push_table(int ncube, const std::vector<FaceTask> &tasks,
                       const std::vector<int> &task_cube, std::vector<int> &push) {
   push.assign(6 * (size_t)std::max(ncube, 0), 0);
@@ -386,6 +440,32 @@ extern "C" int bcmg_interface_plan(int n, int ncube, const int *adj_number, cons
   const bool ok = bcmg::build_push_table(ncube, tasks, task_cube, tbl);
   if (push) std::copy(tbl.begin(), tbl.end(), push);
   return ok ? (int)tasks.size() : -3;
+}
+
+extern "C" int bcmg_interface_closing_plan(int n, int ncube, const int *adj_number,
+                                           const int *csl, const int *const bc_lists[6],
+                                           const int bc_counts[6], const int *ip_minus,
+                                           int nminus, const int *ip_plus, int nplus,
+                                           int *keep_closing, int *edge_cubes, int max_tasks) {
+  std::vector<int> off;
+  std::vector<bcmg::FaceTask> tasks;
+  std::string err;
+  if (ncube < 2 || n < 1 || !adj_number || !csl || !bc_lists || !bc_counts) return -1;
+  if (!bcmg::build_interface_tasks(ncube, adj_number, csl, off, tasks, err)) return -1;
+  std::vector<int> bcc, bcm;
+  if (!bcmg::build_bc_entries(ncube, bc_lists, bc_counts, bcc, bcm, err)) return -1;
+  if ((int)tasks.size() > max_tasks) return -2;
+  std::vector<int> task_cube(tasks.size());
+  for (int c = 1; c < ncube; ++c)
+    for (int t = off[c]; t < off[c + 1]; ++t) task_cube[t] = c;
+  std::vector<char> keep, edge;
+  bcmg::closing_plan(n, ncube, tasks, task_cube, bcc, bcm, ip_minus, nminus, ip_plus, nplus, keep,
+                     edge);
+  if (keep_closing)
+    for (size_t t = 0; t < keep.size(); ++t) keep_closing[t] = keep[t];
+  if (edge_cubes)
+    for (int c = 0; c < ncube; ++c) edge_cubes[c] = edge[c];
+  return (int)tasks.size();
 }
 
 // ---------------------------------------------------------------------------

@@ -30,6 +30,15 @@ void prologue_task_mask(int n, int ncube, const std::vector<FaceTask> &tasks,
                         const std::vector<int> &task_cube, const std::vector<int> &bc_cubes,
                         const std::vector<int> &bc_masks, const int *gc_minus, int nminus,
                         const int *gc_plus, int nplus, std::vector<char> &keep);
+// The closing interface call of split RK stages 1 and 2: keep[t] for the
+// level-jump tasks whose ghost face the next stage's boundary fill or an
+// IBM stencil (IP tables 1-based) reads before the next opening call
+// rewrites it; edge[c] for the cubes whose edge cells such a read sees.
+void closing_plan(int n, int ncube, const std::vector<FaceTask> &tasks,
+                  const std::vector<int> &task_cube, const std::vector<int> &bc_cubes,
+                  const std::vector<int> &bc_masks, const int *ip_minus, int nminus,
+                  const int *ip_plus, int nplus, std::vector<char> &keep,
+                  std::vector<char> &edge);
 // Same-level push table of the split flux kernel (FluxSplitArgs::push):
 // push[6 src + 2 axis + 0] = destination of the task copying src's layers
 // 2, 3 (its side 1), push[6 src + 2 axis + 1] = destination of the task

@@ -570,6 +570,19 @@ int bcmg_interface_plan(int n, int ncube, const int *adj_number, const int *csl,
                         const int *gc_minus, int nminus, const int *gc_plus, int nplus,
                         int *keep_prologue, int *push, int max_tasks);
 
+/* The reduced closing interface call of split-precision RK stages 1 and 2
+ * in a resident context, for the tasks of bcmg_interface_tasks (same order):
+ * keep_closing[t] = 1 for the level-jump tasks whose ghost face is read
+ * before the next stage's opening call rewrites it (by the boundary fill's
+ * y and z faces, or by an IBM stencil reaching into its cube's ghost
+ * layers; IP tables 1-based), edge_cubes[c] = 1 (c < ncube) for the cubes
+ * whose edge fill such a read sees.  Returns the task count, -1 for invalid
+ * input, -2 if max_tasks is too small. */
+int bcmg_interface_closing_plan(int n, int ncube, const int *adj_number, const int *csl,
+                                const int *const bc_lists[6], const int bc_counts[6],
+                                const int *ip_minus, int nminus, const int *ip_plus, int nplus,
+                                int *keep_closing, int *edge_cubes, int max_tasks);
+
 #ifdef __cplusplus
 }
 #endif

@@ -13,7 +13,10 @@ boundaries, ghost cells, the full interface, the update and the full
 interface again every stage (main.cpp:1161-1207).  The library's order
 runs the reduced list ahead of every stage but a step's first, and the
 updating kernel copies the same-level faces of the cells it changes, so the
-closing call keeps only the level jumps and the edge fill."""
+closing call keeps only the level jumps and the edge fill; after RK stages
+1 and 2 it keeps only the level jumps and edge fills that the next stage's
+boundary fill or IBM stencils read before its opening call rewrites them
+(bcmg_interface_closing_plan)."""
 import ctypes as C
 
 import numpy as np
@@ -48,7 +51,20 @@ def _plan(case):
     assert r == nt
     tasks = words[:5 * nt].reshape(-1, 5)
     dst = np.repeat(np.arange(case.ncube), np.diff(off))
-    return tasks, dst, keep[:nt].astype(bool), push.reshape(case.ncube, 6)
+    ipt = [None if t is None else np.ascontiguousarray(t[2], np.int32)
+           for t in (case.ibm_minus, case.ibm_plus)]
+    keep_q = np.zeros(max(nt, 1), np.int32)
+    edge = np.zeros(case.ncube, np.int32)
+    r = lib().bcmg_interface_closing_plan(case.n, case.ncube, adj, csl, C.cast(ptrs, C.c_void_p),
+                                          C.cast(counts, C.c_void_p),
+                                          None if ipt[0] is None else ipt[0].ctypes.data,
+                                          0 if ipt[0] is None else (len(ipt[0]) - 1) // 4,
+                                          None if ipt[1] is None else ipt[1].ctypes.data,
+                                          0 if ipt[1] is None else (len(ipt[1]) - 1) // 4,
+                                          keep_q, edge, cap)
+    assert r == nt
+    return (tasks, dst, keep[:nt].astype(bool), push.reshape(case.ncube, 6),
+            keep_q[:nt].astype(bool), edge.astype(bool))
 
 
 class Model:
@@ -57,7 +73,7 @@ class Model:
         rng = np.random.default_rng(seed)
         self.X = rng.standard_normal((case.ncube, case.S, case.S, case.S))
         self.fluid = case.fws == 1
-        self.tasks, self.dst, self.keep, self.push = _plan(case)
+        self.tasks, self.dst, self.keep, self.push, self.keep_q, self.edge_q = _plan(case)
         self.bc = [(c, m) for c, m in self._bc_masks().items()]
         self.ibm = []
         for t in (case.ibm_minus, case.ibm_plus):
@@ -136,10 +152,12 @@ class Model:
                         X[(c,) + tuple(d)] = X[src, b[0]:b[0] + 2, b[1]:b[1] + 2,
                                                b[2]:b[2] + 2].mean()
 
-    def _edges(self):
+    def _edges(self, cubes=None):
         n, X = self.n, self.X
         nx, nyy = n + 1, n + 2
         for c in range(1, self.case.ncube):
+            if cubes is not None and not cubes[c]:
+                continue
             Q = X[c]
             for i in range(2, nx + 1):
                 Q[i, 1, 1] = 0.5 * (Q[i, 1, 2] + Q[i, 2, 1])
@@ -157,10 +175,10 @@ class Model:
                 Q[nyy, 1, k] = 0.5 * (Q[nx, 1, k] + Q[nyy, 2, k])
                 Q[nyy, nyy, k] = 0.5 * (Q[nx, nyy, k] + Q[nyy, nx, k])
 
-    def interface(self, which):
+    def interface(self, which, edge_cubes=None):
         for t in np.nonzero(which)[0]:
             self._copy(t)
-        self._edges()
+        self._edges(edge_cubes)
 
     def update(self, stage, push):
         n, X = self.n, self.X
@@ -181,9 +199,10 @@ class Model:
                     X[(d,) + dst] = np.where(self.fluid[(c,) + src], X[(c,) + src], X[(d,) + dst])
 
 
-def _run(case, library_order, steps=2, subiters=2, push=None):
+def _run(case, library_order, steps=2, subiters=2, push=None, reduced_closing=None):
     m = Model(case, seed=5)
     push = library_order if push is None else push
+    reduced_closing = library_order if reduced_closing is None else reduced_closing
     every = np.ones(len(m.tasks), bool)
     level = m.tasks[:, 3] != 0
     stage = 0
@@ -195,7 +214,12 @@ def _run(case, library_order, steps=2, subiters=2, push=None):
                 m.ghosts()
                 m.interface(every if (first or not library_order) else m.keep)
                 m.update(stage, push=push)
-                m.interface(level if library_order else every)
+                if not library_order:
+                    m.interface(every)
+                elif reduced_closing and rk < 2:  # RK 1, 2: what is read before the next
+                    m.interface(m.keep_q, m.edge_q)  # opening call rewrites it
+                else:
+                    m.interface(level)
                 stage += 1
     return m.X
 
@@ -240,3 +264,45 @@ def test_model_detects_a_missing_copy():
     assert not np.array_equal(ref[1:], bad[1:])
     # and the closing call without the in-kernel copies loses them
     assert not np.array_equal(ref[1:], _run(case, library_order=True, push=False)[1:])
+
+
+@pytest.mark.parametrize("make,drop", [
+    (lambda: cases.random_case(seed=11, n=4, periodic=False), "edges"),
+    (lambda: cases.random_two_level_case(seed=6, n=8, periodic=False), "tasks")],
+    ids=["random_open_ibm_edges", "two_level_open_tasks"])
+def test_reduced_closing_call_is_needed_where_kept(make, drop):
+    """The reduced closing call of RK stages 1 and 2 keeps exactly what is
+    read before the next opening call: dropping the kept edge fills (boundary
+    z faces, IBM stencils on edges) or the kept level jumps (boundary y and z
+    faces read the ghost rows) changes the result."""
+    case = make()
+    ref = _run(case, library_order=False)
+    assert np.array_equal(ref[1:], _run(case, library_order=True)[1:])
+    orig = Model.__init__
+
+    def patched(self, case, seed):
+        orig(self, case, seed)
+        if drop == "edges":
+            assert self.edge_q.any()
+            self.edge_q = np.zeros_like(self.edge_q)
+        else:
+            assert self.keep_q.any()
+            self.keep_q = np.zeros_like(self.keep_q)
+    Model.__init__ = patched
+    try:
+        bad = _run(case, library_order=True)
+    finally:
+        Model.__init__ = orig
+    assert not np.array_equal(ref[1:], bad[1:])
+
+
+def test_reduced_closing_call_drops_most_of_the_work():
+    """On the two-level sphere (boundary cubes away from the level jumps and
+    the body) the reduced closing call keeps few tasks and edge fills."""
+    case = cases.sphere_ibm(n=8, coarse=2.0, box=((-4, 6), (-4, 4), (-4, 4)),
+                            refine_box=((-2, 2), (-2, 2), (-2, 2)))
+    tasks, _, _, _, keep_q, edge_q = _plan(case)
+    level = tasks[:, 3] != 0
+    assert level.sum() > 0
+    assert keep_q.sum() < level.sum() // 2
+    assert edge_q.sum() < (case.ncube - 1) // 2
