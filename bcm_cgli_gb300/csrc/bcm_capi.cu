@@ -1249,11 +1249,13 @@ int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out,
       std::copy(d->gc_plus + 1, d->gc_plus + 1 + 4 * (size_t)np, gc.begin() + 1 + 4 * (size_t)nm);
       std::copy(d->ip_plus + 1, d->ip_plus + 1 + 4 * (size_t)np, ip.begin() + 1 + 4 * (size_t)nm);
     }
-    // Cases whose cubes with boundary faces hold no IBM entry's cells (ghost
-    // or stencil): their entries form the side table, filled beside the
-    // boundary fill; the other cases' entries stay in the reference's order
-    // after it.  Cases never share cubes, so splitting the table by case
-    // keeps every dependency inside one table.
+    // Cases in which no IBM entry's cell (ghost cell or stencil) lies where
+    // the boundary fill reads or writes: the three layers at each boundary
+    // face of its cube (ghost layers written, the next interior layer read,
+    // and the y and z faces over whole planes).  Their entries form the side
+    // table, filled beside the boundary fill; the other cases' entries stay
+    // in the reference's order after it.  Cases never share cubes, so
+    // splitting the table by case keeps every dependency inside one table.
     const int ne = nm + np;
     auto case_of = [&](int cube) -> int {
       if (!bi) return 0;
@@ -1261,20 +1263,27 @@ int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out,
       return (int)(std::upper_bound(b0.begin(), b0.end(), cube) - b0.begin()) - 1;
     };
     const int ncs = bi ? (int)bi->cases.size() : 1;
-    std::vector<char> ibm_cube((size_t)d->ncube, 0), shared((size_t)ncs, 0);
-    for (int e = 0; e < ne; ++e) {
-      const int g = gc[4 * (size_t)e + 1], q = ip[4 * (size_t)e + 1];
-      if (g > 0 && g < d->ncube) ibm_cube[g] = 1;
-      if (q > 0 && q < d->ncube) ibm_cube[q] = 1;
-    }
-    for (int cb : bcc)
-      if (cb > 0 && cb < d->ncube && ibm_cube[cb]) {
-        const int q = case_of(cb);
-        if (q >= 0 && q < ncs) shared[q] = 1;
+    std::vector<int> bcmask((size_t)d->ncube, 0);
+    for (size_t q = 0; q < bcc.size(); ++q)
+      if (bcc[q] > 0 && bcc[q] < d->ncube) bcmask[bcc[q]] |= bcm[q];
+    auto in_slab = [&](int cube, int i, int j, int k) {
+      if (cube <= 0 || cube >= d->ncube) return true;
+      const int m = bcmask[cube], x[3] = {i, j, k};
+      for (int ax = 0; ax < 3; ++ax) {
+        if ((m >> (2 * ax) & 1) && x[ax] <= 2) return true;
+        if ((m >> (2 * ax + 1) & 1) && x[ax] >= d->n + 1) return true;
       }
-    for (int e = 0; e < ne; ++e) {  // an entry reaching into another case
-      const int q = case_of(gc[4 * (size_t)e + 1]);
-      if (q >= 0 && q < ncs && case_of(ip[4 * (size_t)e + 1]) != q) shared[q] = 1;
+      return false;
+    };
+    std::vector<char> shared((size_t)ncs, 0);
+    for (int e = 0; e < ne; ++e) {
+      const int *G = &gc[4 * (size_t)e + 1], *P = &ip[4 * (size_t)e + 1];
+      const int q = case_of(G[0]);
+      if (q < 0 || q >= ncs) continue;
+      bool hit = case_of(P[0]) != q || in_slab(G[0], G[1], G[2], G[3]);
+      for (int dd = 0; dd < 8 && !hit; ++dd)
+        hit = in_slab(P[0], P[1] + (dd & 1), P[2] + (dd >> 1 & 1), P[3] + (dd >> 2 & 1));
+      if (hit) shared[q] = 1;
     }
     std::vector<char> to_side((size_t)ne, 0);
     int nside = 0;

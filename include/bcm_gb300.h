@@ -340,12 +340,13 @@ int bcmg_case_set_mirror_each_stage(bcmg_case *c, int on);
 
 /* The IBM ghost-cell fill of each stage on a second stream, beside the
  * boundary fill, with the interface call after them waiting for both.  In
- * effect (the default) for every case (of a batch) whose cubes with
- * boundary faces hold no IBM entry's cells (ghost cell or stencil), so the
- * two fills touch disjoint cells; the other cases' entries, and all of them
- * with on = 0, are filled after the boundary fill in the reference's order.
- * Both give the same bits.  bcmg_case_concurrent_ghosts returns 1 where
- * some entries are filled beside the boundary fill. */
+ * effect (the default) for every case (of a batch) in which no IBM entry's
+ * cell (ghost cell or stencil) lies in the three layers the boundary fill
+ * touches at a boundary face of its cube, so the two fills touch disjoint
+ * cells; the other cases' entries, and all of them with on = 0, are filled
+ * after the boundary fill in the reference's order.  Both give the same
+ * bits.  bcmg_case_concurrent_ghosts returns 1 where some entries are
+ * filled beside the boundary fill. */
 int bcmg_case_set_concurrent_ghosts(bcmg_case *c, int on);
 int bcmg_case_concurrent_ghosts(bcmg_case *c);
 

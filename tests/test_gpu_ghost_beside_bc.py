@@ -1,8 +1,9 @@
 """The IBM ghost fill beside the boundary fill (bcmg_case_set_concurrent_ghosts).
 
-Where no cube holds both an IBM entry's cells and a boundary face, a stage
-runs the ghost-fill levels on a second stream while the boundary fill runs,
-and the interface call waits for both.  The states must be the same bits as
+For every case in which no IBM entry's cell (ghost cell or stencil) lies in
+the three layers the boundary fill touches at a boundary face, a stage runs
+that case's ghost-fill levels on a second stream while the boundary fill
+runs, and the interface call waits for both.  The states must be the same bits as
 with the fills one after the other, for FP64 and split precision, RK and
 LU-SGS, eager launches, captured step graphs and convergence-driven graphs,
 single cases and batches.
@@ -52,8 +53,8 @@ def _batch(precision):
 
 
 def _mixed(precision):
-    """A sphere (beside) and a random case whose IBM stencils sit in cubes
-    with boundary faces (in order), in one batch."""
+    """A sphere (beside) and a random case whose IBM cells sit next to
+    boundary faces (in order), in one batch."""
     cs = [_sphere(), cases.random_case(seed=11, n=8, periodic=False, viscous=True)]
     bt = api.BatchContext(cs, precision=precision)
     for q, c in enumerate(cs):
@@ -71,9 +72,9 @@ def test_ghost_fill_beside_boundary_fill_changes_no_bit(make, method, precision)
         assert np.array_equal(x.view(np.uint64), y.view(np.uint64))
 
 
-def test_not_beside_where_cubes_are_shared():
-    """The random test tables put IBM stencils in cubes with boundary faces:
-    the fills stay in the reference's order there."""
+def test_not_beside_where_cells_are_shared():
+    """The random test tables put IBM cells next to boundary faces: the fills
+    stay in the reference's order there."""
     case = G.golden_cases()["random_open_n4"]
     ctx = api.CaseContext(case)
     assert not ctx.concurrent_ghosts()
