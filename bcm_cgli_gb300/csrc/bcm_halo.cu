@@ -306,21 +306,30 @@ cudaError_t launch_interface(const InterfaceArgs &a, int ncubes_total, cudaStrea
 }
 
 // ---------------------------------------------------------------------------
-// Boundary conditions (BCM_X/Y/Z_boundary_condition.cpp), phases x -> y -> z
-// with barriers: y reads x ghosts and z reads y ghosts of the same cube
-// (main.cpp:1161-1165 order).  A cube's work is split into slabs of whole
-// i-planes (blockIdx.y), each of at least three planes: an x face and the
-// interior plane it reads lie in one slab, and a y or z item of plane i
-// reads only cells of plane i, so every dependency stays inside one CTA.
+// Boundary conditions (BCM_X/Y/Z_boundary_condition.cpp) in one pass.  The
+// reference fills the x faces (j, k interior: inflow from cell 2, zero
+// gradient from cell nx), then the y faces over every i (zero gradient from
+// row 2 / nx, interior k), then the z faces over every i, j (slip with w
+// negated from plane 2, zero gradient from plane nx), in that order
+// (main.cpp:1161-1165), so a y face's x-ghost rows copy values the x phase
+// wrote and a z face copies both.  Each value a phase reads is, through at
+// most two earlier phases, a copy or the inflow formula of a cell no phase
+// writes: read() follows that chain.  So every ghost position is formed
+// directly, with the reference's operations, in one pass with no barrier:
+// the same bits (checked on the CPU against the ordered phases for every
+// mask and axis subset, and by the GPU parity tests).  `axes` limits the
+// pass to the faces of one twin call (the others' ghosts are then read as
+// they are).
 // ---------------------------------------------------------------------------
-constexpr int kBcThreads = 512, kBcBatch = 4;
+constexpr int kBcThreads = 256, kBcChunks = 8, kBcBatch = 4;
 
 __global__ void __launch_bounds__(kBcThreads) k_bc(BcArgs a) {
   const int n = a.n, S = n + 4, nx = n + 1, nxx = n + 2, nxxx = n + 3;
   const int c = a.cubes[blockIdx.x];
   if (!case_active(a.bt, c)) return;
   const int m = a.masks[blockIdx.x];
-  const int T = (S + gridDim.y - 1) / gridDim.y, i0 = blockIdx.y * T, i1 = min(S, i0 + T);
+  const int mx = (a.axes & 1) ? (m & 3) : 0, my = (a.axes & 2) ? ((m >> 2) & 3) : 0,
+            mz = (a.axes & 4) ? ((m >> 4) & 3) : 0;
   double *U = a.U1_;
   // Split precision: the mirror values of every write, into both mirror
   // buffers.  The flux kernel writes the next buffer's interior cells and
@@ -332,115 +341,113 @@ __global__ void __launch_bounds__(kBcThreads) k_bc(BcArgs a) {
   float *Mo = M ? (M == a.mir.buf[0] ? a.mir.buf[1] : a.mir.buf[0]) : nullptr;
   double r0 = 0, e0 = 0;
   if (M) mirror_base(a.mir, a.bt, c, r0, e0);
-  auto put = [&](size_t at, float m) {
-    M[at] = m;
-    Mo[at] = m;
-  };
+  const double Uin = a.bt.cube_case ? a.bt.cases[a.bt.cube_case[c]].Uin : a.Uin;
   auto Q = [&](int i, int j, int k) { return U + 5 * cell_index(S, c, i, j, k); };
-  auto at = [&](int i, int j, int k) { return (size_t)5 * cell_index(S, c, i, j, k); };
-  // Zero-gradient and slip faces: both ghost layers take one interior value.
-  // No item of a phase reads a cell another item of that phase writes, so a
-  // thread issues the loads of kBcBatch items before their stores and the
-  // phase is a few memory round trips rather than one per item.
-  // index(w, src, dst1, dst0, negate) describes item w.
-  auto pairs = [&](int total, auto index) {
-    for (int w0 = threadIdx.x; w0 < total; w0 += kBcBatch * kBcThreads) {
-      double x[kBcBatch];
-      size_t d1[kBcBatch], d0[kBcBatch];
-#pragma unroll
-      for (int b = 0; b < kBcBatch; ++b) {
-        const int w = w0 + b * kBcThreads;
-        if (w < total) {
-          size_t src;
-          bool neg;
-          index(w, src, d1[b], d0[b], neg);
-          x[b] = U[src];
-          if (neg) x[b] = -x[b];
-        }
-      }
-#pragma unroll
-      for (int b = 0; b < kBcBatch; ++b)
-        if (w0 + b * kBcThreads < total) {
-          U[d1[b]] = x[b];
-          U[d0[b]] = x[b];
-          if (M) {
-            const float m = mirror_value_hw(x[b], (int)(d1[b] % 5), r0, e0);
-            put(d1[b], m);
-            put(d0[b], m);
-          }
-        }
-    }
+  auto interior = [&](int x) { return x >= 2 && x <= nx; };
+  // component v of the inflow state (:43-80): rho and p from the cell,
+  // u = Uin, v = w = 0
+  auto inflow = [&](const double *q, int v) -> double {
+    const double rho = q[0];
+    if (v == 0) return rho;
+    const double Uu = Uin, Vv = 0., Ww = 0;
+    if (v == 1) return rho * Uu;
+    if (v == 2) return rho * Vv;
+    if (v == 3) return rho * Ww;
+    const double U0 = q[1] / rho, V0 = q[2] / rho, W0 = q[3] / rho;
+    double VV = U0 * U0 + V0 * V0 + W0 * W0;
+    const double P = (q[4] - 0.5 * rho * VV) * (BCMG_K - 1);
+    VV = Uu * Uu + Vv * Vv + Ww * Ww;
+    return P / (BCMG_K - 1) + 0.5 * rho * VV;
   };
-  if (a.axes & 1) {
-    if ((m & 1) && i0 == 0) {  // x lower: inflow, rho and p from cell 2, u = Uin (:43-80)
-      for (int w = threadIdx.x; w < n * n; w += kBcThreads) {
-        const int j = 2 + w / n, k = 2 + w % n;
-        const double *q = Q(2, j, k);
-        double rho = q[0];
-        double U0 = q[1] / rho, V0 = q[2] / rho, W0 = q[3] / rho;
-        double VV = U0 * U0 + V0 * V0 + W0 * W0;
-        double P = (q[4] - 0.5 * rho * VV) * (BCMG_K - 1);
-        double Uu = a.bt.cube_case ? a.bt.cases[a.bt.cube_case[c]].Uin : a.Uin, Vv = 0., Ww = 0;
-        VV = Uu * Uu + Vv * Vv + Ww * Ww;
-        double o[5] = {rho, rho * Uu, rho * Vv, rho * Ww, P / (BCMG_K - 1) + 0.5 * rho * VV};
-        double *d1 = Q(1, j, k), *d0 = Q(0, j, k);
+  // component v of cell (i, j, k) as the reference's order leaves it after
+  // the x phase (upto 1) or after the x and y phases (upto 2)
+  auto read = [&](int i, int j, int k, int upto, int v) -> double {
+    if (upto >= 2 && my && interior(k)) {
+      if ((my & 1) && j <= 1) j = 2;
+      else if ((my & 2) && j >= nxx) j = nx;
+    }
+    if (mx && interior(j) && interior(k)) {
+      if ((mx & 1) && i <= 1) return inflow(Q(2, j, k), v);
+      if ((mx & 2) && i >= nxx) i = nx;
+    }
+    return Q(i, j, k)[v];
+  };
+  // ghost positions: x faces n^2 each, y faces S n each, z faces S^2 each;
+  // each position fills both ghost layers with one value.  Items are
+  // (position, component), component fastest, so a warp's loads and stores
+  // run over whole cells in a row.
+  const int cx = n * n, cy = S * n, cz = S * S;
+  const int nxl = (mx & 1) ? cx : 0, nxu = (mx & 2) ? cx : 0, nyl = (my & 1) ? cy : 0,
+            nyu = (my & 2) ? cy : 0, nzl = (mz & 1) ? cz : 0, nzu = (mz & 2) ? cz : 0;
+  const int items = 5 * (nxl + nxu + nyl + nyu + nzl + nzu);
+  // item w: its value and the offsets of its two destinations
+  auto item = [&](int w, double &x, size_t &d1, size_t &d0) {
+    const int v = w % 5;
+    int q = w / 5;
+    if (q < nxl) {
+      const int j = 2 + q / n, k = 2 + q % n;
+      x = inflow(Q(2, j, k), v);
+      d1 = 5 * cell_index(S, c, 1, j, k) + v; d0 = 5 * cell_index(S, c, 0, j, k) + v;
+      return;
+    }
+    q -= nxl;
+    if (q < nxu) {
+      const int j = 2 + q / n, k = 2 + q % n;
+      x = Q(nx, j, k)[v];
+      d1 = 5 * cell_index(S, c, nxx, j, k) + v; d0 = 5 * cell_index(S, c, nxxx, j, k) + v;
+      return;
+    }
+    q -= nxu;
+    if (q < nyl) {
+      const int i = q / n, k = 2 + q % n;
+      x = read(i, 2, k, 1, v);
+      d1 = 5 * cell_index(S, c, i, 1, k) + v; d0 = 5 * cell_index(S, c, i, 0, k) + v;
+      return;
+    }
+    q -= nyl;
+    if (q < nyu) {
+      const int i = q / n, k = 2 + q % n;
+      x = read(i, nx, k, 1, v);
+      d1 = 5 * cell_index(S, c, i, nxx, k) + v; d0 = 5 * cell_index(S, c, i, nxxx, k) + v;
+      return;
+    }
+    q -= nyu;
+    if (q < nzl) {  // slip wall: rho*w negated (:42-65)
+      const int i = q / S, j = q % S;
+      x = read(i, j, 2, 2, v);
+      if (v == 3) x = -x;
+      d1 = 5 * cell_index(S, c, i, j, 1) + v; d0 = 5 * cell_index(S, c, i, j, 0) + v;
+      return;
+    }
+    q -= nzl;
+    const int i = q / S, j = q % S;
+    x = read(i, j, nx, 2, v);
+    d1 = 5 * cell_index(S, c, i, j, nxx) + v; d0 = 5 * cell_index(S, c, i, j, nxxx) + v;
+  };
+  // kBcBatch items per round, all loaded before any is stored
+  const int stride = gridDim.y * kBcThreads;
+  for (int w0 = blockIdx.y * kBcThreads + threadIdx.x; w0 < items; w0 += kBcBatch * stride) {
+    double x[kBcBatch];
+    size_t d1[kBcBatch], d0[kBcBatch];
 #pragma unroll
-        for (int v = 0; v < 5; ++v) { d1[v] = o[v]; d0[v] = o[v]; }
+    for (int b = 0; b < kBcBatch; ++b)
+      if (w0 + b * stride < items) item(w0 + b * stride, x[b], d1[b], d0[b]);
+#pragma unroll
+    for (int b = 0; b < kBcBatch; ++b)
+      if (w0 + b * stride < items) {
+        U[d1[b]] = x[b];
+        U[d0[b]] = x[b];
         if (M) {
-#pragma unroll
-          for (int v = 0; v < 5; ++v) {
-            const float m = mirror_value_hw(o[v], v, r0, e0);
-            put((d1 - U) + v, m);
-            put((d0 - U) + v, m);
-          }
+          const float mv = mirror_value_hw(x[b], (int)(d1[b] % 5), r0, e0);
+          M[d1[b]] = mv; M[d0[b]] = mv; Mo[d1[b]] = mv; Mo[d0[b]] = mv;
         }
       }
-    }
-    if ((m & 2) && i1 == S)  // x upper: zero gradient (:85-118)
-      pairs(n * n * 5, [&](int w, size_t &src, size_t &d1, size_t &d0, bool &neg) {
-        const int v = w % 5, j = 2 + (w / 5) / n, k = 2 + (w / 5) % n;
-        src = at(nx, j, k) + v;
-        d1 = at(nxx, j, k) + v;
-        d0 = at(nxxx, j, k) + v;
-        neg = false;
-      });
-    __syncthreads();
-  }
-  if ((a.axes & 2) && (m & 12)) {
-    // y lower (:36-59) and upper (:62-85) over the slab's planes (x ghosts too)
-    const int per = (i1 - i0) * n * 5;
-    const int lo = (m & 4) ? 1 : 0, cnt = lo + ((m & 8) ? 1 : 0);
-    pairs(cnt * per, [&](int w, size_t &src, size_t &d1, size_t &d0, bool &neg) {
-      const bool lower = lo && w < per;
-      if (w >= per) w -= per;
-      const int v = w % 5, i = i0 + (w / 5) / n, k = 2 + (w / 5) % n;
-      src = at(i, lower ? 2 : nx, k) + v;
-      d1 = at(i, lower ? 1 : nxx, k) + v;
-      d0 = at(i, lower ? 0 : nxxx, k) + v;
-      neg = false;
-    });
-  }
-  if (a.axes & 2) __syncthreads();
-  if ((a.axes & 4) && (m & 48)) {
-    // z lower: slip wall, rho*w negated (:42-65); z upper (:70-92)
-    const int per = (i1 - i0) * (n + 4) * 5;
-    const int lo = (m & 16) ? 1 : 0, cnt = lo + ((m & 32) ? 1 : 0);
-    pairs(cnt * per, [&](int w, size_t &src, size_t &d1, size_t &d0, bool &neg) {
-      const bool lower = lo && w < per;
-      if (w >= per) w -= per;
-      const int v = w % 5, i = i0 + (w / 5) / (n + 4), j = (w / 5) % (n + 4);
-      src = at(i, j, lower ? 2 : nx) + v;
-      d1 = at(i, j, lower ? 1 : nxx) + v;
-      d0 = at(i, j, lower ? 0 : nxxx) + v;
-      neg = lower && v == 3;
-    });
   }
 }
 
 cudaError_t launch_bc(const BcArgs &a, int ncubes, cudaStream_t s) {
   if (ncubes <= 0) return cudaSuccess;
-  const int S = a.n + 4, slabs = std::max(1, std::min(4, S / 3));  // >= 3 planes each
-  k_bc<<<dim3(ncubes, slabs), kBcThreads, 0, s>>>(a);
+  k_bc<<<dim3(ncubes, kBcChunks), kBcThreads, 0, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -496,65 +503,81 @@ __global__ void __launch_bounds__(kGhostThreads) k_ghost(GhostArgs a, int count)
     o[0] = rh; o[1] = Pp; o[2] = Uu; o[3] = Vv; o[4] = Ww;
   }
   __syncwarp();
-  if (!act || m != 0) return;
+  if (!act) return;
   const double(*X)[7] = sh[g];
-  const double *w = a.weight + (size_t)(e - 1) * 8 + 1;
-  double wl[8];
-#pragma unroll
-  for (int l = 0; l < 8; ++l) wl[l] = w[l];
   const int gc = a.GCindex[b + 1], gi = a.GCindex[b + 2], gj = a.GCindex[b + 3],
             gk = a.GCindex[b + 4];
-  double rho = wl[0] * (X[0][0] - rho0);
-  double P = wl[0] * (X[0][1] - P0);
-  double U = wl[0] * X[0][2], V = wl[0] * X[0][3], W = wl[0] * X[0][4];
-#pragma unroll
-  for (int l = 1; l < 8; ++l) {
-    rho = rho + wl[l] * (X[l][0] - rho0);
-    P = P + wl[l] * (X[l][1] - P0);
-    U = U + wl[l] * X[l][2];
-    V = V + wl[l] * X[l][3];
-    W = W + wl[l] * X[l][4];
-  }
-  rho = rho + rho0;
-  P = P + P0;
-  double VV = U * U + V * V + W * W;
-  double o[5] = {rho, 0.5 * rho * U, 0.5 * rho * V, 0.5 * rho * W,
-                 P / (BCMG_K - 1) + 0.5 * rho * 0.25 * VV};
   // Ghost inside its own stencil (:192-449); like the reference, only the
   // local indices are compared, not the cube.
   const int s = (gi - i) + 2 * (gj - j) + 4 * (gk - k);
   const bool self = (gi - i == 0 || gi - i == 1) && (gj - j == 0 || gj - j == 1) &&
                     (gk - k == 0 || gk - k == 1);
-  if (self) {
-    // bit pattern (di,dj,dk) -> stencil slot in the 000,100,010,001,...
-    // order (patterns 3 and 4 swap)
-    const int sl = s == 3 ? 4 : (s == 4 ? 3 : s);
-    const double wsl = wl[sl], rsl = X[sl][0], psl = X[sl][1];
-    double r2, p2;
-    if (wsl > 0.9999) {
-      r2 = rsl;
-      p2 = psl;
-    } else {
-      double ar = 0, ap = 0;
-      bool first = true;
-      for (int l = 0; l < 8; ++l) {
-        if (l == sl) continue;
-        double tr = wl[l] * (X[l][0] - rho0), tp = wl[l] * (X[l][1] - P0);
-        if (first) { ar = tr; ap = tp; first = false; }
-        else { ar = ar + tr; ap = ap + tp; }
+  // bit pattern (di,dj,dk) -> stencil slot in the 000,100,010,001,...
+  // order (patterns 3 and 4 swap)
+  const int sl = s == 3 ? 4 : (s == 4 ? 3 : s);
+  // Lanes 0..4 form the weighted sums of one quantity each (density, p, u,
+  // v, w), every sum in the reference's term order, into sh[g][q][5] (all
+  // eight terms) and sh[g][q][6] (the seven terms without the ghost's own
+  // slot, for a ghost inside its stencil).  On this part's narrow FP64 pipe
+  // the five chains side by side take a fifth of the issue slots of one lane
+  // forming all five.
+  if (m < 5) {
+    const double *w = a.weight + (size_t)(e - 1) * 8 + 1;
+    double wl[8];
+#pragma unroll
+    for (int l = 0; l < 8; ++l) wl[l] = w[l];
+    const double base = m == 0 ? rho0 : (m == 1 ? P0 : 0.0);
+    auto term = [&](int l) { return m < 2 ? wl[l] * (X[l][m] - base) : wl[l] * X[l][m]; };
+    double acc = term(0);
+#pragma unroll
+    for (int l = 1; l < 8; ++l) acc = acc + term(l);
+    if (m < 2) acc = acc + base;
+    sh[g][m][5] = acc;
+    if (self) {
+      const double wsl = wl[sl];
+      double r;
+      if (m < 2) {
+        if (wsl > 0.9999) {
+          r = X[sl][m];
+        } else {
+          double ar = 0;
+          bool first = true;
+          for (int l = 0; l < 8; ++l) {
+            if (l == sl) continue;
+            const double t = term(l);
+            if (first) { ar = t; first = false; }
+            else { ar = ar + t; }
+          }
+          r = ar / (1 - wsl) + base;
+        }
+      } else {
+        double su = 0;
+        bool first = true;
+        for (int l = 0; l < 8; ++l) {
+          if (l == sl) continue;
+          const double t = term(l);
+          if (first) { su = t; first = false; }
+          else { su = su + t; }
+        }
+        r = su / (2 - wsl);
       }
-      r2 = ar / (1 - wsl) + rho0;
-      p2 = ap / (1 - wsl) + P0;
+      sh[g][m][6] = r;
     }
-    double su = 0, sv = 0, sw = 0;
-    bool first = true;
-    for (int l = 0; l < 8; ++l) {
-      if (l == sl) continue;
-      if (first) { su = wl[l] * X[l][2]; sv = wl[l] * X[l][3]; sw = wl[l] * X[l][4]; first = false; }
-      else { su = su + wl[l] * X[l][2]; sv = sv + wl[l] * X[l][3]; sw = sw + wl[l] * X[l][4]; }
-    }
-    double U2 = su / (2 - wsl), V2 = sv / (2 - wsl), W2 = sw / (2 - wsl);
-    double VV2 = U2 * U2 + V2 * V2 + W2 * W2;
+  }
+  __syncwarp();
+  if (m != 0) return;
+  double o[5];
+  if (!self) {
+    const double rho = X[0][5], P = X[1][5], U = X[2][5], V = X[3][5], W = X[4][5];
+    const double VV = U * U + V * V + W * W;
+    o[0] = rho;
+    o[1] = 0.5 * rho * U;
+    o[2] = 0.5 * rho * V;
+    o[3] = 0.5 * rho * W;
+    o[4] = P / (BCMG_K - 1) + 0.5 * rho * 0.25 * VV;
+  } else {
+    const double r2 = X[0][6], p2 = X[1][6], U2 = X[2][6], V2 = X[3][6], W2 = X[4][6];
+    const double VV2 = U2 * U2 + V2 * V2 + W2 * W2;
     o[0] = r2;
     o[1] = r2 * U2;
     o[2] = r2 * V2;
