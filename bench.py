@@ -37,6 +37,11 @@ sys.path.insert(0, ROOT)
 METRIC = ("cell-subiters/s FP64 vs split-FP32 at ≤1e-5 L2 err; HBM GB/s vs peak")
 UNIT = "cell-subiters/s"
 SUBITERS = 10
+# Contexts the batch is split into for the overlapped end-to-end figure
+# (measured on GB300: two 1.50-1.71e9 cell-subiters/s from run to run,
+# three 1.73e9, four and six 1.73e9; fewer contexts leave a larger share of
+# the first copies and the last read-back exposed).
+E2E_GROUPS = 4
 # Dual-time steps from the initial state after which the split path is
 # compared with the FP64 path (the FP64 leg times these same steps).
 ACC_STEPS = 3
@@ -516,18 +521,25 @@ def measure_twins(api, case, precision_name, subiters=2):
                     "scratch arrays kept), wall clock"}
 
 
-def measure_e2e_pipelined(api, case, precision_name, args, dist):
-    """End to end with the host link overlapped: the batch's cases in two
-    contexts of about equal cells, each on its own stream; per step and half,
-    the host -> device copies of its three time levels (U1_, U1, U1q, from
-    page-locked memory), one dual-time step (a graph launch) and the device
-    -> host copy of its new U1_ are enqueued asynchronously, so one half's
-    copies run while the other half steps.  Same bytes per step as
-    measure_e2e; device-timed (events on both streams, the longer span)."""
+def measure_e2e_pipelined(api, case, precision_name, args, dist, ngroups=None):
+    """End to end with the host link overlapped: the batch's cases in
+    ngroups contexts of about equal cells (consecutive cases), each on its
+    own stream; per step and group, the host -> device copies of its three
+    time levels (U1_, U1, U1q, from page-locked memory), one dual-time step
+    (a graph launch) and the device -> host copy of its new U1_ are enqueued
+    asynchronously, so one group's copies run while the others step.  Same
+    bytes per step as measure_e2e; device-timed (events on every stream, the
+    longest span)."""
+    ngroups = ngroups or E2E_GROUPS
     cs = case.cases
     cells = np.cumsum([c.n_cells for c in cs])
-    k = int(np.argmin(np.abs(cells - cells[-1] / 2))) + 1
-    groups = [cs[:k], cs[k:]]
+    cuts = [0]
+    for g in range(1, ngroups):
+        k = int(np.argmin(np.abs(cells - cells[-1] * g / ngroups))) + 1
+        if k > cuts[-1] and k < len(cs):
+            cuts.append(k)
+    cuts.append(len(cs))
+    groups = [cs[a:b] for a, b in zip(cuts[:-1], cuts[1:])]
     precision = api.PRECISION_SPLIT if precision_name == "split" else api.PRECISION_FP64
     from bcm_cgli_gb300 import autotune
     shape = autotune.lookup(case.n, precision_name, "rk3")
@@ -562,7 +574,7 @@ def measure_e2e_pipelined(api, case, precision_name, args, dist):
     ms = dist.max(max(ctx.timer_elapsed(6, 7) for ctx, _, _ in halves))
     for ctx, _, _ in halves:
         ctx.close()
-    return case.n_cells * SUBITERS * args.steps * dist.world / (ms * 1e-3), len(groups[0])
+    return case.n_cells * SUBITERS * args.steps * dist.world / (ms * 1e-3), cuts
 
 
 def cases_flat(group):
@@ -686,11 +698,12 @@ def run_gpu_arm(args, dist):
         e2e_serial = measure_e2e(ctx, case, args, dist, cell_subiters)
         e2e, e2e_how = e2e_serial, "one context: copy in, step, copy out, in series"
         if is_batch(case) and len(case.cases) >= 2:
-            piped, k = measure_e2e_pipelined(api, case, head, args, dist)
+            piped, cuts = measure_e2e_pipelined(api, case, head, args, dist)
             if piped > e2e:
                 e2e = piped
-                e2e_how = (f"two contexts (cases 0..{k - 1} and {k}..{len(case.cases) - 1}) on "
-                           "their own streams: one half's copies overlap the other's step")
+                parts = ", ".join(f"{a}..{b - 1}" for a, b in zip(cuts[:-1], cuts[1:]))
+                e2e_how = (f"{len(cuts) - 1} contexts (cases {parts}) on their own streams: "
+                           "each one's copies overlap the others' steps")
     peaks = {}
 
     try:
