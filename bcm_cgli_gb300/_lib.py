@@ -143,6 +143,8 @@ def _declare(L):
                                       ip, ip, C.c_int]
     L.bcmg_interface_closing_plan.argtypes = [C.c_int, C.c_int, ip, ip, P, P, P, C.c_int, P,
                                               C.c_int, ip, ip, C.c_int]
+    L.bcmg_ghost_beside_plan.argtypes = [C.c_int, C.c_int, P, P, P, P, C.c_int, P, P, C.c_int,
+                                         ip, C.c_int, ip]
     L.bcmg_ibm_preprocess.argtypes = [
         C.c_int, C.c_int, dp, ip, dp, dp, dp, ip, C.c_int, dp, C.c_int, C.POINTER(C.c_int), ip,
         ip, dp, C.POINTER(C.c_int), ip, ip, dp]

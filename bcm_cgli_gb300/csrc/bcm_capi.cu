@@ -1263,28 +1263,9 @@ int create_common(const bcmg_case_desc *d, const BatchInit *bi, bcmg_case **out,
       return (int)(std::upper_bound(b0.begin(), b0.end(), cube) - b0.begin()) - 1;
     };
     const int ncs = bi ? (int)bi->cases.size() : 1;
-    std::vector<int> bcmask((size_t)d->ncube, 0);
-    for (size_t q = 0; q < bcc.size(); ++q)
-      if (bcc[q] > 0 && bcc[q] < d->ncube) bcmask[bcc[q]] |= bcm[q];
-    auto in_slab = [&](int cube, int i, int j, int k) {
-      if (cube <= 0 || cube >= d->ncube) return true;
-      const int m = bcmask[cube], x[3] = {i, j, k};
-      for (int ax = 0; ax < 3; ++ax) {
-        if ((m >> (2 * ax) & 1) && x[ax] <= 2) return true;
-        if ((m >> (2 * ax + 1) & 1) && x[ax] >= d->n + 1) return true;
-      }
-      return false;
-    };
-    std::vector<char> shared((size_t)ncs, 0);
-    for (int e = 0; e < ne; ++e) {
-      const int *G = &gc[4 * (size_t)e + 1], *P = &ip[4 * (size_t)e + 1];
-      const int q = case_of(G[0]);
-      if (q < 0 || q >= ncs) continue;
-      bool hit = case_of(P[0]) != q || in_slab(G[0], G[1], G[2], G[3]);
-      for (int dd = 0; dd < 8 && !hit; ++dd)
-        hit = in_slab(P[0], P[1] + (dd & 1), P[2] + (dd >> 1 & 1), P[3] + (dd >> 2 & 1));
-      if (hit) shared[q] = 1;
-    }
+    std::vector<int> c0 = bi ? bi->case_cube0 : std::vector<int>{1, d->ncube};
+    std::vector<char> shared;
+    ghost_shared_cases(d->n, d->ncube, bcc, bcm, gc.data(), ip.data(), ne, c0, shared);
     std::vector<char> to_side((size_t)ne, 0);
     int nside = 0;
     if (!bcc.empty())

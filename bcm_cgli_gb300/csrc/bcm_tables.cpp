@@ -364,6 +364,46 @@ void closing_plan(int n, int ncube, const std::vector<FaceTask> &tasks,
   }
 }
 
+// The cases whose IBM ghost fill must follow the boundary fill: some entry's
+// cell (ghost cell or one of its eight stencil cells) lies in the three
+// layers the boundary fill touches at a boundary face of its cube (ghost
+// layers written, the next interior layer read; y and z faces over whole
+// planes), or its stencil lies in another case.  The other cases' entries
+// touch no cell the boundary fill reads or writes.  GC/IP 1-based, ne
+// entries; case_cube0[q] is case q's first cube (ncase + 1 values; a single
+// case: {1, ncube}).
+void ghost_shared_cases(int n, int ncube, const std::vector<int> &bc_cubes,
+                        const std::vector<int> &bc_masks, const int *GC, const int *IP, int ne,
+                        const std::vector<int> &case_cube0, std::vector<char> &shared) {
+  const int ncs = (int)case_cube0.size() - 1;
+  shared.assign((size_t)std::max(ncs, 0), 0);
+  auto case_of = [&](int cube) -> int {
+    return (int)(std::upper_bound(case_cube0.begin(), case_cube0.end(), cube) -
+                 case_cube0.begin()) - 1;
+  };
+  std::vector<int> bcmask((size_t)std::max(ncube, 0), 0);
+  for (size_t q = 0; q < bc_cubes.size(); ++q)
+    if (bc_cubes[q] > 0 && bc_cubes[q] < ncube) bcmask[bc_cubes[q]] |= bc_masks[q];
+  auto in_slab = [&](int cube, int i, int j, int k) {
+    if (cube <= 0 || cube >= ncube) return true;
+    const int m = bcmask[cube], x[3] = {i, j, k};
+    for (int ax = 0; ax < 3; ++ax) {
+      if ((m >> (2 * ax) & 1) && x[ax] <= 2) return true;
+      if ((m >> (2 * ax + 1) & 1) && x[ax] >= n + 1) return true;
+    }
+    return false;
+  };
+  for (int e = 0; e < ne; ++e) {
+    const int *G = &GC[4 * (size_t)e + 1], *P = &IP[4 * (size_t)e + 1];
+    const int q = case_of(G[0]);
+    if (q < 0 || q >= ncs) continue;
+    bool hit = case_of(P[0]) != q || in_slab(G[0], G[1], G[2], G[3]);
+    for (int dd = 0; dd < 8 && !hit; ++dd)
+      hit = in_slab(P[0], P[1] + (dd & 1), P[2] + (dd >> 1 & 1), P[3] + (dd >> 2 & 1));
+    if (hit) shared[q] = 1;
+  }
+}
+
 bool build_push_table(int ncube, const std::vector<FaceTask> &tasks,
                       const std::vector<int> &task_cube, std::vector<int> &push) {
   push.assign(6 * (size_t)std::max(ncube, 0), 0);
@@ -440,6 +480,35 @@ extern "C" int bcmg_interface_plan(int n, int ncube, const int *adj_number, cons
   const bool ok = bcmg::build_push_table(ncube, tasks, task_cube, tbl);
   if (push) std::copy(tbl.begin(), tbl.end(), push);
   return ok ? (int)tasks.size() : -3;
+}
+
+extern "C" int bcmg_ghost_beside_plan(int n, int ncube, const int *const bc_lists[6],
+                                      const int bc_counts[6], const int *gc_minus,
+                                      const int *ip_minus, int nminus, const int *gc_plus,
+                                      const int *ip_plus, int nplus, const int *case_cube0,
+                                      int ncase, int *beside) {
+  if (ncube < 2 || n < 1 || !bc_lists || !bc_counts || ncase < 1 || !case_cube0 || !beside)
+    return -1;
+  std::vector<int> bcc, bcm;
+  std::string err;
+  if (!bcmg::build_bc_entries(ncube, bc_lists, bc_counts, bcc, bcm, err)) return -1;
+  const int ne = std::max(0, nminus) + std::max(0, nplus);
+  std::vector<int> gc(4 * (size_t)ne + 1, 0), ip(4 * (size_t)ne + 1, 0);
+  if (nminus > 0) {
+    if (!gc_minus || !ip_minus) return -1;
+    std::copy(gc_minus + 1, gc_minus + 1 + 4 * (size_t)nminus, gc.begin() + 1);
+    std::copy(ip_minus + 1, ip_minus + 1 + 4 * (size_t)nminus, ip.begin() + 1);
+  }
+  if (nplus > 0) {
+    if (!gc_plus || !ip_plus) return -1;
+    std::copy(gc_plus + 1, gc_plus + 1 + 4 * (size_t)nplus, gc.begin() + 1 + 4 * (size_t)std::max(0, nminus));
+    std::copy(ip_plus + 1, ip_plus + 1 + 4 * (size_t)nplus, ip.begin() + 1 + 4 * (size_t)std::max(0, nminus));
+  }
+  std::vector<int> c0(case_cube0, case_cube0 + ncase + 1);
+  std::vector<char> shared;
+  bcmg::ghost_shared_cases(n, ncube, bcc, bcm, gc.data(), ip.data(), ne, c0, shared);
+  for (int q = 0; q < ncase; ++q) beside[q] = !bcc.empty() && !shared[q];
+  return ncase;
 }
 
 extern "C" int bcmg_interface_closing_plan(int n, int ncube, const int *adj_number,

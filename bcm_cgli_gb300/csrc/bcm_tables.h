@@ -39,6 +39,13 @@ void closing_plan(int n, int ncube, const std::vector<FaceTask> &tasks,
                   const std::vector<int> &bc_masks, const int *ip_minus, int nminus,
                   const int *ip_plus, int nplus, std::vector<char> &keep,
                   std::vector<char> &edge);
+// Per case: whether its IBM ghost fill must follow the boundary fill (an
+// entry's ghost or stencil cell lies in the layers the boundary fill
+// touches, or its stencil is in another case).  GC/IP 1-based, ne entries,
+// case_cube0: first cube of each case plus one past the last.
+void ghost_shared_cases(int n, int ncube, const std::vector<int> &bc_cubes,
+                        const std::vector<int> &bc_masks, const int *GC, const int *IP, int ne,
+                        const std::vector<int> &case_cube0, std::vector<char> &shared);
 // Same-level push table of the split flux kernel (FluxSplitArgs::push):
 // push[6 src + 2 axis + 0] = destination of the task copying src's layers
 // 2, 3 (its side 1), push[6 src + 2 axis + 1] = destination of the task

@@ -579,6 +579,19 @@ int bcmg_interface_plan(int n, int ncube, const int *adj_number, const int *csl,
  * layers; IP tables 1-based), edge_cubes[c] = 1 (c < ncube) for the cubes
  * whose edge fill such a read sees.  Returns the task count, -1 for invalid
  * input, -2 if max_tasks is too small. */
+/* Per case of a resident context (case_cube0: each case's first cube, then
+ * one past the last; {1, ncube} for one case): beside[q] = 1 when the
+ * case's IBM ghost fill may run beside the boundary fill, i.e. none of its
+ * entries' cells (ghost cell, stencil) lies in the three layers the boundary
+ * fill touches at a boundary face of its cube, no stencil lies in another
+ * case, and the context has boundary faces.  Boundary lists 0-based as in
+ * bcmg_case_desc, GC / IP tables 1-based.  Returns ncase, -1 for invalid
+ * input. */
+int bcmg_ghost_beside_plan(int n, int ncube, const int *const bc_lists[6], const int bc_counts[6],
+                           const int *gc_minus, const int *ip_minus, int nminus,
+                           const int *gc_plus, const int *ip_plus, int nplus,
+                           const int *case_cube0, int ncase, int *beside);
+
 int bcmg_interface_closing_plan(int n, int ncube, const int *adj_number, const int *csl,
                                 const int *const bc_lists[6], const int bc_counts[6],
                                 const int *ip_minus, int nminus, const int *ip_plus, int nplus,

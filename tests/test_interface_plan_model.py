@@ -199,7 +199,8 @@ class Model:
                     X[(d,) + dst] = np.where(self.fluid[(c,) + src], X[(c,) + src], X[(d,) + dst])
 
 
-def _run(case, library_order, steps=2, subiters=2, push=None, reduced_closing=None):
+def _run(case, library_order, steps=2, subiters=2, push=None, reduced_closing=None,
+         ghost_first=False):
     m = Model(case, seed=5)
     push = library_order if push is None else push
     reduced_closing = library_order if reduced_closing is None else reduced_closing
@@ -210,8 +211,12 @@ def _run(case, library_order, steps=2, subiters=2, push=None, reduced_closing=No
         for it in range(subiters):
             for rk in range(3):
                 first = it == 0 and rk == 0
-                m.boundary()
-                m.ghosts()
+                if ghost_first:  # the ghost fill no longer waits for the boundary fill
+                    m.ghosts()
+                    m.boundary()
+                else:
+                    m.boundary()
+                    m.ghosts()
                 m.interface(every if (first or not library_order) else m.keep)
                 m.update(stage, push=push)
                 if not library_order:
@@ -306,3 +311,55 @@ def test_reduced_closing_call_drops_most_of_the_work():
     assert level.sum() > 0
     assert keep_q.sum() < level.sum() // 2
     assert edge_q.sum() < (case.ncube - 1) // 2
+
+
+def _beside(case):
+    lists = [np.ascontiguousarray(a, np.int32) for a in case.bc_lists()]
+    ptrs = (C.c_void_p * 6)(*[a.ctypes.data if len(a) else None for a in lists])
+    counts = (C.c_int * 6)(*[len(a) for a in lists])
+    t = [(None, None, 0) if x is None else
+         (np.ascontiguousarray(x[1], np.int32), np.ascontiguousarray(x[2], np.int32),
+          (len(x[1]) - 1) // 4) for x in (case.ibm_minus, case.ibm_plus)]
+    out = np.zeros(1, np.int32)
+    r = lib().bcmg_ghost_beside_plan(
+        case.n, case.ncube, C.cast(ptrs, C.c_void_p), C.cast(counts, C.c_void_p),
+        None if t[0][0] is None else t[0][0].ctypes.data,
+        None if t[0][1] is None else t[0][1].ctypes.data, t[0][2],
+        None if t[1][0] is None else t[1][0].ctypes.data,
+        None if t[1][1] is None else t[1][1].ctypes.data, t[1][2],
+        np.array([1, case.ncube], np.int32), 1, out)
+    assert r == 1
+    return bool(out[0])
+
+
+@pytest.mark.parametrize("make", [
+    lambda: cases.sphere_ibm(n=8, coarse=2.0, box=((-2, 4), (-2, 2), (-2, 2)),
+                             refine_box=((-2, 2), (-2, 2), (-2, 2))),
+    lambda: cases.sphere_ibm(n=8, coarse=2.0, box=((-4, 6), (-4, 4), (-4, 4)),
+                             refine_box=((-2, 2), (-2, 2), (-2, 2))),
+    lambda: cases.random_case(seed=11, n=4, periodic=False),
+    lambda: cases.random_case(seed=3, n=8, periodic=True)],
+    ids=["sphere_small", "sphere", "random_open_ibm", "random_periodic_ibm"])
+def test_ghost_fill_beside_boundary_fill_where_the_plan_allows(make):
+    """Where bcmg_ghost_beside_plan lets the IBM ghost fill run beside the
+    boundary fill, the two touch disjoint cells: with the ghost fill first
+    in every stage the model leaves every cell as the reference's order."""
+    case = make()
+    if not _beside(case):
+        return
+    ref = _run(case, library_order=False)
+    assert np.array_equal(ref[1:], _run(case, library_order=False, ghost_first=True)[1:])
+    assert np.array_equal(ref[1:], _run(case, library_order=True, ghost_first=True)[1:])
+
+
+def test_ghost_beside_plan_sides():
+    """The spheres' IBM cells lie away from their boundary faces (beside);
+    the random tables put IBM cells in boundary layers (in order), and there
+    the order matters: ghost fill first changes the result."""
+    sph = cases.sphere_ibm(n=8, coarse=2.0, box=((-4, 6), (-4, 4), (-4, 4)),
+                           refine_box=((-2, 2), (-2, 2), (-2, 2)))
+    assert _beside(sph)
+    rnd = cases.random_case(seed=11, n=4, periodic=False)
+    assert not _beside(rnd)
+    assert not np.array_equal(_run(rnd, library_order=False)[1:],
+                              _run(rnd, library_order=False, ghost_first=True)[1:])
