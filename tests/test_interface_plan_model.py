@@ -361,5 +361,7 @@ def test_ghost_beside_plan_sides():
     assert _beside(sph)
     rnd = cases.random_case(seed=11, n=4, periodic=False)
     assert not _beside(rnd)
+    # the in-order half of the mixed batch in the GPU on/off comparison
+    assert not _beside(cases.random_case(seed=11, n=8, periodic=False, viscous=True))
     assert not np.array_equal(_run(rnd, library_order=False)[1:],
                               _run(rnd, library_order=False, ghost_first=True)[1:])
