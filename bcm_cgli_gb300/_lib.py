@@ -152,6 +152,12 @@ def _declare(L):
         C.c_int, C.c_int, C.c_int, P, C.c_double, C.c_double, C.c_double, C.c_double,
         C.c_double, C.c_double, dp, ip, dp, dp, dp, P, P, P, ip, P]
     L.BCM_Immersed_boundary.restype = None
+    L.BCM_FWS_Interface.argtypes = [C.c_int] * 8 + [P] * 11 + [P] * 4 + [P] * 3 + [ip, ip, P, P,
+                                                                                   P, ip]
+    L.BCM_FWS_Interface.restype = None
+    L.bcmg_fws_interface.argtypes = [C.c_int, C.c_int, ip, ip, ip]
+    L.bcmg_fws_band_pack.argtypes = [C.c_int, C.c_int, ip, C.c_int, ip, ip]
+    L.bcmg_fws_band_unpack.argtypes = [C.c_int, C.c_int, ip, C.c_int, ip, ip]
     return L
 
 

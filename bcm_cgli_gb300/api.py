@@ -231,6 +231,62 @@ def BCM_Interface_for_case(case, U1_):
     _raise_if_failed("BCM_Interface")
 
 
+def BCM_FWS_Interface(myid, ncube, mPI_Nadj, ncpu_eq, max_nei_eq, nadjX_eq, nadjY_eq, nadjZ_eq,
+                      csl, adj_number, adjX_eq, adjY_eq, adjZ_eq, FWS):
+    """BCM_FWS_Interface (BCM_FWS_Interface.cpp:23-791, setup, on the host) on
+    one process: same-level ghost-face copies of the flags, sign threshold
+    and hole fill of every finest-level cube, FWS updated in place.  The
+    exchange arguments of main.h:55-110 between nadjZ_eq and csl are passed
+    as empty; ncpu_eq must be 0.  adjX/Y/Z_eq are 1-based lists as
+    BCM_Interface_table builds them."""
+    z = np.zeros(4, np.int32)
+    d = np.zeros(4)
+    zp, dd = z.ctypes.data_as(C.c_void_p), d.ctypes.data_as(C.c_void_p)
+    lists = [_ip(a) for a in (adjX_eq, adjY_eq, adjZ_eq)]
+    lib().BCM_FWS_Interface(int(myid), int(ncube), int(mPI_Nadj), int(ncpu_eq), int(max_nei_eq),
+                            int(nadjX_eq), int(nadjY_eq), int(nadjZ_eq), *([zp] * 11),
+                            *([dd] * 4), *([zp] * 3), _ip(csl), _ip(adj_number),
+                            *(a.ctypes.data_as(C.c_void_p) for a in lists), _fws_inplace(FWS))
+    _raise_if_failed("BCM_FWS_Interface")
+
+
+def BCM_FWS_Interface_for_case(case, FWS):
+    """BCM_FWS_Interface with the case's same-level lists (interface_lists)
+    and single-process arguments, like main.cpp:634 on one rank."""
+    X, Y, Z = (lst[0] for lst in interface_lists(case))
+    BCM_FWS_Interface(0, case.ncube, 1, 0, 0, len(X) - 1, len(Y) - 1, len(Z) - 1, case.csl,
+                      case.adj, X, Y, Z, FWS)
+
+
+def fws_interface(n, ncube, csl, adj_number, FWS):
+    """bcmg_fws_interface: BCM_FWS_Interface for any cube edge n, with the
+    same-level pairs found from adj_number; FWS updated in place."""
+    if lib().bcmg_fws_interface(int(n), int(ncube), _ip(csl), _ip(adj_number),
+                                _fws_inplace(FWS)) != 0:
+        raise BcmgError(f"bcmg_fws_interface: {_lib.last_error()}")
+
+
+def fws_band_pack(n, FWS, bands):
+    """Flag bands (rows of 4 ints: cube slot, axis, side, layers) of FWS
+    packed into one int32 buffer, in the state halo's cell order."""
+    bands = np.ascontiguousarray(bands, np.int32).reshape(-1, 4)
+    total = int(bands[:, 3].sum()) * n * n
+    buf = np.zeros(max(total, 1), np.int32)
+    F = np.ascontiguousarray(FWS, np.int32)
+    if lib().bcmg_fws_band_pack(int(n), F.shape[0], F, len(bands), _ip(bands.reshape(-1)),
+                                buf) != 0:
+        raise BcmgError(f"bcmg_fws_band_pack: {_lib.last_error()}")
+    return buf[:total]
+
+
+def fws_band_unpack(n, FWS, bands, buf):
+    """Writes packed flag bands (fws_band_pack's layout) into FWS in place."""
+    bands = np.ascontiguousarray(bands, np.int32).reshape(-1, 4)
+    if lib().bcmg_fws_band_unpack(int(n), FWS.shape[0], _fws_inplace(FWS), len(bands),
+                                  _ip(bands.reshape(-1)), _ip(buf)) != 0:
+        raise BcmgError(f"bcmg_fws_band_unpack: {_lib.last_error()}")
+
+
 # ---------------------------------------------------------------------------
 # Device-resident context
 # ---------------------------------------------------------------------------

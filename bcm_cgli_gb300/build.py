@@ -35,6 +35,7 @@ UNITS = [
     ("bcm_output.cu", ["--fmad=false"]),
     ("bcm_ibm.cu", ["--fmad=false"]),
     ("bcm_tables.cpp", []),
+    ("bcm_flags.cpp", []),
 ]
 
 

@@ -178,6 +178,33 @@ void BCM_Immersed_boundary(int myid, int ncube, int n_wallcube, int *NBC, double
                            double *Zcube, double *Xcnt, double *Ycnt, double *Zcnt, int *FWS,
                            int *wallcube);
 
+/* Replaces BCM_FWS_Interface (main.h:55-110, BCM_FWS_Interface.cpp:23-791;
+ * called at setup, main.cpp:634 and :1070).  In every finest-level cube
+ * (csl == 0): the two ghost layers of each face with a same-level neighbour
+ * take the neighbour's flags from the two interior layers beside the face
+ * (pairs from the caller's 1-based lists adjX_eq / adjY_eq / adjZ_eq, the
+ * neighbour read from slot 1 of adj_number), every flag becomes its sign,
+ * and fluid or ghost cells with both neighbours along an axis solid become
+ * solid until none is left (cells with every index in 1..ncube_x+2).  Other
+ * cubes keep their flags.  Runs on the host (setup, integer work).  One
+ * process: ncpu_eq must be 0; the other exchange arguments are accepted and
+ * unused.  Errors (bad lists, pairs on different levels):
+ * bcmg_last_error(), FWS unchanged. */
+void BCM_FWS_Interface(int myid, int ncube, int mPI_Nadj, int ncpu_eq, int max_nei_eq,
+                       int nadjX_eq, int nadjY_eq, int nadjZ_eq, int *rank_map, int *MPI_cpu,
+                       int *MPI_cube, int *MPI_cpu_adj, int *MPI_cube_adj, int *MPI_direction,
+                       int *MPI_interface, int *neighbor_cpu_eq, int *Ncube_Ncpu_eq,
+                       int *Scube_Ncpu_eq, int *Rcube_Ncpu_eq, double *send_data_curr_eq,
+                       double *recv_data_curr_eq, double *send_data_neig_eq,
+                       double *recv_data_neig_eq, int *Sdir_eq, int *Rdir_eq, int *ist_eq,
+                       int *csl, int *adj_number, int *adjX_eq, int *adjY_eq, int *adjZ_eq,
+                       int *FWS);
+
+/* The same for any cube edge n, with the same-level pairs found from
+ * adj_number as BCM_Interface_table.cpp:96-120 classifies them.  FWS is
+ * [ncube][n+4]^3.  Returns 0, or -1 for invalid input (bcmg_last_error()). */
+int bcmg_fws_interface(int n, int ncube, const int *csl, const int *adj_number, int *FWS);
+
 /* The same preprocessing in memory.  tri: ntri triangles x 3 vertices x
  * (x, y, z), in STL facet order.  Cell centres are formed from the cube
  * corners (BCM_Grid.cpp:124-148).  FWS ([ncube][n+4]^3) is updated in
@@ -480,6 +507,18 @@ int bcmg_shard_plan(int ncube, const int *adj_number, const int *csl, const int 
                     int *proxy_cubes);
 int bcmg_shard_bands(int ncube, const int *adj_number, const int *csl, const int *rank_of_cube,
                      int src_rank, int dst_rank, int cap, int *nband, int *bands);
+
+/* Flags of a sharded run at setup (the cross-rank part of
+ * BCM_FWS_Interface.cpp:136-550): the owning rank packs the flag bands of
+ * its cubes (4 ints per band in local slots: cube, axis, side, layers, as
+ * for bcmg_case_set_halo; layers * n * n ints per band in (layer, first
+ * in-face index, second) order), the receiving rank unpacks them into its
+ * proxy slots and then calls bcmg_fws_interface on its own cubes and
+ * proxies: its cubes' flags equal those of one process holding the whole
+ * case.  Host memory; 0, or -1 for invalid input. */
+int bcmg_fws_band_pack(int n, int ncube, const int *FWS, int nband, const int *bands, int *buf);
+int bcmg_fws_band_unpack(int n, int ncube, int *FWS, int nband, const int *bands,
+                         const int *buf);
 
 /* A rank's context: desc describes its nlocal + nproxy cubes in local
  * numbering (cube slot 1 + i: local_cubes[i], then proxy_cubes) with the

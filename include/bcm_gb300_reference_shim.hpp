@@ -6,9 +6,11 @@
 // the host program (after Resolution.h, so X_size/Ndim are defined), and
 // dropping the reference's BCM_Flux_XYZ_Viscous_Runge_kutta.cpp,
 // BCM_Interface.cpp, BCM_Ghostcell_minus.cpp, BCM_Ghostcell_plus.cpp,
-// BCM_X/Y/Z_boundary_condition.cpp and BCM_Immersed_boundary.cpp from the
-// link, gives main.cpp the same
-// C++ symbols, now running on the GPU through the C ABI of bcm_gb300.h.
+// BCM_X/Y/Z_boundary_condition.cpp, BCM_Immersed_boundary.cpp and
+// BCM_FWS_Interface.cpp from the link, gives main.cpp the same
+// C++ symbols, now running through the C ABI of bcm_gb300.h (the per-stage
+// routines and the IBM preprocessing on the GPU, the flag setup on the
+// host).
 // Call bcmg_set_reference_config() once at start-up with the values of
 // Resolution.h / prm.h (NcubeX, MPI_Ncube, mu_L, rho0, U0, Uin, P0).
 #pragma once
@@ -113,4 +115,22 @@ void BCM_Immersed_boundary(int myid, int ncube, int n_wallcube, int *NBC, double
   ::BCM_Immersed_boundary(myid, ncube, n_wallcube, NBC, Xmin, Xmax, Ymin, Ymax, Zmin, Zmax,
                           cube_size, csl, Xcube, Ycube, Zcube, (double *)Xcnt, (double *)Ycnt,
                           (double *)Zcnt, (int *)FWS, wallcube);
+}
+
+// main.h:55-110 (setup, called at main.cpp:634 and :1070)
+void BCM_FWS_Interface(int myid, int ncube, int mPI_Nadj, int ncpu_eq, int max_nei_eq,
+                       int nadjX_eq, int nadjY_eq, int nadjZ_eq, int (*rank_map)[MPI_Ncube],
+                       int *MPI_cpu, int *MPI_cube, int *MPI_cpu_adj, int *MPI_cube_adj,
+                       int *MPI_direction, int *MPI_interface, int *neighbor_cpu_eq,
+                       int *Ncube_Ncpu_eq, int *Scube_Ncpu_eq, int *Rcube_Ncpu_eq,
+                       double *send_data_curr_eq, double *recv_data_curr_eq,
+                       double *send_data_neig_eq, double *recv_data_neig_eq, int *Sdir_eq,
+                       int *Rdir_eq, int *ist_eq, int *csl, int (*adj_number)[5][7],
+                       int *adjX_eq, int *adjY_eq, int *adjZ_eq, bcmg_shim_flag_t *FWS) {
+  ::BCM_FWS_Interface(myid, ncube, mPI_Nadj, ncpu_eq, max_nei_eq, nadjX_eq, nadjY_eq, nadjZ_eq,
+                      (int *)rank_map, MPI_cpu, MPI_cube, MPI_cpu_adj, MPI_cube_adj,
+                      MPI_direction, MPI_interface, neighbor_cpu_eq, Ncube_Ncpu_eq,
+                      Scube_Ncpu_eq, Rcube_Ncpu_eq, send_data_curr_eq, recv_data_curr_eq,
+                      send_data_neig_eq, recv_data_neig_eq, Sdir_eq, Rdir_eq, ist_eq, csl,
+                      (int *)adj_number, adjX_eq, adjY_eq, adjZ_eq, (int *)FWS);
 }

@@ -264,6 +264,7 @@ class Ref:
         L.ref_set_threads.argtypes = [C.c_int]
         L.ref_output.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp]
         L.ref_ibm.argtypes = [C.c_int, _dp, _ip, _dp, _dp, _dp, _ip]
+        L.ref_fws_interface.argtypes = [_ip]
         L.ref_run.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                               _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.c_int,
                               C.c_int, _ip, _ip, C.c_int, C.c_int, _ip, _ip, C.c_int, C.c_int,
@@ -322,6 +323,12 @@ class Ref:
         finally:
             os.chdir(cwd)
 
+    def fws_interface(self, case, fws):
+        """The reference's BCM_FWS_Interface on one rank, with the same-level
+        lists its BCM_Interface_table built for the case; fws (the case's
+        flags, int32 [ncube][n+4]^3) is updated in place."""
+        self.lib.ref_fws_interface(fws)
+
     def run(self, case, st: State, steps: int, subiters: int):
         xl, xu, yl, yu, zl, zu = (_one_based(a) for a in case.bc_lists())
         nm, Wm, Gm, Im = _ibm(case, -1)
@@ -331,6 +338,67 @@ class Ref:
                          st.Rku1, st.Residual1, len(xl) - 1, len(xu) - 1, xl, xu, len(yl) - 1,
                          len(yu) - 1, yl, yu, len(zl) - 1, len(zu) - 1, zl, zu, nm, Wm, Gm, Im,
                          npl, Wp, Gp, Ip, st.er, st.Emax)
+
+
+def fws_interface(n, ncube, csl, adj, fws):
+    """Restatement of BCM_FWS_Interface (BCM_FWS_Interface.cpp:23-791) on one
+    rank, in numpy; returns the new flags (int32 [ncube][n+4]^3).
+
+    * A double copy of the flags of every finest-level cube (csl == 0)
+      (:111-131); other cubes are never thresholded, so their copy is unused.
+    * Same-level pairs: a cube with any of adj[c][1..4][dir] > 0 whose
+      largest slot value is a cube of the same level, per axis in cube order
+      (BCM_Interface_table.cpp:96-120); the neighbour is adj[c][1][dir].
+      The neighbour's low ghost layers take the cube's layers n, n+1 and the
+      cube's high ghost layers the neighbour's layers 2, 3, over the face's
+      interior (:555-660), X, then Y, then Z.
+    * Threshold at +-0.5 back to -1 / 0 / 1 (:668-700).
+    * Holes (:702-783): a cell with every index in 1..n+2, flag >= 0, and
+      both neighbours along some axis at -1 becomes -1, until none changes.
+      The reference sweeps in place in memory order; the rule is monotone,
+      so all cells of a Jacobi round change at once here and the fixed point
+      is the same.
+    """
+    S = n + 4
+    fws = np.ascontiguousarray(fws, np.int32)
+    csl = np.asarray(csl)
+    adj = np.asarray(adj).reshape(ncube, 5, 7)
+    T = fws.astype(np.float64)
+    I = slice(2, n + 2)
+    for ax in range(3):
+        d = 2 + 2 * ax
+        for c in range(1, ncube):
+            slots = adj[c, 1:5, d]
+            if not (slots > 0).any() or csl[c] != csl[slots.max()]:
+                continue
+            c2 = adj[c, 1, d]
+            for l in range(2):
+                lo, src, hi, src2 = [[I, I, I] for _ in range(4)]
+                lo[ax], src[ax], hi[ax], src2[ax] = l, n + l, n + 2 + l, 2 + l
+                T[(c2, *lo)] = T[(c, *src)]
+                T[(c, *hi)] = T[(c2, *src2)]
+    out = fws.copy()
+    lv = np.nonzero(csl[:ncube] == 0)[0]
+    lv = lv[lv >= 1]
+    if len(lv):
+        t = T[lv]
+        F = np.where(t > 0.5, 1, np.where(t < -0.5, -1, 0)).astype(np.int32)
+        R = slice(1, n + 3)
+        while True:
+            core = F[:, R, R, R]
+            pair = np.zeros(core.shape, bool)
+            for ax in range(3):
+                up, dn = [slice(None), R, R, R], [slice(None), R, R, R]
+                up[1 + ax] = slice(2, n + 4)
+                dn[1 + ax] = slice(0, n + 2)
+                pair |= (F[tuple(up)] + F[tuple(dn)]) == -2
+            hole = (core >= 0) & pair
+            if not hole.any():
+                break
+            core[hole] = -1
+        out[lv] = F
+    assert out.shape == (ncube, S, S, S)
+    return out
 
 
 def reference_available() -> bool:

@@ -49,6 +49,7 @@ REF_SOURCES = [
     "BCM_Z_boundary_condition.cpp",
     "BCM_Output.cpp",
     "BCM_Immersed_boundary.cpp",
+    "BCM_FWS_Interface.cpp",
 ]
 
 

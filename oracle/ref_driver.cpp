@@ -135,6 +135,18 @@ void ref_interface(double *U1_) {
                 L[3], L[4], L[6], L[7], L[8], L[9], L[11], L[12], L[13], L[14], (Cell *)U1_);
 }
 
+/* BCM_FWS_Interface (main.h:55-110) with the same-level lists from
+ * ref_interface_setup and empty single-rank exchange lists; FWS is
+ * [ncube][X_size]^3, changed in place. */
+void ref_fws_interface(int *FWS) {
+  int *z = M.one;
+  double *d = M.dz;
+  int *n = T.n;
+  BCM_FWS_Interface(0, T.ncube, MPI_Nadj, 0, 0, n[0], n[5], n[10], M.rank_map, z, z, z, z, z,
+                    z, z, z, z, z, d, d, d, d, z, z, z, T.csl, T.adj, T.lists[0], T.lists[5],
+                    T.lists[10], (Flag *)FWS);
+}
+
 /*
  * The reference time loop (main.cpp:1146-1357) for `steps` physical steps of
  * exactly `subiters` pseudo-time sub-iterations each (the reference's own loop

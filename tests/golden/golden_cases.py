@@ -46,6 +46,31 @@ def horizon_cases():
     return {"vortex_full": (cases.isentropic_vortex(ncx=4, n=16, dT=1e-3), 100, 10)}
 
 
+def flag_cases():
+    """Cases for the flag-field interface fixtures (BCM_FWS_Interface):
+    random flags with many solid cells, so that holes form and fill in
+    chains; every cube on the finest level (csl = 0, the only level the
+    routine changes) except in the two-level case, whose coarse cubes must
+    keep their flags.  A one-cube periodic box makes a cube its own
+    neighbour on every axis."""
+    def finest(case):
+        case.csl = np.zeros_like(case.csl)
+        return case
+    return {
+        "flags_periodic_n8": finest(cases.random_case(seed=21, ncx=2, ncy=2, ncz=1, n=8,
+                                                      periodic=True, solid_frac=0.35,
+                                                      ghost_frac=0.2)),
+        "flags_open_n4": finest(cases.random_case(seed=22, ncx=3, ncy=2, ncz=2, n=4,
+                                                  periodic=False, solid_frac=0.4,
+                                                  ghost_frac=0.2)),
+        "flags_two_level_n4": cases.random_two_level_case(seed=23, n=4, periodic=True,
+                                                          solid_frac=0.4, ghost_frac=0.2),
+        "flags_one_cube_n4": finest(cases.random_case(seed=24, ncx=1, ncy=1, ncz=1, n=4,
+                                                      periodic=True, solid_frac=0.45,
+                                                      ghost_frac=0.2)),
+    }
+
+
 def ibm_cases():
     """(case, triangles) pairs for the IBM preprocessing fixtures: a sphere of
     diameter 1 on a two-level grid of n=8 cubes (fine cubes of edge 1, cells

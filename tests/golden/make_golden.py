@@ -8,6 +8,7 @@ output array plus the norms.  Run here, where the reference sources exist:
     python tests/golden/make_golden.py            # everything
     python tests/golden/make_golden.py --ibm-only # the IBM preprocessing records
     python tests/golden/make_golden.py --horizon  # the long-run records only
+    python tests/golden/make_golden.py --flags    # the flag-interface records only
 """
 import hashlib
 import json
@@ -22,8 +23,8 @@ sys.path[:0] = [ROOT, os.path.join(ROOT, "oracle"), HERE]
 import numpy as np  # noqa: E402
 
 import oracle as O  # noqa: E402
-from golden_cases import (RUN_STEPS, RUN_SUBITERS, canonical, golden_cases,  # noqa: E402
-                          horizon_cases, ibm_cases)
+from golden_cases import (RUN_STEPS, RUN_SUBITERS, canonical, flag_cases,  # noqa: E402
+                          golden_cases, horizon_cases, ibm_cases)
 from bcm_cgli_gb300 import cases as _cases  # noqa: E402
 
 
@@ -69,12 +70,33 @@ def horizon_records():
     return out
 
 
+def flag_records():
+    """Digests of the flags after the reference's BCM_FWS_Interface on one
+    rank (its own same-level lists), the input flags' digest, and how many
+    flags it changed."""
+    out = {}
+    for name, case in flag_cases().items():
+        fws = case.fws.copy()
+        O.Ref(case).fws_interface(case, fws)
+        out[name] = {"input": digest(case.fws), "fws": digest(fws),
+                     "changed": int((fws != case.fws).sum())}
+        print(name, "done", file=sys.stderr)
+    return out
+
+
 def main():
     path = os.path.join(HERE, "golden.json")
     if "--horizon" in sys.argv:
         with open(path) as f:
             doc = json.load(f)
         doc["horizon"] = horizon_records()
+        with open(path, "w") as f:
+            json.dump(doc, f, indent=1)
+        return
+    if "--flags" in sys.argv:
+        with open(path) as f:
+            doc = json.load(f)
+        doc["flags"] = flag_records()
         with open(path, "w") as f:
             json.dump(doc, f, indent=1)
         return
@@ -125,7 +147,8 @@ def main():
         json.dump({"generator": "tests/golden/make_golden.py (reference compiled by "
                                 "oracle/ref_build.py, OMP_NUM_THREADS=1)",
                    "steps": RUN_STEPS, "subiters": RUN_SUBITERS, "cases": out,
-                   "ibm": ibm_records(), "horizon": horizon_records()}, f, indent=1)
+                   "ibm": ibm_records(), "horizon": horizon_records(),
+                   "flags": flag_records()}, f, indent=1)
 
 
 if __name__ == "__main__":

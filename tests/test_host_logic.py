@@ -326,6 +326,39 @@ def test_reference_shim_compiles_against_main_h(tmp_path):
     assert r.returncode == 0, r.stderr[-2000:]
 
 
+SHIM_ROUTINES = ("BCM_Flux_XYZ_Viscous_Runge_kutta", "BCM_X_boundary_condition",
+                 "BCM_Y_boundary_condition", "BCM_Z_boundary_condition", "BCM_Ghostcell_minus",
+                 "BCM_Ghostcell_plus", "BCM_Interface", "BCM_Immersed_boundary",
+                 "BCM_FWS_Interface")
+
+
+@pytest.mark.skipif(not O.reference_available(), reason="reference sources not on this host")
+def test_reference_shim_defines_main_h_symbols(tmp_path):
+    """A signature that differs from main.h would only add an overload; so a
+    caller compiled against main.h alone takes the address of every replaced
+    routine, and the shim's object must define each C++ symbol it needs."""
+    inc = ["-I", O.ref_build.REF_DIR, "-I", os.path.join(ROOT, "include"),
+           "-I", os.path.join(ROOT, "oracle", "mpi_stub")]
+    caller = tmp_path / "caller.cpp"
+    caller.write_text('#include "Resolution.h"\n#include "main.h"\nvoid *routines[] = {' +
+                      ", ".join(f"(void *)&{f}" for f in SHIM_ROUTINES) + "};\n")
+    shim = tmp_path / "shim.cpp"
+    shim.write_text('#include "Resolution.h"\n#include "main.h"\n'
+                    '#include "bcm_gb300_reference_shim.hpp"\n')
+    syms = {}
+    for src in (caller, shim):
+        obj = src.with_suffix(".o")
+        r = subprocess.run(["g++", "-std=c++17", "-c", "-w", *inc, str(src), "-o", str(obj)],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr[-2000:]
+        out = subprocess.run(["nm", str(obj)], capture_output=True, text=True).stdout
+        syms[src.name] = [line.split() for line in out.splitlines()]
+    needed = {s[-1] for s in syms["caller.cpp"] if s[-2] == "U" and "BCM_" in s[-1]}
+    defined = {s[-1] for s in syms["shim.cpp"] if s[-2] == "T"}
+    assert len(needed) == len(SHIM_ROUTINES)
+    assert needed <= defined, sorted(needed - defined)
+
+
 def test_batch_create_rejects_mismatched_cases_before_touching_the_gpu():
     """bcmg_batch_create validates every case on the host first: different n,
     out-of-range adjacency and boundary entries are refused with an error
