@@ -316,6 +316,20 @@ def cpu_sample(case, subiters=1, threads=None):
                       f"{dt:.2f} s"}
 
 
+def cpu_single_thread(case):
+    """The same restatement on one thread (the setting the reference's
+    parity runs use): one sub-iteration of the workload's smallest case."""
+    O, runner, _ = _port(1)
+    c = min(case.cases if is_batch(case) else [case], key=lambda m: m.n_cells)
+    st = O.State(c)
+    t0 = time.perf_counter()
+    runner.run(c, st, 1, 1)
+    dt = time.perf_counter() - t0
+    return {"value": c.n_cells / dt, "unit": UNIT, "cores": 1,
+            "sample": f"1 sub-iteration of the workload's smallest case ({c.n_cells} cells), "
+                      f"1 OpenMP thread, {dt:.2f} s"}
+
+
 def run_reference_arm(args, dist):
     """The reference's CPU algorithm (C restatement of the reference loop;
     the reference's own sources are not on the GPU host) on all host cores.
@@ -783,6 +797,7 @@ def run_gpu_arm(args, dist):
         line["converged_step"] = conv
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample(case, subiters=1)
+        line["cpu_baseline"]["single_thread"] = cpu_single_thread(case)
     for m in (m_head, m_other):
         if m is not None:
             m["ctx"].close()
