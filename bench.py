@@ -462,13 +462,15 @@ def measure_e2e(ctx, case, args, dist, cell_subiters):
     levels a host-held solver passes), one dual-time step, device -> host of
     the step's result, the new state U1_ (after the time shift U1 equals it
     on the interior and U1q is the previous U1, which the host holds),
-    through the public C ABI; device-timed."""
+    through the public C ABI; device-timed, and the host clock over the same
+    region (returned second)."""
     hU, hold = pinned_like(case.U)
     hU1, hold1 = pinned_like(case.U)
     hU1q, hold1q = pinned_like(case.U)
     oU, ohold = pinned_like(case.U)
     dist.barrier()
     ctx.sync()
+    t0 = time.perf_counter()
     ctx.timer_mark(2)
     for _ in range(args.steps):
         ctx.set_state(hU, hU1, hU1q)
@@ -476,9 +478,10 @@ def measure_e2e(ctx, case, args, dist, cell_subiters):
         ctx.get_result(oU)
     ctx.timer_mark(3)
     ctx.sync()
+    wall = dist.max(time.perf_counter() - t0)
     dist.barrier()
     ms_e2e = dist.max(ctx.timer_elapsed(2, 3))
-    return cell_subiters / (ms_e2e * 1e-3)
+    return cell_subiters / (ms_e2e * 1e-3), cell_subiters / wall
 
 
 def measure_twins(api, case, precision_name, subiters=2):
@@ -543,7 +546,8 @@ def measure_e2e_pipelined(api, case, precision_name, args, dist, ngroups=None):
     (a graph launch) and the device -> host copy of its new U1_ are enqueued
     asynchronously, so one group's copies run while the others step.  Same
     bytes per step as measure_e2e; device-timed (events on every stream, the
-    longest span)."""
+    longest span), and the host clock from before the first copy is enqueued
+    until every stream has finished (returned second)."""
     ngroups = ngroups or E2E_GROUPS
     cs = case.cases
     cells = np.cumsum([c.n_cells for c in cs])
@@ -573,6 +577,7 @@ def measure_e2e_pipelined(api, case, precision_name, args, dist, ngroups=None):
     dist.barrier()
     for ctx, _, _ in halves:
         ctx.sync()
+    t0 = time.perf_counter()
     for ctx, _, _ in halves:
         ctx.timer_mark(6)
     for _ in range(args.steps):
@@ -584,11 +589,13 @@ def measure_e2e_pipelined(api, case, precision_name, args, dist, ngroups=None):
         ctx.timer_mark(7)
     for ctx, _, _ in halves:
         ctx.sync()
+    wall = dist.max(time.perf_counter() - t0)
     dist.barrier()
     ms = dist.max(max(ctx.timer_elapsed(6, 7) for ctx, _, _ in halves))
     for ctx, _, _ in halves:
         ctx.close()
-    return case.n_cells * SUBITERS * args.steps * dist.world / (ms * 1e-3), cuts
+    done = case.n_cells * SUBITERS * args.steps * dist.world
+    return done / (ms * 1e-3), cuts, done / wall
 
 
 def cases_flat(group):
@@ -706,15 +713,15 @@ def run_gpu_arm(args, dist):
 
     ctx = m_head["ctx"]
     cell_subiters = case.n_cells * SUBITERS * args.steps * dist.world
-    e2e = e2e_serial = None
+    e2e = e2e_serial = e2e_wall = None
     e2e_how = None
     if not args.no_e2e:
-        e2e_serial = measure_e2e(ctx, case, args, dist, cell_subiters)
+        e2e_serial, e2e_wall = measure_e2e(ctx, case, args, dist, cell_subiters)
         e2e, e2e_how = e2e_serial, "one context: copy in, step, copy out, in series"
         if is_batch(case) and len(case.cases) >= 2:
-            piped, cuts = measure_e2e_pipelined(api, case, head, args, dist)
+            piped, cuts, piped_wall = measure_e2e_pipelined(api, case, head, args, dist)
             if piped > e2e:
-                e2e = piped
+                e2e, e2e_wall = piped, piped_wall
                 parts = ", ".join(f"{a}..{b - 1}" for a, b in zip(cuts[:-1], cuts[1:]))
                 e2e_how = (f"{len(cuts) - 1} contexts (cases {parts}) on their own streams: "
                            "each one's copies overlap the others' steps")
@@ -757,7 +764,8 @@ def run_gpu_arm(args, dist):
             "roofline": roofline(m_head, head),
             "e2e": ({"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 3 * case.U.nbytes,
                      "d2h_bytes_per_step": case.U.nbytes, "how": e2e_how,
-                     "serial_value": e2e_serial} if e2e is not None else None),
+                     "serial_value": e2e_serial, "wall_value": e2e_wall}
+                    if e2e is not None else None),
             "gpu_launches": m_head["launches"], "clocks": m_head["clocks"],
             "launch_shapes": m_head["tuning"],
             "fp64_alu": {"measured_fma_gflops": fp64_gflops,
