@@ -216,7 +216,7 @@ def test_two_ranks_exchange_flag_bands():
     import torch.multiprocessing as mp
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
-    port = 29900 + os.getpid() % 90
+    port = 28100 + os.getpid() % 800  # a range no other test uses
     ps = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
     for p in ps:
         p.start()
