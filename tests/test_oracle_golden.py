@@ -58,11 +58,25 @@ def test_full_loop_matches_reference_digests(port, name):
     assert [repr(float(x)) for x in st.Emax] == rec["run_emax"]
 
 
-@pytest.mark.skipif(not O.reference_available(), reason="reference sources not on this host")
-@pytest.mark.parametrize("seed", [21, 22, 23])
-def test_port_equals_reference_directly(port, seed):
+def _direct_cases():
+    """Random 2x2x2 boxes, and the degenerate grids: one periodic cube (each
+    face its own neighbour), a 3x2x2 open box (boundary faces on every side,
+    cubes with one neighbour along an axis) and a case without IBM tables."""
     from bcm_cgli_gb300 import cases
-    case = cases.random_case(seed=seed, n=4, periodic=bool(seed % 2), viscous=True)
+    out = {f"random_{s}": (lambda s=s: cases.random_case(seed=s, n=4, periodic=bool(s % 2),
+                                                         viscous=True)) for s in (21, 22, 23)}
+    out["one_cube_periodic"] = lambda: cases.random_case(seed=24, ncx=1, ncy=1, ncz=1, n=4,
+                                                         periodic=True)
+    out["open_3x2x2"] = lambda: cases.random_case(seed=25, ncx=3, ncy=2, ncz=2, n=4,
+                                                  periodic=False)
+    out["no_ibm"] = lambda: cases.random_case(seed=26, n=4, periodic=False, with_ibm=False)
+    return out
+
+
+@pytest.mark.skipif(not O.reference_available(), reason="reference sources not on this host")
+@pytest.mark.parametrize("name", list(_direct_cases()))
+def test_port_equals_reference_directly(port, name):
+    case = _direct_cases()[name]()
     ref = O.Ref(case)
     ref.set_threads(1)
     a, b = O.State(case), O.State(case)
