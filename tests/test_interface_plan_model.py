@@ -236,9 +236,11 @@ def _run(case, library_order, steps=2, subiters=2, push=None, reduced_closing=No
     lambda: cases.random_two_level_case(seed=1, n=4),
     lambda: cases.random_two_level_case(seed=6, n=8, periodic=False),
     lambda: cases.sphere_ibm(n=8, coarse=2.0, box=((-2, 4), (-2, 2), (-2, 2)),
-                             refine_box=((-2, 2), (-2, 2), (-2, 2)))],
+                             refine_box=((-2, 2), (-2, 2), (-2, 2))),
+    lambda: cases.random_case(seed=24, ncx=1, ncy=1, ncz=1, n=4, periodic=True),
+    lambda: cases.random_case(seed=25, ncx=3, ncy=2, ncz=1, n=4, periodic=False)],
     ids=["tgv_periodic", "random_periodic_ibm", "random_open_ibm", "two_level_periodic",
-         "two_level_open", "sphere_two_level_ibm"])
+         "two_level_open", "sphere_two_level_ibm", "one_cube_periodic", "open_3x2x1"])
 def test_library_order_equals_reference_order(make):
     case = make()
     a = _run(case, library_order=False)
