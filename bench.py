@@ -273,11 +273,13 @@ def _port(threads=None):
 
 # The CPU arms time the C restatement of the reference loop: the reference's
 # own sources are not on the GPU host.  On an x86 host where both build, the
-# restatement runs at 0.72-0.82 of the reference's compiled code (1 and 8
-# threads, vortex and Taylor-Green cubes; oracle/time_port_vs_reference.py),
-# so this baseline understates the reference's CPU rate by about a quarter.
+# restatement runs at 0.77-0.81 of the reference's compiled code on one thread
+# and 0.71-0.93 on 8 over repeated runs (vortex and Taylor-Green cubes;
+# oracle/time_port_vs_reference.py), so this baseline understates the
+# reference's CPU rate by up to about a quarter.
 PORT_NOTE = ("C restatement of the reference loop (the reference's sources are not on this "
-             "host); on an x86 host it ran at 0.72-0.82 of the reference's own compiled code "
+             "host); on an x86 host it ran at 0.77-0.81 (1 thread) and 0.71-0.93 (8 threads) of "
+             "the reference's own compiled code "
              "(oracle/time_port_vs_reference.py)")
 
 
