@@ -229,3 +229,26 @@ def test_two_ranks_exchange_flag_bands():
             case = G.flag_cases()[name]
             want = _restated(case)
             assert np.array_equal(got, want[own]), (name, rank)
+
+
+def test_synthetic_sphere_flags_against_the_setup_routine():
+    """What the routine would change on the benchmark's sphere grids after
+    their IBM preprocessing (main.cpp:1070 runs it there; the synthetic
+    builders do not): nothing on the 1,584-cube sphere, and 312 ghost-layer
+    flags next to the body on the batch's grids (fine cubes of edge 0.5),
+    240 fluid -> ghost and 72 ghost -> fluid."""
+    port = O.Port()
+
+    def pre(case, tris):
+        return port.ibm(case, case.fws, tris)
+    single = cases.sphere_ibm(preprocess=pre)
+    assert np.array_equal(_restated(single), single.fws)
+    grid = cases.sphere_cubes(64, preprocess=pre)  # the body's 64 fine cubes of every batch case
+    out = _restated(grid)
+    changed = np.argwhere(out != grid.fws)
+    n = grid.n
+    assert len(changed) == 312
+    assert all(min(x[1:]) < 2 or max(x[1:]) > n + 1 for x in changed)  # ghost layers only
+    before, after = grid.fws[tuple(changed.T)], out[tuple(changed.T)]
+    assert int(((before == 1) & (after == 0)).sum()) == 240
+    assert int(((before == 0) & (after == 1)).sum()) == 72
